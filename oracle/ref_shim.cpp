@@ -1,0 +1,293 @@
+// C entry points over the reference zest library (sebsassi/zest), used ONLY as
+// test infrastructure: to generate golden fixtures under tests/golden/ and as
+// the timed CPU baseline of bench.py's reference arm.  It is compiled from the
+// reference's own headers and sources by oracle/build_ref.py into oracle/_ref/.
+// Nothing in the product (zest_gb300/, include/) links or calls this file.
+//
+// Every function calls the reference's public API unchanged:
+//   zest::zt::GLQTransformer<...>   include/zernike_glq_transformer.hpp:511-965
+//   zest::st::GLQTransformer<...>   include/sh_glq_transformer.hpp:513-1213
+//   zest::Rotor                     include/rotor.hpp:95-401
+//   zest::WignerdPiHalfCollection   include/wignerd_collection.hpp:66-110
+//   zest::st::PlmRecursion          include/plm_recursion.hpp:62-362
+//   zest::zt::RadialZernikeRecursion include/radial_zernike_recursion.hpp:38-297
+//   zest::gl::gl_nodes_and_weights  include/gauss_legendre.hpp:1549-1565
+//   zest::{zt,st}::GridEvaluator    include/grid_evaluator.hpp:52-325
+#include <array>
+#include <chrono>
+#include <cstddef>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "zernike_glq_transformer.hpp"
+#include "sh_glq_transformer.hpp"
+#include "rotor.hpp"
+#include "wignerd_collection.hpp"
+#include "grid_evaluator.hpp"
+
+using zest::zt::ZernikeNorm;
+using zest::st::SHNorm;
+using zest::st::SHPhase;
+
+namespace {
+
+template <typename F>
+int dispatch_zt(int zn, int sn, int sp, F&& f) {
+    const int code = (zn & 1) | ((sn & 1) << 1) | ((sp & 1) << 2);
+    switch (code) {
+    case 0: f.template operator()<ZernikeNorm::normed, SHNorm::geo, SHPhase::none>(); return 0;
+    case 1: f.template operator()<ZernikeNorm::unnormed, SHNorm::geo, SHPhase::none>(); return 0;
+    case 2: f.template operator()<ZernikeNorm::normed, SHNorm::qm, SHPhase::none>(); return 0;
+    case 3: f.template operator()<ZernikeNorm::unnormed, SHNorm::qm, SHPhase::none>(); return 0;
+    case 4: f.template operator()<ZernikeNorm::normed, SHNorm::geo, SHPhase::cs>(); return 0;
+    case 5: f.template operator()<ZernikeNorm::unnormed, SHNorm::geo, SHPhase::cs>(); return 0;
+    case 6: f.template operator()<ZernikeNorm::normed, SHNorm::qm, SHPhase::cs>(); return 0;
+    case 7: f.template operator()<ZernikeNorm::unnormed, SHNorm::qm, SHPhase::cs>(); return 0;
+    }
+    return -1;
+}
+
+template <typename F>
+int dispatch_st(int sn, int sp, F&& f) {
+    const int code = (sn & 1) | ((sp & 1) << 1);
+    switch (code) {
+    case 0: f.template operator()<SHNorm::geo, SHPhase::none>(); return 0;
+    case 1: f.template operator()<SHNorm::qm, SHPhase::none>(); return 0;
+    case 2: f.template operator()<SHNorm::geo, SHPhase::cs>(); return 0;
+    case 3: f.template operator()<SHNorm::qm, SHPhase::cs>(); return 0;
+    }
+    return -1;
+}
+
+zest::RotationType rot_type(int t) {
+    return t ? zest::RotationType::coordinate : zest::RotationType::object;
+}
+
+using ZtLayout = zest::zt::DefaultLayout;
+using StLonLat = zest::st::LonLatLayout<>;
+using StLatLon = zest::st::LatLonLayout<>;
+
+}  // namespace
+
+extern "C" {
+
+int ref_gl_nodes_weights(std::size_t n, int packed, int angle_style, double* nodes, double* weights) {
+    namespace gl = zest::gl;
+    const std::size_t parity = n & 1;
+    const std::size_t sz = packed ? gl::PackedLayout::size(n) : n;
+    std::vector<double> nd(sz), wt(sz);
+    if (packed) {
+        if (angle_style) gl::gl_nodes_and_weights<gl::PackedLayout, gl::GLNodeStyle::angle>(nd, wt, parity);
+        else gl::gl_nodes_and_weights<gl::PackedLayout, gl::GLNodeStyle::cos>(nd, wt, parity);
+    } else {
+        if (angle_style) gl::gl_nodes_and_weights<gl::UnpackedLayout, gl::GLNodeStyle::angle>(nd, wt, parity);
+        else gl::gl_nodes_and_weights<gl::UnpackedLayout, gl::GLNodeStyle::cos>(nd, wt, parity);
+    }
+    std::memcpy(nodes, nd.data(), sz * sizeof(double));
+    std::memcpy(weights, wt.data(), sz * sizeof(double));
+    return 0;
+}
+
+int ref_plm_real(std::size_t order, int sn, int sp, std::size_t nz, const double* z, double* out) {
+    return dispatch_st(sn, sp, [&]<SHNorm N, SHPhase P>() {
+        zest::st::PlmRecursion rec(order);
+        std::vector<double> zz(z, z + nz);
+        std::vector<double> buf(zest::st::PlmLayout::size(order) * nz);
+        zest::st::PlmVecSpan<double, N, P> plm(buf, order, nz);
+        rec.plm_real(std::span<const double>(zz), plm);
+        std::memcpy(out, buf.data(), buf.size() * sizeof(double));
+    });
+}
+
+int ref_radial_zernike(std::size_t order, int zn, std::size_t nr, const double* r, double* out) {
+    std::vector<double> rr(r, r + nr);
+    std::vector<double> buf(zest::zt::RadialZernikeLayout::size(order) * nr);
+    zest::zt::RadialZernikeRecursion rec(order);
+    if (zn == 0) {
+        zest::zt::RadialZernikeVecSpan<double, ZernikeNorm::normed> span(buf, order, nr);
+        rec.zernike<ZernikeNorm::normed>(std::span<const double>(rr), span);
+    } else {
+        zest::zt::RadialZernikeVecSpan<double, ZernikeNorm::unnormed> span(buf, order, nr);
+        rec.zernike<ZernikeNorm::unnormed>(std::span<const double>(rr), span);
+    }
+    std::memcpy(out, buf.data(), buf.size() * sizeof(double));
+    return 0;
+}
+
+int ref_zt_grid_points(std::size_t order, double* lon, double* colat, double* r) {
+    zest::zt::BallGLQGridPoints<ZtLayout> pts(order);
+    auto a = pts.longitudes();
+    auto b = pts.lat_glq_nodes();
+    auto c = pts.rad_glq_nodes();
+    std::memcpy(lon, a.data(), a.size() * sizeof(double));
+    std::memcpy(colat, b.data(), b.size() * sizeof(double));
+    std::memcpy(r, c.data(), c.size() * sizeof(double));
+    return 0;
+}
+
+int ref_zt_forward(int zn, int sn, int sp, std::size_t grid_order, std::size_t exp_order,
+                   const double* grid, double* coeffs) {
+    return dispatch_zt(zn, sn, sp, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
+        zest::zt::GLQTransformer<Z, N, P, ZtLayout> tr(grid_order);
+        zest::zt::BallGLQGridSpan<const double, ZtLayout> g(grid, grid_order);
+        zest::zt::RealZernikeSpan<std::array<double, 2>, Z, N, P> e(
+            reinterpret_cast<std::array<double, 2>*>(coeffs), exp_order);
+        tr.forward_transform(g, e);
+    });
+}
+
+int ref_zt_backward(int zn, int sn, int sp, std::size_t exp_order, std::size_t grid_order,
+                    const double* coeffs, double* grid) {
+    return dispatch_zt(zn, sn, sp, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
+        zest::zt::GLQTransformer<Z, N, P, ZtLayout> tr(grid_order);
+        zest::zt::BallGLQGridSpan<double, ZtLayout> g(grid, grid_order);
+        zest::zt::RealZernikeSpan<const std::array<double, 2>, Z, N, P> e(
+            reinterpret_cast<const std::array<double, 2>*>(coeffs), exp_order);
+        tr.backward_transform(e, g);
+    });
+}
+
+int ref_st_grid_points(std::size_t order, int latlon, double* lon, double* colat) {
+    auto copy = [&](auto& pts) {
+        auto a = pts.longitudes();
+        auto b = pts.glq_nodes();
+        std::memcpy(lon, a.data(), a.size() * sizeof(double));
+        std::memcpy(colat, b.data(), b.size() * sizeof(double));
+    };
+    if (latlon) { zest::st::SphereGLQGridPoints<StLatLon> p(order); copy(p); }
+    else { zest::st::SphereGLQGridPoints<StLonLat> p(order); copy(p); }
+    return 0;
+}
+
+int ref_st_forward(int sn, int sp, int latlon, std::size_t grid_order, std::size_t exp_order,
+                   const double* grid, double* coeffs) {
+    return dispatch_st(sn, sp, [&]<SHNorm N, SHPhase P>() {
+        auto run = [&]<typename Lay>() {
+            zest::st::GLQTransformer<N, P, Lay> tr(grid_order);
+            zest::st::SphereGLQGridSpan<const double, Lay> g(grid, grid_order);
+            zest::st::RealSHSpan<std::array<double, 2>, N, P> e(
+                reinterpret_cast<std::array<double, 2>*>(coeffs), exp_order);
+            tr.forward_transform(g, e);
+        };
+        if (latlon) run.template operator()<StLatLon>();
+        else run.template operator()<StLonLat>();
+    });
+}
+
+int ref_st_backward(int sn, int sp, int latlon, std::size_t exp_order, std::size_t grid_order,
+                    const double* coeffs, double* grid) {
+    return dispatch_st(sn, sp, [&]<SHNorm N, SHPhase P>() {
+        auto run = [&]<typename Lay>() {
+            zest::st::GLQTransformer<N, P, Lay> tr(grid_order);
+            zest::st::SphereGLQGridSpan<double, Lay> g(grid, grid_order);
+            zest::st::RealSHSpan<const std::array<double, 2>, N, P> e(
+                reinterpret_cast<const std::array<double, 2>*>(coeffs), exp_order);
+            tr.backward_transform(e, g);
+        };
+        if (latlon) run.template operator()<StLatLon>();
+        else run.template operator()<StLonLat>();
+    });
+}
+
+int ref_wignerd(std::size_t order, double* out) {
+    zest::WignerdPiHalfCollection w(order);
+    auto m = w.matrices();
+    std::memcpy(out, m.data(), m.size() * sizeof(double));
+    return 0;
+}
+
+int ref_zt_rotate(int zn, int sn, int sp, std::size_t order, double* coeffs, const double* euler, int type) {
+    return dispatch_zt(zn, sn, sp, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
+        zest::WignerdPiHalfCollection w(order);
+        zest::Rotor rot(order);
+        zest::zt::RealZernikeSpan<std::array<double, 2>, Z, N, P> e(
+            reinterpret_cast<std::array<double, 2>*>(coeffs), order);
+        rot.rotate(e, w, std::array<double, 3>{euler[0], euler[1], euler[2]}, rot_type(type));
+    });
+}
+
+int ref_zt_rotate_matrix(int zn, int sn, int sp, std::size_t order, double* coeffs, const double* mat, int type) {
+    return dispatch_zt(zn, sn, sp, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
+        zest::WignerdPiHalfCollection w(order);
+        zest::Rotor rot(order);
+        zest::zt::RealZernikeSpan<std::array<double, 2>, Z, N, P> e(
+            reinterpret_cast<std::array<double, 2>*>(coeffs), order);
+        std::array<std::array<double, 3>, 3> m{};
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) m[i][j] = mat[3 * i + j];
+        rot.rotate(e, w, m, rot_type(type));
+    });
+}
+
+int ref_st_rotate(int sn, int sp, std::size_t order, double* coeffs, const double* euler, int type) {
+    return dispatch_st(sn, sp, [&]<SHNorm N, SHPhase P>() {
+        zest::WignerdPiHalfCollection w(order);
+        zest::Rotor rot(order);
+        zest::st::RealSHSpan<std::array<double, 2>, N, P> e(
+            reinterpret_cast<std::array<double, 2>*>(coeffs), order);
+        rot.rotate(e, w, std::array<double, 3>{euler[0], euler[1], euler[2]}, rot_type(type));
+    });
+}
+
+int ref_zt_polar_rotate(int zn, int sn, int sp, std::size_t order, double* coeffs, double angle, int type) {
+    return dispatch_zt(zn, sn, sp, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
+        zest::Rotor rot(order);
+        zest::zt::RealZernikeSpan<std::array<double, 2>, Z, N, P> e(
+            reinterpret_cast<std::array<double, 2>*>(coeffs), order);
+        rot.polar_rotate(e, angle, rot_type(type));
+    });
+}
+
+int ref_st_polar_rotate(int sn, int sp, std::size_t order, double* coeffs, double angle, int type) {
+    return dispatch_st(sn, sp, [&]<SHNorm N, SHPhase P>() {
+        zest::Rotor rot(order);
+        zest::st::RealSHSpan<std::array<double, 2>, N, P> e(
+            reinterpret_cast<std::array<double, 2>*>(coeffs), order);
+        rot.polar_rotate(e, angle, rot_type(type));
+    });
+}
+
+int ref_zt_evaluate(int zn, int sn, int sp, std::size_t order, const double* coeffs,
+                    std::size_t nlon, const double* lon, std::size_t nlat, const double* colat,
+                    std::size_t nrad, const double* rad, double* out) {
+    return dispatch_zt(zn, sn, sp, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
+        zest::zt::GridEvaluator ev(order, nlon, nlat, nrad);
+        zest::zt::RealZernikeSpan<const std::array<double, 2>, Z, N, P> e(
+            reinterpret_cast<const std::array<double, 2>*>(coeffs), order);
+        auto res = ev.evaluate(e, std::span<const double>(lon, nlon), std::span<const double>(colat, nlat),
+                               std::span<const double>(rad, nrad));
+        std::memcpy(out, res.data(), res.size() * sizeof(double));
+    });
+}
+
+// CPU baseline: forward then backward transform of `batch` Zernike functions
+// of one order, one reference transformer per std::thread.  Returns seconds.
+double ref_zt_fwd_bwd_batch(int zn, int sn, int sp, std::size_t order, std::size_t batch,
+                            const double* grids, double* coeffs, double* grids_out, int nthreads) {
+    const std::size_t gsz = ZtLayout::size(order);
+    const std::size_t csz = zest::zt::RealZernikeExpansionGeo::size(order);
+    double secs = 0.0;
+    dispatch_zt(zn, sn, sp, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
+        auto t0 = std::chrono::steady_clock::now();
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthreads; ++t) {
+            pool.emplace_back([&, t]() {
+                zest::zt::GLQTransformer<Z, N, P, ZtLayout> tr(order);
+                for (std::size_t b = t; b < batch; b += nthreads) {
+                    zest::zt::BallGLQGridSpan<const double, ZtLayout> g(grids + b * gsz, order);
+                    zest::zt::RealZernikeSpan<std::array<double, 2>, Z, N, P> e(
+                        reinterpret_cast<std::array<double, 2>*>(coeffs + 2 * b * csz), order);
+                    tr.forward_transform(g, e);
+                    zest::zt::BallGLQGridSpan<double, ZtLayout> go(grids_out + b * gsz, order);
+                    tr.backward_transform(e, go);
+                }
+            });
+        }
+        for (auto& th : pool) th.join();
+        secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    });
+    return secs;
+}
+
+}  // extern "C"

@@ -1,0 +1,165 @@
+"""Pin the CPU oracle (oracle/zest_oracle.c) to the reference's golden vectors
+(tests/golden/, generated from the compiled reference) and to the closed-form
+known-answer cases of the reference's own tests.  No GPU needed."""
+import numpy as np
+import pytest
+
+from oracle import tri_idx, tri_size, zidx, zt_coeff_size, zt_grid_shape
+
+CONVS_ZT = [(1, 0, 0), (0, 0, 0), (1, 1, 0), (0, 1, 0), (1, 1, 1), (0, 1, 1), (1, 0, 1), (0, 0, 1)]
+CONVS_ST = [(0, 0), (1, 0), (0, 1), (1, 1)]
+
+
+def relmax(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 8, 21, 24, 69, 70, 71, 101, 104, 201, 208, 512, 1024])
+@pytest.mark.parametrize("packed", [0, 1])
+def test_gl_nodes_weights(oracle, golden, n, packed):
+    g = golden("gl")
+    x, w = oracle.gl_nodes_weights(n, bool(packed))
+    assert np.max(np.abs(x - g[f"x_{n}_{packed}"])) < 1e-15
+    assert np.max(np.abs(w - g[f"w_{n}_{packed}"]) / g[f"w_{n}_{packed}"]) < 2e-15
+
+
+def test_gl_weights_sum_to_two(oracle):
+    # tests/test_gauss_legendre.cpp:127-165 (weights of the rule sum to 2)
+    for n in [1, 2, 7, 64, 201, 1024]:
+        _, w = oracle.gl_nodes_weights(n)
+        assert abs(w.sum() - 2.0) < 1e-13
+
+
+@pytest.mark.parametrize("sn,sp", CONVS_ST)
+def test_plm_table(oracle, golden, sn, sp):
+    t = golden("tables")
+    assert relmax(oracle.plm_real(20, sn, sp, t["z"]), t[f"plm_{sn}_{sp}"]) < 1e-15
+
+
+def test_plm_closed_forms(oracle):
+    # tests/test_plm_recursion.cpp:39-202: geodesy-normalised closed forms, no CS phase,
+    # real (sqrt2 for m>0): P10 = sqrt3 z, P11 = -sqrt2 sqrt(3/2) sqrt(1-z^2), ...
+    z = np.array([1.0, -1.0, 0.0, 0.974, 0.3])
+    p = oracle.plm_real(4, 0, 0, z)
+    u = np.sqrt(1 - z * z)
+    np.testing.assert_allclose(p[tri_idx(0, 0)], 1.0, atol=1e-14)
+    np.testing.assert_allclose(p[tri_idx(1, 0)], np.sqrt(3) * z, atol=1e-14)
+    np.testing.assert_allclose(p[tri_idx(1, 1)], -np.sqrt(3) * u, atol=1e-14)
+    np.testing.assert_allclose(p[tri_idx(2, 0)], np.sqrt(5) * 0.5 * (3 * z * z - 1), atol=1e-14)
+    np.testing.assert_allclose(p[tri_idx(2, 2)], np.sqrt(15) / 2 * u * u, atol=1e-14)
+    np.testing.assert_allclose(p[tri_idx(3, 3)], -np.sqrt(35 / 8) * u ** 3, atol=1e-13)
+
+
+@pytest.mark.parametrize("zn", [0, 1])
+def test_radial_table(oracle, golden, zn):
+    t = golden("tables")
+    assert relmax(oracle.radial_zernike(20, zn, t["r"]), t[f"rz_{zn}"]) < 1e-15
+
+
+def test_radial_closed_forms(oracle):
+    # tests/test_radial_zernike_recursion.cpp:137-553 (unnormalised closed forms)
+    from oracle import rad_idx
+    r = np.linspace(0.0, 1.0, 9)
+    z = oracle.radial_zernike(7, 1, r)
+    r2 = r * r
+    np.testing.assert_allclose(z[rad_idx(2, 0)], 2.5 * r2 - 1.5, atol=1e-14)
+    np.testing.assert_allclose(z[rad_idx(4, 0)], (63 * r2 * r2 - 70 * r2 + 15) / 8, atol=1e-13)
+    np.testing.assert_allclose(z[rad_idx(5, 5)], r ** 5, atol=1e-14)
+    # R_nl(1) = 1 for every unnormalised polynomial
+    assert np.max(np.abs(z[:, -1] - 1.0)) < 1e-12
+
+
+def test_wignerd_table(oracle, golden):
+    assert relmax(oracle.wignerd(16), golden("tables")["wignerd_16"]) == 0.0
+
+
+def test_wignerd_closed_forms(oracle):
+    # tests/test_rotor.cpp:91-259: d^1(pi/2) and d^2_{00}(pi/2) = -1/2
+    d = oracle.wignerd(3)
+    off1 = 1
+    assert abs(d[off1 + 2 * 1 + 0] + 1 / np.sqrt(2)) < 1e-15  # d^1_{10}
+    assert abs(d[off1 + 2 * 1 + 1] - 0.5) < 1e-15             # d^1_{11}
+    off2 = 5
+    assert abs(d[off2 + 0] + 0.5) < 1e-15                     # d^2_{00}
+
+
+def test_zt_config1(oracle, golden):
+    g = golden("zt_config1")
+    c = oracle.zt_forward(g["grid"], 20)
+    assert relmax(c, g["coeffs"]) < 1e-13
+    rt = oracle.zt_backward(g["coeffs"], 20)
+    assert relmax(rt, g["roundtrip"]) < 1e-13
+
+
+@pytest.mark.parametrize("L", [1, 2, 3, 6, 11, 16])
+@pytest.mark.parametrize("conv", CONVS_ZT)
+def test_zt_random(oracle, golden, L, conv):
+    key = f"{L}_{conv[0]}{conv[1]}{conv[2]}"
+    z = golden("zt_random")
+    if "c_" + key not in z:
+        pytest.skip("fixture holds this order for one convention only")
+    assert relmax(oracle.zt_backward(z["c_" + key], L, L, *conv), z["g_" + key]) < 1e-13
+    assert relmax(oracle.zt_forward(z["g_" + key], L, L, *conv), z["f_" + key]) < 1e-13
+
+
+def test_zt_order_mismatch(oracle, golden):
+    z = golden("zt_random")
+    assert relmax(oracle.zt_backward(z["trunc_c"], 9, 6), z["trunc_g96"]) < 1e-13
+    assert relmax(oracle.zt_forward(z["trunc_g99"], 9, 6), z["trunc_f96"]) < 1e-13
+    assert relmax(oracle.zt_forward(z["trunc_g99"], 9, 12), z["trunc_f9_12"]) < 1e-13
+    assert relmax(oracle.zt_backward(z["trunc_c6"], 6, 9), z["trunc_g69"]) < 1e-13
+
+
+def test_zt_kat_z000(oracle):
+    # tests/test_zernike_glq_transformer.cpp:57-136: the constant function
+    # znorm*shnorm expands to the single unit coefficient Z000.
+    for zn, sn, sp in CONVS_ZT:
+        L = 6
+        znorm = np.sqrt(3.0) if zn == 0 else 1.0
+        shnorm = 0.5 / np.sqrt(np.pi) if sn == 1 else 1.0
+        grid = np.full(zt_grid_shape(L), znorm * shnorm)
+        c = oracle.zt_forward(grid, L, L, zn, sn, sp)
+        ref = np.zeros_like(c)
+        ref[0, 0] = 1.0
+        assert np.max(np.abs(c - ref)) < 1e-10
+
+
+@pytest.mark.parametrize("L", [1, 2, 5, 8, 16, 24])
+@pytest.mark.parametrize("latlon", [0, 1])
+@pytest.mark.parametrize("conv", CONVS_ST)
+def test_st_random(oracle, golden, L, latlon, conv):
+    key = f"{L}_{latlon}_{conv[0]}{conv[1]}"
+    s = golden("st_random")
+    if "c_" + key not in s:
+        pytest.skip("fixture holds this order for one convention only")
+    assert relmax(oracle.st_backward(s["c_" + key], L, L, *conv, bool(latlon)), s["g_" + key]) < 1e-13
+    assert relmax(oracle.st_forward(s["g_" + key], L, L, *conv, bool(latlon)), s["f_" + key]) < 1e-13
+
+
+@pytest.mark.parametrize("L", [2, 5, 10, 17])
+def test_rotations(oracle, golden, L):
+    r = golden("rotation")
+    assert relmax(oracle.zt_rotate(r[f"zc_{L}"], L, r[f"ze_{L}"], 0), r[f"zobj_{L}"]) < 1e-13
+    assert relmax(oracle.zt_rotate(r[f"zc_{L}"], L, r[f"ze_{L}"], 1), r[f"zcoord_{L}"]) < 1e-13
+    assert relmax(oracle.zt_polar_rotate(r[f"zc_{L}"], L, r[f"ze_{L}"][0], 0), r[f"zpolar_{L}"]) < 1e-13
+    e = oracle.euler_from_matrix(r[f"zmat_{L}"])
+    assert relmax(oracle.zt_rotate(r[f"zc_{L}"], L, e, 0), r[f"zmatobj_{L}"]) < 1e-13
+    assert relmax(oracle.st_rotate(r[f"sc_{L}"], L + 3, r[f"ze_{L}"], 0), r[f"sobj_{L}"]) < 1e-13
+    assert relmax(oracle.st_rotate(r[f"sc_{L}"], L + 3, r[f"ze_{L}"], 1), r[f"scoord_{L}"]) < 1e-13
+    assert relmax(oracle.st_polar_rotate(r[f"sc_{L}"], L + 3, r[f"ze_{L}"][1], 1), r[f"spolar_{L}"]) < 1e-13
+
+
+def test_identity_rotation(oracle):
+    # tests/test_rotor.cpp:277-505: zero Euler angles leave an expansion unchanged
+    rng = np.random.default_rng(3)
+    L = 9
+    c = rng.normal(size=(zt_coeff_size(L), 2))
+    for n in range(L):
+        for l in range(n & 1, n + 1, 2):
+            c[zidx(n, l, 0), 1] = 0.0
+    out = oracle.zt_rotate(c, L, np.zeros(3), 0)
+    assert np.max(np.abs(out - c)) < 1e-13
+    s = rng.normal(size=(tri_size(L), 2))
+    for l in range(L):
+        s[tri_idx(l, 0), 1] = 0.0
+    assert np.max(np.abs(oracle.st_rotate(s, L, np.zeros(3), 0) - s)) < 1e-13
