@@ -1,0 +1,397 @@
+"""Benchmark of the headline workload: Zernike GLQ forward + backward
+transforms at order 200 on a batch of 64 functions (the reference's
+zt::GLQTransformerGeo), in the split-precision form (BF16 fixed-point slices
+on tcgen05) and in the plain FP64 form on the same GPU.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision split|fp64|auto] [--order 200] [--batch 64]
+
+One step = forward_transform then backward_transform of the whole batch
+(grid -> coefficients -> grid).  Inputs: coefficients drawn i.i.d.
+N(0, (n+1)^-3) for valid (n,l,m), Im(m=0) = 0, seeds 1..batch, synthesised to
+the order-200 ball grid by the FP64 backward transform (synthetic data; the
+reference publishes no dataset).  The batch of grids (8.5 GB) is larger than
+L2, so every step streams its inputs from HBM.
+
+Prints one JSON line (rank 0).  `value` is transforms/s over the timed region
+with inputs resident in HBM; `e2e` is the same metric through the C-ABI with
+pinned host buffers (host<->device copies inside the timed region).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Zernike fwd+bwd transforms/s, order 200x64: split-prec vs FP64 GPU at 1e-11 err"
+UNIT = "transforms/s"
+
+
+# --------------------------------------------------------------------------
+def zt_flops_per_function(L: int) -> dict:
+    """Canonical (reference-algorithm) flop count of one forward+backward
+    transform: 2 * [2 nlat nrad L(L+1) + 4 nrad T(L) + 2.5 nrad nlat nlon log2 nlon]."""
+    nlon, nlat, nrad = 2 * L - 1, L + 1, (L + 1 + 7) // 8 * 8
+    T = (L + 1) * (L + 3) * (2 * L + 1) // 24
+    leg = 2 * nlat * nrad * L * (L + 1)
+    rad = 4 * nrad * T
+    fft = 2.5 * nrad * nlat * nlon * np.log2(nlon)
+    return {"legendre": 2 * leg, "radial": 2 * rad, "fft": 2 * fft, "total": 2 * (leg + rad + fft)}
+
+
+def zt_coeffs(L: int, batch: int, seed0: int = 1) -> np.ndarray:
+    """c_nlm ~ N(0, (n+1)^-3) i.i.d., Im(m=0) = 0, seed seed0 + b for item b."""
+    from zest_gb300 import zt_coeff_size
+    T = zt_coeff_size(L)
+    n_of = np.zeros(T, dtype=np.int64)
+    m_of = np.zeros(T, dtype=np.int64)
+    for n in range(L):
+        for l in range(n & 1, n + 1, 2):
+            base = (n + 1) * (n + 3) * (2 * n + 1) // 24 + (l * l) // 4
+            n_of[base:base + l + 1] = n
+            m_of[base:base + l + 1] = np.arange(l + 1)
+    sd = (n_of + 1.0) ** -1.5
+    out = np.empty((batch, T, 2))
+    for b in range(batch):
+        rng = np.random.default_rng(seed0 + b)
+        x = rng.standard_normal((T, 2)) * sd[:, None]
+        x[m_of == 0, 1] = 0.0
+        out[b] = x
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append(parts)
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        smax = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        power = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[4 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(self.rows), "reasons": reasons}
+
+
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return {"hbm_gbs": p["hbm_gbs"], "bf16_tflops": p["bf16_tflops"],
+                "bf16_tflops_sustained": p.get("bf16_tflops_sustained"), "source": "measured"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+# --------------------------------------------------------------------------
+def cpu_reference_sample(grids_host: np.ndarray, L: int, nthreads: int):
+    """The reference zest library (oracle/_ref) on the host cores: one
+    function per thread, forward + backward.  Returns (transforms/s, kind, sample)."""
+    from oracle import Reference
+    try:
+        ref = Reference()
+        kind = "reference"
+        n = min(nthreads, grids_host.shape[0])
+        secs, _, _ = ref.zt_fwd_bwd_batch(grids_host[:n], L, nthreads)
+        return n / secs, kind, f"{n} order-{L} functions fwd+bwd, one per thread on {nthreads} threads"
+    except (FileNotFoundError, OSError):
+        from oracle import Oracle
+        orc = Oracle()
+        t0 = time.perf_counter()
+        c = orc.zt_forward(grids_host[0], L)
+        orc.zt_backward(c, L)
+        secs = time.perf_counter() - t0
+        return 1.0 / secs, "port", f"1 order-{L} function fwd+bwd, oracle port, 1 thread"
+
+
+def run_reference_arm(args, rank: int, world: int) -> None:
+    """`--impl reference`: the reference CPU implementation on the host cores."""
+    if rank != 0:
+        return
+    from oracle import Reference
+    L, nthreads = args.order, os.cpu_count() or 1
+    try:
+        ref = Reference()
+    except (FileNotFoundError, OSError) as exc:
+        print(json.dumps({"impl": "reference", "unavailable": f"reference library not built: {exc}"}))
+        return
+    per_step = nthreads  # one function per core and step (a bounded sample of the 64-function batch)
+    coeffs = zt_coeffs(L, per_step)
+    grids = np.stack([ref.zt_backward(coeffs[b], L) for b in range(per_step)])
+    for _ in range(args.warmup):
+        ref.zt_fwd_bwd_batch(grids, L, nthreads)
+    times = []
+    for _ in range(args.steps):
+        secs, _, _ = ref.zt_fwd_bwd_batch(grids, L, nthreads)
+        times.append(secs)
+    total = sum(times)
+    value = per_step * args.steps / total
+    sample = f"{per_step} order-{L} functions fwd+bwd per step, one per thread"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "zernike_glq_fwd_bwd", "order": L, "batch": per_step, "threads": nthreads,
+                   "transformer": "GLQTransformerGeo", "build": "g++ -O3 (-mcpu=native on aarch64)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "reference", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# --------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["split", "fp64", "auto"], default="auto")
+    ap.add_argument("--order", type=int, default=200)
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--slices", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+
+    import torch
+    import zest_gb300 as zg
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+        dist = tdist
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    L, B = args.order, args.batch
+    ctx = zg.Context(local_rank)
+    precision = args.precision
+    if precision == "auto":
+        try:
+            ctx.set_precision(zg.PRECISION_SPLIT, args.slices)
+            precision = "split"
+        except zg.ZestGPUError:
+            precision = "fp64"
+    ctx.set_precision(zg.PRECISION_FP64)
+
+    gsz = int(np.prod(zg.zt_grid_shape(L)))
+    csz = 2 * zg.zt_coeff_size(L)
+    coeffs_h = zt_coeffs(L, B, seed0=1 + rank * B)
+    coeffs_d = torch.from_numpy(coeffs_h.ravel()).cuda()
+    grids_d = ctx.zt_backward(coeffs_d, L, batch=B)          # FP64 synthesis of the inputs
+    cbuf = torch.empty(B * csz, dtype=torch.float64, device="cuda")
+    gout = torch.empty(B * gsz, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+
+    def step():
+        ctx.zt_forward(grids_d, L, batch=B, out=cbuf)
+        ctx.zt_backward(cbuf, L, batch=B, out=gout)
+
+    def timed(nsteps: int, nwarm: int, sampler=None):
+        for _ in range(nwarm):
+            step()
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        n0 = zg.launch_count()
+        ctx.profile(True)
+        ctx.profile_read(reset=True)
+        if sampler:
+            sampler.start()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(nsteps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        clocks = sampler.stop() if sampler else None
+        prof = ctx.profile_read(reset=True)
+        ctx.profile(False)
+        launches = zg.launch_count() - n0
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, prof, launches, clocks
+
+    # ---- plain FP64 form (always measured: it is the ratio's denominator) ----
+    fp64_steps = max(1, min(args.steps, 2)) if precision == "split" else args.steps
+    fp64_warm = 1 if precision == "split" else args.warmup
+    sampler = ClockSampler(local_rank) if precision == "fp64" else None
+    ms64, prof64, launches64, clocks64 = timed(fp64_steps, fp64_warm, sampler)
+    ref_coeffs = cbuf.clone()
+    ref_grids = gout.clone()
+    result = {"fp64": {"ms_per_step": ms64 / fp64_steps, "value": world * B * fp64_steps / (ms64 * 1e-3),
+                       "stages_ms": {k: v[0] / fp64_steps for k, v in prof64.items()}}}
+
+    flops = zt_flops_per_function(L)
+    peaks = measured_peaks()
+    if precision == "split":
+        ctx.set_precision(zg.PRECISION_SPLIT, args.slices)
+        sampler = ClockSampler(local_rank)
+        ms, prof, launches, clocks = timed(args.steps, args.warmup, sampler)
+        err_c = float(((cbuf - ref_coeffs).abs().reshape(B, -1).amax(1)
+                       / ref_coeffs.abs().reshape(B, -1).amax(1)).max())
+        err_g = float(((gout - ref_grids).abs().reshape(B, -1).amax(1)
+                       / ref_grids.abs().reshape(B, -1).amax(1)).max())
+        dtype = "bf16-slices (7-bit fixed point), fp32 exact partial sums, fp64 recombination"
+    else:
+        ms, prof, launches, clocks = ms64, prof64, launches64, clocks64
+        err_c = err_g = 0.0
+        dtype = "f64"
+    value = world * B * args.steps / (ms * 1e-3)
+
+    # ---- roofline of the dominant stage, from the live CUDA-event stage timings ----
+    steps_run = args.steps
+    stage_ms = {k: v[0] / steps_run for k, v in prof.items()}
+    stage_n = {k: v[1] / steps_run for k, v in prof.items()}
+    if precision == "split":
+        gemm_ms = stage_ms.get("split_gemm", float("nan"))
+        nprod = int(os.environ.get("ZEST_SPLIT_PRODUCTS", "0")) or None
+        algo = prof_split_flops(ctx, L, B)
+        achieved = algo / (gemm_ms * 1e-3) / 1e12 if gemm_ms == gemm_ms else None
+        roofline = {"bound": "tensor", "kernel": "split_gemm", "achieved": achieved,
+                    "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                    "frac": achieved / peaks["bf16_tflops"] if achieved else None, "traffic": None,
+                    "algorithmic": "BF16 MMA flops of the slice products per step", "peak_source": peaks["source"],
+                    "products": nprod}
+    else:
+        # FP64 form: the dominant stage is the folded Legendre contraction, bound by
+        # the FP64 pipe (1.20 TFLOP/s DFMA measured on this GPU model)
+        leg_ms = stage_ms.get("legendre_fwd", 0.0) + stage_ms.get("legendre_bwd", 0.0)
+        leg_flops = B * flops["legendre"] / 2.0  # folded: half the reference's Legendre flops
+        achieved = leg_flops / (leg_ms * 1e-3) / 1e12 if leg_ms else None
+        roofline = {"bound": "fp64", "kernel": "legendre_fwd+legendre_bwd", "achieved": achieved,
+                    "peak": 1.20, "unit": "TFLOP/s", "frac": achieved / 1.20 if achieved else None,
+                    "traffic": None, "peak_source": "DFMA microbenchmark on GB300 (1.20 TFLOP/s)"}
+
+    # ---- end to end through the C-ABI with pinned host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        gh = torch.empty(B * gsz, dtype=torch.float64, pin_memory=True)
+        gh.copy_(grids_d.cpu())
+        ch = torch.empty(B * csz, dtype=torch.float64, pin_memory=True)
+        go = torch.empty(B * gsz, dtype=torch.float64, pin_memory=True)
+
+        def e2e_step():
+            ctx.zt_forward(gh, L, batch=B, out=ch)
+            ctx.zt_backward(ch, L, batch=B, out=go)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        n_e2e = max(1, min(args.steps, 3))
+        for _ in range(n_e2e):
+            e2e_step()
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        if dist is not None:
+            t = torch.tensor([secs], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            secs = float(t.item())
+        e2e = {"value": world * B * n_e2e / secs, "unit": UNIT,
+               "h2d_bytes_per_step": B * (gsz + csz) * 8, "d2h_bytes_per_step": B * (csz + gsz) * 8,
+               "host_buffers": "pinned", "steps": n_e2e}
+        del gh, ch, go
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        grids_host = grids_d[: 16 * gsz].reshape(16, -1).cpu().numpy() if B >= 16 else \
+            grids_d.reshape(B, -1).cpu().numpy()
+        v, kind, sample = cpu_reference_sample(np.ascontiguousarray(grids_host), L, os.cpu_count() or 1)
+        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": kind, "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": {"workload": "zernike_glq_fwd_bwd", "order": L, "batch": B, "precision": precision,
+                       "conventions": "GLQTransformerGeo (unnormed Zernike, 4pi SH, no CS phase)",
+                       "grid": list(zg.zt_grid_shape(L)), "l2": "inputs larger than L2 (batch of grids 8.5 GB)",
+                       "parallelism": f"replicas x{world}"},
+            "fp64_gpu": {"value": result["fp64"]["value"], "ms_per_step": result["fp64"]["ms_per_step"],
+                         "stages_ms": result["fp64"]["stages_ms"]},
+            "split_vs_fp64": value / result["fp64"]["value"] if precision == "split" else None,
+            "max_rel_err_vs_fp64": {"coeffs": err_c, "grid": err_g} if precision == "split" else None,
+            "stages_ms": stage_ms, "stage_launches_per_step": stage_n,
+            "canonical_gflop_per_function": flops["total"] / 1e9,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clocks,
+        }
+        print(json.dumps(line))
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def prof_split_flops(ctx, L, B) -> float:
+    """BF16 tensor flops of the split-precision contractions of one step, as
+    reported by the library."""
+    import zest_gb300 as zg
+    return float(zg.split_flops_per_step(ctx, L, B))
+
+
+if __name__ == "__main__":
+    main()

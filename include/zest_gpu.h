@@ -1,0 +1,171 @@
+/*
+ * zest_gpu.h -- C-ABI of the GB300-native Gauss-Legendre-quadrature transform
+ * and rotation path of zest (sebsassi/zest).
+ *
+ * The reference exposes this path only as a C++20 template API; the C++
+ * headers under include/zest/ keep that API and forward every call to the
+ * entry points declared here.  Each entry point names the reference interface
+ * it replaces (file:line in the reference repository).
+ *
+ * Conventions
+ *   - Every function returns an int status (ZEST_GPU_OK == 0).  Nothing aborts
+ *     or traps; on failure zest_gpu_last_error() holds a message.
+ *   - Buffers are plain pointers + sizes.  `mem` says whether the data
+ *     pointers are host (ZEST_MEM_HOST) or device (ZEST_MEM_DEVICE) memory;
+ *     host buffers are staged through device scratch owned by the context.
+ *   - A context is bound to one device and one CUDA stream and is not
+ *     thread-safe (like the reference's transformers, which hold scratch).
+ *     Calls are asynchronous on that stream for device buffers and
+ *     synchronous for host buffers.
+ *   - Batches are contiguous: item b of a batch of grids starts at
+ *     grids + b * grid_size(order); item b of a batch of expansions starts at
+ *     coeffs + 2 * b * coeff_size(order) (pairs {cos, sin} as in the
+ *     reference's std::array<double, 2> elements).
+ *
+ * Data layouts (identical to the reference):
+ *   Zernike grid   [lon][lat][rad] = (2L-1, L+1, pad8(L+1))
+ *                  include/zernike_glq_transformer.hpp:50-131
+ *   Zernike coeffs idx(n,l,m) = (n+1)(n+3)(2n+1)/24 + floor(l^2/4) + m
+ *                  include/layout.hpp:385-420
+ *   SH grid        LonLat [lon][lat] = (2L-1, pad8(L));
+ *                  LatLon [lat][lon] = (L, pad8(2L-1))
+ *                  include/sh_glq_transformer.hpp:48-197
+ *   SH coeffs      idx(l,m) = l(l+1)/2 + m, include/layout.hpp:203-240
+ */
+#ifndef ZEST_GPU_H
+#define ZEST_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define ZEST_GPU_OK 0
+#define ZEST_GPU_ERR_INVALID 1     /* invalid argument (order, size, enum, null pointer) */
+#define ZEST_GPU_ERR_OOM 2         /* device allocation failed */
+#define ZEST_GPU_ERR_CUDA 3        /* a CUDA runtime call or kernel launch failed */
+#define ZEST_GPU_ERR_TIMEOUT 4     /* a bounded in-kernel wait gave up */
+#define ZEST_GPU_ERR_UNSUPPORTED 5 /* valid request this build does not support */
+
+/* ---- conventions: zest::zt::ZernikeNorm (zernike_conventions.hpp:35),
+ *      zest::st::SHNorm, zest::st::SHPhase (sh_conventions.hpp:35-47) ---- */
+#define ZEST_ZERNIKE_NORMED 0
+#define ZEST_ZERNIKE_UNNORMED 1
+#define ZEST_SH_GEO 0
+#define ZEST_SH_QM 1
+#define ZEST_SH_PHASE_NONE 0
+#define ZEST_SH_PHASE_CS 1
+/* zest::RotationType, include/rotor.hpp:38-44 */
+#define ZEST_ROTATION_OBJECT 0
+#define ZEST_ROTATION_COORDINATE 1
+/* SH grid layouts: LonLatLayout (the default) / LatLonLayout */
+#define ZEST_LAYOUT_LONLAT 0
+#define ZEST_LAYOUT_LATLON 1
+/* arithmetic of the contractions */
+#define ZEST_PRECISION_FP64 0  /* FP64 everywhere (plain form) */
+#define ZEST_PRECISION_SPLIT 1 /* BF16 fixed-point slices on tcgen05, exact FP32 partial sums, FP64 recombination */
+/* memory kinds of data pointers */
+#define ZEST_MEM_DEVICE 0
+#define ZEST_MEM_HOST 1
+
+typedef struct zest_gpu_context zest_gpu_context;
+
+/* ---- context ---- */
+/* Creates a context on `device` bound to `stream` (a cudaStream_t; NULL = the
+ * legacy default stream).  Replaces the scratch/caches a reference
+ * transformer holds (zernike_glq_transformer.hpp:951-964). */
+int zest_gpu_ctx_create(zest_gpu_context** ctx, int device, void* stream);
+int zest_gpu_ctx_destroy(zest_gpu_context* ctx);
+/* Message of the last failing call on this thread ("" if none). */
+const char* zest_gpu_last_error(void);
+/* Precision of the dense contractions; `slices` = number of 7-bit BF16
+ * slices per operand for ZEST_PRECISION_SPLIT (4..8, 0 = default 6). */
+int zest_gpu_set_precision(zest_gpu_context* ctx, int precision, int slices);
+int zest_gpu_synchronize(zest_gpu_context* ctx);
+/* Releases cached tables and scratch (they are rebuilt on demand). */
+int zest_gpu_trim(zest_gpu_context* ctx);
+
+/* ---- profiling (no reference counterpart: the reference times whole calls
+ *      with nanobench, benchmarks/benchmark_zernike_glq_forward_transform.cpp) ----
+ * When enabled, every pipeline stage launched on the context stream is
+ * bracketed by CUDA events; zest_gpu_profile_read synchronizes the stream and
+ * returns the accumulated milliseconds and stage counts for the first n
+ * stages (reset != 0 clears them). */
+int zest_gpu_profile_enable(zest_gpu_context* ctx, int enable);
+int zest_gpu_profile_read(zest_gpu_context* ctx, int reset, double* ms, long long* count, int n);
+int zest_gpu_profile_stage_count(void);
+const char* zest_gpu_profile_stage_name(int stage);
+/* Number of kernels this library has launched in this process. */
+unsigned long long zest_gpu_launch_count(void);
+
+/* ---- sizes (doubles for grids, pairs for coefficients) ---- */
+size_t zest_gpu_zt_grid_size(size_t order);
+size_t zest_gpu_zt_coeff_size(size_t order);
+size_t zest_gpu_st_grid_size(size_t order, int layout);
+size_t zest_gpu_st_coeff_size(size_t order);
+
+/* ---- Zernike GLQ transforms ----
+ * forward: zt::GLQTransformer<...>::forward_transform(BallGLQGridSpan<const double>,
+ *          RealZernikeSpan<std::array<double,2>,...>)  zernike_glq_transformer.hpp:640-655
+ *          (and the container-returning overload :687-693).  The expansion is
+ *          truncated to min(exp_order, grid_order); higher coefficients are zeroed.
+ * backward: ::backward_transform(RealZernikeSpan<const ...>, BallGLQGridSpan<double>)
+ *          zernike_glq_transformer.hpp:663-679 (and :701-707). */
+int zest_gpu_zt_forward(zest_gpu_context* ctx, int zernike_norm, int sh_norm, int sh_phase,
+                        size_t grid_order, size_t exp_order, size_t batch,
+                        const double* grids, double* coeffs, int mem);
+int zest_gpu_zt_backward(zest_gpu_context* ctx, int zernike_norm, int sh_norm, int sh_phase,
+                         size_t exp_order, size_t grid_order, size_t batch,
+                         const double* coeffs, double* grids, int mem);
+
+/* ---- SH GLQ transforms ----
+ * st::GLQTransformer<...>::forward_transform  sh_glq_transformer.hpp:632-647 (:709-714)
+ * st::GLQTransformer<...>::backward_transform sh_glq_transformer.hpp:655-668 (:723-728) */
+int zest_gpu_st_forward(zest_gpu_context* ctx, int sh_norm, int sh_phase, int layout,
+                        size_t grid_order, size_t exp_order, size_t batch,
+                        const double* grids, double* coeffs, int mem);
+int zest_gpu_st_backward(zest_gpu_context* ctx, int sh_norm, int sh_phase, int layout,
+                         size_t exp_order, size_t grid_order, size_t batch,
+                         const double* coeffs, double* grids, int mem);
+
+/* ---- rotations (in place) ----
+ * Rotor::rotate(real Zernike expansion, WignerdPiHalfCollection, euler, type)
+ *   rotor.hpp:214-243; (real SH expansion) rotor.hpp:125-141.
+ * `euler` holds 3 angles (alpha, beta, gamma, intrinsic ZYZ) per batch item.
+ * The rotation-matrix overloads (rotor.hpp:264-300) map to
+ * zest_gpu_euler_from_matrix followed by these calls. */
+int zest_gpu_zt_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
+                       double* coeffs, const double* euler, int rotation_type, int mem);
+int zest_gpu_st_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
+                       double* coeffs, const double* euler, int rotation_type, int mem);
+/* Rotor::polar_rotate, rotor.hpp:316-378 (one angle per batch item). */
+int zest_gpu_zt_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
+                             double* coeffs, const double* angles, int rotation_type, int mem);
+int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
+                             double* coeffs, const double* angles, int rotation_type, int mem);
+/* euler_angles_from_rotation_matrix, rotor.hpp:53-63 (row-major 3x3, host). */
+int zest_gpu_euler_from_matrix(const double* matrix, double* euler);
+
+/* ---- tables (device generated, FP64) ----
+ * gl::gl_nodes_and_weights<Layout, GLNodeStyle::cos>, gauss_legendre.hpp:1549-1565
+ *   (host solve; packed = 1 for PackedLayout).  */
+int zest_gpu_gl_nodes_weights(size_t n, int packed, double* nodes, double* weights);
+/* st::PlmRecursion::plm_real(span z, PlmVecSpan), plm_recursion.hpp:109-113;
+ * out[idx(l,m) * nz + i]. */
+int zest_gpu_plm_table(zest_gpu_context* ctx, size_t order, int sh_norm, int sh_phase,
+                       size_t nz, const double* z, double* out, int mem);
+/* zt::RadialZernikeRecursion::zernike(span r, RadialZernikeVecSpan),
+ * radial_zernike_recursion.hpp:152-288; out[(floor((n+1)^2/4) + l/2) * nr + k]. */
+int zest_gpu_radial_table(zest_gpu_context* ctx, size_t order, int zernike_norm,
+                          size_t nr, const double* r, double* out, int mem);
+/* WignerdPiHalfCollection(order).matrices(), wignerd_collection.hpp:66-110,
+ * src/wignerd_collection.cpp:29-98; size order(order+1)(2order+1)/6. */
+int zest_gpu_wignerd_table(zest_gpu_context* ctx, size_t order, double* out, int mem);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ZEST_GPU_H */

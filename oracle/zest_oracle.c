@@ -162,10 +162,10 @@ void oracle_gl_nodes_weights(sz n, int packed, double* nodes, double* weights) {
             nodes[nu - k] = x;
             weights[nu - k] = w;
         } else {
-            nodes[n - k] = x;
-            weights[n - k] = w;
             nodes[k - 1] = -x;
             weights[k - 1] = w;
+            nodes[n - k] = x; /* the middle node of an odd rule stays +0 */
+            weights[n - k] = w;
         }
     }
 }

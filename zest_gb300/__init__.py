@@ -1,0 +1,342 @@
+"""zest_gb300 -- GB300-native (sm_103a) Gauss-Legendre-quadrature transforms
+and rotations of zest (sebsassi/zest), bound through the C-ABI of
+include/zest_gpu.h.
+
+This module is a thin ctypes binding: every call goes to libzest_gb300.so,
+which must be built (``python -m zest_gb300.build``).  There is no CPU
+fallback: without the library, or without a GB300, calls raise.
+
+Arrays: numpy arrays are host memory (staged by the library); torch CUDA
+tensors are device memory (used in place, on the context's stream).  All data
+is float64 in the reference's layouts (see include/zest_gpu.h).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libzest_gb300.so")
+
+# conventions (zest::zt::ZernikeNorm, zest::st::SHNorm, zest::st::SHPhase)
+ZERNIKE_NORMED, ZERNIKE_UNNORMED = 0, 1
+SH_GEO, SH_QM = 0, 1
+SH_PHASE_NONE, SH_PHASE_CS = 0, 1
+ROTATION_OBJECT, ROTATION_COORDINATE = 0, 1
+LAYOUT_LONLAT, LAYOUT_LATLON = 0, 1
+PRECISION_FP64, PRECISION_SPLIT = 0, 1
+MEM_DEVICE, MEM_HOST = 0, 1
+
+# the reference's transformer aliases (zernike_glq_transformer.hpp:967-1025)
+ZT_ACOUSTICS = (ZERNIKE_UNNORMED, SH_QM, SH_PHASE_NONE)
+ZT_NORMAL_ACOUSTICS = (ZERNIKE_NORMED, SH_QM, SH_PHASE_NONE)
+ZT_QM = (ZERNIKE_UNNORMED, SH_QM, SH_PHASE_CS)
+ZT_NORMAL_QM = (ZERNIKE_NORMED, SH_QM, SH_PHASE_CS)
+ZT_GEO = (ZERNIKE_UNNORMED, SH_GEO, SH_PHASE_NONE)
+ZT_NORMAL_GEO = (ZERNIKE_NORMED, SH_GEO, SH_PHASE_NONE)
+# sh_glq_transformer.hpp:1215-1240
+ST_ACOUSTICS = (SH_QM, SH_PHASE_NONE)
+ST_QM = (SH_QM, SH_PHASE_CS)
+ST_GEO = (SH_GEO, SH_PHASE_NONE)
+
+
+class ZestGPUError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"zest_gpu error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def library() -> ctypes.CDLL:
+    """Loads libzest_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ZestGPUError(-1, f"{LIB_PATH} is missing: build it with `python -m zest_gb300.build`")
+        lib = ctypes.CDLL(LIB_PATH)
+        _declare(lib)
+        _lib = lib
+    return _lib
+
+
+_sz = ctypes.c_size_t
+_i = ctypes.c_int
+_vp = ctypes.c_void_p
+
+_SIGNATURES = {
+    "zest_gpu_ctx_create": [ctypes.POINTER(_vp), _i, _vp],
+    "zest_gpu_ctx_destroy": [_vp],
+    "zest_gpu_set_precision": [_vp, _i, _i],
+    "zest_gpu_synchronize": [_vp],
+    "zest_gpu_trim": [_vp],
+    "zest_gpu_zt_forward": [_vp, _i, _i, _i, _sz, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_zt_backward": [_vp, _i, _i, _i, _sz, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_st_forward": [_vp, _i, _i, _i, _sz, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_st_backward": [_vp, _i, _i, _i, _sz, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_zt_rotate": [_vp, _sz, _sz, _vp, _vp, _i, _i],
+    "zest_gpu_st_rotate": [_vp, _sz, _sz, _vp, _vp, _i, _i],
+    "zest_gpu_zt_polar_rotate": [_vp, _sz, _sz, _vp, _vp, _i, _i],
+    "zest_gpu_st_polar_rotate": [_vp, _sz, _sz, _vp, _vp, _i, _i],
+    "zest_gpu_euler_from_matrix": [_vp, _vp],
+    "zest_gpu_gl_nodes_weights": [_sz, _i, _vp, _vp],
+    "zest_gpu_plm_table": [_vp, _sz, _i, _i, _sz, _vp, _vp, _i],
+    "zest_gpu_radial_table": [_vp, _sz, _i, _sz, _vp, _vp, _i],
+    "zest_gpu_wignerd_table": [_vp, _sz, _vp, _i],
+    "zest_gpu_profile_enable": [_vp, _i],
+    "zest_gpu_profile_read": [_vp, _i, _vp, _vp, _i],
+    "zest_gpu_profile_stage_count": [],
+}
+_SIZE_FUNCS = {
+    "zest_gpu_zt_grid_size": [_sz],
+    "zest_gpu_zt_coeff_size": [_sz],
+    "zest_gpu_st_grid_size": [_sz, _i],
+    "zest_gpu_st_coeff_size": [_sz],
+}
+
+
+def _declare(lib):
+    for name, args in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _i
+    for name, args in _SIZE_FUNCS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = _sz
+    lib.zest_gpu_last_error.argtypes = []
+    lib.zest_gpu_last_error.restype = ctypes.c_char_p
+    lib.zest_gpu_profile_stage_name.argtypes = [_i]
+    lib.zest_gpu_profile_stage_name.restype = ctypes.c_char_p
+    lib.zest_gpu_launch_count.argtypes = []
+    lib.zest_gpu_launch_count.restype = ctypes.c_ulonglong
+
+
+def exported_symbols() -> list[str]:
+    return sorted(list(_SIGNATURES) + list(_SIZE_FUNCS)
+                  + ["zest_gpu_last_error", "zest_gpu_profile_stage_name", "zest_gpu_launch_count"])
+
+
+def launch_count() -> int:
+    """Kernels launched by the library so far in this process."""
+    return int(library().zest_gpu_launch_count())
+
+
+def _check(code: int):
+    if code != 0:
+        msg = library().zest_gpu_last_error().decode(errors="replace")
+        raise ZestGPUError(code, msg)
+
+
+# ---- shapes ----
+def pad8(n: int) -> int:
+    return (n + 7) & ~7
+
+
+def zt_grid_shape(order: int):
+    return (2 * order - 1 if order else 0, order + 1, pad8(order + 1))
+
+
+def zt_coeff_size(order: int) -> int:
+    return (order + 1) * (order + 3) * (2 * order + 1) // 24
+
+
+def st_grid_shape(order: int, layout: int = LAYOUT_LONLAT):
+    if layout == LAYOUT_LATLON:
+        return (order, pad8(2 * order - 1 if order else 0))
+    return (2 * order - 1 if order else 0, pad8(order))
+
+
+def st_coeff_size(order: int) -> int:
+    return order * (order + 1) // 2
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _ptr(x, want_size: int):
+    """(pointer, mem kind) of a float64 numpy array (host) or torch CUDA tensor."""
+    if _is_torch(x):
+        import torch
+        if x.dtype != torch.float64 or not x.is_contiguous():
+            raise ValueError("torch tensors must be contiguous float64")
+        if x.numel() != want_size:
+            raise ValueError(f"expected {want_size} elements, got {x.numel()}")
+        return ctypes.c_void_p(x.data_ptr()), (MEM_DEVICE if x.is_cuda else MEM_HOST)
+    if not isinstance(x, np.ndarray) or x.dtype != np.float64 or not x.flags["C_CONTIGUOUS"]:
+        raise ValueError("numpy arrays must be C-contiguous float64")
+    if x.size != want_size:
+        raise ValueError(f"expected {want_size} elements, got {x.size}")
+    return ctypes.c_void_p(x.ctypes.data), MEM_HOST
+
+
+class Context:
+    """A device + stream with cached tables and scratch (zest_gpu_context)."""
+
+    def __init__(self, device: int = 0, stream: Optional[int] = None):
+        lib = library()
+        h = _vp()
+        _check(lib.zest_gpu_ctx_create(ctypes.byref(h), device, _vp(stream or 0)))
+        self._h = h
+        self.lib = lib
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.zest_gpu_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_precision(self, precision: int, slices: int = 0):
+        _check(self.lib.zest_gpu_set_precision(self._h, precision, slices))
+
+    def synchronize(self):
+        _check(self.lib.zest_gpu_synchronize(self._h))
+
+    def trim(self):
+        _check(self.lib.zest_gpu_trim(self._h))
+
+    def profile(self, enable: bool = True):
+        _check(self.lib.zest_gpu_profile_enable(self._h, int(enable)))
+
+    def profile_read(self, reset: bool = True) -> dict:
+        """{stage: (milliseconds, count)} accumulated since the last reset."""
+        n = int(self.lib.zest_gpu_profile_stage_count())
+        ms = np.zeros(n)
+        cnt = np.zeros(n, dtype=np.int64)
+        _check(self.lib.zest_gpu_profile_read(self._h, int(reset), _vp(ms.ctypes.data), _vp(cnt.ctypes.data), n))
+        out = {}
+        for i in range(n):
+            if cnt[i]:
+                out[self.lib.zest_gpu_profile_stage_name(i).decode()] = (float(ms[i]), int(cnt[i]))
+        return out
+
+    # ---- Zernike ----
+    def zt_forward(self, grids, grid_order: int, exp_order: Optional[int] = None, batch: int = 1,
+                   conv=ZT_GEO, out=None):
+        exp_order = grid_order if exp_order is None else exp_order
+        gsz = int(np.prod(zt_grid_shape(grid_order))) * batch
+        csz = 2 * zt_coeff_size(exp_order) * batch
+        gp, gm = _ptr(grids, gsz)
+        if out is None:
+            out = self._alloc_like(grids, csz)
+        cp, cm = _ptr(out, csz)
+        if gm != cm:
+            raise ValueError("input and output must both be host or both be device memory")
+        _check(self.lib.zest_gpu_zt_forward(self._h, *conv, grid_order, exp_order, batch, gp, cp, gm))
+        return out
+
+    def zt_backward(self, coeffs, exp_order: int, grid_order: Optional[int] = None, batch: int = 1,
+                    conv=ZT_GEO, out=None):
+        grid_order = exp_order if grid_order is None else grid_order
+        gsz = int(np.prod(zt_grid_shape(grid_order))) * batch
+        csz = 2 * zt_coeff_size(exp_order) * batch
+        cp, cm = _ptr(coeffs, csz)
+        if out is None:
+            out = self._alloc_like(coeffs, gsz)
+        gp, gm = _ptr(out, gsz)
+        if gm != cm:
+            raise ValueError("input and output must both be host or both be device memory")
+        _check(self.lib.zest_gpu_zt_backward(self._h, *conv, exp_order, grid_order, batch, cp, gp, cm))
+        return out
+
+    # ---- SH ----
+    def st_forward(self, grids, grid_order: int, exp_order: Optional[int] = None, batch: int = 1,
+                   conv=ST_GEO, layout: int = LAYOUT_LONLAT, out=None):
+        exp_order = grid_order if exp_order is None else exp_order
+        gsz = int(np.prod(st_grid_shape(grid_order, layout))) * batch
+        csz = 2 * st_coeff_size(exp_order) * batch
+        gp, gm = _ptr(grids, gsz)
+        if out is None:
+            out = self._alloc_like(grids, csz)
+        cp, cm = _ptr(out, csz)
+        _check(self.lib.zest_gpu_st_forward(self._h, *conv, layout, grid_order, exp_order, batch, gp, cp, gm))
+        return out
+
+    def st_backward(self, coeffs, exp_order: int, grid_order: Optional[int] = None, batch: int = 1,
+                    conv=ST_GEO, layout: int = LAYOUT_LONLAT, out=None):
+        grid_order = exp_order if grid_order is None else grid_order
+        gsz = int(np.prod(st_grid_shape(grid_order, layout))) * batch
+        csz = 2 * st_coeff_size(exp_order) * batch
+        cp, cm = _ptr(coeffs, csz)
+        if out is None:
+            out = self._alloc_like(coeffs, gsz)
+        gp, gm = _ptr(out, gsz)
+        _check(self.lib.zest_gpu_st_backward(self._h, *conv, layout, exp_order, grid_order, batch, cp, gp, cm))
+        return out
+
+    # ---- rotations (in place) ----
+    def zt_rotate(self, coeffs, order: int, euler, batch: int = 1, rotation_type: int = ROTATION_OBJECT):
+        cp, cm = _ptr(coeffs, 2 * zt_coeff_size(order) * batch)
+        ep, em = _ptr(euler, 3 * batch)
+        _check(self.lib.zest_gpu_zt_rotate(self._h, order, batch, cp, ep, rotation_type, cm))
+        return coeffs
+
+    def st_rotate(self, coeffs, order: int, euler, batch: int = 1, rotation_type: int = ROTATION_OBJECT):
+        cp, cm = _ptr(coeffs, 2 * st_coeff_size(order) * batch)
+        ep, em = _ptr(euler, 3 * batch)
+        _check(self.lib.zest_gpu_st_rotate(self._h, order, batch, cp, ep, rotation_type, cm))
+        return coeffs
+
+    def zt_polar_rotate(self, coeffs, order: int, angles, batch: int = 1, rotation_type: int = ROTATION_OBJECT):
+        cp, cm = _ptr(coeffs, 2 * zt_coeff_size(order) * batch)
+        ap, am = _ptr(angles, batch)
+        _check(self.lib.zest_gpu_zt_polar_rotate(self._h, order, batch, cp, ap, rotation_type, cm))
+        return coeffs
+
+    def st_polar_rotate(self, coeffs, order: int, angles, batch: int = 1, rotation_type: int = ROTATION_OBJECT):
+        cp, cm = _ptr(coeffs, 2 * st_coeff_size(order) * batch)
+        ap, am = _ptr(angles, batch)
+        _check(self.lib.zest_gpu_st_polar_rotate(self._h, order, batch, cp, ap, rotation_type, cm))
+        return coeffs
+
+    # ---- tables ----
+    def plm_table(self, order: int, sh_norm: int, sh_phase: int, z: np.ndarray) -> np.ndarray:
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        out = np.zeros((order * (order + 1) // 2, z.size))
+        _check(self.lib.zest_gpu_plm_table(self._h, order, sh_norm, sh_phase, z.size,
+                                           _vp(z.ctypes.data), _vp(out.ctypes.data), MEM_HOST))
+        return out
+
+    def radial_table(self, order: int, zernike_norm: int, r: np.ndarray) -> np.ndarray:
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        out = np.zeros((((order + 1) * (order + 1)) // 4, r.size))
+        _check(self.lib.zest_gpu_radial_table(self._h, order, zernike_norm, r.size,
+                                              _vp(r.ctypes.data), _vp(out.ctypes.data), MEM_HOST))
+        return out
+
+    def wignerd_table(self, order: int) -> np.ndarray:
+        out = np.zeros(order * (order + 1) * (2 * order + 1) // 6)
+        _check(self.lib.zest_gpu_wignerd_table(self._h, order, _vp(out.ctypes.data), MEM_HOST))
+        return out
+
+    @staticmethod
+    def _alloc_like(x, n):
+        if _is_torch(x):
+            import torch
+            return torch.empty(n, dtype=torch.float64, device=x.device)
+        return np.empty(n, dtype=np.float64)
+
+
+def gl_nodes_weights(n: int, packed: bool = False):
+    sz = (n + 1) // 2 if packed else n
+    x = np.zeros(sz)
+    w = np.zeros(sz)
+    _check(library().zest_gpu_gl_nodes_weights(n, int(packed), _vp(x.ctypes.data), _vp(w.ctypes.data)))
+    return x, w
+
+
+def euler_from_matrix(mat) -> np.ndarray:
+    m = np.ascontiguousarray(mat, dtype=np.float64).reshape(9)
+    e = np.zeros(3)
+    _check(library().zest_gpu_euler_from_matrix(_vp(m.ctypes.data), _vp(e.ctypes.data)))
+    return e

@@ -1,0 +1,163 @@
+// Context and per-order plan structures of the GLQ path, shared by the FP64
+// driver (zest_gpu.cu) and the split-precision driver (split.cu).
+#pragma once
+
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "split.cuh"
+
+namespace zgpu {
+
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    int ensure(size_t n) {
+        if (n <= bytes && p) return ZEST_GPU_OK;
+        release();
+        if (n == 0) n = 16;
+        if (cudaMalloc(&p, n) != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            return fail(ZEST_GPU_ERR_OOM, "device allocation of " + std::to_string(n) + " bytes failed");
+        }
+        bytes = n;
+        return ZEST_GPU_OK;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+template <class T>
+inline int upload(DevBuf& buf, const std::vector<T>& v, cudaStream_t s) {
+    ZG_TRY(buf.ensure(v.size() * sizeof(T)));
+    if (!v.empty()) ZG_CUDA_TRY(cudaMemcpyAsync(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    ZG_CUDA_TRY(cudaStreamSynchronize(s));  // host vector may die after return
+    return ZEST_GPU_OK;
+}
+
+struct FftEntry {
+    FftPlan plan;
+    DevBuf tw;
+};
+
+// Folded Legendre tables (forward: weights * quadrature prefactor folded in;
+// backward: 1/2 for m > 0) with their group offsets.
+struct LegTables {
+    int L = 0, nnodes = 0;  // nnodes = folded node count (ld)
+    int j0u = 0, j0d = 0;
+    DevBuf Pf, Pb, off;
+    std::vector<long long> off_h;
+    std::map<int, std::unique_ptr<DevBuf>> cnt;  // per truncation order Lm
+};
+
+struct RadTables {
+    int L = 0, nr = 0;
+    DevBuf Rf, Rb, off;
+    std::vector<long long> off_h;
+    std::map<int, std::unique_ptr<DevBuf>> cnt;
+};
+
+struct ZtPlan {
+    ZtShape sh{};
+    LegTables leg;
+    RadTables rad;
+    std::vector<double> lat_nodes, lat_w, rad_nodes, rad_w;  // host copies (r = (1+x)/2)
+};
+
+struct StPlan {
+    StShape sh{};
+    LegTables leg;
+};
+
+struct TileEntry {
+    DevBuf buf;
+    int count = 0;
+};
+
+// CUDA-event timing of pipeline stages on the context stream.
+struct Profiler {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>> pending;
+    double ms[ST_COUNT] = {};
+    long long count[ST_COUNT] = {};
+    cudaEvent_t get() {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+    ~Profiler() {
+        for (auto& t : pending) {
+            cudaEventDestroy(std::get<1>(t));
+            cudaEventDestroy(std::get<2>(t));
+        }
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+
+}  // namespace zgpu
+
+using namespace zgpu;
+
+struct zest_gpu_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int precision = ZEST_PRECISION_FP64;
+    int slices = 6;
+    std::map<std::tuple<int, int, int, int>, std::unique_ptr<ZtPlan>> zt_plans;
+    std::map<std::tuple<int, int, int, int>, std::unique_ptr<StPlan>> st_plans;
+    std::map<int, std::unique_ptr<FftEntry>> ffts;
+    std::map<int, std::unique_ptr<DevBuf>> wigner;
+    std::map<std::tuple<int, int>, std::pair<std::unique_ptr<DevBuf>, int>> vec_lists;
+    std::map<std::tuple<int, int, int, int, int>, std::unique_ptr<TileEntry>> tiles;
+    DevBuf s0, s1;          // transform scratch (spectra, flm)
+    DevBuf in_stage, out_stage, aux_stage;  // host <-> device staging
+    DevBuf phase;           // rotation phases
+    std::unique_ptr<SplitState, SplitDeleter> split;
+    Profiler prof;
+};
+
+namespace zgpu {
+// Brackets one pipeline stage with events when profiling is on.
+struct StageScope {
+    zest_gpu_context* ctx;
+    int stage;
+    cudaEvent_t e0 = nullptr;
+    StageScope(zest_gpu_context* c, int st) : ctx(c), stage(st) {
+        if (ctx->prof.on) {
+            e0 = ctx->prof.get();
+            cudaEventRecord(e0, ctx->stream);
+        }
+    }
+    ~StageScope() {
+        if (e0) {
+            cudaEvent_t e1 = ctx->prof.get();
+            cudaEventRecord(e1, ctx->stream);
+            ctx->prof.pending.emplace_back(stage, e0, e1);
+        }
+    }
+};
+}  // namespace zgpu
+
+

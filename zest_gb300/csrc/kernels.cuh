@@ -1,0 +1,73 @@
+// Launchers of the FP64 kernels of the GLQ path (fft.cu, gemm64.cu, rotate.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace zgpu {
+
+// ---- longitude FFT ----------------------------------------------------------
+struct FftPlan {
+    int N = 0;            // transform length
+    int nst = 0;          // number of Stockham stages
+    int radix[24] = {};   // radix of each stage (product = N)
+    const double2* tw = nullptr;  // device table W_t = exp(-2 pi i t / N), t < N
+};
+size_t fft_smem_bytes(int N, int NC);
+// forward: x(b, i, col) at x + b*xb + i*si + col*sc, i < N, col < C
+//          -> F[((b*nm + m)*C + col)*2 + {re,im}] = conj(X_m), m < nm
+int launch_rfft_fwd(cudaStream_t s, const FftPlan& plan, const double* x, long long xb, long long si, long long sc,
+                    int C, int nm, int batch, int lon_fast, double* F);
+// inverse (Hermitian, factor 1): F as above -> x
+int launch_rfft_inv(cudaStream_t s, const FftPlan& plan, const double* F, int C, int nm, int batch, int lon_fast,
+                    double* x, long long xb, long long si, long long sc);
+
+// ---- grouped FP64 contractions ------------------------------------------------
+// Per-call metadata of the folded Legendre / radial stages, all device pointers.
+struct LegMeta {
+    const double* P = nullptr;      // folded Legendre table (rows x ld)
+    const long long* off = nullptr; // row offset of group (m, p) = 2m + p
+    const int* cnt = nullptr;       // rows of group (m, p) with l < Lm
+    int ld = 0;                     // = number of folded nodes Kh
+    int j0u = 0, j0d = 0;           // latitude index of folded node 0, north / south
+};
+struct RadMeta {
+    const double* R = nullptr;      // radial table (rows x nr)
+    const long long* off = nullptr; // row offset of group l
+    const int* cnt = nullptr;       // rows (n = l, l+2, .. < Lm) of group l
+};
+struct TileList {
+    const int4* tiles = nullptr;    // {group, row0, col0, -}
+    int count = 0;
+};
+
+// Zernike (G: [b][m][lat][rad][2], flm: [tri(l,m)][b][rad][2], coeffs: [b][zidx][2])
+int launch_zt_leg_fwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* G, double* flm, int Lg,
+                      int nlat, int nrad, int batch);
+int launch_zt_leg_bwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* flm, double* G, int Lg,
+                      int nlat, int nrad, int batch);
+int launch_zt_rad_fwd(cudaStream_t s, const RadMeta& rm, const TileList& tl, const double* flm, double* coeffs,
+                      int nrad, int batch, long long coeff_stride);
+int launch_zt_rad_bwd(cudaStream_t s, const RadMeta& rm, const TileList& tl, const double* coeffs, double* flm,
+                      int nrad, int batch, long long coeff_stride);
+// SH (X: [b][m][lat][2], coeffs: [b][tri][2])
+int launch_st_leg_fwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* X, double* coeffs,
+                      int Lg, int nlat, int batch, long long coeff_stride);
+int launch_st_leg_bwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* coeffs, double* X,
+                      int Lg, int nlat, int batch, long long coeff_stride);
+// tile shapes (rows x cols per CTA) of the launches above
+void zt_tile_shape(int& bm, int& bn);
+void st_tile_shape(int& bm, int& bn);
+
+// ---- rotations ------------------------------------------------------------------
+// Rotor::rotate on a batch of real expansions (in place).  kind 0 = Zernike,
+// 1 = SH; vec_list holds the nvec rotated (n, l) vectors of one expansion.
+// phase_scratch: 6 * L * batch doubles.
+int launch_rotate_vectors(cudaStream_t s, int kind, int L, int batch, double* coeffs, long long cstride,
+                          const int2* vec_list, int nvec, const double* wigner, const double* euler, int type,
+                          double* phase_scratch);
+int launch_polar_vectors(cudaStream_t s, int kind, int L, int batch, double* coeffs, long long cstride,
+                         const int2* vec_list, int nvec, const double* angles, int type);
+
+}  // namespace zgpu

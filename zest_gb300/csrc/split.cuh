@@ -1,0 +1,23 @@
+// Split-precision (BF16 fixed-point slices on tcgen05) form of the Zernike
+// contractions; see split.cu.
+#pragma once
+
+struct zest_gpu_context;
+
+namespace zgpu {
+
+struct ZtPlan;
+struct SplitState;  // per-context state of the split path, defined in split.cu
+void destroy_split(SplitState* s);
+struct SplitDeleter {
+    void operator()(SplitState* s) const { destroy_split(s); }
+};
+
+// ZEST_GPU_OK when the split path is available on the current device.
+int split_available();
+int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm, int batch, const double* grids,
+                     double* coeffs);
+int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int Lm, int batch, const double* coeffs,
+                      double* grids);
+
+}  // namespace zgpu

@@ -1,0 +1,816 @@
+// C-ABI of the GB300 GLQ transform and rotation path (include/zest_gpu.h).
+//
+// A context owns one device + stream, the per-order tables (generated on the
+// device, FP64), the FFT plans, the tile lists of the grouped contractions and
+// the scratch buffers -- the GPU counterpart of the scratch a reference
+// transformer holds (zernike_glq_transformer.hpp:951-964).  Tables are built
+// once per (order, conventions) and cached, like the reference's resize().
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+#include "context.cuh"
+#include "kernels.cuh"
+#include "split.cuh"
+#include "tables.cuh"
+#include "zest_gpu.h"
+
+namespace zgpu {
+
+static thread_local std::string g_last_error;
+static std::atomic<unsigned long long> g_launches{0};
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int launch_check(const char* what) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ZEST_GPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return ZEST_GPU_OK;
+}
+
+}  // namespace zgpu
+
+using namespace zgpu;
+
+namespace zgpu {
+
+// ---------------------------------------------------------------------------
+static int set_device(zest_gpu_context* ctx) {
+    ZG_CUDA_TRY(cudaSetDevice(ctx->device));
+    return ZEST_GPU_OK;
+}
+
+static void factorize(int N, FftPlan& p) {
+    p.N = N;
+    p.nst = 0;
+    int n = N;
+    while (n % 4 == 0) { p.radix[p.nst++] = 4; n /= 4; }
+    while (n % 2 == 0) { p.radix[p.nst++] = 2; n /= 2; }
+    for (int q = 3; n > 1; q += 2)
+        while (n % q == 0) { p.radix[p.nst++] = q; n /= q; }
+}
+
+static int get_fft(zest_gpu_context* ctx, int N, const FftPlan** out) {
+    auto it = ctx->ffts.find(N);
+    if (it == ctx->ffts.end()) {
+        auto e = std::make_unique<FftEntry>();
+        factorize(N, e->plan);
+        if (e->plan.nst > 24) return fail(ZEST_GPU_ERR_UNSUPPORTED, "FFT length has too many factors");
+        if (fft_smem_bytes(N, 1) > 220 * 1024) return fail(ZEST_GPU_ERR_UNSUPPORTED, "FFT length too large");
+        std::vector<double> tw(2 * (size_t)N);
+        const double pi = 3.14159265358979323846264338327950288;
+        for (int t = 0; t < N; ++t) {
+            // W_t = exp(-2 pi i t/N), evaluated on the reduced angle for accuracy
+            const double ang = 2.0 * pi * double(t) / double(N);
+            tw[2 * t] = std::cos(ang);
+            tw[2 * t + 1] = -std::sin(ang);
+        }
+        ZG_TRY(upload(e->tw, tw, ctx->stream));
+        e->plan.tw = e->tw.as<double2>();
+        it = ctx->ffts.emplace(N, std::move(e)).first;
+    }
+    *out = &it->second->plan;
+    return ZEST_GPU_OK;
+}
+
+// Folded Legendre tables at nodes z (nnodes of them), scale_f per node.
+static int build_leg(zest_gpu_context* ctx, LegTables& t, int L, int sh_norm, int sh_phase,
+                     const std::vector<double>& z, const std::vector<double>& scale_f) {
+    cudaStream_t s = ctx->stream;
+    t.L = L;
+    t.nnodes = int(z.size());
+    t.off_h.assign(2 * (size_t)L + 1, 0);
+    long long rows = 0;
+    for (int m = 0; m < L; ++m)
+        for (int p = 0; p < 2; ++p) {
+            t.off_h[2 * m + p] = rows;
+            const int cnt = (L - m - p > 0) ? (L - m - p + 1) / 2 : 0;
+            rows += cnt;
+        }
+    t.off_h[2 * (size_t)L] = rows;
+    ZG_TRY(upload(t.off, t.off_h, s));
+    const size_t bytes = (size_t)rows * t.nnodes * sizeof(double);
+    ZG_TRY(t.Pf.ensure(bytes));
+    ZG_TRY(t.Pb.ensure(bytes));
+    DevBuf dz, ds;
+    ZG_TRY(upload(dz, z, s));
+    ZG_TRY(upload(ds, scale_f, s));
+    ZG_TRY(launch_plm_gemm(s, L, L, sh_norm, sh_phase, t.nnodes, dz.as<double>(), t.Pf.as<double>(),
+                           t.off.as<long long>(), ds.as<double>(), t.nnodes, 1.0));
+    ZG_TRY(launch_plm_gemm(s, L, L, sh_norm, sh_phase, t.nnodes, dz.as<double>(), t.Pb.as<double>(),
+                           t.off.as<long long>(), nullptr, t.nnodes, 0.5));
+    ZG_CUDA_TRY(cudaStreamSynchronize(s));
+    return ZEST_GPU_OK;
+}
+
+static int leg_cnt(zest_gpu_context* ctx, LegTables& t, int Lm, const int** out) {
+    auto it = t.cnt.find(Lm);
+    if (it == t.cnt.end()) {
+        std::vector<int> c(2 * (size_t)t.L, 0);
+        for (int m = 0; m < t.L; ++m)
+            for (int p = 0; p < 2; ++p) c[2 * m + p] = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
+        auto b = std::make_unique<DevBuf>();
+        ZG_TRY(upload(*b, c, ctx->stream));
+        it = t.cnt.emplace(Lm, std::move(b)).first;
+    }
+    *out = it->second->as<int>();
+    return ZEST_GPU_OK;
+}
+
+static int rad_cnt(zest_gpu_context* ctx, RadTables& t, int Lm, const int** out) {
+    auto it = t.cnt.find(Lm);
+    if (it == t.cnt.end()) {
+        std::vector<int> c((size_t)t.L, 0);
+        for (int l = 0; l < t.L; ++l) c[l] = (Lm - l > 0) ? (Lm - l + 1) / 2 : 0;
+        auto b = std::make_unique<DevBuf>();
+        ZG_TRY(upload(*b, c, ctx->stream));
+        it = t.cnt.emplace(Lm, std::move(b)).first;
+    }
+    *out = it->second->as<int>();
+    return ZEST_GPU_OK;
+}
+
+static int get_zt_plan(zest_gpu_context* ctx, int L, int zn, int sn, int sp, ZtPlan** out) {
+    auto key = std::make_tuple(L, zn, sn, sp);
+    auto it = ctx->zt_plans.find(key);
+    if (it != ctx->zt_plans.end()) {
+        *out = it->second.get();
+        return ZEST_GPU_OK;
+    }
+    auto p = std::make_unique<ZtPlan>();
+    p->sh = zt_shape(L);
+    const int nt = int(p->sh.nlat), nr = int(p->sh.nrad), np = int(p->sh.nlon);
+    p->lat_nodes.resize(nt);
+    p->lat_w.resize(nt);
+    p->rad_nodes.resize(nr);
+    p->rad_w.resize(nr);
+    gl_nodes_weights(nt, false, p->lat_nodes.data(), p->lat_w.data());
+    gl_nodes_weights(nr, false, p->rad_nodes.data(), p->rad_w.data());
+    for (auto& x : p->rad_nodes) x = 0.5 * (1.0 + x);
+    // folded latitude nodes: the non-negative half, ascending from the equator
+    const int kh = (nt + 1) / 2;
+    p->leg.j0u = nt - kh;
+    p->leg.j0d = kh - 1;
+    const double pi = 3.14159265358979323846264338327950288;
+    // quadrature prefactor sh_norm * 1/2 * 2 pi / nlon (zernike_glq_transformer.hpp:710-720)
+    const double shn = sn ? 1.0 : 1.0 / (4.0 * pi);
+    const double pref = shn * 0.5 * ((2.0 * pi) / double(np));
+    std::vector<double> z(kh), sc(kh);
+    for (int j = 0; j < kh; ++j) {
+        z[j] = p->lat_nodes[p->leg.j0u + j];
+        sc[j] = p->lat_w[p->leg.j0u + j] * pref;
+        if (p->leg.j0u + j == p->leg.j0d - j) sc[j] *= 0.5;  // equator node appears in both halves
+    }
+    ZG_TRY(build_leg(ctx, p->leg, L, sn, sp, z, sc));
+    // radial tables: forward R_nl(r_k) r_k^2 u_k (2n+3 if unnormed), backward R_nl(r_k)
+    RadTables& rt = p->rad;
+    rt.L = L;
+    rt.nr = nr;
+    rt.off_h.assign((size_t)L + 1, 0);
+    long long rows = 0;
+    for (int l = 0; l < L; ++l) {
+        rt.off_h[l] = rows;
+        rows += (L - l + 1) / 2;
+    }
+    rt.off_h[L] = rows;
+    ZG_TRY(upload(rt.off, rt.off_h, ctx->stream));
+    ZG_TRY(rt.Rf.ensure((size_t)rows * nr * sizeof(double)));
+    ZG_TRY(rt.Rb.ensure((size_t)rows * nr * sizeof(double)));
+    std::vector<double> rw(nr);
+    for (int k = 0; k < nr; ++k) rw[k] = p->rad_nodes[k] * p->rad_nodes[k] * p->rad_w[k];
+    DevBuf dr, drw;
+    ZG_TRY(upload(dr, p->rad_nodes, ctx->stream));
+    ZG_TRY(upload(drw, rw, ctx->stream));
+    ZG_TRY(launch_radial_gemm(ctx->stream, L, L, zn, nr, dr.as<double>(), rt.Rf.as<double>(), rt.off.as<long long>(),
+                              drw.as<double>(), zn == ZEST_ZERNIKE_UNNORMED));
+    ZG_TRY(launch_radial_gemm(ctx->stream, L, L, zn, nr, dr.as<double>(), rt.Rb.as<double>(), rt.off.as<long long>(),
+                              nullptr, 0));
+    ZG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    *out = p.get();
+    ctx->zt_plans.emplace(key, std::move(p));
+    return ZEST_GPU_OK;
+}
+
+static int get_st_plan(zest_gpu_context* ctx, int L, int sn, int sp, int layout, StPlan** out) {
+    auto key = std::make_tuple(L, sn, sp, layout);
+    auto it = ctx->st_plans.find(key);
+    if (it != ctx->st_plans.end()) {
+        *out = it->second.get();
+        return ZEST_GPU_OK;
+    }
+    auto p = std::make_unique<StPlan>();
+    p->sh = st_shape(L, layout);
+    const int nt = int(p->sh.nlat), np = int(p->sh.nlon);
+    const int nu = (nt + 1) / 2;
+    std::vector<double> pn(nu), pw(nu);
+    gl_nodes_weights(nt, true, pn.data(), pw.data());
+    p->leg.j0u = nt - nu;
+    p->leg.j0d = nu - 1;
+    const double pi = 3.14159265358979323846264338327950288;
+    // prefactor sh_norm * 2 pi / nlon (sh_glq_transformer.hpp:757-765); the
+    // reference folds the middle node of an odd grid twice -- kept as is.
+    const double shn = sn ? 1.0 : 1.0 / (4.0 * pi);
+    const double pref = shn * (2.0 * pi) / double(np);
+    std::vector<double> sc(nu);
+    for (int j = 0; j < nu; ++j) sc[j] = pw[j] * pref;
+    ZG_TRY(build_leg(ctx, p->leg, L, sn, sp, pn, sc));
+    *out = p.get();
+    ctx->st_plans.emplace(key, std::move(p));
+    return ZEST_GPU_OK;
+}
+
+// Tile lists of the grouped contractions, cached per (kind, L, Lm, batch).
+// kinds: 0 zt_leg_fwd, 1 zt_leg_bwd, 2 zt_rad_fwd, 3 zt_rad_bwd, 4 st_leg_fwd, 5 st_leg_bwd
+static int get_tiles(zest_gpu_context* ctx, int kind, int L, int Lm, int batch, int aux, TileList* tl) {
+    auto key = std::make_tuple(kind, L, Lm, batch, aux);
+    auto it = ctx->tiles.find(key);
+    if (it == ctx->tiles.end()) {
+        int bm, bn;
+        if (kind <= 3) zt_tile_shape(bm, bn);
+        else st_tile_shape(bm, bn);
+        std::vector<int4> v;
+        auto add = [&](int g, long long M, long long N) {
+            for (long long r = 0; r < M; r += bm)
+                for (long long c = 0; c < N; c += bn) v.push_back(make_int4(g, int(r), int(c), 0));
+        };
+        const ZtShape zs = zt_shape(L);
+        const long long nr2 = 2 * zs.nrad;
+        switch (kind) {
+        case 0:
+            for (int m = 0; m < Lm; ++m)
+                for (int p = 0; p < 2; ++p) {
+                    const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
+                    if (cnt) add(2 * m + p, cnt, batch * nr2);
+                }
+            break;
+        case 1:
+            for (int m = 0; m < L; ++m) add(m, aux, batch * nr2);  // aux = folded node count
+            break;
+        case 2:
+            for (int l = 0; l < Lm; ++l) add(l, (Lm - l + 1) / 2, (long long)(l + 1) * batch * 2);
+            break;
+        case 3:
+            for (int l = 0; l < Lm; ++l) add(l, zs.nrad, (long long)(l + 1) * batch * 2);
+            break;
+        case 4:
+            for (int m = 0; m < Lm; ++m)
+                for (int p = 0; p < 2; ++p) {
+                    const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
+                    if (cnt) add(2 * m + p, cnt, 2LL * batch);
+                }
+            break;
+        case 5:
+            for (int m = 0; m < L; ++m) add(m, aux, 2LL * batch);
+            break;
+        }
+        if (v.size() > 0x7fffffff) return fail(ZEST_GPU_ERR_UNSUPPORTED, "tile count overflow");
+        auto e = std::make_unique<TileEntry>();
+        e->count = int(v.size());
+        ZG_TRY(upload(e->buf, v, ctx->stream));
+        it = ctx->tiles.emplace(key, std::move(e)).first;
+    }
+    tl->tiles = it->second->buf.as<int4>();
+    tl->count = it->second->count;
+    return ZEST_GPU_OK;
+}
+
+static bool valid01(int x) { return x == 0 || x == 1; }
+
+// ---------------------------------------------------------------------------
+// Zernike transforms on device pointers.
+int zt_forward_dev(zest_gpu_context* ctx, int zn, int sn, int sp, int Lg, int Le, int batch, const double* grids,
+                   double* coeffs) {
+    cudaStream_t s = ctx->stream;
+    const long long csz = 2 * zsize(Le);
+    if (batch == 0 || Le == 0) return ZEST_GPU_OK;
+    ZG_CUDA_TRY(cudaMemsetAsync(coeffs, 0, (size_t)batch * csz * sizeof(double), s));
+    if (Lg == 0) return ZEST_GPU_OK;
+    const int Lm = Lg < Le ? Lg : Le;
+    ZtPlan* plan;
+    ZG_TRY(get_zt_plan(ctx, Lg, zn, sn, sp, &plan));
+    if (ctx->precision == ZEST_PRECISION_SPLIT)
+        return split_zt_forward(ctx, *plan, Lg, Le, Lm, batch, grids, coeffs);
+    const ZtShape& sh = plan->sh;
+    const FftPlan* fft;
+    ZG_TRY(get_fft(ctx, int(sh.nlon), &fft));
+    const long long cols = sh.nlat * sh.nrad;
+    ZG_TRY(ctx->s0.ensure((size_t)batch * Lg * cols * 2 * sizeof(double)));
+    ZG_TRY(ctx->s1.ensure((size_t)tri_size(Lm) * batch * 2 * sh.nrad * sizeof(double)));
+    double* G = ctx->s0.as<double>();
+    double* flm = ctx->s1.as<double>();
+    {
+        StageScope sc(ctx, ST_FFT_FWD);
+        ZG_TRY(launch_rfft_fwd(s, *fft, grids, sh.size(), cols, 1, int(cols), Lg, batch, 0, G));
+    }
+    LegMeta lm;
+    lm.P = plan->leg.Pf.as<double>();
+    lm.off = plan->leg.off.as<long long>();
+    ZG_TRY(leg_cnt(ctx, plan->leg, Lm, &lm.cnt));
+    lm.ld = plan->leg.nnodes;
+    lm.j0u = plan->leg.j0u;
+    lm.j0d = plan->leg.j0d;
+    TileList tl;
+    ZG_TRY(get_tiles(ctx, 0, Lg, Lm, batch, 0, &tl));
+    {
+        StageScope sc(ctx, ST_LEG_FWD);
+        ZG_TRY(launch_zt_leg_fwd(s, lm, tl, G, flm, Lg, int(sh.nlat), int(sh.nrad), batch));
+    }
+    RadMeta rm;
+    rm.R = plan->rad.Rf.as<double>();
+    rm.off = plan->rad.off.as<long long>();
+    ZG_TRY(rad_cnt(ctx, plan->rad, Lm, &rm.cnt));
+    ZG_TRY(get_tiles(ctx, 2, Lg, Lm, batch, 0, &tl));
+    StageScope sc(ctx, ST_RAD_FWD);
+    return launch_zt_rad_fwd(s, rm, tl, flm, coeffs, int(sh.nrad), batch, csz);
+}
+
+int zt_backward_dev(zest_gpu_context* ctx, int zn, int sn, int sp, int Le, int Lg, int batch, const double* coeffs,
+                    double* grids) {
+    cudaStream_t s = ctx->stream;
+    if (batch == 0 || Lg == 0) return ZEST_GPU_OK;
+    const ZtShape shg = zt_shape(Lg);
+    const int Lm = Lg < Le ? Lg : Le;
+    if (Lm == 0) {
+        ZG_CUDA_TRY(cudaMemsetAsync(grids, 0, (size_t)batch * shg.size() * sizeof(double), s));
+        return ZEST_GPU_OK;
+    }
+    const long long csz = 2 * zsize(Le);
+    ZtPlan* plan;
+    ZG_TRY(get_zt_plan(ctx, Lg, zn, sn, sp, &plan));
+    if (ctx->precision == ZEST_PRECISION_SPLIT)
+        return split_zt_backward(ctx, *plan, Le, Lg, Lm, batch, coeffs, grids);
+    const ZtShape& sh = plan->sh;
+    const FftPlan* fft;
+    ZG_TRY(get_fft(ctx, int(sh.nlon), &fft));
+    const long long cols = sh.nlat * sh.nrad;
+    ZG_TRY(ctx->s0.ensure((size_t)batch * Lg * cols * 2 * sizeof(double)));
+    ZG_TRY(ctx->s1.ensure((size_t)tri_size(Lm) * batch * 2 * sh.nrad * sizeof(double)));
+    double* G = ctx->s0.as<double>();
+    double* flm = ctx->s1.as<double>();
+    RadMeta rm;
+    rm.R = plan->rad.Rb.as<double>();
+    rm.off = plan->rad.off.as<long long>();
+    ZG_TRY(rad_cnt(ctx, plan->rad, Lm, &rm.cnt));
+    TileList tl;
+    ZG_TRY(get_tiles(ctx, 3, Lg, Lm, batch, 0, &tl));
+    {
+        StageScope sc(ctx, ST_RAD_BWD);
+        ZG_TRY(launch_zt_rad_bwd(s, rm, tl, coeffs, flm, int(sh.nrad), batch, csz));
+    }
+    LegMeta lm;
+    lm.P = plan->leg.Pb.as<double>();
+    lm.off = plan->leg.off.as<long long>();
+    ZG_TRY(leg_cnt(ctx, plan->leg, Lm, &lm.cnt));
+    lm.ld = plan->leg.nnodes;
+    lm.j0u = plan->leg.j0u;
+    lm.j0d = plan->leg.j0d;
+    ZG_TRY(get_tiles(ctx, 1, Lg, Lm, batch, lm.ld, &tl));
+    {
+        StageScope sc(ctx, ST_LEG_BWD);
+        ZG_TRY(launch_zt_leg_bwd(s, lm, tl, flm, G, Lg, int(sh.nlat), int(sh.nrad), batch));
+    }
+    StageScope sc(ctx, ST_FFT_INV);
+    return launch_rfft_inv(s, *fft, G, int(cols), Lg, batch, 0, grids, sh.size(), cols, 1);
+}
+
+int st_forward_dev(zest_gpu_context* ctx, int sn, int sp, int layout, int Lg, int Le, int batch,
+                   const double* grids, double* coeffs) {
+    cudaStream_t s = ctx->stream;
+    const long long csz = 2 * tri_size(Le);
+    if (batch == 0 || Le == 0) return ZEST_GPU_OK;
+    ZG_CUDA_TRY(cudaMemsetAsync(coeffs, 0, (size_t)batch * csz * sizeof(double), s));
+    if (Lg == 0) return ZEST_GPU_OK;
+    const int Lm = Lg < Le ? Lg : Le;
+    StPlan* plan;
+    ZG_TRY(get_st_plan(ctx, Lg, sn, sp, layout, &plan));
+    const StShape& sh = plan->sh;
+    const FftPlan* fft;
+    ZG_TRY(get_fft(ctx, int(sh.nlon), &fft));
+    ZG_TRY(ctx->s0.ensure((size_t)batch * Lg * sh.nlat * 2 * sizeof(double)));
+    double* X = ctx->s0.as<double>();
+    {
+        StageScope sc(ctx, ST_FFT_FWD);
+        if (layout == ZEST_LAYOUT_LATLON)
+            ZG_TRY(launch_rfft_fwd(s, *fft, grids, sh.size(), 1, sh.nlon, int(sh.nlat), Lg, batch, 1, X));
+        else
+            ZG_TRY(launch_rfft_fwd(s, *fft, grids, sh.size(), sh.nlat, 1, int(sh.nlat), Lg, batch, 0, X));
+    }
+    LegMeta lm;
+    lm.P = plan->leg.Pf.as<double>();
+    lm.off = plan->leg.off.as<long long>();
+    ZG_TRY(leg_cnt(ctx, plan->leg, Lm, &lm.cnt));
+    lm.ld = plan->leg.nnodes;
+    lm.j0u = plan->leg.j0u;
+    lm.j0d = plan->leg.j0d;
+    TileList tl;
+    ZG_TRY(get_tiles(ctx, 4, Lg, Lm, batch, 0, &tl));
+    StageScope sc(ctx, ST_LEG_FWD);
+    return launch_st_leg_fwd(s, lm, tl, X, coeffs, Lg, int(sh.nlat), batch, csz);
+}
+
+int st_backward_dev(zest_gpu_context* ctx, int sn, int sp, int layout, int Le, int Lg, int batch,
+                    const double* coeffs, double* grids) {
+    cudaStream_t s = ctx->stream;
+    if (batch == 0 || Lg == 0) return ZEST_GPU_OK;
+    const StShape shg = st_shape(Lg, layout);
+    const int Lm = Lg < Le ? Lg : Le;
+    if (Lm == 0) {
+        ZG_CUDA_TRY(cudaMemsetAsync(grids, 0, (size_t)batch * shg.size() * sizeof(double), s));
+        return ZEST_GPU_OK;
+    }
+    const long long csz = 2 * tri_size(Le);
+    StPlan* plan;
+    ZG_TRY(get_st_plan(ctx, Lg, sn, sp, layout, &plan));
+    const StShape& sh = plan->sh;
+    const FftPlan* fft;
+    ZG_TRY(get_fft(ctx, int(sh.nlon), &fft));
+    ZG_TRY(ctx->s0.ensure((size_t)batch * Lg * sh.nlat * 2 * sizeof(double)));
+    double* X = ctx->s0.as<double>();
+    LegMeta lm;
+    lm.P = plan->leg.Pb.as<double>();
+    lm.off = plan->leg.off.as<long long>();
+    ZG_TRY(leg_cnt(ctx, plan->leg, Lm, &lm.cnt));
+    lm.ld = plan->leg.nnodes;
+    lm.j0u = plan->leg.j0u;
+    lm.j0d = plan->leg.j0d;
+    TileList tl;
+    ZG_TRY(get_tiles(ctx, 5, Lg, Lm, batch, lm.ld, &tl));
+    {
+        StageScope sc(ctx, ST_LEG_BWD);
+        ZG_TRY(launch_st_leg_bwd(s, lm, tl, coeffs, X, Lg, int(sh.nlat), batch, csz));
+    }
+    StageScope sc(ctx, ST_FFT_INV);
+    if (layout == ZEST_LAYOUT_LATLON)
+        return launch_rfft_inv(s, *fft, X, int(sh.nlat), Lg, batch, 1, grids, sh.size(), 1, sh.nlon);
+    return launch_rfft_inv(s, *fft, X, int(sh.nlat), Lg, batch, 0, grids, sh.size(), sh.nlat, 1);
+}
+
+// ---------------------------------------------------------------------------
+static int get_wigner(zest_gpu_context* ctx, int L, const double** out) {
+    auto it = ctx->wigner.find(L);
+    if (it == ctx->wigner.end()) {
+        auto b = std::make_unique<DevBuf>();
+        ZG_TRY(b->ensure((size_t)wig_off(L) * sizeof(double)));
+        ZG_TRY(launch_wignerd(ctx->stream, L, b->as<double>()));
+        it = ctx->wigner.emplace(L, std::move(b)).first;
+    }
+    *out = it->second->as<double>();
+    return ZEST_GPU_OK;
+}
+
+// rotated (n, l) vectors of one expansion, grouped by l
+static int get_vectors(zest_gpu_context* ctx, int kind, int L, const int2** out, int* nvec) {
+    auto key = std::make_tuple(kind, L);
+    auto it = ctx->vec_lists.find(key);
+    if (it == ctx->vec_lists.end()) {
+        std::vector<int2> v;
+        for (int l = 0; l < L; ++l) {
+            if (kind == 0) {
+                for (int n = (l == 0 ? 2 : l); n < L; n += 2) v.push_back(make_int2(n, l));
+            } else if (l >= 1) {
+                v.push_back(make_int2(l, l));
+            }
+        }
+        auto b = std::make_unique<DevBuf>();
+        ZG_TRY(upload(*b, v, ctx->stream));
+        it = ctx->vec_lists.emplace(key, std::make_pair(std::move(b), int(v.size()))).first;
+    }
+    *out = it->second.first->as<int2>();
+    *nvec = it->second.second;
+    return ZEST_GPU_OK;
+}
+
+int rotate_dev(zest_gpu_context* ctx, int kind, int L, int batch, double* coeffs, const double* euler, int type) {
+    if (batch == 0 || L <= 1) return ZEST_GPU_OK;
+    const double* wig;
+    ZG_TRY(get_wigner(ctx, L, &wig));
+    const int2* vl;
+    int nvec;
+    ZG_TRY(get_vectors(ctx, kind, L, &vl, &nvec));
+    ZG_TRY(ctx->phase.ensure((size_t)batch * 6 * L * sizeof(double)));
+    const long long cstride = kind == 0 ? 2 * zsize(L) : 2 * tri_size(L);
+    StageScope sc(ctx, ST_ROTATE);
+    return launch_rotate_vectors(ctx->stream, kind, L, batch, coeffs, cstride, vl, nvec, wig, euler, type,
+                                 ctx->phase.as<double>());
+}
+
+int polar_dev(zest_gpu_context* ctx, int kind, int L, int batch, double* coeffs, const double* angles, int type) {
+    if (batch == 0 || L <= 1) return ZEST_GPU_OK;
+    const int2* vl;
+    int nvec;
+    ZG_TRY(get_vectors(ctx, kind, L, &vl, &nvec));
+    const long long cstride = kind == 0 ? 2 * zsize(L) : 2 * tri_size(L);
+    StageScope sc(ctx, ST_ROTATE);
+    return launch_polar_vectors(ctx->stream, kind, L, batch, coeffs, cstride, vl, nvec, angles, type);
+}
+
+}  // namespace zgpu
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+namespace {
+
+constexpr size_t kMaxOrder = 4096;
+
+int check_ctx(zest_gpu_context* ctx) {
+    if (!ctx) return fail(ZEST_GPU_ERR_INVALID, "null context");
+    return set_device(ctx);
+}
+
+// Runs `body(in_dev, out_dev)` on device pointers, staging host buffers.
+template <class F>
+int with_staging(zest_gpu_context* ctx, int mem, const double* in, size_t in_n, double* out, size_t out_n, F&& body) {
+    if (mem == ZEST_MEM_DEVICE) return body(in, out);
+    if (mem != ZEST_MEM_HOST) return fail(ZEST_GPU_ERR_INVALID, "mem must be ZEST_MEM_HOST or ZEST_MEM_DEVICE");
+    cudaStream_t s = ctx->stream;
+    ZG_TRY(ctx->in_stage.ensure(in_n * sizeof(double)));
+    ZG_TRY(ctx->out_stage.ensure(out_n * sizeof(double)));
+    if (in_n) {
+        StageScope sc(ctx, ST_COPY_H2D);
+        ZG_CUDA_TRY(cudaMemcpyAsync(ctx->in_stage.p, in, in_n * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    ZG_TRY(body(ctx->in_stage.as<double>(), ctx->out_stage.as<double>()));
+    if (out_n) {
+        StageScope sc(ctx, ST_COPY_D2H);
+        ZG_CUDA_TRY(cudaMemcpyAsync(out, ctx->out_stage.p, out_n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    ZG_CUDA_TRY(cudaStreamSynchronize(s));
+    return ZEST_GPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int zest_gpu_ctx_create(zest_gpu_context** out, int device, void* stream) {
+    if (!out) return fail(ZEST_GPU_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(ZEST_GPU_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= n) return fail(ZEST_GPU_ERR_INVALID, "device index out of range");
+    ZG_CUDA_TRY(cudaSetDevice(device));
+    int major = 0, minor = 0;
+    ZG_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device));
+    ZG_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device));
+    if (major != 10 || minor != 3)
+        return fail(ZEST_GPU_ERR_UNSUPPORTED, "this library is built for sm_103a (GB300) only; device is sm_" +
+                                                  std::to_string(major) + std::to_string(minor));
+    auto* ctx = new zest_gpu_context();
+    ctx->device = device;
+    ctx->stream = static_cast<cudaStream_t>(stream);
+    *out = ctx;
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_ctx_destroy(zest_gpu_context* ctx) {
+    if (!ctx) return ZEST_GPU_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete ctx;
+    return ZEST_GPU_OK;
+}
+
+const char* zest_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int zest_gpu_set_precision(zest_gpu_context* ctx, int precision, int slices) {
+    ZG_TRY(check_ctx(ctx));
+    if (precision != ZEST_PRECISION_FP64 && precision != ZEST_PRECISION_SPLIT)
+        return fail(ZEST_GPU_ERR_INVALID, "unknown precision");
+    if (slices == 0) slices = 6;
+    if (slices < 4 || slices > 8) return fail(ZEST_GPU_ERR_INVALID, "slices must be in 4..8");
+    if (precision == ZEST_PRECISION_SPLIT) ZG_TRY(split_available());
+    ctx->precision = precision;
+    ctx->slices = slices;
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_synchronize(zest_gpu_context* ctx) {
+    ZG_TRY(check_ctx(ctx));
+    ZG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_trim(zest_gpu_context* ctx) {
+    ZG_TRY(check_ctx(ctx));
+    ZG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ctx->zt_plans.clear();
+    ctx->st_plans.clear();
+    ctx->ffts.clear();
+    ctx->wigner.clear();
+    ctx->vec_lists.clear();
+    ctx->tiles.clear();
+    ctx->s0.release();
+    ctx->s1.release();
+    ctx->in_stage.release();
+    ctx->out_stage.release();
+    ctx->aux_stage.release();
+    ctx->phase.release();
+    ctx->split.reset();
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_profile_enable(zest_gpu_context* ctx, int enable) {
+    ZG_TRY(check_ctx(ctx));
+    ctx->prof.on = enable != 0;
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_profile_read(zest_gpu_context* ctx, int reset, double* ms, long long* count, int n) {
+    ZG_TRY(check_ctx(ctx));
+    ZG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    Profiler& p = ctx->prof;
+    for (auto& t : p.pending) {
+        float el = 0.f;
+        ZG_CUDA_TRY(cudaEventElapsedTime(&el, std::get<1>(t), std::get<2>(t)));
+        p.ms[std::get<0>(t)] += el;
+        p.count[std::get<0>(t)] += 1;
+        p.pool.push_back(std::get<1>(t));
+        p.pool.push_back(std::get<2>(t));
+    }
+    p.pending.clear();
+    for (int i = 0; i < n && i < ST_COUNT; ++i) {
+        if (ms) ms[i] = p.ms[i];
+        if (count) count[i] = p.count[i];
+    }
+    if (reset)
+        for (int i = 0; i < ST_COUNT; ++i) {
+            p.ms[i] = 0.0;
+            p.count[i] = 0;
+        }
+    return ZEST_GPU_OK;
+}
+
+const char* zest_gpu_profile_stage_name(int stage) { return stage_name(stage); }
+int zest_gpu_profile_stage_count(void) { return ST_COUNT; }
+unsigned long long zest_gpu_launch_count(void) { return g_launches.load(); }
+
+size_t zest_gpu_zt_grid_size(size_t order) { return (size_t)zt_shape((long long)order).size(); }
+size_t zest_gpu_zt_coeff_size(size_t order) { return (size_t)zsize((long long)order); }
+size_t zest_gpu_st_grid_size(size_t order, int layout) {
+    return (size_t)st_shape((long long)order, layout == ZEST_LAYOUT_LATLON).size();
+}
+size_t zest_gpu_st_coeff_size(size_t order) { return (size_t)tri_size((long long)order); }
+
+int zest_gpu_zt_forward(zest_gpu_context* ctx, int zn, int sn, int sp, size_t grid_order, size_t exp_order,
+                        size_t batch, const double* grids, double* coeffs, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(zn) || !valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (grid_order > kMaxOrder || exp_order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t gn = batch * zest_gpu_zt_grid_size(grid_order), cn = batch * 2 * zest_gpu_zt_coeff_size(exp_order);
+    if ((gn && !grids) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, grids, gn, coeffs, cn, [&](const double* in, double* out) {
+        return zt_forward_dev(ctx, zn, sn, sp, int(grid_order), int(exp_order), int(batch), in, out);
+    });
+}
+
+int zest_gpu_zt_backward(zest_gpu_context* ctx, int zn, int sn, int sp, size_t exp_order, size_t grid_order,
+                         size_t batch, const double* coeffs, double* grids, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(zn) || !valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (grid_order > kMaxOrder || exp_order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t gn = batch * zest_gpu_zt_grid_size(grid_order), cn = batch * 2 * zest_gpu_zt_coeff_size(exp_order);
+    if ((gn && !grids) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, coeffs, cn, grids, gn, [&](const double* in, double* out) {
+        return zt_backward_dev(ctx, zn, sn, sp, int(exp_order), int(grid_order), int(batch), in, out);
+    });
+}
+
+int zest_gpu_st_forward(zest_gpu_context* ctx, int sn, int sp, int layout, size_t grid_order, size_t exp_order,
+                        size_t batch, const double* grids, double* coeffs, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn) || !valid01(sp) || !valid01(layout)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention/layout");
+    if (grid_order > kMaxOrder || exp_order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t gn = batch * zest_gpu_st_grid_size(grid_order, layout), cn = batch * 2 * zest_gpu_st_coeff_size(exp_order);
+    if ((gn && !grids) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, grids, gn, coeffs, cn, [&](const double* in, double* out) {
+        return st_forward_dev(ctx, sn, sp, layout, int(grid_order), int(exp_order), int(batch), in, out);
+    });
+}
+
+int zest_gpu_st_backward(zest_gpu_context* ctx, int sn, int sp, int layout, size_t exp_order, size_t grid_order,
+                         size_t batch, const double* coeffs, double* grids, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn) || !valid01(sp) || !valid01(layout)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention/layout");
+    if (grid_order > kMaxOrder || exp_order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t gn = batch * zest_gpu_st_grid_size(grid_order, layout), cn = batch * 2 * zest_gpu_st_coeff_size(exp_order);
+    if ((gn && !grids) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, coeffs, cn, grids, gn, [&](const double* in, double* out) {
+        return st_backward_dev(ctx, sn, sp, layout, int(exp_order), int(grid_order), int(batch), in, out);
+    });
+}
+
+static int rotate_common(zest_gpu_context* ctx, int kind, size_t order, size_t batch, double* coeffs,
+                         const double* angles, int nang, int type, int mem, bool polar) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(type)) return fail(ZEST_GPU_ERR_INVALID, "invalid rotation type");
+    if (order > 2048) return fail(ZEST_GPU_ERR_INVALID, "rotation order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t cn = batch * 2 * (kind == 0 ? zest_gpu_zt_coeff_size(order) : zest_gpu_st_coeff_size(order));
+    const size_t an = batch * nang;
+    if ((cn && !coeffs) || (an && !angles)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    auto run = [&](double* c, const double* a) {
+        return polar ? polar_dev(ctx, kind, int(order), int(batch), c, a, type)
+                     : rotate_dev(ctx, kind, int(order), int(batch), c, a, type);
+    };
+    if (mem == ZEST_MEM_DEVICE) return run(coeffs, angles);
+    if (mem != ZEST_MEM_HOST) return fail(ZEST_GPU_ERR_INVALID, "mem must be ZEST_MEM_HOST or ZEST_MEM_DEVICE");
+    cudaStream_t s = ctx->stream;
+    ZG_TRY(ctx->in_stage.ensure(cn * sizeof(double)));
+    ZG_TRY(ctx->aux_stage.ensure(an * sizeof(double)));
+    if (cn) ZG_CUDA_TRY(cudaMemcpyAsync(ctx->in_stage.p, coeffs, cn * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (an) ZG_CUDA_TRY(cudaMemcpyAsync(ctx->aux_stage.p, angles, an * sizeof(double), cudaMemcpyHostToDevice, s));
+    ZG_TRY(run(ctx->in_stage.as<double>(), ctx->aux_stage.as<double>()));
+    if (cn) ZG_CUDA_TRY(cudaMemcpyAsync(coeffs, ctx->in_stage.p, cn * sizeof(double), cudaMemcpyDeviceToHost, s));
+    ZG_CUDA_TRY(cudaStreamSynchronize(s));
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_zt_rotate(zest_gpu_context* ctx, size_t order, size_t batch, double* coeffs, const double* euler,
+                       int rotation_type, int mem) {
+    return rotate_common(ctx, 0, order, batch, coeffs, euler, 3, rotation_type, mem, false);
+}
+int zest_gpu_st_rotate(zest_gpu_context* ctx, size_t order, size_t batch, double* coeffs, const double* euler,
+                       int rotation_type, int mem) {
+    return rotate_common(ctx, 1, order, batch, coeffs, euler, 3, rotation_type, mem, false);
+}
+int zest_gpu_zt_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch, double* coeffs, const double* angles,
+                             int rotation_type, int mem) {
+    return rotate_common(ctx, 0, order, batch, coeffs, angles, 1, rotation_type, mem, true);
+}
+int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch, double* coeffs, const double* angles,
+                             int rotation_type, int mem) {
+    return rotate_common(ctx, 1, order, batch, coeffs, angles, 1, rotation_type, mem, true);
+}
+
+int zest_gpu_euler_from_matrix(const double* r, double* e) {
+    if (!r || !e) return fail(ZEST_GPU_ERR_INVALID, "null pointer");
+    // euler_angles_from_rotation_matrix, include/rotor.hpp:53-63 (as written there)
+    const double r22sq = r[8] * r[8];
+    const double by = std::sqrt((1.0 + r22sq) * (1.0 - r22sq));
+    e[0] = std::atan2(r[5], r[2]);
+    e[1] = std::atan2(by, r[8]);
+    e[2] = std::atan2(r[7], -r[6]);
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_gl_nodes_weights(size_t n, int packed, double* nodes, double* weights) {
+    if (n > (1u << 20)) return fail(ZEST_GPU_ERR_INVALID, "too many nodes");
+    if (n && (!nodes || !weights)) return fail(ZEST_GPU_ERR_INVALID, "null pointer");
+    gl_nodes_weights(long(n), packed != 0, nodes, weights);
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_plm_table(zest_gpu_context* ctx, size_t order, int sn, int sp, size_t nz, const double* z, double* out,
+                       int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (order > kMaxOrder || nz > (1u << 20)) return fail(ZEST_GPU_ERR_INVALID, "size too large");
+    const size_t on = (size_t)tri_size((long long)order) * nz;
+    if ((nz && !z) || (on && !out)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, z, nz, out, on, [&](const double* zi, double* o) {
+        return launch_plm_ref(ctx->stream, int(order), sn, sp, int(nz), zi, o);
+    });
+}
+
+int zest_gpu_radial_table(zest_gpu_context* ctx, size_t order, int zn, size_t nr, const double* r, double* out,
+                          int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(zn)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (order > kMaxOrder || nr > (1u << 20)) return fail(ZEST_GPU_ERR_INVALID, "size too large");
+    const size_t on = (size_t)((((long long)order + 1) * ((long long)order + 1)) >> 2) * nr;
+    if ((nr && !r) || (on && !out)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, r, nr, out, on, [&](const double* ri, double* o) {
+        return launch_radial_ref(ctx->stream, int(order), zn, int(nr), ri, o);
+    });
+}
+
+int zest_gpu_wignerd_table(zest_gpu_context* ctx, size_t order, double* out, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (order > 2048) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    const size_t on = (size_t)wig_off((long long)order);
+    if (on && !out) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, nullptr, 0, out, on, [&](const double*, double* o) {
+        return launch_wignerd(ctx->stream, int(order), o);
+    });
+}
+
+}  // extern "C"
