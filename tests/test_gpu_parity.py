@@ -26,7 +26,8 @@ def relmax(a, b):
 @pytest.fixture(scope="module")
 def ctx():
     import zest_gb300
-    zest_gb300.build.build()
+    from zest_gb300 import build
+    build.build()
     c = zest_gb300.Context(0)
     yield c
     c.close()
