@@ -148,6 +148,14 @@ int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
 /* euler_angles_from_rotation_matrix, rotor.hpp:53-63 (row-major 3x3, host). */
 int zest_gpu_euler_from_matrix(const double* matrix, double* euler);
 
+/* ---- split-precision dense product (no reference counterpart) ----
+ * C = A B^T for row-major FP64 A (M x K) and B (N x K), K <= 256, evaluated
+ * with the context's slice count on the tcgen05 path used by
+ * ZEST_PRECISION_SPLIT (BF16 fixed-point slices, exact FP32 partial sums,
+ * FP64 recombination).  Exposed to test and measure the emulation itself. */
+int zest_gpu_split_gemm(zest_gpu_context* ctx, size_t M, size_t N, size_t K, const double* A, const double* B,
+                        double* C, int mem);
+
 /* ---- tables (device generated, FP64) ----
  * gl::gl_nodes_and_weights<Layout, GLNodeStyle::cos>, gauss_legendre.hpp:1549-1565
  *   (host solve; packed = 1 for PackedLayout).  */

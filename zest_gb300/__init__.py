@@ -90,6 +90,7 @@ _SIGNATURES = {
     "zest_gpu_profile_enable": [_vp, _i],
     "zest_gpu_profile_read": [_vp, _i, _vp, _vp, _i],
     "zest_gpu_profile_stage_count": [],
+    "zest_gpu_split_gemm": [_vp, _sz, _sz, _sz, _vp, _vp, _vp, _i],
 }
 _SIZE_FUNCS = {
     "zest_gpu_zt_grid_size": [_sz],
@@ -298,6 +299,19 @@ class Context:
         ap, am = _ptr(angles, batch)
         _check(self.lib.zest_gpu_st_polar_rotate(self._h, order, batch, cp, ap, rotation_type, cm))
         return coeffs
+
+    def split_gemm(self, A: np.ndarray, B: np.ndarray) -> np.ndarray:
+        """C = A B^T through the split-precision tensor-core path (host arrays)."""
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        M, K = A.shape
+        N, K2 = B.shape
+        if K != K2:
+            raise ValueError("inner dimensions differ")
+        C = np.zeros((M, N))
+        _check(self.lib.zest_gpu_split_gemm(self._h, M, N, K, _vp(A.ctypes.data), _vp(B.ctypes.data),
+                                            _vp(C.ctypes.data), MEM_HOST))
+        return C
 
     # ---- tables ----
     def plm_table(self, order: int, sh_norm: int, sh_phase: int, z: np.ndarray) -> np.ndarray:

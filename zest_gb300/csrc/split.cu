@@ -1,21 +1,1144 @@
-// Split-precision form of the Zernike contractions (placeholder until the
-// tcgen05 kernels land: reports "unsupported", never falls back).
+// Split-precision form of the Zernike GLQ transforms on tcgen05 tensor cores.
+//
+// Every dense contraction of the path -- the longitude DFT (as a matrix
+// product with the cos/sin table, folded over x_i +- x_{N-i}), the folded
+// Legendre sums and the radial sums -- is evaluated as
+//     C[r, n] = sum_k A[r, k] B[n, k]
+// with FP64 operands represented exactly enough in BF16 fixed-point slices:
+//   * each operand row gets an exponent e (|x| < 2^e over the row) and its
+//     values are rounded to v = round(x 2^{7S - e}), |v| <= 2^{7S};
+//   * v is cut into S signed base-128 digits d_s (|d_s| <= 128), each exact
+//     in BF16: x = 2^{e - 7S} sum_s d_s 128^{S-1-s};
+//   * the products d_s(A) d_t(B) with s + t = level <= S-1 accumulate in one
+//     FP32 TMEM accumulator per level.  Products are integers <= 2^14, so a
+//     level with (level+1) products is exact while (level+1) K 2^14 <= 2^24:
+//     levels 0..3 are exact for K <= 256; the rounding of deeper levels is
+//     below 2^-45 relative to the result;
+//   * the epilogue recombines the levels by integer Horner in int64
+//     (T = sum_level 128^{S-1-level} acc_level) and builds the FP64 result
+//     2^{eA + eB - 7S - 7} T with integer operations only.
+// Only the tables (P_lm, R_nl, cos/sin) are prepared in FP64; the FFT,
+// Legendre and radial arithmetic of the forward and backward transforms runs
+// on the tensor cores.  S = 6 keeps 42 bits per operand and 21 products.
+//
+// Kernel: warp-specialised, persistent, one CTA per SM.  Warp 0 issues TMA
+// loads (SWIZZLE_32B, one 16-wide K block of all S slices of A and B per
+// pipeline stage), warp 1 issues tcgen05.mma (M = 128 operand rows,
+// N = table rows per tile, all S level accumulators resident in TMEM), warps
+// 2..9 read the accumulators back (tcgen05.ld), recombine and store through a
+// stage-specific epilogue.  Every wait is bounded (about 2 s); on timeout the
+// kernel records an error code and winds down instead of hanging.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 #include "common.cuh"
 #include "context.cuh"
 #include "split.cuh"
 
 namespace zgpu {
 
-struct SplitState {};
+// ===========================================================================
+// Device helpers (inline PTX)
+// ===========================================================================
+namespace {
+
+constexpr int SP_THREADS = 320;  // 10 warps
+constexpr int SP_STAGES = 4;
+constexpr int SP_M = 128;
+constexpr int SP_KB = 16;        // K elements per pipeline stage (32 bytes of bf16)
+constexpr long long SP_TIMEOUT_NS = 2000000000LL;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ unsigned long long gtime() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\t"
+        "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
+        "r"(bytes)
+        : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile(
+        "{\n\t.reg .b64 st;\n\t"
+        "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait on an mbarrier phase; false (and the error flag set) on timeout
+// or when another role already gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = gtime();
+    for (unsigned it = 1;; ++it) {
+        if (mbar_try(bar, parity)) return true;
+        if ((it & 255) == 0) {
+            if (*(volatile int*)err) return false;
+            if (gtime() - t0 > (unsigned long long)SP_TIMEOUT_NS) {
+                atomicCAS(err, 0, code);
+                return false;
+            }
+        }
+    }
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void umma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// K-major operand tile, SWIZZLE_32B: rows of 32 bytes, 8-row groups 256 bytes apart.
+__device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+    d |= (uint64_t)(16u >> 4) << 16;           // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(256u >> 4) << 32;          // stride byte offset: 8 rows x 32 B
+    d |= (uint64_t)1 << 46;                    // descriptor version for tcgen05
+    d |= (uint64_t)6 << 61;                    // SWIZZLE_32B
+    return d;
+}
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+    return (1u << 4)                       // D format F32
+           | (1u << 7)                     // A format BF16
+           | (1u << 10)                    // B format BF16
+           | ((uint32_t)(N >> 3) << 17)    // N / 8
+           | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+
+// 2^E * T for an integer T with |T| < 2^63, assembled with integer operations
+// (round to nearest even to 53 bits; results below the normal range flush to 0).
+__device__ __forceinline__ double i64_ldexp(long long T, int E) {
+    if (T == 0) return 0.0;
+    const unsigned long long sgn = T < 0 ? (1ull << 63) : 0ull;
+    unsigned long long a = T < 0 ? (unsigned long long)(-T) : (unsigned long long)T;
+    int lz = __clzll((long long)a);
+    unsigned long long n = a << lz;
+    unsigned long long mant = n >> 11;
+    const unsigned long long rest = n & 0x7FFull;
+    if (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) {
+        ++mant;
+        if (mant >> 53) {
+            mant >>= 1;
+            --lz;
+        }
+    }
+    const int biased = (63 - lz) + E + 1023;
+    if (biased <= 0) return 0.0;
+    if (biased >= 2047) return __longlong_as_double((long long)(sgn | 0x7FF0000000000000ull));
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)biased << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+// fixed point: round(x 2^{7S-e}) as int64 (|x| < 2^e)
+__device__ __forceinline__ long long to_fixed(double x, int e, int S) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int E = int((bits >> 52) & 0x7FF);
+    if (E == 0) return 0;  // zero and subnormals
+    const unsigned long long M = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = 1075 + e - 7 * S - E;
+    long long v;
+    if (sh >= 63) v = 0;
+    else if (sh > 0) v = (long long)((M + (1ull << (sh - 1))) >> sh);
+    else v = (long long)(M << (-sh));
+    return (bits >> 63) ? -v : v;
+}
+
+__device__ __forceinline__ int biased_exp(double x) {
+    return int(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
+}  // namespace
+
+// ===========================================================================
+// Slicing kernel: FP64 operand rows -> S BF16 digit slices + row exponents
+// ===========================================================================
+namespace {
+
+constexpr int SL_ROWS = 16;
+constexpr int SL_KMAX = 256;
+
+// Loaders return the pair (up, dn) of operand element (row, k); the folded
+// operands are fix(up) + fix(dn) (fold = 1) or fix(up) - fix(dn) (fold = 2),
+// computed exactly in integers at the row's scale.
+struct RowMajorLoader {  // tables and dense operands: p[r*ld + k]
+    static constexpr bool ROW_FAST = false;
+    const double* p;
+    long long ld;
+    __device__ void get(long long r, int k, double& up, double& dn) const {
+        up = p[r * ld + k];
+        dn = 0.0;
+    }
+};
+
+struct DftFwdLoader {  // rows (b, col) of the ball grid; cos: x_k (+ x_{N-k}); sin: x_{k+1} - x_{N-k-1}
+    static constexpr bool ROW_FAST = true;
+    const double* grid;
+    long long gsz;
+    int C, N, sin;
+    __device__ void get(long long r, int k, double& up, double& dn) const {
+        const long long b = r / C, col = r - b * C;
+        const double* x = grid + b * gsz + col;
+        if (sin) {
+            const int i = k + 1;
+            up = x[(long long)i * C];
+            dn = x[(long long)(N - i) * C];
+        } else if (k == 0) {
+            up = x[0];
+            dn = 0.0;
+        } else {
+            up = x[(long long)k * C];
+            dn = x[(long long)(N - k) * C];
+        }
+    }
+};
+
+struct LegFwdLoader {  // rows (m, b, kc); K = folded latitude node
+    static constexpr bool ROW_FAST = true;
+    const double* G;
+    int B, L, Nt, nr2, j0u, j0d;
+    __device__ void get(long long r, int k, double& up, double& dn) const {
+        const long long mb = r / nr2;
+        const int kc = int(r - mb * nr2);
+        const int m = int(mb / B), b = int(mb - (long long)m * B);
+        const double* base = G + ((long long)b * L + m) * Nt * nr2 + kc;
+        up = base[(long long)(j0u + k) * nr2];
+        dn = base[(long long)(j0d - k) * nr2];
+    }
+};
+
+struct RadFwdLoader {  // rows ((t B + b) 2 + c); K = radial node
+    static constexpr bool ROW_FAST = false;
+    const double* flm;
+    int nr;
+    __device__ void get(long long r, int k, double& up, double& dn) const {
+        up = flm[((r >> 1) * nr + k) * 2 + (r & 1)];
+        dn = 0.0;
+    }
+};
+
+struct RadBwdLoader {  // rows ((tri(l,m) B + b) 2 + c); K = i, n = l + 2i
+    static constexpr bool ROW_FAST = false;
+    const double* coeffs;
+    long long cs;
+    int B, Lm;
+    __device__ void get(long long r, int k, double& up, double& dn) const {
+        const long long tb = r >> 1;
+        const int c = int(r & 1);
+        const long long t = tb / B;
+        const int b = int(tb - t * B);
+        int l = int((sqrtf(8.0f * float(t) + 1.0f) - 1.0f) * 0.5f);
+        while ((long long)(l + 1) * (l + 2) / 2 <= t) ++l;
+        while ((long long)l * (l + 1) / 2 > t) --l;
+        const int m = int(t - (long long)l * (l + 1) / 2);
+        const int n = l + 2 * k;
+        up = (n < Lm) ? coeffs[b * cs + zidx(n, l, m) * 2 + c] : 0.0;
+        dn = 0.0;
+    }
+};
+
+struct LegBwdLoader {  // rows (m, b, kc); K = i, l = m + p + 2i
+    static constexpr bool ROW_FAST = true;
+    const double* flm;
+    int B, nr2, p, Lm;
+    __device__ void get(long long r, int k, double& up, double& dn) const {
+        const long long mb = r / nr2;
+        const int kc = int(r - mb * nr2);
+        const int m = int(mb / B), b = int(mb - (long long)m * B);
+        const int l = m + p + 2 * k;
+        up = (l < Lm) ? flm[(tri_idx(l, m) * B + b) * nr2 + kc] : 0.0;
+        dn = 0.0;
+    }
+};
+
+struct DftBwdLoader {  // rows (b, col); cos: Re F_m; sin: Im F_{k+1}
+    static constexpr bool ROW_FAST = true;
+    const double* G;
+    int B, L, C, sin;
+    __device__ void get(long long r, int k, double& up, double& dn) const {
+        const long long b = r / C, col = r - b * C;
+        const int m = sin ? k + 1 : k;
+        up = G[((b * L + m) * C + col) * 2 + sin];
+        dn = 0.0;
+    }
+};
+
+template <class Loader>
+__global__ void __launch_bounds__(256) slice_kernel(Loader ld, long long rows, int K, int Kp, int S, int fold,
+                                                    __nv_bfloat16* __restrict__ out, long long slice_stride,
+                                                    int* __restrict__ ex) {
+    __shared__ double vu[SL_ROWS][SL_KMAX];
+    __shared__ double vd[SL_ROWS][SL_KMAX];
+    __shared__ int emax[SL_ROWS];
+    const long long row0 = (long long)blockIdx.x * SL_ROWS;
+    if (threadIdx.x < SL_ROWS) emax[threadIdx.x] = 0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < SL_ROWS * K; e += blockDim.x) {
+        int r, k;
+        if (Loader::ROW_FAST) { r = e % SL_ROWS; k = e / SL_ROWS; }
+        else { k = e % K; r = e / K; }
+        double up = 0.0, dn = 0.0;
+        if (row0 + r < rows) ld.get(row0 + r, k, up, dn);
+        vu[r][k] = up;
+        vd[r][k] = dn;
+        const int ee = max(biased_exp(up), biased_exp(dn));
+        if (ee) atomicMax(&emax[r], ee);
+    }
+    __syncthreads();
+    const int hk = Kp >> 1;  // pairs of k per row
+    for (int e = threadIdx.x; e < SL_ROWS * hk; e += blockDim.x) {
+        const int r = e / hk, k = (e - r * hk) * 2;
+        const long long row = row0 + r;
+        if (row >= rows) continue;
+        const int er = emax[r] - 1022 + (fold ? 1 : 0);
+        long long v[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int kk = k + q;
+            long long x = 0;
+            if (kk < K) {
+                x = to_fixed(vu[r][kk], er, S);
+                if (fold == 1) x += to_fixed(vd[r][kk], er, S);
+                else if (fold == 2) x -= to_fixed(vd[r][kk], er, S);
+            }
+            v[q] = x;
+        }
+        const unsigned long long a0 = v[0] < 0 ? (unsigned long long)(-v[0]) : (unsigned long long)v[0];
+        const unsigned long long a1 = v[1] < 0 ? (unsigned long long)(-v[1]) : (unsigned long long)v[1];
+        for (int s = 0; s < S; ++s) {
+            const int shift = 7 * (S - 1 - s);
+            int d0 = int(s == 0 ? (a0 >> shift) : ((a0 >> shift) & 127ull));
+            int d1 = int(s == 0 ? (a1 >> shift) : ((a1 >> shift) & 127ull));
+            if (v[0] < 0) d0 = -d0;
+            if (v[1] < 0) d1 = -d1;
+            __nv_bfloat162 pr;
+            pr.x = __float2bfloat16_rn(float(d0));
+            pr.y = __float2bfloat16_rn(float(d1));
+            *reinterpret_cast<__nv_bfloat162*>(out + s * slice_stride + row * Kp + k) = pr;
+        }
+        if (k == 0) ex[row] = er;
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+// GEMM kernel
+// ===========================================================================
+struct SplitUnit {
+    int a_row0;   // first operand row of the tile (row index inside the slice array)
+    int a_rows;   // valid rows (<= 128)
+    int b_row0;   // first table row
+    int n;        // valid table rows (<= NT)
+    int ksteps;   // 16-wide K blocks
+    int flags;    // bit 0: A map, bit 1: B map, bit 2: parity / RMW
+    int g;        // group (m or l)
+    int aux;      // group-relative index of the first table row
+};
+
+namespace {
+
+struct EpiDense {  // C[row][b_row0 + n] (debug / utility GEMM)
+    double* C;
+    long long ldc;
+    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
+        C[(long long)row * ldc + u.b_row0 + n] = v;
+    }
+};
+struct EpiDftFwd {  // rows (b, col): conj X_m -> G[b][m][col][re, im]
+    double* G;
+    int C, L;
+    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
+        const int b = row / C, col = row - b * C;
+        if ((u.flags & 2) == 0) {
+            const int m = u.aux + n;
+            double* g = G + (((long long)b * L + m) * C + col) * 2;
+            g[0] = v;
+            if (m == 0) g[1] = 0.0;
+        } else {
+            const int m = 1 + u.aux + n;
+            G[(((long long)b * L + m) * C + col) * 2 + 1] = v;
+        }
+    }
+};
+struct EpiLegFwd {  // rows (m, b, kc) -> flm[tri(l,m)][b][kc]
+    double* flm;
+    int B, nr2;
+    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
+        const int m = u.g, p = (u.flags >> 2) & 1;
+        const long long local = row - (long long)m * B * nr2;
+        const int b = int(local / nr2), kc = int(local - (long long)b * nr2);
+        const int l = m + p + 2 * (u.aux + n);
+        flm[(tri_idx(l, m) * B + b) * nr2 + kc] = v;
+    }
+};
+struct EpiRadFwd {  // rows ((tri(l,m) B + b) 2 + c) -> coeffs[b][zidx(n,l,m)][c]
+    double* coeffs;
+    int B;
+    long long cs;
+    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
+        const int l = u.g;
+        const int tb = row >> 1, c = row & 1;
+        const int t = tb / B, b = tb - t * B;
+        const int m = t - int(tri_idx(l, 0));
+        coeffs[b * cs + zidx(l + 2 * (u.aux + n), l, m) * 2 + c] = v;
+    }
+};
+struct EpiRadBwd {  // rows ((t B + b) 2 + c) -> flm[(t B + b)][k][c]
+    double* flm;
+    int nr;
+    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
+        const int k = u.aux + n;
+        flm[((long long)(row >> 1) * nr + k) * 2 + (row & 1)] = v;
+    }
+};
+struct EpiLegBwd {  // rows (m, b, kc) -> G north/south pair (conjugated); parity 1 adds/subtracts
+    double* G;
+    int B, L, Nt, nr2, j0u, j0d;
+    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
+        const int m = u.g;
+        const long long local = row - (long long)m * B * nr2;
+        const int b = int(local / nr2), kc = int(local - (long long)b * nr2);
+        const int jh = u.aux + n;
+        const double x = (kc & 1) ? -v : v;
+        double* base = G + ((long long)b * L + m) * Nt * nr2 + kc;
+        double* up = base + (long long)(j0u + jh) * nr2;
+        double* dn = base + (long long)(j0d - jh) * nr2;
+        if (((u.flags >> 2) & 1) == 0) {
+            *up = x;
+            *dn = x;
+        } else {
+            *up += x;
+            *dn -= x;
+        }
+    }
+};
+struct EpiDftBwd {  // rows (b, col) -> grid[b][i][col] and grid[b][N-i][col]
+    double* grid;
+    int C, N;
+    long long gsz;
+    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
+        const long long b = row / C, col = row - b * C;
+        double* x = grid + b * gsz + col;
+        if ((u.flags & 2) == 0) {
+            const int i = u.aux + n;
+            x[(long long)i * C] = v;
+            if (i > 0) x[(long long)(N - i) * C] = v;
+        } else {
+            const int i = 1 + u.aux + n;
+            x[(long long)i * C] += v;
+            x[(long long)(N - i) * C] -= v;
+        }
+    }
+};
+
+struct SplitParams {
+    const SplitUnit* units;
+    int nunits;
+    int a_rows_total[2];  // rows per slice of the two A slice arrays
+    int b_rows_total[2];
+    const int* ea[2];
+    const int* eb[2];
+    int* err;
+};
+
+template <int S, int NT, class Epi>
+__global__ void __launch_bounds__(SP_THREADS, 1)
+    split_gemm_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUtensorMap mapA1,
+                      const __grid_constant__ CUtensorMap mapB0, const __grid_constant__ CUtensorMap mapB1,
+                      const SplitParams P, const Epi epi) {
+    constexpr int A_TILE = SP_M * 32;                       // bytes of one slice, 16 K elements
+    constexpr int B_TILE = ((NT * 32 + 1023) / 1024) * 1024;
+    constexpr int STAGE = S * (A_TILE + B_TILE);
+    constexpr uint32_t TX = S * (SP_M * 32 + NT * 32);
+    constexpr uint32_t IDESC = idesc_bf16_f32(SP_M, NT);
+    static_assert(S * NT <= 512, "levels must fit in TMEM");
+
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + SP_STAGES * STAGE);
+    uint64_t* empty = full + SP_STAGES;
+    uint64_t* tfull = empty + SP_STAGES;
+    uint64_t* tempty = tfull + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < SP_STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(tfull, 1);
+        mbar_init(tempty, 8);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        tmem_alloc(tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            int it = 0;
+            bool ok = true;
+            for (int ui = blockIdx.x; ui < P.nunits && ok; ui += gridDim.x) {
+                const SplitUnit u = P.units[ui];
+                const CUtensorMap* ma = (u.flags & 1) ? &mapA1 : &mapA0;
+                const CUtensorMap* mb = (u.flags & 2) ? &mapB1 : &mapB0;
+                const int arows = P.a_rows_total[u.flags & 1];
+                const int brows = P.b_rows_total[(u.flags >> 1) & 1];
+                for (int kb = 0; kb < u.ksteps; ++kb, ++it) {
+                    const int st = it % SP_STAGES;
+                    const uint32_t ph = (it / SP_STAGES) & 1;
+                    if (!mbar_wait(&empty[st], ph ^ 1, P.err, 1)) { ok = false; break; }
+                    mbar_expect_tx(&full[st], TX);
+                    unsigned char* sa = smem + st * STAGE;
+                    unsigned char* sb = sa + S * A_TILE;
+#pragma unroll
+                    for (int s = 0; s < S; ++s) tma_load_2d(sa + s * A_TILE, ma, &full[st], kb * SP_KB, s * arows + u.a_row0);
+#pragma unroll
+                    for (int t = 0; t < S; ++t) tma_load_2d(sb + t * B_TILE, mb, &full[st], kb * SP_KB, t * brows + u.b_row0);
+                }
+            }
+            // drain: wait (bounded) for the copies this thread issued
+            for (int q = 0; q < SP_STAGES && it > 0; ++q) {
+                const int j = it - 1 - q;
+                if (j < 0) break;
+                mbar_wait(&full[j % SP_STAGES], (j / SP_STAGES) & 1, P.err, 5);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            int it = 0, tile = 0;
+            bool ok = true;
+            for (int ui = blockIdx.x; ui < P.nunits && ok; ui += gridDim.x, ++tile) {
+                const SplitUnit u = P.units[ui];
+                if (!mbar_wait(tempty, (tile & 1) ^ 1, P.err, 2)) { ok = false; break; }
+                tc_fence_after();
+                for (int kb = 0; kb < u.ksteps; ++kb, ++it) {
+                    const int st = it % SP_STAGES;
+                    const uint32_t ph = (it / SP_STAGES) & 1;
+                    if (!mbar_wait(&full[st], ph, P.err, 3)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t sa = smem_u32(smem + st * STAGE);
+                    const uint32_t sb = sa + S * A_TILE;
+#pragma unroll
+                    for (int d = 0; d < S; ++d) {
+#pragma unroll
+                        for (int s = 0; s <= d; ++s) {
+                            const int t = d - s;
+                            umma_bf16(tmem + d * NT, desc_sw32(sa + s * A_TILE), desc_sw32(sb + t * B_TILE), IDESC,
+                                      (kb > 0 || s > 0) ? 1u : 0u);
+                        }
+                    }
+                    umma_commit(&empty[st]);
+                }
+                if (ok) umma_commit(tfull);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue ----------------
+        const int q = warp & 3;             // TMEM lane quarter of this warp
+        const int half = (warp - 2) >> 2;   // which half of the columns
+        int tile = 0;
+        for (int ui = blockIdx.x; ui < P.nunits; ui += gridDim.x, ++tile) {
+            const SplitUnit u = P.units[ui];
+            const bool got = mbar_wait(tfull, tile & 1, P.err, 4);
+            if (!__all_sync(0xffffffffu, got)) break;
+            tc_fence_after();
+            const int r = 32 * q + lane;
+            const bool rv = r < u.a_rows;
+            const int row = u.a_row0 + r;
+            const int amap = u.flags & 1, bmap = (u.flags >> 1) & 1;
+            const int ea = rv ? P.ea[amap][row] : 0;
+            for (int c0 = half * (NT / 2); c0 < (half + 1) * (NT / 2); c0 += 8) {
+                long long T[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) T[j] = 0;
+#pragma unroll
+                for (int d = 0; d < S; ++d) {
+                    uint32_t v[8];
+                    tmem_ld8(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(d * NT + c0), v);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) T[j] = T[j] * 128 + (long long)__float2int_rn(__uint_as_float(v[j]));
+                }
+                if (rv) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int n = c0 + j;
+                        if (n < u.n) {
+                            const int E = ea + P.eb[bmap][u.b_row0 + n] - 7 * S - 7;
+                            epi(u, row, n, i64_ldexp(T[j], E));
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 512);
+    }
+}
+
+template <int S, int NT>
+constexpr size_t split_smem_bytes() {
+    return (size_t)SP_STAGES * S * (SP_M * 32 + ((NT * 32 + 1023) / 1024) * 1024) + 1024 + 256;
+}
+
+}  // namespace
+
+// ===========================================================================
+// Host side
+// ===========================================================================
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// [S][rows][Kp] bf16 slice array -> 2D map (Kp, S*rows), box (16, box_rows), 32B swizzle
+int make_map(CUtensorMap* map, const void* base, long long rows, int Kp, int S, int box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return fail(ZEST_GPU_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+    if ((long long)S * rows >= (1ll << 31)) return fail(ZEST_GPU_ERR_UNSUPPORTED, "slice array too tall for TMA");
+    cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)(S * rows)};
+    cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+    cuuint32_t box[2] = {16, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(ZEST_GPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
+    return ZEST_GPU_OK;
+}
+
+inline int r16(int k) { return (k + 15) & ~15; }
+
+int n_tile(int S) { return S == 4 ? 128 : (S == 5 ? 96 : 80); }
+
+}  // namespace
+
+// Slice arrays of one operand: [S][rows][Kp] bf16 + per-row exponents.
+struct SliceArray {
+    DevBuf data, ex;
+    long long rows = 0;
+    int Kp = 0;
+    int S = 0;
+    int ensure(long long r, int kp, int s) {
+        rows = r;
+        Kp = kp;
+        S = s;
+        ZG_TRY(data.ensure((size_t)s * r * kp * 2 + 256));
+        ZG_TRY(ex.ensure((size_t)r * 4 + 16));
+        return ZEST_GPU_OK;
+    }
+    __nv_bfloat16* ptr() const { return data.as<__nv_bfloat16>(); }
+};
+
+// Sliced tables of one Zernike plan for one slice count.
+struct ZtSplitTables {
+    int S = 0;
+    SliceArray dft_cos_f, dft_sin_f, leg_f, rad_f, rad_bT, leg_bT, dft_cos_b, dft_sin_b;
+};
+
+struct SplitState {
+    int err_init = 0;
+    DevBuf err;                 // device error flag of the GEMM kernels
+    SliceArray op[2];           // data operands of the current stage
+    std::map<std::tuple<const void*, int>, std::unique_ptr<ZtSplitTables>> zt_tables;  // per (plan, S)
+    std::map<std::tuple<int, int, int, int, int>, std::pair<std::unique_ptr<DevBuf>, int>> units;
+    DevBuf tmp;                 // FP64 staging of generated tables
+};
+
 void destroy_split(SplitState* s) { delete s; }
 
-int split_available() { return fail(ZEST_GPU_ERR_UNSUPPORTED, "split precision is not built in this library"); }
+namespace {
 
-int split_zt_forward(zest_gpu_context*, ZtPlan&, int, int, int, int, const double*, double*) {
-    return split_available();
+template <class Loader>
+int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S, int fold, SliceArray& out) {
+    if (rows <= 0) return ZEST_GPU_OK;
+    if (K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: K above 256");
+    const long long blocks = (rows + SL_ROWS - 1) / SL_ROWS;
+    slice_kernel<Loader><<<(unsigned)blocks, 256, 0, s>>>(ld, rows, K, out.Kp, S, fold, out.ptr(), rows * out.Kp,
+                                                         out.ex.as<int>());
+    return launch_check("slice_kernel");
 }
-int split_zt_backward(zest_gpu_context*, ZtPlan&, int, int, int, int, const double*, double*) {
-    return split_available();
+
+int get_state(zest_gpu_context* ctx, SplitState** out) {
+    if (!ctx->split) {
+        ctx->split.reset(new SplitState());
+        ZG_TRY(ctx->split->err.ensure(16));
+        ZG_CUDA_TRY(cudaMemsetAsync(ctx->split->err.p, 0, 16, ctx->stream));
+    }
+    *out = ctx->split.get();
+    return ZEST_GPU_OK;
+}
+
+// FP64 table generators
+__global__ void dft_table_kernel(double* __restrict__ out, int rows, int K, int ld, int N, int row_off, int col_off,
+                                 int mode) {
+    // mode 0: cos(2 pi r c / N); 1: sin(2 pi r c / N); 2: (c>0 ? 2 : 1) cos; 3: -2 sin
+    // r = row + row_off, c = col + col_off ; laid out [row][col] with stride ld
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y;
+    if (r >= rows || c >= ld) return;
+    double v = 0.0;
+    if (c < K) {
+        const long long rr = r + row_off, cc = c + col_off;
+        const long long t = (rr * cc) % N;
+        double sn, cs;
+        sincospi(2.0 * double(t) / double(N), &sn, &cs);
+        if (mode == 0) v = cs;
+        else if (mode == 1) v = sn;
+        else if (mode == 2) v = (cc > 0 ? 2.0 : 1.0) * cs;
+        else v = -2.0 * sn;
+    }
+    out[(long long)r * ld + c] = v;
+}
+
+// out[(blk*nrow + k) * ld + i] = in[(off[blk] + i) * nrow + k] for i < cnt[blk] else 0
+__global__ void transpose_blocks_kernel(const double* __restrict__ in, const long long* __restrict__ off,
+                                        const int* __restrict__ cnt, int nrow, int ld, double* __restrict__ out) {
+    const int blk = blockIdx.y;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nrow * ld) return;
+    const int k = e / ld, i = e - k * ld;
+    out[((long long)blk * nrow + k) * ld + i] = (i < cnt[blk]) ? in[(off[blk] + i) * nrow + k] : 0.0;
+}
+
+int slice_table(zest_gpu_context* ctx, const double* src, long long rows, int K, int ld, int S, SliceArray& dst) {
+    ZG_TRY(dst.ensure(rows, r16(K), S));
+    return launch_slice(ctx->stream, RowMajorLoader{src, ld}, rows, K, S, 0, dst);
+}
+
+int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, ZtSplitTables** out) {
+    auto key = std::make_tuple((const void*)&plan, S);
+    auto it = st->zt_tables.find(key);
+    if (it != st->zt_tables.end()) {
+        *out = it->second.get();
+        return ZEST_GPU_OK;
+    }
+    cudaStream_t s = ctx->stream;
+    auto t = std::make_unique<ZtSplitTables>();
+    t->S = S;
+    const int L = int(plan.sh.L), N = int(plan.sh.nlon), nr = int(plan.sh.nrad), kh = plan.leg.nnodes;
+    // DFT tables
+    {
+        const int ld = r16(L);
+        ZG_TRY(st->tmp.ensure((size_t)L * ld * sizeof(double)));
+        double* tmp = st->tmp.as<double>();
+        auto gen = [&](int rows, int K, int row_off, int col_off, int mode, SliceArray& dst) -> int {
+            dim3 grid((ld + 127) / 128, rows);
+            dft_table_kernel<<<grid, 128, 0, s>>>(tmp, rows, K, ld, N, row_off, col_off, mode);
+            ZG_TRY(launch_check("dft_table_kernel"));
+            return slice_table(ctx, tmp, rows, K, ld, S, dst);
+        };
+        // forward: cos rows m in [0,L), cols i in [0,L); sin rows m in [1,L), cols i in [1,L)
+        ZG_TRY(gen(L, L, 0, 0, 0, t->dft_cos_f));
+        if (L > 1) ZG_TRY(gen(L - 1, L - 1, 1, 1, 1, t->dft_sin_f));
+        // backward: cos rows i in [0,L), cols m in [0,L); sin rows i in [1,L), cols m in [1,L)
+        ZG_TRY(gen(L, L, 0, 0, 2, t->dft_cos_b));
+        if (L > 1) ZG_TRY(gen(L - 1, L - 1, 1, 1, 3, t->dft_sin_b));
+        ZG_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    // forward Legendre and radial tables (FP64 tables of the plain form)
+    ZG_TRY(slice_table(ctx, plan.leg.Pf.as<double>(), plan.leg.off_h[2 * (size_t)L], kh, kh, S, t->leg_f));
+    ZG_TRY(slice_table(ctx, plan.rad.Rf.as<double>(), plan.rad.off_h[L], nr, nr, S, t->rad_f));
+    // backward tables: transposed blocks
+    {
+        const int kl = r16((L + 1) / 2);
+        // Legendre: per (m,p) block [kh][cnt] from Pb
+        std::vector<int> cnt(2 * (size_t)L);
+        for (int m = 0; m < L; ++m)
+            for (int p = 0; p < 2; ++p) cnt[2 * m + p] = (L - m - p > 0) ? (L - m - p + 1) / 2 : 0;
+        DevBuf dcnt;
+        ZG_TRY(upload(dcnt, cnt, s));
+        ZG_TRY(st->tmp.ensure((size_t)2 * L * kh * kl * sizeof(double)));
+        dim3 g1((kh * kl + 255) / 256, 2 * L);
+        transpose_blocks_kernel<<<g1, 256, 0, s>>>(plan.leg.Pb.as<double>(), plan.leg.off.as<long long>(),
+                                                   dcnt.as<int>(), kh, kl, st->tmp.as<double>());
+        ZG_TRY(launch_check("transpose_blocks_kernel"));
+        ZG_TRY(slice_table(ctx, st->tmp.as<double>(), (long long)2 * L * kh, kl, kl, S, t->leg_bT));
+        ZG_CUDA_TRY(cudaStreamSynchronize(s));
+        // radial: per l block [nr][cnt(l)] from Rb
+        std::vector<int> rc((size_t)L);
+        for (int l = 0; l < L; ++l) rc[l] = (L - l + 1) / 2;
+        DevBuf drc;
+        ZG_TRY(upload(drc, rc, s));
+        ZG_TRY(st->tmp.ensure((size_t)L * nr * kl * sizeof(double)));
+        dim3 g2((nr * kl + 255) / 256, L);
+        transpose_blocks_kernel<<<g2, 256, 0, s>>>(plan.rad.Rb.as<double>(), plan.rad.off.as<long long>(),
+                                                   drc.as<int>(), nr, kl, st->tmp.as<double>());
+        ZG_TRY(launch_check("transpose_blocks_kernel"));
+        ZG_TRY(slice_table(ctx, st->tmp.as<double>(), (long long)L * nr, kl, kl, S, t->rad_bT));
+        ZG_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    *out = t.get();
+    st->zt_tables.emplace(key, std::move(t));
+    return ZEST_GPU_OK;
+}
+
+template <int S, int NT, class Epi>
+int run_gemm_t(zest_gpu_context* ctx, const std::vector<SplitUnit>& units, const SliceArray& A0,
+               const SliceArray& A1, const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
+    if (units.empty()) return ZEST_GPU_OK;
+    SplitState* st;
+    ZG_TRY(get_state(ctx, &st));
+    cudaStream_t s = ctx->stream;
+    CUtensorMap ma0, ma1, mb0, mb1;
+    ZG_TRY(make_map(&ma0, A0.ptr(), A0.rows, A0.Kp, S, SP_M));
+    ZG_TRY(make_map(&ma1, A1.ptr(), A1.rows, A1.Kp, S, SP_M));
+    ZG_TRY(make_map(&mb0, B0.ptr(), B0.rows, B0.Kp, S, NT));
+    ZG_TRY(make_map(&mb1, B1.ptr(), B1.rows, B1.Kp, S, NT));
+    // units are uploaded once per distinct list (cached by content size + first entries)
+    DevBuf ubuf;
+    ZG_TRY(ubuf.ensure(units.size() * sizeof(SplitUnit)));
+    ZG_CUDA_TRY(cudaMemcpyAsync(ubuf.p, units.data(), units.size() * sizeof(SplitUnit), cudaMemcpyHostToDevice, s));
+    SplitParams P;
+    P.units = ubuf.as<SplitUnit>();
+    P.nunits = int(units.size());
+    P.a_rows_total[0] = int(A0.rows);
+    P.a_rows_total[1] = int(A1.rows);
+    P.b_rows_total[0] = int(B0.rows);
+    P.b_rows_total[1] = int(B1.rows);
+    P.ea[0] = A0.ex.as<int>();
+    P.ea[1] = A1.ex.as<int>();
+    P.eb[0] = B0.ex.as<int>();
+    P.eb[1] = B1.ex.as<int>();
+    P.err = st->err.as<int>();
+    const size_t smem = split_smem_bytes<S, NT>();
+    ZG_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<S, NT, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    int nsm = 0;
+    ZG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int grid = std::min<int>(int(units.size()), nsm);
+    {
+        StageScope sc(ctx, ST_SPLIT_GEMM);
+        split_gemm_kernel<S, NT, Epi><<<grid, SP_THREADS, smem, s>>>(ma0, ma1, mb0, mb1, P, epi);
+        ZG_TRY(launch_check("split_gemm_kernel"));
+    }
+    // the unit list must outlive the kernel
+    ZG_CUDA_TRY(cudaStreamSynchronize(s));
+    int herr = 0;
+    ZG_CUDA_TRY(cudaMemcpy(&herr, st->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+        cudaMemset(st->err.p, 0, sizeof(int));
+        return fail(ZEST_GPU_ERR_TIMEOUT, "split GEMM: bounded wait expired (code " + std::to_string(herr) + ")");
+    }
+    return ZEST_GPU_OK;
+}
+
+template <class Epi>
+int run_gemm(zest_gpu_context* ctx, int S, const std::vector<SplitUnit>& units, const SliceArray& A0,
+             const SliceArray& A1, const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
+    switch (S) {
+    case 4: return run_gemm_t<4, 128>(ctx, units, A0, A1, B0, B1, epi);
+    case 5: return run_gemm_t<5, 96>(ctx, units, A0, A1, B0, B1, epi);
+    case 6: return run_gemm_t<6, 80>(ctx, units, A0, A1, B0, B1, epi);
+    }
+    return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path supports 4..6 slices");
+}
+
+// tiles of a group: operand rows [a0, a0 + arows) x table rows [b0, b0 + nrows)
+void add_units(std::vector<SplitUnit>& v, long long a0, long long arows, int b0, int nrows, int NT, int ksteps,
+               int flags, int g) {
+    if (arows <= 0 || nrows <= 0 || ksteps <= 0) return;
+    for (long long r = 0; r < arows; r += SP_M)
+        for (int c = 0; c < nrows; c += NT) {
+            SplitUnit u;
+            u.a_row0 = int(a0 + r);
+            u.a_rows = int(std::min<long long>(SP_M, arows - r));
+            u.b_row0 = b0 + c;
+            u.n = std::min(NT, nrows - c);
+            u.ksteps = ksteps;
+            u.flags = flags;
+            u.g = g;
+            u.aux = c;
+            v.push_back(u);
+        }
+}
+
+}  // namespace
+
+// ===========================================================================
+// Split-precision Zernike transforms
+// ===========================================================================
+int split_available() {
+    int dev = 0, major = 0, minor = 0;
+    ZG_CUDA_TRY(cudaGetDevice(&dev));
+    ZG_CUDA_TRY(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    ZG_CUDA_TRY(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+    if (major != 10 || minor != 3) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path needs sm_103a");
+    if (!encode_fn()) return fail(ZEST_GPU_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+    return ZEST_GPU_OK;
+}
+
+int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm, int batch, const double* grids,
+                     double* coeffs) {
+    (void)Le;
+    const int S = ctx->slices;
+    const int NT = n_tile(S);
+    cudaStream_t s = ctx->stream;
+    SplitState* st;
+    ZG_TRY(get_state(ctx, &st));
+    if (Lg < 2 || Lg > SL_KMAX || plan.sh.nrad > SL_KMAX)
+        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: orders 2..255");
+    ZtSplitTables* tb;
+    ZG_TRY(build_zt_tables(ctx, st, plan, S, &tb));
+    const ZtShape& sh = plan.sh;
+    const int C = int(sh.nlat * sh.nrad), N = int(sh.nlon), nt = int(sh.nlat), nr = int(sh.nrad), nr2 = 2 * nr;
+    const int kh = plan.leg.nnodes;
+    const long long csz = 2 * zsize(Le);
+    // scratch: G (FP64 spectra) and flm
+    ZG_TRY(ctx->s0.ensure((size_t)batch * Lg * C * 2 * sizeof(double)));
+    ZG_TRY(ctx->s1.ensure((size_t)tri_size(Lm) * batch * nr2 * sizeof(double)));
+    double* G = ctx->s0.as<double>();
+    double* flm = ctx->s1.as<double>();
+
+    // ---- longitude DFT: folded cos/sin products ----
+    {
+        const long long rows = (long long)batch * C;
+        ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
+        ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
+        {
+            StageScope sc(ctx, ST_SPLIT_SLICE);
+            ZG_TRY(launch_slice(s, DftFwdLoader{grids, sh.size(), C, N, 0}, rows, Lg, S, 1, st->op[0]));
+            if (Lg > 1) ZG_TRY(launch_slice(s, DftFwdLoader{grids, sh.size(), C, N, 1}, rows, Lg - 1, S, 2, st->op[1]));
+        }
+        std::vector<SplitUnit> u;
+        for (long long r = 0; r < rows; r += SP_M) {
+            add_units(u, r, std::min<long long>(SP_M, rows - r), 0, Lm, NT, r16(Lg) / 16, 0, 0);
+            if (Lm > 1) add_units(u, r, std::min<long long>(SP_M, rows - r), 0, Lm - 1, NT, r16(Lg - 1) / 16, 1 | 2, 0);
+        }
+        ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[1], tb->dft_cos_f, tb->dft_sin_f, EpiDftFwd{G, C, Lg}));
+    }
+    // ---- Legendre (folded over the equator) ----
+    {
+        const long long per_m = (long long)batch * nr2;
+        const long long rows = (long long)Lm * per_m;
+        ZG_TRY(st->op[0].ensure(rows, r16(kh), S));
+        ZG_TRY(st->op[1].ensure(rows, r16(kh), S));
+        {
+            StageScope sc(ctx, ST_SPLIT_SLICE);
+            LegFwdLoader ld{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d};
+            ZG_TRY(launch_slice(s, ld, rows, kh, S, 1, st->op[0]));
+            ZG_TRY(launch_slice(s, ld, rows, kh, S, 2, st->op[1]));
+        }
+        std::vector<SplitUnit> u;
+        for (int m = 0; m < Lm; ++m)
+            for (int p = 0; p < 2; ++p) {
+                const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
+                add_units(u, (long long)m * per_m, per_m, int(plan.leg.off_h[2 * m + p]), cnt, NT, r16(kh) / 16,
+                          p | (p << 2), m);
+            }
+        ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd{flm, batch, nr2}));
+    }
+    // ---- radial ----
+    {
+        const long long rows = tri_size(Lm) * batch * 2;
+        ZG_TRY(st->op[0].ensure(rows, r16(nr), S));
+        {
+            StageScope sc(ctx, ST_SPLIT_SLICE);
+            ZG_TRY(launch_slice(s, RadFwdLoader{flm, nr}, rows, nr, S, 0, st->op[0]));
+        }
+        std::vector<SplitUnit> u;
+        for (int l = 0; l < Lm; ++l)
+            add_units(u, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, int(plan.rad.off_h[l]),
+                      (Lm - l + 1) / 2, NT, r16(nr) / 16, 0, l);
+        ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd{coeffs, batch, csz}));
+    }
+    return ZEST_GPU_OK;
+}
+
+int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int Lm, int batch, const double* coeffs,
+                      double* grids) {
+    const int S = ctx->slices;
+    const int NT = n_tile(S);
+    cudaStream_t s = ctx->stream;
+    SplitState* st;
+    ZG_TRY(get_state(ctx, &st));
+    if (Lg < 2 || Lg > SL_KMAX || plan.sh.nrad > SL_KMAX)
+        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: orders 2..255");
+    ZtSplitTables* tb;
+    ZG_TRY(build_zt_tables(ctx, st, plan, S, &tb));
+    const ZtShape& sh = plan.sh;
+    const int C = int(sh.nlat * sh.nrad), N = int(sh.nlon), nt = int(sh.nlat), nr = int(sh.nrad), nr2 = 2 * nr;
+    const int kh = plan.leg.nnodes;
+    const int kl = r16((Lg + 1) / 2);
+    const long long csz = 2 * zsize(Le);
+    ZG_TRY(ctx->s0.ensure((size_t)batch * Lg * C * 2 * sizeof(double)));
+    ZG_TRY(ctx->s1.ensure((size_t)tri_size(Lm) * batch * nr2 * sizeof(double)));
+    double* G = ctx->s0.as<double>();
+    double* flm = ctx->s1.as<double>();
+
+    // ---- radial: coefficients -> flm ----
+    {
+        const long long rows = tri_size(Lm) * batch * 2;
+        ZG_TRY(st->op[0].ensure(rows, kl, S));
+        {
+            StageScope sc(ctx, ST_SPLIT_SLICE);
+            ZG_TRY(launch_slice(s, RadBwdLoader{coeffs, csz, batch, Lm}, rows, (Lm + 1) / 2, S, 0, st->op[0]));
+        }
+        std::vector<SplitUnit> u;
+        for (int l = 0; l < Lm; ++l)
+            add_units(u, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, l * nr, nr, NT,
+                      r16((Lm - l + 1) / 2) / 16, 0, l);
+        ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd{flm, nr}));
+    }
+    // ---- Legendre: flm -> G (north/south unfold; parity 1 read-modify-write) ----
+    {
+        const long long per_m = (long long)batch * nr2;
+        const long long rows = (long long)Lm * per_m;
+        ZG_TRY(st->op[0].ensure(rows, kl, S));
+        ZG_TRY(st->op[1].ensure(rows, kl, S));
+        {
+            StageScope sc(ctx, ST_SPLIT_SLICE);
+            ZG_TRY(launch_slice(s, LegBwdLoader{flm, batch, nr2, 0, Lm}, rows, (Lm + 1) / 2, S, 0, st->op[0]));
+            ZG_TRY(launch_slice(s, LegBwdLoader{flm, batch, nr2, 1, Lm}, rows, Lm / 2, S, 0, st->op[1]));
+        }
+        if (Lm < Lg) {
+            StageScope sc(ctx, ST_MEMSET);
+            ZG_CUDA_TRY(cudaMemset2DAsync(G + (size_t)Lm * C * 2, (size_t)Lg * C * 2 * sizeof(double), 0,
+                                          (size_t)(Lg - Lm) * C * 2 * sizeof(double), batch, s));
+        }
+        for (int p = 0; p < 2; ++p) {
+            std::vector<SplitUnit> u;
+            for (int m = 0; m < Lm; ++m) {
+                const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
+                if (cnt == 0) continue;
+                add_units(u, (long long)m * per_m, per_m, (2 * m + p) * kh, kh, NT, r16(cnt) / 16, p | (p << 2), m);
+            }
+            ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
+                            EpiLegBwd{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d}));
+        }
+    }
+    // ---- longitude: inverse real DFT, cos pass then sin read-modify-write pass ----
+    {
+        const long long rows = (long long)batch * C;
+        ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
+        ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
+        {
+            StageScope sc(ctx, ST_SPLIT_SLICE);
+            ZG_TRY(launch_slice(s, DftBwdLoader{G, batch, Lg, C, 0}, rows, Lg, S, 0, st->op[0]));
+            if (Lg > 1) ZG_TRY(launch_slice(s, DftBwdLoader{G, batch, Lg, C, 1}, rows, Lg - 1, S, 0, st->op[1]));
+        }
+        std::vector<SplitUnit> u;
+        for (long long r = 0; r < rows; r += SP_M)
+            add_units(u, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, r16(Lg) / 16, 0, 0);
+        ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
+                        EpiDftBwd{grids, C, N, sh.size()}));
+        if (Lg > 1) {
+            std::vector<SplitUnit> v;
+            for (long long r = 0; r < rows; r += SP_M)
+                add_units(v, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT, r16(Lg - 1) / 16, 1 | 2 | 4, 0);
+            ZG_TRY(run_gemm(ctx, S, v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
+                            EpiDftBwd{grids, C, N, sh.size()}));
+        }
+    }
+    return ZEST_GPU_OK;
+}
+
+// Dense FP64 product C = A B^T through the split path (A: M x K, B: N x K,
+// row-major, device pointers); used to test the emulation itself.
+int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A, const double* B, double* C) {
+    const int S = ctx->slices;
+    const int NT = n_tile(S);
+    if (K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split GEMM: K above 256");
+    SplitState* st;
+    ZG_TRY(get_state(ctx, &st));
+    SliceArray a, b;
+    ZG_TRY(a.ensure(M, r16(K), S));
+    ZG_TRY(b.ensure(N, r16(K), S));
+    ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{A, K}, M, K, S, 0, a));
+    ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{B, K}, N, K, S, 0, b));
+    std::vector<SplitUnit> u;
+    add_units(u, 0, M, 0, N, NT, r16(K) / 16, 0, 0);
+    return run_gemm(ctx, S, u, a, a, b, b, EpiDense{C, N});
 }
 
 }  // namespace zgpu

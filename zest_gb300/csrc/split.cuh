@@ -19,5 +19,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
                      double* coeffs);
 int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int Lm, int batch, const double* coeffs,
                       double* grids);
+// C = A B^T (A: M x K, B: N x K, C: M x N, row-major FP64 device buffers)
+int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A, const double* B, double* C);
 
 }  // namespace zgpu

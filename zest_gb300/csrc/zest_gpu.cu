@@ -761,6 +761,27 @@ int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch, 
     return rotate_common(ctx, 1, order, batch, coeffs, angles, 1, rotation_type, mem, true);
 }
 
+int zest_gpu_split_gemm(zest_gpu_context* ctx, size_t M, size_t N, size_t K, const double* A, const double* B,
+                        double* C, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (M > (1u << 24) || N > (1u << 20) || K > 256) return fail(ZEST_GPU_ERR_INVALID, "split GEMM size out of range");
+    if ((M * K && !A) || (N * K && !B) || (M * N && !C)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    if (M == 0 || N == 0) return ZEST_GPU_OK;
+    if (mem == ZEST_MEM_DEVICE) return split_dense_gemm(ctx, int(M), int(N), int(K), A, B, C);
+    if (mem != ZEST_MEM_HOST) return fail(ZEST_GPU_ERR_INVALID, "mem must be ZEST_MEM_HOST or ZEST_MEM_DEVICE");
+    cudaStream_t s = ctx->stream;
+    ZG_TRY(ctx->in_stage.ensure(M * K * sizeof(double)));
+    ZG_TRY(ctx->aux_stage.ensure(N * K * sizeof(double)));
+    ZG_TRY(ctx->out_stage.ensure(M * N * sizeof(double)));
+    ZG_CUDA_TRY(cudaMemcpyAsync(ctx->in_stage.p, A, M * K * sizeof(double), cudaMemcpyHostToDevice, s));
+    ZG_CUDA_TRY(cudaMemcpyAsync(ctx->aux_stage.p, B, N * K * sizeof(double), cudaMemcpyHostToDevice, s));
+    ZG_TRY(split_dense_gemm(ctx, int(M), int(N), int(K), ctx->in_stage.as<double>(), ctx->aux_stage.as<double>(),
+                            ctx->out_stage.as<double>()));
+    ZG_CUDA_TRY(cudaMemcpyAsync(C, ctx->out_stage.p, M * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    ZG_CUDA_TRY(cudaStreamSynchronize(s));
+    return ZEST_GPU_OK;
+}
+
 int zest_gpu_euler_from_matrix(const double* r, double* e) {
     if (!r || !e) return fail(ZEST_GPU_ERR_INVALID, "null pointer");
     // euler_angles_from_rotation_matrix, include/rotor.hpp:53-63 (as written there)
