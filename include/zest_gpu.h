@@ -96,6 +96,10 @@ int zest_gpu_trim(zest_gpu_context* ctx);
 int zest_gpu_profile_enable(zest_gpu_context* ctx, int enable);
 int zest_gpu_profile_read(zest_gpu_context* ctx, int reset, double* ms, long long* count, int n);
 int zest_gpu_profile_stage_count(void);
+/* BF16 tensor-core flops of the split-precision products issued while
+ * profiling: `useful` counts valid rows x table rows x K x slice products,
+ * `issued` the whole 128-row tiles as executed (reset != 0 clears them). */
+int zest_gpu_profile_flops(zest_gpu_context* ctx, int reset, double* useful, double* issued);
 const char* zest_gpu_profile_stage_name(int stage);
 /* Number of kernels this library has launched in this process. */
 unsigned long long zest_gpu_launch_count(void);
@@ -149,7 +153,7 @@ int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
 int zest_gpu_euler_from_matrix(const double* matrix, double* euler);
 
 /* ---- split-precision dense product (no reference counterpart) ----
- * C = A B^T for row-major FP64 A (M x K) and B (N x K), K <= 256, evaluated
+ * C = A B^T for row-major FP64 A (M x K) and B (N x K), K <= 992, evaluated
  * with the context's slice count on the tcgen05 path used by
  * ZEST_PRECISION_SPLIT (BF16 fixed-point slices, exact FP32 partial sums,
  * FP64 recombination).  Exposed to test and measure the emulation itself. */

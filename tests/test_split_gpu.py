@@ -1,0 +1,191 @@
+"""Split-precision form (BF16 fixed-point slices on tcgen05, exact FP32 level
+sums, FP64 recombination).
+
+The emulated product is checked first on integer inputs, where it must be
+exact, then on random FP64 data against numpy's FP64 product; the Zernike
+transforms in split precision are checked against the FP64 path and the
+oracle.  Tolerance: 1e-11 relative max-norm (the precision target of the split
+form), max|x - x_ref| / max|x_ref|."""
+import numpy as np
+import pytest
+
+from oracle import zidx, zt_coeff_size
+
+pytestmark = pytest.mark.gpu
+
+SPLIT_TOL = 1e-11
+
+
+def relmax(a, b):
+    a = np.asarray(a).ravel()
+    b = np.asarray(b).ravel()
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import zest_gb300
+    from zest_gb300 import build
+    build.build()
+    c = zest_gb300.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture()
+def split(ctx):
+    import zest_gb300
+    ctx.set_precision(zest_gb300.PRECISION_SPLIT, 6)
+    yield ctx
+    ctx.set_precision(zest_gb300.PRECISION_FP64)
+
+
+def rand_zt(rng, L, power=1.5, batch=1):
+    c = np.zeros((batch, zt_coeff_size(L), 2))
+    for n in range(L):
+        for l in range(n & 1, n + 1, 2):
+            for m in range(l + 1):
+                c[:, zidx(n, l, m)] = rng.normal(size=(batch, 2)) * (n + 1) ** -power
+                if m == 0:
+                    c[:, zidx(n, l, m), 1] = 0.0
+    return c
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 80, 16), (1, 1, 1), (129, 81, 17), (300, 200, 208), (1000, 37, 256)])
+def test_split_gemm_exact_on_integers(split, M, N, K):
+    # integers with |x| < 2^20 are represented exactly by 6 slices of 7 bits,
+    # and the level sums are exact: the product must be exact
+    rng = np.random.default_rng(M + N + K)
+    A = rng.integers(-(1 << 19), 1 << 19, size=(M, K)).astype(np.float64)
+    B = rng.integers(-(1 << 19), 1 << 19, size=(N, K)).astype(np.float64)
+    C = split.split_gemm(A, B)
+    ref = A @ B.T
+    # integer products exceed 2^53 only past ~2^40 magnitudes; compare exactly where representable
+    assert np.max(np.abs(C - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-15
+
+
+@pytest.mark.parametrize("S", [4, 5, 6])
+def test_split_gemm_random(ctx, S):
+    import zest_gb300
+    ctx.set_precision(zest_gb300.PRECISION_SPLIT, S)
+    try:
+        rng = np.random.default_rng(S)
+        A = rng.normal(size=(517, 201)) * np.exp(rng.normal(size=(517, 1)))
+        B = rng.normal(size=(93, 201))
+        C = ctx.split_gemm(A, B)
+        err = relmax(C, A @ B.T)
+        bound = {4: 1e-7, 5: 1e-9, 6: 5e-12}[S]
+        assert err < bound, err
+    finally:
+        ctx.set_precision(zest_gb300.PRECISION_FP64)
+
+
+def split_model(A, B, S):
+    """Integer model of the split product (balanced base-128 digits of the
+    row-scaled operands, levels 0..S summed exactly, 2^(eA+eB-7S-14) scaling)."""
+    def digits(X):
+        E = np.frexp(np.abs(X).max(axis=1))[1]
+        e = E + 1
+        v = np.rint(X * np.exp2(7 * S - e)[:, None]).astype(np.int64)
+        d = np.zeros((S,) + X.shape, dtype=np.int64)
+        w = v.copy()
+        for s in range(S - 1, 0, -1):
+            r = w & 127
+            r = np.where(r >= 64, r - 128, r)
+            d[s] = r
+            w = (w - r) >> 7
+        d[0] = w
+        return d, e
+    da, ea = digits(A)
+    db, eb = digits(B)
+    T = np.zeros((A.shape[0], B.shape[0]), dtype=object)
+    for lev in range(S + 1):
+        acc = np.zeros((A.shape[0], B.shape[0]), dtype=np.int64)
+        for s in range(S):
+            t = lev - s
+            if 0 <= t < S:
+                acc += da[s] @ db[t].T
+        T = T * 128 + acc.astype(object)
+    return T.astype(float) * np.exp2(ea[:, None] + eb[None, :] - 7 * S - 14)
+
+
+@pytest.mark.parametrize("K", [1, 16, 33, 64])
+def test_split_gemm_matches_integer_model(split, K):
+    # the kernel computes exactly the model's integer arithmetic (exact level
+    # sums for these sizes), so the results agree to the last bit
+    rng = np.random.default_rng(100 + K)
+    A = rng.normal(size=(130, K)) * np.exp(rng.normal(size=(130, 1)))
+    B = rng.normal(size=(70, K))
+    C = split.split_gemm(A, B)
+    np.testing.assert_array_equal(C, split_model(A, B, 6))
+
+
+@pytest.mark.parametrize("L,batch", [(2, 1), (7, 3), (20, 2), (64, 2)])
+def test_split_zt_vs_fp64(ctx, L, batch):
+    import zest_gb300
+    rng = np.random.default_rng(L)
+    c = rand_zt(rng, L, batch=batch).ravel()
+    g64 = ctx.zt_backward(c, L, batch=batch)
+    f64 = ctx.zt_forward(g64, L, batch=batch)
+    ctx.set_precision(zest_gb300.PRECISION_SPLIT, 6)
+    try:
+        gs = ctx.zt_backward(c, L, batch=batch)
+        fs = ctx.zt_forward(g64, L, batch=batch)
+    finally:
+        ctx.set_precision(zest_gb300.PRECISION_FP64)
+    assert relmax(gs, g64) < SPLIT_TOL
+    assert relmax(fs, f64) < SPLIT_TOL
+
+
+def test_split_zt_config1_vs_golden(split, golden):
+    g = golden("zt_config1")
+    c = split.zt_forward(np.ascontiguousarray(g["grid"]).ravel(), 20)
+    assert relmax(c, g["coeffs"]) < SPLIT_TOL
+    rt = split.zt_backward(np.ascontiguousarray(g["coeffs"]).ravel(), 20)
+    assert relmax(rt, g["roundtrip"]) < SPLIT_TOL
+
+
+def test_split_zt_vs_oracle(split, oracle):
+    rng = np.random.default_rng(5)
+    L = 33
+    c = rand_zt(rng, L)
+    g = split.zt_backward(c.ravel(), L)
+    assert relmax(g, oracle.zt_backward(c[0], L)) < SPLIT_TOL
+    f = split.zt_forward(g, L)
+    assert relmax(f, oracle.zt_forward(g, L)) < SPLIT_TOL
+
+
+def test_split_zt_truncation(ctx):
+    import zest_gb300
+    rng = np.random.default_rng(9)
+    c = rand_zt(rng, 12).ravel()
+    ref_b = ctx.zt_backward(c, 12, 16)
+    g = ctx.zt_backward(c, 12, 12)
+    ref_f = ctx.zt_forward(g, 12, 9)
+    ctx.set_precision(zest_gb300.PRECISION_SPLIT, 6)
+    try:
+        assert relmax(ctx.zt_backward(c, 12, 16), ref_b) < SPLIT_TOL
+        assert relmax(ctx.zt_forward(g, 12, 9), ref_f) < SPLIT_TOL
+    finally:
+        ctx.set_precision(zest_gb300.PRECISION_FP64)
+
+
+def test_split_zt_full_size_error_budget(ctx):
+    # the headline workload's accuracy: order 200, split vs FP64 at 1e-11
+    import zest_gb300
+    rng = np.random.default_rng(200)
+    L, batch = 200, 2
+    c = rand_zt(rng, L, batch=batch).ravel()
+    g64 = ctx.zt_backward(c, L, batch=batch)
+    f64 = ctx.zt_forward(g64, L, batch=batch)
+    ctx.set_precision(zest_gb300.PRECISION_SPLIT, 6)
+    try:
+        gs = ctx.zt_backward(c, L, batch=batch)
+        fs = ctx.zt_forward(g64, L, batch=batch)
+    finally:
+        ctx.set_precision(zest_gb300.PRECISION_FP64)
+    for b in range(batch):
+        n = g64.size // batch
+        assert relmax(gs[b * n:(b + 1) * n], g64[b * n:(b + 1) * n]) < SPLIT_TOL
+        k = f64.size // batch
+        assert relmax(fs[b * k:(b + 1) * k], f64[b * k:(b + 1) * k]) < SPLIT_TOL

@@ -91,6 +91,7 @@ _SIGNATURES = {
     "zest_gpu_profile_read": [_vp, _i, _vp, _vp, _i],
     "zest_gpu_profile_stage_count": [],
     "zest_gpu_split_gemm": [_vp, _sz, _sz, _sz, _vp, _vp, _vp, _i],
+    "zest_gpu_profile_flops": [_vp, _i, _vp, _vp],
 }
 _SIZE_FUNCS = {
     "zest_gpu_zt_grid_size": [_sz],
@@ -208,6 +209,13 @@ class Context:
 
     def profile(self, enable: bool = True):
         _check(self.lib.zest_gpu_profile_enable(self._h, int(enable)))
+
+    def profile_flops(self, reset: bool = True):
+        """(useful, issued) BF16 tensor flops of the split products since the last reset."""
+        u = ctypes.c_double(0.0)
+        i = ctypes.c_double(0.0)
+        _check(self.lib.zest_gpu_profile_flops(self._h, int(reset), ctypes.byref(u), ctypes.byref(i)))
+        return u.value, i.value
 
     def profile_read(self, reset: bool = True) -> dict:
         """{stage: (milliseconds, count)} accumulated since the last reset."""

@@ -5,21 +5,25 @@
 // Legendre sums and the radial sums -- is evaluated as
 //     C[r, n] = sum_k A[r, k] B[n, k]
 // with FP64 operands represented exactly enough in BF16 fixed-point slices:
-//   * each operand row gets an exponent e (|x| < 2^e over the row) and its
-//     values are rounded to v = round(x 2^{7S - e}), |v| <= 2^{7S};
-//   * v is cut into S signed base-128 digits d_s (|d_s| <= 128), each exact
-//     in BF16: x = 2^{e - 7S} sum_s d_s 128^{S-1-s};
-//   * the products d_s(A) d_t(B) with s + t = level <= S-1 accumulate in one
-//     FP32 TMEM accumulator per level.  Products are integers <= 2^14, so a
-//     level with (level+1) products is exact while (level+1) K 2^14 <= 2^24:
-//     levels 0..3 are exact for K <= 256; the rounding of deeper levels is
-//     below 2^-45 relative to the result;
-//   * the epilogue recombines the levels by integer Horner in int64
-//     (T = sum_level 128^{S-1-level} acc_level) and builds the FP64 result
-//     2^{eA + eB - 7S - 7} T with integer operations only.
+//   * each operand row gets an exponent e (|x| < 2^(e-1) over the row) and
+//     its values are rounded to v = round(x 2^{7S - e}), |v| <= 2^{7S-1};
+//   * v is cut into S balanced base-128 digits d_s in [-64, 63] (the leading
+//     one in [-65, 65]), each exact in BF16: x = 2^{e - 7S} sum_s d_s 128^{S-1-s};
+//   * the products d_s(A) d_t(B) with s + t = level <= S accumulate in one
+//     FP32 TMEM accumulator per level (S+1 levels, S(S+1)/2 + S-1 products).
+//     Products are integers of magnitude <= 65^2 < 2^12.05, so a level with
+//     p products is exact while p K 65^2 <= 2^24: levels 0..3 are exact for
+//     K <= 992; deeper levels weigh <= 2^-28 of level 0, so their FP32
+//     rounding is below 2^-50 of the result.  Keeping level S (and not only
+//     0..S-1) makes the dropped terms (levels > S, <= 2^12 2^-7(S+1) each)
+//     negligible next to the 2^-7S representation error;
+//   * the epilogue recombines the levels by integer Horner (int64, the last
+//     step in 128 bits: T = sum_level 128^{S-level} acc_level) and builds the
+//     FP64 result 2^{eA + eB - 7S - 14} T with integer operations only.
 // Only the tables (P_lm, R_nl, cos/sin) are prepared in FP64; the FFT,
 // Legendre and radial arithmetic of the forward and backward transforms runs
-// on the tensor cores.  S = 6 keeps 42 bits per operand and 21 products.
+// on the tensor cores.  S = 6 keeps 41 bits per operand and 26 products
+// (about 1e-12 relative error per product against FP64).
 //
 // Kernel: warp-specialised, persistent, one CTA per SM.  Warp 0 issues TMA
 // loads (SWIZZLE_32B, one 16-wide K block of all S slices of A and B per
@@ -160,12 +164,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
            | ((uint32_t)(M >> 4) << 24);   // M / 16
 }
 
-// 2^E * T for an integer T with |T| < 2^63, assembled with integer operations
+// (-1)^neg 2^E a for a 64-bit magnitude a, assembled with integer operations
 // (round to nearest even to 53 bits; results below the normal range flush to 0).
-__device__ __forceinline__ double i64_ldexp(long long T, int E) {
-    if (T == 0) return 0.0;
-    const unsigned long long sgn = T < 0 ? (1ull << 63) : 0ull;
-    unsigned long long a = T < 0 ? (unsigned long long)(-T) : (unsigned long long)T;
+__device__ __forceinline__ double u64_ldexp(unsigned long long a, bool neg, int E) {
+    if (a == 0) return 0.0;
+    const unsigned long long sgn = neg ? (1ull << 63) : 0ull;
     int lz = __clzll((long long)a);
     unsigned long long n = a << lz;
     unsigned long long mant = n >> 11;
@@ -183,7 +186,19 @@ __device__ __forceinline__ double i64_ldexp(long long T, int E) {
     return __longlong_as_double((long long)(sgn | ((unsigned long long)biased << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
-// fixed point: round(x 2^{7S-e}) as int64 (|x| < 2^e)
+// 2^E (128 hi + lo) for |hi| < 2^62: the last Horner step in 128-bit integers.
+__device__ __forceinline__ double horner_ldexp(long long hi, int lo, int E) {
+    const __int128 T = (__int128)hi * 128 + lo;
+    const bool neg = T < 0;
+    const unsigned __int128 a = neg ? (unsigned __int128)(-T) : (unsigned __int128)T;
+    const unsigned long long top = (unsigned long long)(a >> 64);
+    if (top == 0) return u64_ldexp((unsigned long long)a, neg, E);
+    const int extra = 64 - __clzll((long long)top);                  // bits above 64
+    const unsigned long long sticky = ((unsigned long long)a & ((1ull << extra) - 1)) ? 1ull : 0ull;
+    return u64_ldexp((unsigned long long)(a >> extra) | sticky, neg, E + extra);
+}
+
+// fixed point: round(x 2^{7S-e}) as int64 (|x| < 2^(e-1)), ties to even
 __device__ __forceinline__ long long to_fixed(double x, int e, int S) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
     const int E = int((bits >> 52) & 0x7FF);
@@ -191,9 +206,14 @@ __device__ __forceinline__ long long to_fixed(double x, int e, int S) {
     const unsigned long long M = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     const int sh = 1075 + e - 7 * S - E;
     long long v;
-    if (sh >= 63) v = 0;
-    else if (sh > 0) v = (long long)((M + (1ull << (sh - 1))) >> sh);
-    else v = (long long)(M << (-sh));
+    if (sh >= 63) {
+        v = 0;
+    } else if (sh > 0) {  // round to nearest, ties to even
+        const unsigned long long q = M >> sh, rem = M & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+        v = (long long)(q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull));
+    } else {
+        v = (long long)(M << (-sh));
+    }
     return (bits >> 63) ? -v : v;
 }
 
@@ -208,8 +228,12 @@ __device__ __forceinline__ int biased_exp(double x) {
 // ===========================================================================
 namespace {
 
-constexpr int SL_ROWS = 16;
-constexpr int SL_KMAX = 256;
+constexpr int SL_KMAX = 992;  // K bound of exact level sums (balanced 7-bit digits)
+
+inline int slice_rows_per_block(int K) {
+    int r = 4096 / (K > 0 ? K : 1);
+    return r < 2 ? 2 : (r > 16 ? 16 : r);
+}
 
 // Loaders return the pair (up, dn) of operand element (row, k); the folded
 // operands are fix(up) + fix(dn) (fold = 1) or fix(up) - fix(dn) (fold = 2),
@@ -316,57 +340,70 @@ struct DftBwdLoader {  // rows (b, col); cos: Re F_m; sin: Im F_{k+1}
     }
 };
 
+// One CTA converts R rows (R = slice_rows_per_block(K)) of K values: the
+// FP64 values are staged in shared memory (dynamic: 2 R K doubles) while the
+// row maxima are found, then every value is rounded to the row's fixed-point
+// grid, folded exactly in integers where requested, and split into balanced
+// base-128 digits, written as S BF16 slices.
 template <class Loader>
-__global__ void __launch_bounds__(256) slice_kernel(Loader ld, long long rows, int K, int Kp, int S, int fold,
+__global__ void __launch_bounds__(256) slice_kernel(Loader ld, long long rows, int K, int Kp, int S, int fold, int R,
                                                     __nv_bfloat16* __restrict__ out, long long slice_stride,
                                                     int* __restrict__ ex) {
-    __shared__ double vu[SL_ROWS][SL_KMAX];
-    __shared__ double vd[SL_ROWS][SL_KMAX];
-    __shared__ int emax[SL_ROWS];
-    const long long row0 = (long long)blockIdx.x * SL_ROWS;
-    if (threadIdx.x < SL_ROWS) emax[threadIdx.x] = 0;
+    extern __shared__ double sl_smem[];
+    double* vu = sl_smem;
+    double* vd = sl_smem + (size_t)R * K;
+    __shared__ int emax[16];
+    const long long row0 = (long long)blockIdx.x * R;
+    if (threadIdx.x < 16) emax[threadIdx.x] = 0;
     __syncthreads();
-    for (int e = threadIdx.x; e < SL_ROWS * K; e += blockDim.x) {
+    for (int e = threadIdx.x; e < R * K; e += blockDim.x) {
         int r, k;
-        if (Loader::ROW_FAST) { r = e % SL_ROWS; k = e / SL_ROWS; }
+        if (Loader::ROW_FAST) { r = e % R; k = e / R; }
         else { k = e % K; r = e / K; }
         double up = 0.0, dn = 0.0;
         if (row0 + r < rows) ld.get(row0 + r, k, up, dn);
-        vu[r][k] = up;
-        vd[r][k] = dn;
+        vu[r * K + k] = up;
+        vd[r * K + k] = dn;
         const int ee = max(biased_exp(up), biased_exp(dn));
         if (ee) atomicMax(&emax[r], ee);
     }
     __syncthreads();
     const int hk = Kp >> 1;  // pairs of k per row
-    for (int e = threadIdx.x; e < SL_ROWS * hk; e += blockDim.x) {
+    for (int e = threadIdx.x; e < R * hk; e += blockDim.x) {
         const int r = e / hk, k = (e - r * hk) * 2;
         const long long row = row0 + r;
         if (row >= rows) continue;
-        const int er = emax[r] - 1022 + (fold ? 1 : 0);
+        // |x| < 2^(E_max - 1022); one more bit of headroom for the balanced
+        // leading digit, and one for a folded sum
+        const int er = emax[r] - 1022 + 1 + (fold ? 1 : 0);
         long long v[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             const int kk = k + q;
             long long x = 0;
             if (kk < K) {
-                x = to_fixed(vu[r][kk], er, S);
-                if (fold == 1) x += to_fixed(vd[r][kk], er, S);
-                else if (fold == 2) x -= to_fixed(vd[r][kk], er, S);
+                x = to_fixed(vu[r * K + kk], er, S);
+                if (fold == 1) x += to_fixed(vd[r * K + kk], er, S);
+                else if (fold == 2) x -= to_fixed(vd[r * K + kk], er, S);
             }
             v[q] = x;
         }
-        const unsigned long long a0 = v[0] < 0 ? (unsigned long long)(-v[0]) : (unsigned long long)v[0];
-        const unsigned long long a1 = v[1] < 0 ? (unsigned long long)(-v[1]) : (unsigned long long)v[1];
+        int dg[2][8];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            long long w = v[q];
+            for (int s = S - 1; s >= 1; --s) {
+                int rem = int(w & 127);
+                if (rem >= 64) rem -= 128;
+                dg[q][s] = rem;
+                w = (w - rem) >> 7;
+            }
+            dg[q][0] = int(w);
+        }
         for (int s = 0; s < S; ++s) {
-            const int shift = 7 * (S - 1 - s);
-            int d0 = int(s == 0 ? (a0 >> shift) : ((a0 >> shift) & 127ull));
-            int d1 = int(s == 0 ? (a1 >> shift) : ((a1 >> shift) & 127ull));
-            if (v[0] < 0) d0 = -d0;
-            if (v[1] < 0) d1 = -d1;
             __nv_bfloat162 pr;
-            pr.x = __float2bfloat16_rn(float(d0));
-            pr.y = __float2bfloat16_rn(float(d1));
+            pr.x = __float2bfloat16_rn(float(dg[0][s]));
+            pr.y = __float2bfloat16_rn(float(dg[1][s]));
             *reinterpret_cast<__nv_bfloat162*>(out + s * slice_stride + row * Kp + k) = pr;
         }
         if (k == 0) ex[row] = er;
@@ -495,7 +532,7 @@ struct SplitParams {
     int* err;
 };
 
-template <int S, int NT, class Epi>
+template <int S, int NT, class Epi>  // S slices, S+1 levels, NT table rows per tile
 __global__ void __launch_bounds__(SP_THREADS, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUtensorMap mapA1,
                       const __grid_constant__ CUtensorMap mapB0, const __grid_constant__ CUtensorMap mapB1,
@@ -505,7 +542,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     constexpr int STAGE = S * (A_TILE + B_TILE);
     constexpr uint32_t TX = S * (SP_M * 32 + NT * 32);
     constexpr uint32_t IDESC = idesc_bf16_f32(SP_M, NT);
-    static_assert(S * NT <= 512, "levels must fit in TMEM");
+    static_assert((S + 1) * NT <= 512, "levels must fit in TMEM");
 
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -583,12 +620,13 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                     const uint32_t sa = smem_u32(smem + st * STAGE);
                     const uint32_t sb = sa + S * A_TILE;
 #pragma unroll
-                    for (int d = 0; d < S; ++d) {
+                    for (int d = 0; d <= S; ++d) {
+                        const int s0 = d < S ? 0 : 1;
 #pragma unroll
-                        for (int s = 0; s <= d; ++s) {
+                        for (int s = s0; s <= d && s < S; ++s) {
                             const int t = d - s;
                             umma_bf16(tmem + d * NT, desc_sw32(sa + s * A_TILE), desc_sw32(sb + t * B_TILE), IDESC,
-                                      (kb > 0 || s > 0) ? 1u : 0u);
+                                      (kb > 0 || s > s0) ? 1u : 0u);
                         }
                     }
                     umma_commit(&empty[st]);
@@ -614,23 +652,28 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             const int ea = rv ? P.ea[amap][row] : 0;
             for (int c0 = half * (NT / 2); c0 < (half + 1) * (NT / 2); c0 += 8) {
                 long long T[8];
+                int last[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) T[j] = 0;
 #pragma unroll
-                for (int d = 0; d < S; ++d) {
+                for (int d = 0; d <= S; ++d) {
                     uint32_t v[8];
                     tmem_ld8(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(d * NT + c0), v);
                     tmem_ld_wait();
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) T[j] = T[j] * 128 + (long long)__float2int_rn(__uint_as_float(v[j]));
+                    for (int j = 0; j < 8; ++j) {
+                        const int a = __float2int_rn(__uint_as_float(v[j]));
+                        if (d < S) T[j] = T[j] * 128 + a;
+                        else last[j] = a;
+                    }
                 }
                 if (rv) {
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         const int n = c0 + j;
                         if (n < u.n) {
-                            const int E = ea + P.eb[bmap][u.b_row0 + n] - 7 * S - 7;
-                            epi(u, row, n, i64_ldexp(T[j], E));
+                            const int E = ea + P.eb[bmap][u.b_row0 + n] - 7 * S - 14;
+                            epi(u, row, n, horner_ldexp(T[j], last[j], E));
                         }
                     }
                 }
@@ -699,7 +742,8 @@ int make_map(CUtensorMap* map, const void* base, long long rows, int Kp, int S, 
 
 inline int r16(int k) { return (k + 15) & ~15; }
 
-int n_tile(int S) { return S == 4 ? 128 : (S == 5 ? 96 : 80); }
+// table rows per tile: S+1 level accumulators of NT columns fill the 512 TMEM columns
+int n_tile(int S) { return S == 4 ? 96 : (S == 5 ? 80 : 64); }
 
 }  // namespace
 
@@ -726,13 +770,21 @@ struct ZtSplitTables {
     SliceArray dft_cos_f, dft_sin_f, leg_f, rad_f, rad_bT, leg_bT, dft_cos_b, dft_sin_b;
 };
 
+// Work list of one GEMM launch, with its tensor-core work.
+struct UnitList {
+    std::vector<SplitUnit> v;
+    double useful = 0.0;  // 2 * rows * table rows * K * products, valid tiles only
+    double issued = 0.0;  // the same for full 128 x NT x 16k tiles
+    DevBuf dev;
+};
+
 struct SplitState {
-    int err_init = 0;
     DevBuf err;                 // device error flag of the GEMM kernels
     SliceArray op[2];           // data operands of the current stage
     std::map<std::tuple<const void*, int>, std::unique_ptr<ZtSplitTables>> zt_tables;  // per (plan, S)
-    std::map<std::tuple<int, int, int, int, int>, std::pair<std::unique_ptr<DevBuf>, int>> units;
+    std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<UnitList>> units;  // cached work lists
     DevBuf tmp;                 // FP64 staging of generated tables
+    double useful_flops = 0.0, issued_flops = 0.0;  // accumulated while profiling
 };
 
 void destroy_split(SplitState* s) { delete s; }
@@ -742,10 +794,13 @@ namespace {
 template <class Loader>
 int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S, int fold, SliceArray& out) {
     if (rows <= 0) return ZEST_GPU_OK;
-    if (K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: K above 256");
-    const long long blocks = (rows + SL_ROWS - 1) / SL_ROWS;
-    slice_kernel<Loader><<<(unsigned)blocks, 256, 0, s>>>(ld, rows, K, out.Kp, S, fold, out.ptr(), rows * out.Kp,
-                                                         out.ex.as<int>());
+    if (K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: K above 992");
+    const int R = slice_rows_per_block(K);
+    const size_t smem = (size_t)2 * R * K * sizeof(double);
+    ZG_CUDA_TRY(cudaFuncSetAttribute(slice_kernel<Loader>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    const long long blocks = (rows + R - 1) / R;
+    slice_kernel<Loader><<<(unsigned)blocks, 256, smem, s>>>(ld, rows, K, out.Kp, S, fold, R, out.ptr(),
+                                                            rows * out.Kp, out.ex.as<int>());
     return launch_check("slice_kernel");
 }
 
@@ -864,8 +919,9 @@ int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, 
 }
 
 template <int S, int NT, class Epi>
-int run_gemm_t(zest_gpu_context* ctx, const std::vector<SplitUnit>& units, const SliceArray& A0,
-               const SliceArray& A1, const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
+int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const SliceArray& A1, const SliceArray& B0,
+               const SliceArray& B1, const Epi& epi) {
+    const std::vector<SplitUnit>& units = ul.v;
     if (units.empty()) return ZEST_GPU_OK;
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
@@ -875,12 +931,17 @@ int run_gemm_t(zest_gpu_context* ctx, const std::vector<SplitUnit>& units, const
     ZG_TRY(make_map(&ma1, A1.ptr(), A1.rows, A1.Kp, S, SP_M));
     ZG_TRY(make_map(&mb0, B0.ptr(), B0.rows, B0.Kp, S, NT));
     ZG_TRY(make_map(&mb1, B1.ptr(), B1.rows, B1.Kp, S, NT));
-    // units are uploaded once per distinct list (cached by content size + first entries)
-    DevBuf ubuf;
-    ZG_TRY(ubuf.ensure(units.size() * sizeof(SplitUnit)));
-    ZG_CUDA_TRY(cudaMemcpyAsync(ubuf.p, units.data(), units.size() * sizeof(SplitUnit), cudaMemcpyHostToDevice, s));
+    if (!ul.dev.p) {  // work lists are uploaded once and cached with their key
+        ZG_TRY(ul.dev.ensure(units.size() * sizeof(SplitUnit)));
+        ZG_CUDA_TRY(cudaMemcpyAsync(ul.dev.p, units.data(), units.size() * sizeof(SplitUnit),
+                                    cudaMemcpyHostToDevice, s));
+    }
+    if (ctx->prof.on) {
+        st->useful_flops += ul.useful;
+        st->issued_flops += ul.issued;
+    }
     SplitParams P;
-    P.units = ubuf.as<SplitUnit>();
+    P.units = ul.dev.as<SplitUnit>();
     P.nunits = int(units.size());
     P.a_rows_total[0] = int(A0.rows);
     P.a_rows_total[1] = int(A1.rows);
@@ -902,7 +963,7 @@ int run_gemm_t(zest_gpu_context* ctx, const std::vector<SplitUnit>& units, const
         split_gemm_kernel<S, NT, Epi><<<grid, SP_THREADS, smem, s>>>(ma0, ma1, mb0, mb1, P, epi);
         ZG_TRY(launch_check("split_gemm_kernel"));
     }
-    // the unit list must outlive the kernel
+    // surface a bounded-wait timeout of this launch to the caller
     ZG_CUDA_TRY(cudaStreamSynchronize(s));
     int herr = 0;
     ZG_CUDA_TRY(cudaMemcpy(&herr, st->err.p, sizeof(int), cudaMemcpyDeviceToHost));
@@ -913,21 +974,40 @@ int run_gemm_t(zest_gpu_context* ctx, const std::vector<SplitUnit>& units, const
     return ZEST_GPU_OK;
 }
 
+inline int products(int S) { return S * (S + 1) / 2 + S - 1; }
+
+// Returns the cached work list of `key`, built by `build` on first use.
+template <class Build>
+int get_units(zest_gpu_context* ctx, std::tuple<int, int, int, int, int, int> key, Build&& build, UnitList** out) {
+    SplitState* st;
+    ZG_TRY(get_state(ctx, &st));
+    auto it = st->units.find(key);
+    if (it == st->units.end()) {
+        auto ul = std::make_unique<UnitList>();
+        build(*ul);
+        it = st->units.emplace(key, std::move(ul)).first;
+    }
+    *out = it->second.get();
+    return ZEST_GPU_OK;
+}
+
 template <class Epi>
-int run_gemm(zest_gpu_context* ctx, int S, const std::vector<SplitUnit>& units, const SliceArray& A0,
-             const SliceArray& A1, const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
+int run_gemm(zest_gpu_context* ctx, int S, UnitList& ul, const SliceArray& A0, const SliceArray& A1,
+             const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
     switch (S) {
-    case 4: return run_gemm_t<4, 128>(ctx, units, A0, A1, B0, B1, epi);
-    case 5: return run_gemm_t<5, 96>(ctx, units, A0, A1, B0, B1, epi);
-    case 6: return run_gemm_t<6, 80>(ctx, units, A0, A1, B0, B1, epi);
+    case 4: return run_gemm_t<4, 96>(ctx, ul, A0, A1, B0, B1, epi);
+    case 5: return run_gemm_t<5, 80>(ctx, ul, A0, A1, B0, B1, epi);
+    case 6: return run_gemm_t<6, 64>(ctx, ul, A0, A1, B0, B1, epi);
     }
     return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path supports 4..6 slices");
 }
 
-// tiles of a group: operand rows [a0, a0 + arows) x table rows [b0, b0 + nrows)
-void add_units(std::vector<SplitUnit>& v, long long a0, long long arows, int b0, int nrows, int NT, int ksteps,
-               int flags, int g) {
-    if (arows <= 0 || nrows <= 0 || ksteps <= 0) return;
+// tiles of a group: operand rows [a0, a0 + arows) x table rows [b0, b0 + nrows), K = kk
+void add_units(UnitList& ul, int S, long long a0, long long arows, int b0, int nrows, int NT, int kk, int flags,
+               int g) {
+    if (arows <= 0 || nrows <= 0 || kk <= 0) return;
+    const int ksteps = r16(kk) / 16;
+    const double P = products(S);
     for (long long r = 0; r < arows; r += SP_M)
         for (int c = 0; c < nrows; c += NT) {
             SplitUnit u;
@@ -939,9 +1019,14 @@ void add_units(std::vector<SplitUnit>& v, long long a0, long long arows, int b0,
             u.flags = flags;
             u.g = g;
             u.aux = c;
-            v.push_back(u);
+            ul.v.push_back(u);
+            ul.useful += 2.0 * u.a_rows * u.n * kk * P;
+            ul.issued += 2.0 * SP_M * NT * 16.0 * ksteps * P;
         }
 }
+
+// work-list keys: (stage, Lg, Lm, batch, S, pass)
+enum { WK_DFT_F = 0, WK_LEG_F, WK_RAD_F, WK_RAD_B, WK_LEG_B, WK_DFT_B, WK_DENSE };
 
 }  // namespace
 
@@ -967,7 +1052,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
     if (Lg < 2 || Lg > SL_KMAX || plan.sh.nrad > SL_KMAX)
-        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: orders 2..255");
+        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: orders 2..983");
     ZtSplitTables* tb;
     ZG_TRY(build_zt_tables(ctx, st, plan, S, &tb));
     const ZtShape& sh = plan.sh;
@@ -990,12 +1075,14 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
             ZG_TRY(launch_slice(s, DftFwdLoader{grids, sh.size(), C, N, 0}, rows, Lg, S, 1, st->op[0]));
             if (Lg > 1) ZG_TRY(launch_slice(s, DftFwdLoader{grids, sh.size(), C, N, 1}, rows, Lg - 1, S, 2, st->op[1]));
         }
-        std::vector<SplitUnit> u;
-        for (long long r = 0; r < rows; r += SP_M) {
-            add_units(u, r, std::min<long long>(SP_M, rows - r), 0, Lm, NT, r16(Lg) / 16, 0, 0);
-            if (Lm > 1) add_units(u, r, std::min<long long>(SP_M, rows - r), 0, Lm - 1, NT, r16(Lg - 1) / 16, 1 | 2, 0);
-        }
-        ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[1], tb->dft_cos_f, tb->dft_sin_f, EpiDftFwd{G, C, Lg}));
+        UnitList* u;
+        ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
+            for (long long r = 0; r < rows; r += SP_M) {
+                add_units(ul, S, r, std::min<long long>(SP_M, rows - r), 0, Lm, NT, Lg, 0, 0);
+                if (Lm > 1) add_units(ul, S, r, std::min<long long>(SP_M, rows - r), 0, Lm - 1, NT, Lg - 1, 1 | 2, 0);
+            }
+        }, &u));
+        ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_f, tb->dft_sin_f, EpiDftFwd{G, C, Lg}));
     }
     // ---- Legendre (folded over the equator) ----
     {
@@ -1009,14 +1096,16 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
             ZG_TRY(launch_slice(s, ld, rows, kh, S, 1, st->op[0]));
             ZG_TRY(launch_slice(s, ld, rows, kh, S, 2, st->op[1]));
         }
-        std::vector<SplitUnit> u;
-        for (int m = 0; m < Lm; ++m)
-            for (int p = 0; p < 2; ++p) {
-                const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
-                add_units(u, (long long)m * per_m, per_m, int(plan.leg.off_h[2 * m + p]), cnt, NT, r16(kh) / 16,
-                          p | (p << 2), m);
-            }
-        ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd{flm, batch, nr2}));
+        UnitList* u;
+        ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
+            for (int m = 0; m < Lm; ++m)
+                for (int p = 0; p < 2; ++p) {
+                    const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
+                    add_units(ul, S, (long long)m * per_m, per_m, int(plan.leg.off_h[2 * m + p]), cnt, NT, kh,
+                              p | (p << 2), m);
+                }
+        }, &u));
+        ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd{flm, batch, nr2}));
     }
     // ---- radial ----
     {
@@ -1026,11 +1115,13 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
             StageScope sc(ctx, ST_SPLIT_SLICE);
             ZG_TRY(launch_slice(s, RadFwdLoader{flm, nr}, rows, nr, S, 0, st->op[0]));
         }
-        std::vector<SplitUnit> u;
-        for (int l = 0; l < Lm; ++l)
-            add_units(u, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, int(plan.rad.off_h[l]),
-                      (Lm - l + 1) / 2, NT, r16(nr) / 16, 0, l);
-        ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd{coeffs, batch, csz}));
+        UnitList* u;
+        ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
+            for (int l = 0; l < Lm; ++l)
+                add_units(ul, S, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, int(plan.rad.off_h[l]),
+                          (Lm - l + 1) / 2, NT, nr, 0, l);
+        }, &u));
+        ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd{coeffs, batch, csz}));
     }
     return ZEST_GPU_OK;
 }
@@ -1043,7 +1134,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
     if (Lg < 2 || Lg > SL_KMAX || plan.sh.nrad > SL_KMAX)
-        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: orders 2..255");
+        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: orders 2..983");
     ZtSplitTables* tb;
     ZG_TRY(build_zt_tables(ctx, st, plan, S, &tb));
     const ZtShape& sh = plan.sh;
@@ -1064,11 +1155,13 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             StageScope sc(ctx, ST_SPLIT_SLICE);
             ZG_TRY(launch_slice(s, RadBwdLoader{coeffs, csz, batch, Lm}, rows, (Lm + 1) / 2, S, 0, st->op[0]));
         }
-        std::vector<SplitUnit> u;
-        for (int l = 0; l < Lm; ++l)
-            add_units(u, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, l * nr, nr, NT,
-                      r16((Lm - l + 1) / 2) / 16, 0, l);
-        ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd{flm, nr}));
+        UnitList* u;
+        ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_B), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
+            for (int l = 0; l < Lm; ++l)
+                add_units(ul, S, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, l * nr, nr, NT,
+                          (Lm - l + 1) / 2, 0, l);
+        }, &u));
+        ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd{flm, nr}));
     }
     // ---- Legendre: flm -> G (north/south unfold; parity 1 read-modify-write) ----
     {
@@ -1087,13 +1180,15 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                                           (size_t)(Lg - Lm) * C * 2 * sizeof(double), batch, s));
         }
         for (int p = 0; p < 2; ++p) {
-            std::vector<SplitUnit> u;
-            for (int m = 0; m < Lm; ++m) {
-                const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
-                if (cnt == 0) continue;
-                add_units(u, (long long)m * per_m, per_m, (2 * m + p) * kh, kh, NT, r16(cnt) / 16, p | (p << 2), m);
-            }
-            ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
+            UnitList* u;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_B), Lg, Lm, batch, S, p), [&](UnitList& ul) {
+                for (int m = 0; m < Lm; ++m) {
+                    const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
+                    if (cnt == 0) continue;
+                    add_units(ul, S, (long long)m * per_m, per_m, (2 * m + p) * kh, kh, NT, cnt, p | (p << 2), m);
+                }
+            }, &u));
+            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
                             EpiLegBwd{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d}));
         }
     }
@@ -1107,16 +1202,20 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             ZG_TRY(launch_slice(s, DftBwdLoader{G, batch, Lg, C, 0}, rows, Lg, S, 0, st->op[0]));
             if (Lg > 1) ZG_TRY(launch_slice(s, DftBwdLoader{G, batch, Lg, C, 1}, rows, Lg - 1, S, 0, st->op[1]));
         }
-        std::vector<SplitUnit> u;
-        for (long long r = 0; r < rows; r += SP_M)
-            add_units(u, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, r16(Lg) / 16, 0, 0);
-        ZG_TRY(run_gemm(ctx, S, u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
+        UnitList* u;
+        ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
+            for (long long r = 0; r < rows; r += SP_M)
+                add_units(ul, S, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, Lg, 0, 0);
+        }, &u));
+        ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
                         EpiDftBwd{grids, C, N, sh.size()}));
         if (Lg > 1) {
-            std::vector<SplitUnit> v;
-            for (long long r = 0; r < rows; r += SP_M)
-                add_units(v, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT, r16(Lg - 1) / 16, 1 | 2 | 4, 0);
-            ZG_TRY(run_gemm(ctx, S, v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
+            UnitList* v;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 1), [&](UnitList& ul) {
+                for (long long r = 0; r < rows; r += SP_M)
+                    add_units(ul, S, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT, Lg - 1, 1 | 2 | 4, 0);
+            }, &v));
+            ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
                             EpiDftBwd{grids, C, N, sh.size()}));
         }
     }
@@ -1128,7 +1227,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
 int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A, const double* B, double* C) {
     const int S = ctx->slices;
     const int NT = n_tile(S);
-    if (K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split GEMM: K above 256");
+    if (K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split GEMM: K above 992");
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
     SliceArray a, b;
@@ -1136,9 +1235,16 @@ int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A
     ZG_TRY(b.ensure(N, r16(K), S));
     ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{A, K}, M, K, S, 0, a));
     ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{B, K}, N, K, S, 0, b));
-    std::vector<SplitUnit> u;
-    add_units(u, 0, M, 0, N, NT, r16(K) / 16, 0, 0);
+    UnitList u;
+    add_units(u, S, 0, M, 0, N, NT, K, 0, 0);
     return run_gemm(ctx, S, u, a, a, b, b, EpiDense{C, N});
+}
+
+void split_flops(zest_gpu_context* ctx, bool reset, double* useful, double* issued) {
+    SplitState* st = ctx->split.get();
+    if (useful) *useful = st ? st->useful_flops : 0.0;
+    if (issued) *issued = st ? st->issued_flops : 0.0;
+    if (reset && st) st->useful_flops = st->issued_flops = 0.0;
 }
 
 }  // namespace zgpu

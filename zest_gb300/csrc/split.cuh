@@ -21,5 +21,9 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                       double* grids);
 // C = A B^T (A: M x K, B: N x K, C: M x N, row-major FP64 device buffers)
 int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A, const double* B, double* C);
+// BF16 tensor-core flops of the split GEMM launches since the last reset
+// (counted while profiling is enabled): useful = valid rows x table rows x K,
+// issued = whole 128-row tiles as executed.
+void split_flops(zest_gpu_context* ctx, bool reset, double* useful, double* issued);
 
 }  // namespace zgpu

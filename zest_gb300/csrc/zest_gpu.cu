@@ -656,6 +656,12 @@ int zest_gpu_profile_read(zest_gpu_context* ctx, int reset, double* ms, long lon
 }
 
 const char* zest_gpu_profile_stage_name(int stage) { return stage_name(stage); }
+
+int zest_gpu_profile_flops(zest_gpu_context* ctx, int reset, double* useful, double* issued) {
+    ZG_TRY(check_ctx(ctx));
+    split_flops(ctx, reset != 0, useful, issued);
+    return ZEST_GPU_OK;
+}
 int zest_gpu_profile_stage_count(void) { return ST_COUNT; }
 unsigned long long zest_gpu_launch_count(void) { return g_launches.load(); }
 
@@ -764,7 +770,7 @@ int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch, 
 int zest_gpu_split_gemm(zest_gpu_context* ctx, size_t M, size_t N, size_t K, const double* A, const double* B,
                         double* C, int mem) {
     ZG_TRY(check_ctx(ctx));
-    if (M > (1u << 24) || N > (1u << 20) || K > 256) return fail(ZEST_GPU_ERR_INVALID, "split GEMM size out of range");
+    if (M > (1u << 24) || N > (1u << 20) || K > 992) return fail(ZEST_GPU_ERR_INVALID, "split GEMM size out of range");
     if ((M * K && !A) || (N * K && !B) || (M * N && !C)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
     if (M == 0 || N == 0) return ZEST_GPU_OK;
     if (mem == ZEST_MEM_DEVICE) return split_dense_gemm(ctx, int(M), int(N), int(K), A, B, C);
