@@ -287,18 +287,28 @@ def main():
 
     flops = zt_flops_per_function(L)
     peaks = measured_peaks()
+    def relerr(x, ref):
+        return float(((x - ref).abs().reshape(B, -1).amax(1) / ref.abs().reshape(B, -1).amax(1)).max())
+
+    errors = None
     if precision == "split":
         ctx.set_precision(zg.PRECISION_SPLIT, args.slices)
         sampler = ClockSampler(local_rank)
         ms, prof, launches, clocks, tflops = timed(args.steps, args.warmup, sampler)
-        err_c = float(((cbuf - ref_coeffs).abs().reshape(B, -1).amax(1)
-                       / ref_coeffs.abs().reshape(B, -1).amax(1)).max())
-        err_g = float(((gout - ref_grids).abs().reshape(B, -1).amax(1)
-                       / ref_grids.abs().reshape(B, -1).amax(1)).max())
+        err_rt = relerr(gout, ref_grids)          # split fwd -> split bwd vs fp64 fwd -> fp64 bwd
+        # each transform on identical inputs: forward of the same grids, backward of the same coefficients
+        ctx.zt_forward(grids_d, L, batch=B, out=cbuf)
+        err_c = relerr(cbuf, ref_coeffs)
+        ctx.zt_backward(ref_coeffs, L, batch=B, out=gout)
+        ctx.set_precision(zg.PRECISION_FP64)
+        g64 = ctx.zt_backward(ref_coeffs, L, batch=B)
+        err_g = relerr(gout, g64)
+        del g64
+        errors = {"forward_coeffs": err_c, "backward_grid": err_g, "roundtrip_grid": err_rt,
+                  "measure": "max over the batch of max|x - x_fp64| / max|x_fp64| per function"}
         dtype = "bf16-slices (7-bit fixed point), fp32 exact partial sums, fp64 recombination"
     else:
         ms, prof, launches, clocks, tflops = ms64, prof64, launches64, clocks64, (0.0, 0.0)
-        err_c = err_g = 0.0
         dtype = "f64"
     value = world * B * args.steps / (ms * 1e-3)
 
@@ -329,6 +339,8 @@ def main():
 
     # ---- end to end through the C-ABI with pinned host buffers ----
     e2e = None
+    if precision == "split":
+        ctx.set_precision(zg.PRECISION_SPLIT, args.slices)
     if not args.no_e2e:
         gh = torch.empty(B * gsz, dtype=torch.float64, pin_memory=True)
         gh.copy_(grids_d.cpu())
@@ -376,7 +388,7 @@ def main():
             "fp64_gpu": {"value": result["fp64"]["value"], "ms_per_step": result["fp64"]["ms_per_step"],
                          "stages_ms": result["fp64"]["stages_ms"]},
             "split_vs_fp64": value / result["fp64"]["value"] if precision == "split" else None,
-            "max_rel_err_vs_fp64": {"coeffs": err_c, "grid": err_g} if precision == "split" else None,
+            "max_rel_err_vs_fp64": errors,
             "stages_ms": stage_ms, "stage_launches_per_step": stage_n,
             "canonical_gflop_per_function": flops["total"] / 1e9,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,

@@ -109,15 +109,17 @@ def split_model(A, B, S):
     return T.astype(float) * np.exp2(ea[:, None] + eb[None, :] - 7 * S - 14)
 
 
-@pytest.mark.parametrize("K", [1, 16, 33, 64])
+@pytest.mark.parametrize("K", [1, 16, 33, 64, 208])
 def test_split_gemm_matches_integer_model(split, K):
-    # the kernel computes exactly the model's integer arithmetic (exact level
-    # sums for these sizes), so the results agree to the last bit
+    # levels 0..3 are exact in the kernel and levels 4..6 share one FP32
+    # accumulator (weight <= 2^-28 of level 0): the kernel agrees with the
+    # all-integer model far below the emulation's own error
     rng = np.random.default_rng(100 + K)
     A = rng.normal(size=(130, K)) * np.exp(rng.normal(size=(130, 1)))
     B = rng.normal(size=(70, K))
     C = split.split_gemm(A, B)
-    np.testing.assert_array_equal(C, split_model(A, B, 6))
+    model = split_model(A, B, 6)
+    assert np.max(np.abs(C - model)) <= 1e-13 * np.max(np.abs(model))
 
 
 @pytest.mark.parametrize("L,batch", [(2, 1), (7, 3), (20, 2), (64, 2)])

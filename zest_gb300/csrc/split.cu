@@ -9,34 +9,38 @@
 //     its values are rounded to v = round(x 2^{7S - e}), |v| <= 2^{7S-1};
 //   * v is cut into S balanced base-128 digits d_s in [-64, 63] (the leading
 //     one in [-65, 65]), each exact in BF16: x = 2^{e - 7S} sum_s d_s 128^{S-1-s};
-//   * the products d_s(A) d_t(B) with s + t = level <= S accumulate in one
-//     FP32 TMEM accumulator per level (S+1 levels, S(S+1)/2 + S-1 products).
-//     Products are integers of magnitude <= 65^2 < 2^12.05, so a level with
-//     p products is exact while p K 65^2 <= 2^24: levels 0..3 are exact for
-//     K <= 992; deeper levels weigh <= 2^-28 of level 0, so their FP32
-//     rounding is below 2^-50 of the result.  Keeping level S (and not only
-//     0..S-1) makes the dropped terms (levels > S, <= 2^12 2^-7(S+1) each)
-//     negligible next to the 2^-7S representation error;
-//   * the epilogue recombines the levels by integer Horner (int64, the last
-//     step in 128 bits: T = sum_level 128^{S-level} acc_level) and builds the
-//     FP64 result 2^{eA + eB - 7S - 14} T with integer operations only.
+//   * the products d_s(A) d_t(B) with s + t = level <= S (S(S+1)/2 + S-1
+//     products) accumulate in FP32 TMEM accumulators.  Products are integers
+//     of magnitude <= 65^2 < 2^12.05, so a level with p products is exact
+//     while p K 65^2 <= 2^24: levels 0..3 get their own, exact, accumulators
+//     for K <= 992.  Levels 4..S weigh <= 2^-28 of level 0 and share one
+//     accumulator: their products read table slices pre-scaled by 2^-7 and
+//     2^-14 (exact in BF16), so its FP32 rounding stays below 2^-50 of the
+//     result.  Keeping level S makes the dropped levels > S negligible next
+//     to the 2^-7S representation error;
+//   * the epilogue recombines the five accumulators by integer Horner
+//     (T = 64 sum_a 128^{4-a} acc_a, the exact levels as integers, the shared
+//     one rounded to 2^-6 of its unit; |T| < 2^57 for K <= 992) and builds
+//     the FP64 result 2^{eA + eB - 48} T with integer operations only.
 // Only the tables (P_lm, R_nl, cos/sin) are prepared in FP64; the FFT,
 // Legendre and radial arithmetic of the forward and backward transforms runs
 // on the tensor cores.  S = 6 keeps 41 bits per operand and 26 products
 // (about 1e-12 relative error per product against FP64).
 //
 // Kernel: warp-specialised, persistent, one CTA per SM.  Warp 0 issues TMA
-// loads (SWIZZLE_32B, one 16-wide K block of all S slices of A and B per
-// pipeline stage), warp 1 issues tcgen05.mma (M = 128 operand rows,
-// N = table rows per tile, all S level accumulators resident in TMEM), warps
-// 2..9 read the accumulators back (tcgen05.ld), recombine and store through a
-// stage-specific epilogue.  Every wait is bounded (about 2 s); on timeout the
+// loads (SWIZZLE_32B, one 16-wide K block of all S data slices and the
+// needed table slices per pipeline stage), warp 1 issues tcgen05.mma
+// (M = 128 operand rows, N = 96 table rows per tile, five accumulators
+// resident in TMEM), warps 2..9 read the accumulators back (tcgen05.ld),
+// recombine and store through a stage-specific epilogue.  Every wait is bounded (about 2 s); on timeout the
 // kernel records an error code and winds down instead of hanging.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -186,17 +190,6 @@ __device__ __forceinline__ double u64_ldexp(unsigned long long a, bool neg, int 
     return __longlong_as_double((long long)(sgn | ((unsigned long long)biased << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
-// 2^E (128 hi + lo) for |hi| < 2^62: the last Horner step in 128-bit integers.
-__device__ __forceinline__ double horner_ldexp(long long hi, int lo, int E) {
-    const __int128 T = (__int128)hi * 128 + lo;
-    const bool neg = T < 0;
-    const unsigned __int128 a = neg ? (unsigned __int128)(-T) : (unsigned __int128)T;
-    const unsigned long long top = (unsigned long long)(a >> 64);
-    if (top == 0) return u64_ldexp((unsigned long long)a, neg, E);
-    const int extra = 64 - __clzll((long long)top);                  // bits above 64
-    const unsigned long long sticky = ((unsigned long long)a & ((1ull << extra) - 1)) ? 1ull : 0ull;
-    return u64_ldexp((unsigned long long)(a >> extra) | sticky, neg, E + extra);
-}
 
 // fixed point: round(x 2^{7S-e}) as int64 (|x| < 2^(e-1)), ties to even
 __device__ __forceinline__ long long to_fixed(double x, int e, int S) {
@@ -347,8 +340,8 @@ struct DftBwdLoader {  // rows (b, col); cos: Re F_m; sin: Im F_{k+1}
 // base-128 digits, written as S BF16 slices.
 template <class Loader>
 __global__ void __launch_bounds__(256) slice_kernel(Loader ld, long long rows, int K, int Kp, int S, int fold, int R,
-                                                    __nv_bfloat16* __restrict__ out, long long slice_stride,
-                                                    int* __restrict__ ex) {
+                                                    int copies, __nv_bfloat16* __restrict__ out,
+                                                    long long slice_stride, int* __restrict__ ex) {
     extern __shared__ double sl_smem[];
     double* vu = sl_smem;
     double* vd = sl_smem + (size_t)R * K;
@@ -400,11 +393,14 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, long long rows, i
             }
             dg[q][0] = int(w);
         }
-        for (int s = 0; s < S; ++s) {
-            __nv_bfloat162 pr;
-            pr.x = __float2bfloat16_rn(float(dg[0][s]));
-            pr.y = __float2bfloat16_rn(float(dg[1][s]));
-            *reinterpret_cast<__nv_bfloat162*>(out + s * slice_stride + row * Kp + k) = pr;
+        for (int c = 0; c < copies; ++c) {
+            const float sc = c == 0 ? 1.0f : (c == 1 ? 0.0078125f : 0.00006103515625f);  // 1, 2^-7, 2^-14
+            for (int s = 0; s < S; ++s) {
+                __nv_bfloat162 pr;
+                pr.x = __float2bfloat16_rn(float(dg[0][s]) * sc);
+                pr.y = __float2bfloat16_rn(float(dg[1][s]) * sc);
+                *reinterpret_cast<__nv_bfloat162*>(out + (c * S + s) * slice_stride + row * Kp + k) = pr;
+            }
         }
         if (k == 0) ex[row] = er;
     }
@@ -428,96 +424,144 @@ struct SplitUnit {
 
 namespace {
 
-struct EpiDense {  // C[row][b_row0 + n] (debug / utility GEMM)
+// Epilogues map (operand row, table row) of a tile to an output location.
+// row(u, r) is evaluated once per row and tile; store() once per element.
+// RMW epilogues expose load() so that the old values are fetched before the
+// accumulators are read (hiding the memory latency).
+struct EpiDense {  // C[row][b_row0 + n] (utility GEMM)
+    static constexpr bool RMW = false;
     double* C;
     long long ldc;
-    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
-        C[(long long)row * ldc + u.b_row0 + n] = v;
-    }
+    struct Row { double* p; };
+    __device__ Row row(const SplitUnit& u, int r) const { return Row{C + (long long)r * ldc + u.b_row0}; }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double*) const { R.p[n] = v; }
 };
 struct EpiDftFwd {  // rows (b, col): conj X_m -> G[b][m][col][re, im]
+    static constexpr bool RMW = false;
     double* G;
     int C, L;
-    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
-        const int b = row / C, col = row - b * C;
-        if ((u.flags & 2) == 0) {
-            const int m = u.aux + n;
-            double* g = G + (((long long)b * L + m) * C + col) * 2;
-            g[0] = v;
-            if (m == 0) g[1] = 0.0;
-        } else {
-            const int m = 1 + u.aux + n;
-            G[(((long long)b * L + m) * C + col) * 2 + 1] = v;
-        }
+    struct Row { double* p; };  // &G[b][m0][col][re or im]
+    __device__ Row row(const SplitUnit& u, int r) const {
+        const int b = r / C, col = r - b * C;
+        const int sin = (u.flags >> 1) & 1;
+        const int m0 = u.aux + sin;
+        return Row{G + (((long long)b * L + m0) * C + col) * 2 + sin};
+    }
+    __device__ void store(const Row& R, const SplitUnit& u, int n, double v, const double*) const {
+        double* g = R.p + (long long)n * C * 2;
+        g[0] = v;
+        if (((u.flags >> 1) & 1) == 0 && u.aux + n == 0) g[1] = 0.0;  // Im X_0 = 0
     }
 };
-struct EpiLegFwd {  // rows (m, b, kc) -> flm[tri(l,m)][b][kc]
+struct EpiLegFwd {  // rows (m, b, kc) -> flm[tri(l,m)][b][kc], l = m + p + 2 (aux + n)
+    static constexpr bool RMW = false;
     double* flm;
     int B, nr2;
-    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
+    struct Row { double* p; int m; };
+    __device__ Row row(const SplitUnit& u, int r) const {
         const int m = u.g, p = (u.flags >> 2) & 1;
-        const long long local = row - (long long)m * B * nr2;
-        const int b = int(local / nr2), kc = int(local - (long long)b * nr2);
-        const int l = m + p + 2 * (u.aux + n);
-        flm[(tri_idx(l, m) * B + b) * nr2 + kc] = v;
+        const long long local = r - (long long)m * B * nr2;
+        const int l0 = m + p + 2 * u.aux;
+        return Row{flm + (tri_idx(l0, m) * B) * nr2 + local, m};
+    }
+    __device__ void store(const Row& R, const SplitUnit& u, int n, double v, const double*) const {
+        // tri(l + 2n, m) - tri(l, m) = n (2 l + 2 n + 1), l = l0
+        const int p = (u.flags >> 2) & 1;
+        const long long l0 = R.m + p + 2 * u.aux;
+        const long long dt = (long long)n * (2 * l0 + 2 * n + 1);
+        R.p[dt * B * nr2] = v;
     }
 };
 struct EpiRadFwd {  // rows ((tri(l,m) B + b) 2 + c) -> coeffs[b][zidx(n,l,m)][c]
+    static constexpr bool RMW = false;
     double* coeffs;
     int B;
     long long cs;
-    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
+    struct Row { double* p; long long zl0; };
+    __device__ Row row(const SplitUnit& u, int r) const {
         const int l = u.g;
-        const int tb = row >> 1, c = row & 1;
+        const int tb = r >> 1, c = r & 1;
         const int t = tb / B, b = tb - t * B;
         const int m = t - int(tri_idx(l, 0));
-        coeffs[b * cs + zidx(l + 2 * (u.aux + n), l, m) * 2 + c] = v;
+        const long long n0 = l + 2 * u.aux;
+        return Row{coeffs + b * cs + 2 * m + c, n0};
+    }
+    __device__ void store(const Row& R, const SplitUnit& u, int n, double v, const double*) const {
+        const long long nn = R.zl0 + 2 * n;
+        const int l = u.g;
+        R.p[2 * ((nn + 1) * (nn + 3) * (2 * nn + 1) / 24 + ((l * l) >> 2))] = v;
     }
 };
 struct EpiRadBwd {  // rows ((t B + b) 2 + c) -> flm[(t B + b)][k][c]
+    static constexpr bool RMW = false;
     double* flm;
     int nr;
-    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
-        const int k = u.aux + n;
-        flm[((long long)(row >> 1) * nr + k) * 2 + (row & 1)] = v;
+    struct Row { double* p; };
+    __device__ Row row(const SplitUnit& u, int r) const {
+        return Row{flm + ((long long)(r >> 1) * nr + u.aux) * 2 + (r & 1)};
     }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double*) const { R.p[2 * n] = v; }
 };
 struct EpiLegBwd {  // rows (m, b, kc) -> G north/south pair (conjugated); parity 1 adds/subtracts
+    static constexpr bool RMW = true;
     double* G;
     int B, L, Nt, nr2, j0u, j0d;
-    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
+    struct Row { double* up; double* dn; double sg; bool rmw; };
+    __device__ Row row(const SplitUnit& u, int r) const {
         const int m = u.g;
-        const long long local = row - (long long)m * B * nr2;
+        const long long local = r - (long long)m * B * nr2;
         const int b = int(local / nr2), kc = int(local - (long long)b * nr2);
-        const int jh = u.aux + n;
-        const double x = (kc & 1) ? -v : v;
         double* base = G + ((long long)b * L + m) * Nt * nr2 + kc;
-        double* up = base + (long long)(j0u + jh) * nr2;
-        double* dn = base + (long long)(j0d - jh) * nr2;
-        if (((u.flags >> 2) & 1) == 0) {
+        return Row{base + (long long)(j0u + u.aux) * nr2, base + (long long)(j0d - u.aux) * nr2,
+                   (kc & 1) ? -1.0 : 1.0, ((u.flags >> 2) & 1) != 0};
+    }
+    __device__ void load(const Row& R, int n, double* old) const {
+        if (R.rmw) {
+            old[0] = R.up[(long long)n * nr2];
+            old[1] = R.dn[-(long long)n * nr2];
+        }
+    }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        const double x = R.sg * v;
+        double* up = R.up + (long long)n * nr2;
+        double* dn = R.dn - (long long)n * nr2;
+        if (!R.rmw) {
             *up = x;
             *dn = x;
+        } else if (up == dn) {  // the equator node: its parity-1 contribution is zero
+            *up = old[0] + x;
         } else {
-            *up += x;
-            *dn -= x;
+            *up = old[0] + x;
+            *dn = old[1] - x;
         }
     }
 };
 struct EpiDftBwd {  // rows (b, col) -> grid[b][i][col] and grid[b][N-i][col]
+    static constexpr bool RMW = true;
     double* grid;
     int C, N;
     long long gsz;
-    __device__ void operator()(const SplitUnit& u, int row, int n, double v) const {
-        const long long b = row / C, col = row - b * C;
-        double* x = grid + b * gsz + col;
-        if ((u.flags & 2) == 0) {
-            const int i = u.aux + n;
-            x[(long long)i * C] = v;
-            if (i > 0) x[(long long)(N - i) * C] = v;
+    struct Row { double* x; int i0; bool rmw; };
+    __device__ Row row(const SplitUnit& u, int r) const {
+        const long long b = r / C, col = r - b * C;
+        const bool sin = ((u.flags >> 1) & 1) != 0;
+        return Row{grid + b * gsz + col, u.aux + (sin ? 1 : 0), sin};
+    }
+    __device__ void load(const Row& R, int n, double* old) const {
+        if (R.rmw) {
+            const int i = R.i0 + n;
+            old[0] = R.x[(long long)i * C];
+            old[1] = R.x[(long long)(N - i) * C];
+        }
+    }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        const int i = R.i0 + n;
+        if (!R.rmw) {
+            R.x[(long long)i * C] = v;
+            if (i > 0) R.x[(long long)(N - i) * C] = v;
         } else {
-            const int i = 1 + u.aux + n;
-            x[(long long)i * C] += v;
-            x[(long long)(N - i) * C] -= v;
+            R.x[(long long)i * C] = old[0] + v;
+            R.x[(long long)(N - i) * C] = old[1] - v;
         }
     }
 };
@@ -526,35 +570,63 @@ struct SplitParams {
     const SplitUnit* units;
     int nunits;
     int a_rows_total[2];  // rows per slice of the two A slice arrays
-    int b_rows_total[2];
+    int b_rows_total[2];  // rows per slice of the two B (table) slice arrays
     const int* ea[2];
     const int* eb[2];
     int* err;
+    unsigned long long* dbg;  // optional cycle counters (null in normal use)
 };
 
-template <int S, int NT, class Epi>  // S slices, S+1 levels, NT table rows per tile
+// Product schedule.  Levels 0..3 have their own exact accumulators; levels
+// 4..S share accumulator 4: level-5 products read table slices pre-scaled by
+// 2^-7 and level-6 products slices pre-scaled by 2^-14 (exact in BF16), so
+// accumulator 4 holds acc_4 + acc_5 / 2^7 + acc_6 / 2^14 in level-4 units.
+// The table slice array holds S unscaled, S x 2^-7 and S x 2^-14 slices.
+template <int S>
+struct Sched {
+    static constexpr int NACC = 5;
+    static constexpr int U = S < 5 ? S : 5;                     // unscaled B slices used (t <= 4)
+    static constexpr int N7 = S >= 5 ? (S == 6 ? 6 : 4) : 0;    // 2^-7 slices used by level 5
+    static constexpr int T7 = S == 6 ? 0 : 1;                   // first t of those
+    static constexpr int N14 = S == 6 ? 5 : 0;                  // 2^-14 slices used by level 6
+    static constexpr int NB = U + N7 + N14;                     // B tiles per stage
+    // table slice index of stage tile j
+    __host__ __device__ static constexpr int bslice(int j) {
+        return j < U ? j : (j < U + N7 ? S + T7 + (j - U) : 2 * S + 1 + (j - U - N7));
+    }
+    // stage tile of the B operand of product (s, t) at level d
+    __host__ __device__ static constexpr int btile(int d, int t) {
+        return d <= 4 ? t : (d == 5 ? U + (t - T7) : U + N7 + (t - 1));
+    }
+};
+
+template <int S, int NT, class Epi>  // S slices, NT table rows per tile
 __global__ void __launch_bounds__(SP_THREADS, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUtensorMap mapA1,
                       const __grid_constant__ CUtensorMap mapB0, const __grid_constant__ CUtensorMap mapB1,
                       const SplitParams P, const Epi epi) {
-    constexpr int A_TILE = SP_M * 32;                       // bytes of one slice, 16 K elements
+    using SC = Sched<S>;
+    constexpr int NST = S == 6 ? 3 : 4;
+    constexpr int A_TILE = SP_M * 32;                            // one slice, 16 K elements
     constexpr int B_TILE = ((NT * 32 + 1023) / 1024) * 1024;
-    constexpr int STAGE = S * (A_TILE + B_TILE);
-    constexpr uint32_t TX = S * (SP_M * 32 + NT * 32);
+    constexpr int STAGE = S * A_TILE + SC::NB * B_TILE;
+    constexpr uint32_t TX = S * (SP_M * 32) + SC::NB * (NT * 32);
     constexpr uint32_t IDESC = idesc_bf16_f32(SP_M, NT);
-    static_assert((S + 1) * NT <= 512, "levels must fit in TMEM");
+    static_assert(SC::NACC * NT <= 512, "accumulators must fit in TMEM");
+    static_assert(NT % 32 == 0, "each epilogue warp owns whole 16-column chunks");
 
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + SP_STAGES * STAGE);
-    uint64_t* empty = full + SP_STAGES;
-    uint64_t* tfull = empty + SP_STAGES;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * STAGE);
+    uint64_t* empty = full + NST;
+    uint64_t* tfull = empty + NST;
     uint64_t* tempty = tfull + 1;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long t_start = clock64();
     if (threadIdx.x == 0) {
-        for (int s = 0; s < SP_STAGES; ++s) {
+        for (int s = 0; s < NST; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
@@ -583,23 +655,26 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                 const int arows = P.a_rows_total[u.flags & 1];
                 const int brows = P.b_rows_total[(u.flags >> 1) & 1];
                 for (int kb = 0; kb < u.ksteps; ++kb, ++it) {
-                    const int st = it % SP_STAGES;
-                    const uint32_t ph = (it / SP_STAGES) & 1;
+                    const int st = it % NST;
+                    const uint32_t ph = (it / NST) & 1;
+                    const long long w0 = clock64();
                     if (!mbar_wait(&empty[st], ph ^ 1, P.err, 1)) { ok = false; break; }
+                    if (P.dbg) atomicAdd(&P.dbg[0], (unsigned long long)(clock64() - w0));
                     mbar_expect_tx(&full[st], TX);
                     unsigned char* sa = smem + st * STAGE;
                     unsigned char* sb = sa + S * A_TILE;
 #pragma unroll
                     for (int s = 0; s < S; ++s) tma_load_2d(sa + s * A_TILE, ma, &full[st], kb * SP_KB, s * arows + u.a_row0);
 #pragma unroll
-                    for (int t = 0; t < S; ++t) tma_load_2d(sb + t * B_TILE, mb, &full[st], kb * SP_KB, t * brows + u.b_row0);
+                    for (int j = 0; j < SC::NB; ++j)
+                        tma_load_2d(sb + j * B_TILE, mb, &full[st], kb * SP_KB, SC::bslice(j) * brows + u.b_row0);
                 }
             }
             // drain: wait (bounded) for the copies this thread issued
-            for (int q = 0; q < SP_STAGES && it > 0; ++q) {
+            for (int q = 0; q < NST && it > 0; ++q) {
                 const int j = it - 1 - q;
                 if (j < 0) break;
-                mbar_wait(&full[j % SP_STAGES], (j / SP_STAGES) & 1, P.err, 5);
+                mbar_wait(&full[j % NST], (j / NST) & 1, P.err, 5);
             }
         }
         __syncwarp();
@@ -610,23 +685,33 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             bool ok = true;
             for (int ui = blockIdx.x; ui < P.nunits && ok; ui += gridDim.x, ++tile) {
                 const SplitUnit u = P.units[ui];
+                const long long w0 = clock64();
                 if (!mbar_wait(tempty, (tile & 1) ^ 1, P.err, 2)) { ok = false; break; }
+                if (P.dbg) atomicAdd(&P.dbg[1], (unsigned long long)(clock64() - w0));
                 tc_fence_after();
                 for (int kb = 0; kb < u.ksteps; ++kb, ++it) {
-                    const int st = it % SP_STAGES;
-                    const uint32_t ph = (it / SP_STAGES) & 1;
+                    const int st = it % NST;
+                    const uint32_t ph = (it / NST) & 1;
+                    const long long w1 = clock64();
                     if (!mbar_wait(&full[st], ph, P.err, 3)) { ok = false; break; }
+                    if (P.dbg) atomicAdd(&P.dbg[2], (unsigned long long)(clock64() - w1));
                     tc_fence_after();
-                    const uint32_t sa = smem_u32(smem + st * STAGE);
-                    const uint32_t sb = sa + S * A_TILE;
+                    // descriptors differ only in the start-address field (address >> 4)
+                    const uint64_t da = desc_sw32(smem_u32(smem + st * STAGE));
+                    const uint64_t db = da + (uint64_t)((S * A_TILE) >> 4);
+                    bool first[SC::NACC];
+#pragma unroll
+                    for (int a = 0; a < SC::NACC; ++a) first[a] = (kb == 0);
 #pragma unroll
                     for (int d = 0; d <= S; ++d) {
-                        const int s0 = d < S ? 0 : 1;
+                        const int acc = d < 4 ? d : 4;
 #pragma unroll
-                        for (int s = s0; s <= d && s < S; ++s) {
+                        for (int s = 0; s < S; ++s) {
                             const int t = d - s;
-                            umma_bf16(tmem + d * NT, desc_sw32(sa + s * A_TILE), desc_sw32(sb + t * B_TILE), IDESC,
-                                      (kb > 0 || s > s0) ? 1u : 0u);
+                            if (t < 0 || t >= S) continue;
+                            umma_bf16(tmem + acc * NT, da + (uint64_t)((s * A_TILE) >> 4),
+                                      db + (uint64_t)((SC::btile(d, t) * B_TILE) >> 4), IDESC, first[acc] ? 0u : 1u);
+                            first[acc] = false;
                         }
                     }
                     umma_commit(&empty[st]);
@@ -637,54 +722,86 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
         __syncwarp();
     } else {
         // ---------------- epilogue ----------------
-        const int q = warp & 3;             // TMEM lane quarter of this warp
-        const int half = (warp - 2) >> 2;   // which half of the columns
+        const int q = warp & 3;              // TMEM lane quarter of this warp
+        const int half = (warp - 2) >> 2;    // which half of the columns
+        const int col0 = half * (NT / 2);
         int tile = 0;
         for (int ui = blockIdx.x; ui < P.nunits; ui += gridDim.x, ++tile) {
             const SplitUnit u = P.units[ui];
-            const bool got = mbar_wait(tfull, tile & 1, P.err, 4);
-            if (!__all_sync(0xffffffffu, got)) break;
-            tc_fence_after();
             const int r = 32 * q + lane;
             const bool rv = r < u.a_rows;
-            const int row = u.a_row0 + r;
+            const int row = u.a_row0 + (rv ? r : 0);
             const int amap = u.flags & 1, bmap = (u.flags >> 1) & 1;
-            const int ea = rv ? P.ea[amap][row] : 0;
-            for (int c0 = half * (NT / 2); c0 < (half + 1) * (NT / 2); c0 += 8) {
+            // exponents: the row's, and this warp's columns (one per lane, read by shuffles)
+            const int ea = P.ea[amap][row];
+            // NT/2 <= 64 columns per warp: lane l holds the exponents of columns col0 + l and col0 + 32 + l
+            const int ca = col0 + lane, cb = col0 + 32 + lane;
+            const int eb_a = (ca < col0 + NT / 2 && ca < u.n) ? P.eb[bmap][u.b_row0 + ca] : 0;
+            const int eb_b = (cb < col0 + NT / 2 && cb < u.n) ? P.eb[bmap][u.b_row0 + cb] : 0;
+            const typename Epi::Row R = epi.row(u, row);
+            const long long w0 = clock64();
+            const bool got = mbar_wait(tfull, tile & 1, P.err, 4);
+            const long long w1 = clock64();
+            if (!__all_sync(0xffffffffu, got)) break;
+            tc_fence_after();
+            for (int c0 = col0; c0 < col0 + NT / 2; c0 += 8) {
+                double old[8][2];
+                if constexpr (Epi::RMW) {
+                    if (rv) {
+#pragma unroll
+                        for (int j = 0; j < 8; ++j)
+                            if (c0 + j < u.n) epi.load(R, c0 + j, old[j]);
+                    }
+                }
                 long long T[8];
-                int last[8];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) T[j] = 0;
 #pragma unroll
-                for (int d = 0; d <= S; ++d) {
+                for (int a = 0; a < SC::NACC; ++a) {
                     uint32_t v[8];
-                    tmem_ld8(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(d * NT + c0), v);
+                    tmem_ld8(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * NT + c0), v);
                     tmem_ld_wait();
+                    // 32-bit conversions only: exact levels are integers below 2^24 and the
+                    // shared accumulator times 2^6 stays below 2^31 for K <= 992
+                    if (a < SC::NACC - 1) {  // exact levels 0..3
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        const int a = __float2int_rn(__uint_as_float(v[j]));
-                        if (d < S) T[j] = T[j] * 128 + a;
-                        else last[j] = a;
+                        for (int j = 0; j < 8; ++j)
+                            T[j] = (T[j] << 7) + (long long)__float2int_rn(__uint_as_float(v[j]));
+                    } else {  // shared levels 4..S, kept to 2^-6 of a level-4 unit
+#pragma unroll
+                        for (int j = 0; j < 8; ++j)
+                            T[j] = (T[j] << 13) + (long long)__float2int_rn(64.0f * __uint_as_float(v[j]));
                     }
                 }
-                if (rv) {
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        const int n = c0 + j;
-                        if (n < u.n) {
-                            const int E = ea + P.eb[bmap][u.b_row0 + n] - 7 * S - 14;
-                            epi(u, row, n, horner_ldexp(T[j], last[j], E));
-                        }
+                for (int j = 0; j < 8; ++j) {
+                    const int n = c0 + j;
+                    const int idx = n - col0;
+                    const int e1 = __shfl_sync(0xffffffffu, eb_a, idx & 31);
+                    const int e2 = __shfl_sync(0xffffffffu, eb_b, idx & 31);
+                    const int eb = idx < 32 ? e1 : e2;
+                    if (rv && n < u.n) {
+                        const long long Tj = T[j];
+                        const double v = u64_ldexp(Tj < 0 ? (unsigned long long)(-Tj) : (unsigned long long)Tj,
+                                                   Tj < 0, ea + eb - 48);
+                        epi.store(R, u, n, v, old[j]);
                     }
                 }
             }
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(tempty);
+            if (lane == 0) {
+                mbar_arrive(tempty);
+                if (P.dbg && warp == 2) {
+                    atomicAdd(&P.dbg[3], (unsigned long long)(w1 - w0));
+                    atomicAdd(&P.dbg[4], (unsigned long long)(clock64() - w1));
+                }
+            }
         }
     }
     tc_fence_before();
     __syncthreads();
+    if (P.dbg && threadIdx.x == 0) atomicAdd(&P.dbg[5], (unsigned long long)(clock64() - t_start));
     if (warp == 1) {
         tc_fence_after();
         tmem_dealloc(tmem, 512);
@@ -693,7 +810,8 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
 
 template <int S, int NT>
 constexpr size_t split_smem_bytes() {
-    return (size_t)SP_STAGES * S * (SP_M * 32 + ((NT * 32 + 1023) / 1024) * 1024) + 1024 + 256;
+    constexpr int NST = S == 6 ? 3 : 4;
+    return (size_t)NST * (S * SP_M * 32 + Sched<S>::NB * (((NT * 32 + 1023) / 1024) * 1024)) + 1024 + 256;
 }
 
 }  // namespace
@@ -742,22 +860,26 @@ int make_map(CUtensorMap* map, const void* base, long long rows, int Kp, int S, 
 
 inline int r16(int k) { return (k + 15) & ~15; }
 
-// table rows per tile: S+1 level accumulators of NT columns fill the 512 TMEM columns
-int n_tile(int S) { return S == 4 ? 96 : (S == 5 ? 80 : 64); }
+// table rows per tile: five accumulators of NT columns within the 512 TMEM columns
+int n_tile(int) { return 96; }
 
 }  // namespace
 
 // Slice arrays of one operand: [S][rows][Kp] bf16 + per-row exponents.
+// Slice arrays of one operand: [copies * S][rows][Kp] bf16 + per-row exponents.
+// Tables carry three copies (digits, digits x 2^-7, digits x 2^-14).
 struct SliceArray {
     DevBuf data, ex;
     long long rows = 0;
     int Kp = 0;
     int S = 0;
-    int ensure(long long r, int kp, int s) {
+    int copies = 1;
+    int ensure(long long r, int kp, int s, int c = 1) {
         rows = r;
         Kp = kp;
         S = s;
-        ZG_TRY(data.ensure((size_t)s * r * kp * 2 + 256));
+        copies = c;
+        ZG_TRY(data.ensure((size_t)c * s * r * kp * 2 + 256));
         ZG_TRY(ex.ensure((size_t)r * 4 + 16));
         return ZEST_GPU_OK;
     }
@@ -784,6 +906,8 @@ struct SplitState {
     std::map<std::tuple<const void*, int>, std::unique_ptr<ZtSplitTables>> zt_tables;  // per (plan, S)
     std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<UnitList>> units;  // cached work lists
     DevBuf tmp;                 // FP64 staging of generated tables
+    DevBuf cycles;              // role wait counters, kept when ZEST_GPU_SPLIT_CYCLES is set
+    bool cycles_on = false;
     double useful_flops = 0.0, issued_flops = 0.0;  // accumulated while profiling
 };
 
@@ -799,7 +923,7 @@ int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S,
     const size_t smem = (size_t)2 * R * K * sizeof(double);
     ZG_CUDA_TRY(cudaFuncSetAttribute(slice_kernel<Loader>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
     const long long blocks = (rows + R - 1) / R;
-    slice_kernel<Loader><<<(unsigned)blocks, 256, smem, s>>>(ld, rows, K, out.Kp, S, fold, R, out.ptr(),
+    slice_kernel<Loader><<<(unsigned)blocks, 256, smem, s>>>(ld, rows, K, out.Kp, S, fold, R, out.copies, out.ptr(),
                                                             rows * out.Kp, out.ex.as<int>());
     return launch_check("slice_kernel");
 }
@@ -807,6 +931,7 @@ int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S,
 int get_state(zest_gpu_context* ctx, SplitState** out) {
     if (!ctx->split) {
         ctx->split.reset(new SplitState());
+        ctx->split->cycles_on = std::getenv("ZEST_GPU_SPLIT_CYCLES") != nullptr;
         ZG_TRY(ctx->split->err.ensure(16));
         ZG_CUDA_TRY(cudaMemsetAsync(ctx->split->err.p, 0, 16, ctx->stream));
     }
@@ -847,7 +972,7 @@ __global__ void transpose_blocks_kernel(const double* __restrict__ in, const lon
 }
 
 int slice_table(zest_gpu_context* ctx, const double* src, long long rows, int K, int ld, int S, SliceArray& dst) {
-    ZG_TRY(dst.ensure(rows, r16(K), S));
+    ZG_TRY(dst.ensure(rows, r16(K), S, 3));
     return launch_slice(ctx->stream, RowMajorLoader{src, ld}, rows, K, S, 0, dst);
 }
 
@@ -927,10 +1052,11 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
     ZG_TRY(get_state(ctx, &st));
     cudaStream_t s = ctx->stream;
     CUtensorMap ma0, ma1, mb0, mb1;
-    ZG_TRY(make_map(&ma0, A0.ptr(), A0.rows, A0.Kp, S, SP_M));
-    ZG_TRY(make_map(&ma1, A1.ptr(), A1.rows, A1.Kp, S, SP_M));
-    ZG_TRY(make_map(&mb0, B0.ptr(), B0.rows, B0.Kp, S, NT));
-    ZG_TRY(make_map(&mb1, B1.ptr(), B1.rows, B1.Kp, S, NT));
+    if (B0.copies != 3 || B1.copies != 3) return fail(ZEST_GPU_ERR_INVALID, "split GEMM: table slices lack scaled copies");
+    ZG_TRY(make_map(&ma0, A0.ptr(), A0.rows, A0.Kp, S * A0.copies, SP_M));
+    ZG_TRY(make_map(&ma1, A1.ptr(), A1.rows, A1.Kp, S * A1.copies, SP_M));
+    ZG_TRY(make_map(&mb0, B0.ptr(), B0.rows, B0.Kp, S * 3, NT));
+    ZG_TRY(make_map(&mb1, B1.ptr(), B1.rows, B1.Kp, S * 3, NT));
     if (!ul.dev.p) {  // work lists are uploaded once and cached with their key
         ZG_TRY(ul.dev.ensure(units.size() * sizeof(SplitUnit)));
         ZG_CUDA_TRY(cudaMemcpyAsync(ul.dev.p, units.data(), units.size() * sizeof(SplitUnit),
@@ -952,6 +1078,12 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
     P.eb[0] = B0.ex.as<int>();
     P.eb[1] = B1.ex.as<int>();
     P.err = st->err.as<int>();
+    P.dbg = nullptr;
+    if (st->cycles_on) {
+        ZG_TRY(st->cycles.ensure(8 * sizeof(unsigned long long)));
+        ZG_CUDA_TRY(cudaMemsetAsync(st->cycles.p, 0, 8 * sizeof(unsigned long long), s));
+        P.dbg = st->cycles.as<unsigned long long>();
+    }
     const size_t smem = split_smem_bytes<S, NT>();
     ZG_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<S, NT, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
@@ -970,6 +1102,15 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
     if (herr) {
         cudaMemset(st->err.p, 0, sizeof(int));
         return fail(ZEST_GPU_ERR_TIMEOUT, "split GEMM: bounded wait expired (code " + std::to_string(herr) + ")");
+    }
+    if (P.dbg) {  // mean cycles per CTA in each wait, and in the epilogue's own work
+        unsigned long long c[8];
+        ZG_CUDA_TRY(cudaMemcpy(c, P.dbg, sizeof(c), cudaMemcpyDeviceToHost));
+        std::fprintf(stderr,
+                     "split_gemm S=%d units=%zu grid=%d: total %.0f | producer waits %.0f | mma waits tmem %.0f, "
+                     "smem %.0f | epilogue waits %.0f, works %.0f (cycles per CTA)\n",
+                     S, units.size(), grid, double(c[5]) / grid, double(c[0]) / grid, double(c[1]) / grid,
+                     double(c[2]) / grid, double(c[3]) / grid, double(c[4]) / grid);
     }
     return ZEST_GPU_OK;
 }
@@ -996,8 +1137,8 @@ int run_gemm(zest_gpu_context* ctx, int S, UnitList& ul, const SliceArray& A0, c
              const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
     switch (S) {
     case 4: return run_gemm_t<4, 96>(ctx, ul, A0, A1, B0, B1, epi);
-    case 5: return run_gemm_t<5, 80>(ctx, ul, A0, A1, B0, B1, epi);
-    case 6: return run_gemm_t<6, 64>(ctx, ul, A0, A1, B0, B1, epi);
+    case 5: return run_gemm_t<5, 96>(ctx, ul, A0, A1, B0, B1, epi);
+    case 6: return run_gemm_t<6, 96>(ctx, ul, A0, A1, B0, B1, epi);
     }
     return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path supports 4..6 slices");
 }
@@ -1232,7 +1373,7 @@ int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A
     ZG_TRY(get_state(ctx, &st));
     SliceArray a, b;
     ZG_TRY(a.ensure(M, r16(K), S));
-    ZG_TRY(b.ensure(N, r16(K), S));
+    ZG_TRY(b.ensure(N, r16(K), S, 3));
     ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{A, K}, M, K, S, 0, a));
     ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{B, K}, N, K, S, 0, b));
     UnitList u;
