@@ -152,6 +152,46 @@ int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
 /* euler_angles_from_rotation_matrix, rotor.hpp:53-63 (row-major 3x3, host). */
 int zest_gpu_euler_from_matrix(const double* matrix, double* euler);
 
+/* ---- Zernike rotation that allocates no device memory ----
+ * No counterpart in the reference: its rotations run on the host.  Same
+ * operation and result as zest_gpu_zt_rotate with ZEST_MEM_DEVICE (the same
+ * kernels, in place on `coeffs`), for callers that must not allocate device
+ * memory while they run: a process whose device memory is owned by another
+ * allocator that reserved it up front (a framework's caching allocator, a
+ * server that sized its pools at start-up), where an allocation from inside
+ * a library can fail or squeeze those pools; and a caller with latency-bound
+ * work on other streams, because cudaFree and a growing cudaMalloc can
+ * synchronize the whole device.
+ *
+ * All pointers are device memory of the current device; `stream` is a
+ * cudaStream_t of that device (NULL: the default stream).  `wignerd` is a
+ * Wigner d(pi/2) table of order `wignerd_order` >= `order`, as written by
+ * zest_gpu_wignerd_table, allocated and filled by the caller beforehand.
+ * There is no context: the call allocates nothing, neither through this
+ * library nor through any allocating library routine.  Its scratch (the
+ * list of rotated (n, l) vectors and the phase tables) is one fixed array
+ * of ZEST_GPU_NOALLOC_SCRATCH_BYTES inside the library's device image, one
+ * per device; nothing in it has to start at zero, since each call writes
+ * every byte it reads.  A call needs 8 nvec(order) bytes (rounded up to 256)
+ * plus 48 order batch bytes, nvec(order) ~ order^2 / 4; larger requests
+ * return ZEST_GPU_ERR_UNSUPPORTED and do nothing.  Orders above 1447 never
+ * fit; order 200 fits up to batch 428, order 64 up to batch 1362.
+ *
+ * The first call on each device sets up: it looks up the array's address
+ * with cudaGetSymbolAddress, which also loads the library's kernels onto the
+ * device.  Make that first call with the device current and before any
+ * stream capture on it.  Later calls on that device only launch kernels.
+ *
+ * The array is shared by every caller in the process: two calls that can
+ * run at the same time on one device (on streams without ordering between
+ * them, or from different host threads) race on it and give wrong results.
+ * Issue them on one stream, or order them with events.  The call returns
+ * once its kernels are queued; synchronize `stream` before reading. */
+#define ZEST_GPU_NOALLOC_SCRATCH_BYTES 4194304
+int zest_gpu_zt_rotate_noalloc(void* stream, size_t order, size_t batch, double* coeffs,
+                               const double* euler, int rotation_type,
+                               const double* wignerd, size_t wignerd_order);
+
 /* ---- split-precision dense product (no reference counterpart) ----
  * C = A B^T for row-major FP64 A (M x K) and B (N x K), K <= 992, evaluated
  * with the context's slice count on the tcgen05 path used by

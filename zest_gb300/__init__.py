@@ -29,6 +29,8 @@ ROTATION_OBJECT, ROTATION_COORDINATE = 0, 1
 LAYOUT_LONLAT, LAYOUT_LATLON = 0, 1
 PRECISION_FP64, PRECISION_SPLIT = 0, 1
 MEM_DEVICE, MEM_HOST = 0, 1
+# status codes of the C-ABI (ZEST_GPU_ERR_*)
+OK, ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED = 0, 1, 2, 3, 4, 5
 
 # the reference's transformer aliases (zernike_glq_transformer.hpp:967-1025)
 ZT_ACOUSTICS = (ZERNIKE_UNNORMED, SH_QM, SH_PHASE_NONE)
@@ -92,6 +94,7 @@ _SIGNATURES = {
     "zest_gpu_profile_stage_count": [],
     "zest_gpu_split_gemm": [_vp, _sz, _sz, _sz, _vp, _vp, _vp, _i],
     "zest_gpu_profile_flops": [_vp, _i, _vp, _vp],
+    "zest_gpu_zt_rotate_noalloc": [_vp, _sz, _sz, _vp, _vp, _i, _vp, _sz],
 }
 _SIZE_FUNCS = {
     "zest_gpu_zt_grid_size": [_sz],
