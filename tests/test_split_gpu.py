@@ -81,39 +81,47 @@ def test_split_gemm_random(ctx, S):
 
 
 def split_model(A, B, S):
-    """Integer model of the split product (balanced base-128 digits of the
-    row-scaled operands, levels 0..S summed exactly, 2^(eA+eB-7S-14) scaling)."""
+    """Integer model of the split product: balanced base-2^bits digits of the
+    row-scaled operands (8-bit digits for K <= 256, 7-bit above), the levels
+    kept by the kernel (0..S-1 with 8-bit digits, 0..S with 7-bit) summed
+    exactly, scaled by 2^(eA + eB - bits (top level + 2))."""
+    K = A.shape[1]
+    bits = 8 if K <= 256 else 7
+    top = S - 1 if bits == 8 else S
+    base = 1 << bits
+
     def digits(X):
         E = np.frexp(np.abs(X).max(axis=1))[1]
         e = E + 1
-        v = np.rint(X * np.exp2(7 * S - e)[:, None]).astype(np.int64)
+        v = np.rint(X * np.exp2(bits * S - e)[:, None]).astype(np.int64)
         d = np.zeros((S,) + X.shape, dtype=np.int64)
         w = v.copy()
         for s in range(S - 1, 0, -1):
-            r = w & 127
-            r = np.where(r >= 64, r - 128, r)
+            r = w & (base - 1)
+            r = np.where(r >= base // 2, r - base, r)
             d[s] = r
-            w = (w - r) >> 7
+            w = (w - r) >> bits
         d[0] = w
         return d, e
     da, ea = digits(A)
     db, eb = digits(B)
     T = np.zeros((A.shape[0], B.shape[0]), dtype=object)
-    for lev in range(S + 1):
+    for lev in range(top + 1):
         acc = np.zeros((A.shape[0], B.shape[0]), dtype=np.int64)
         for s in range(S):
             t = lev - s
             if 0 <= t < S:
                 acc += da[s] @ db[t].T
-        T = T * 128 + acc.astype(object)
-    return T.astype(float) * np.exp2(ea[:, None] + eb[None, :] - 7 * S - 14)
+        T = T * base + acc.astype(object)
+    return T.astype(float) * np.exp2(ea[:, None] + eb[None, :] - bits * (top + 2))
 
 
-@pytest.mark.parametrize("K", [1, 16, 33, 64, 208])
+@pytest.mark.parametrize("K", [1, 16, 33, 64, 208, 256, 257, 400])
 def test_split_gemm_matches_integer_model(split, K):
-    # levels 0..3 are exact in the kernel and levels 4..6 share one FP32
-    # accumulator (weight <= 2^-28 of level 0): the kernel agrees with the
-    # all-integer model far below the emulation's own error
+    # The kernel sums levels 0..3 exactly and levels 4 and up in one shared
+    # FP32 accumulator, whose products weigh at most 2^-28 of level 0: the
+    # kernel must agree with the all-integer model to 1e-13 of the largest
+    # entry, on both sides of the 8-bit/7-bit digit switch at K = 256.
     rng = np.random.default_rng(100 + K)
     A = rng.normal(size=(130, K)) * np.exp(rng.normal(size=(130, 1)))
     B = rng.normal(size=(70, K))

@@ -55,8 +55,8 @@ namespace zgpu {
 // ===========================================================================
 namespace {
 
-constexpr int SP_THREADS = 320;  // 10 warps
-constexpr int SP_STAGES = 4;
+constexpr int SP_EPI_WARPS = 12;                  // epilogue warps: three per TMEM lane quarter
+constexpr int SP_THREADS = 32 * (2 + SP_EPI_WARPS);  // + TMA producer + MMA issuer
 constexpr int SP_M = 128;
 constexpr int SP_KB = 16;        // K elements per pipeline stage (32 bytes of bf16)
 constexpr long long SP_TIMEOUT_NS = 2000000000LL;
@@ -148,6 +148,11 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                  : "r"(taddr));
 }
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t (&r)[4]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // K-major operand tile, SWIZZLE_32B: rows of 32 bytes, 8-row groups 256 bytes apart.
@@ -191,13 +196,13 @@ __device__ __forceinline__ double u64_ldexp(unsigned long long a, bool neg, int 
 }
 
 
-// fixed point: round(x 2^{7S-e}) as int64 (|x| < 2^(e-1)), ties to even
-__device__ __forceinline__ long long to_fixed(double x, int e, int S) {
+// fixed point: round(x 2^{nbits-e}) as int64 (|x| < 2^(e-1)), ties to even
+__device__ __forceinline__ long long to_fixed(double x, int e, int nbits) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
     const int E = int((bits >> 52) & 0x7FF);
     if (E == 0) return 0;  // zero and subnormals
     const unsigned long long M = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = 1075 + e - 7 * S - E;
+    const int sh = 1075 + e - nbits - E;
     long long v;
     if (sh >= 63) {
         v = 0;
@@ -222,6 +227,10 @@ __device__ __forceinline__ int biased_exp(double x) {
 namespace {
 
 constexpr int SL_KMAX = 992;  // K bound of exact level sums (balanced 7-bit digits)
+constexpr int SL_K8MAX = 256; // K bound of exact level sums with balanced 8-bit digits
+
+// digit width of a contraction of length K: 8 bits while the exact levels stay exact
+inline int digit_bits(int K) { return K <= SL_K8MAX ? 8 : 7; }
 
 inline int slice_rows_per_block(int K) {
     int r = 4096 / (K > 0 ? K : 1);
@@ -337,10 +346,11 @@ struct DftBwdLoader {  // rows (b, col); cos: Re F_m; sin: Im F_{k+1}
 // FP64 values are staged in shared memory (dynamic: 2 R K doubles) while the
 // row maxima are found, then every value is rounded to the row's fixed-point
 // grid, folded exactly in integers where requested, and split into balanced
-// base-128 digits, written as S BF16 slices.
+// base-2^bits digits, written as S BF16 slices (and copies scaled by 2^-bits,
+// 2^-2bits).
 template <class Loader>
-__global__ void __launch_bounds__(256) slice_kernel(Loader ld, long long rows, int K, int Kp, int S, int fold, int R,
-                                                    int copies, __nv_bfloat16* __restrict__ out,
+__global__ void __launch_bounds__(256) slice_kernel(Loader ld, long long rows, int K, int Kp, int S, int bits,
+                                                    int fold, int R, int copies, __nv_bfloat16* __restrict__ out,
                                                     long long slice_stride, int* __restrict__ ex) {
     extern __shared__ double sl_smem[];
     double* vu = sl_smem;
@@ -375,26 +385,28 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, long long rows, i
             const int kk = k + q;
             long long x = 0;
             if (kk < K) {
-                x = to_fixed(vu[r * K + kk], er, S);
-                if (fold == 1) x += to_fixed(vd[r * K + kk], er, S);
-                else if (fold == 2) x -= to_fixed(vd[r * K + kk], er, S);
+                x = to_fixed(vu[r * K + kk], er, bits * S);
+                if (fold == 1) x += to_fixed(vd[r * K + kk], er, bits * S);
+                else if (fold == 2) x -= to_fixed(vd[r * K + kk], er, bits * S);
             }
             v[q] = x;
         }
         int dg[2][8];
+        const long long mask = (1ll << bits) - 1;
+        const int halfv = 1 << (bits - 1), base = 1 << bits;
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             long long w = v[q];
             for (int s = S - 1; s >= 1; --s) {
-                int rem = int(w & 127);
-                if (rem >= 64) rem -= 128;
+                int rem = int(w & mask);
+                if (rem >= halfv) rem -= base;
                 dg[q][s] = rem;
-                w = (w - rem) >> 7;
+                w = (w - rem) >> bits;
             }
             dg[q][0] = int(w);
         }
         for (int c = 0; c < copies; ++c) {
-            const float sc = c == 0 ? 1.0f : (c == 1 ? 0.0078125f : 0.00006103515625f);  // 1, 2^-7, 2^-14
+            const float sc = __int_as_float((127 - bits * c) << 23);  // 2^{-bits c}, exact
             for (int s = 0; s < S; ++s) {
                 __nv_bfloat162 pr;
                 pr.x = __float2bfloat16_rn(float(dg[0][s]) * sc);
@@ -577,36 +589,69 @@ struct SplitParams {
     unsigned long long* dbg;  // optional cycle counters (null in normal use)
 };
 
-// Product schedule.  Levels 0..3 have their own exact accumulators; levels
-// 4..S share accumulator 4: level-5 products read table slices pre-scaled by
-// 2^-7 and level-6 products slices pre-scaled by 2^-14 (exact in BF16), so
-// accumulator 4 holds acc_4 + acc_5 / 2^7 + acc_6 / 2^14 in level-4 units.
-// The table slice array holds S unscaled, S x 2^-7 and S x 2^-14 slices.
-template <int S>
+// Product schedule of S slices of BITS-bit digits.  Levels d = s + t up to
+// DMAX are kept (DMAX = S with 7-bit digits, S - 1 with 8-bit digits).
+// Levels below MB = 4 have their own exact accumulators; levels MB..DMAX
+// share the last one: a level-(MB + c) product reads table slices pre-scaled
+// by 2^{-BITS c} (exact in BF16), so the shared accumulator holds
+// sum_c acc_{MB+c} 2^{-BITS c} in level-MB units.  (The tensor cores'
+// FP32 accumulation does not round these fractional sums to nearest, so the
+// shared accumulator must weigh little: from level 3 on, 2^-24 of level 0,
+// its error reaches 1e-12 of the result at K = 208; from level 4 on it stays
+// near 1e-15.)  Table slice arrays
+// hold the S unscaled slices followed by the scaled copies (copy c at slice
+// c S).  Stage tiles: copy 0 for t < U, then copy c >= 1 for t in
+// [t0(c), t0(c) + cnt(c)).
+template <int S, int BITS>
 struct Sched {
-    static constexpr int NACC = 5;
-    static constexpr int U = S < 5 ? S : 5;                     // unscaled B slices used (t <= 4)
-    static constexpr int N7 = S >= 5 ? (S == 6 ? 6 : 4) : 0;    // 2^-7 slices used by level 5
-    static constexpr int T7 = S == 6 ? 0 : 1;                   // first t of those
-    static constexpr int N14 = S == 6 ? 5 : 0;                  // 2^-14 slices used by level 6
-    static constexpr int NB = U + N7 + N14;                     // B tiles per stage
+    static constexpr int DMAX = BITS == 8 ? S - 1 : S;
+    static constexpr int MB = 4;
+    static constexpr int NACC = (DMAX < MB ? DMAX : MB) + 1;
+    static constexpr int NCOPY = DMAX < MB ? 1 : DMAX - MB + 1;
+    static constexpr int U = (DMAX < MB ? DMAX : MB) + 1 < S ? (DMAX < MB ? DMAX : MB) + 1 : S;
+    __host__ __device__ static constexpr int t0(int c) { return MB + c - (S - 1) > 0 ? MB + c - (S - 1) : 0; }
+    __host__ __device__ static constexpr int cnt(int c) { return (MB + c < S - 1 ? MB + c : S - 1) - t0(c) + 1; }
+    __host__ __device__ static constexpr int first(int c) {
+        int j = U;
+        for (int q = 1; q < c; ++q) j += cnt(q);
+        return j;
+    }
+    static constexpr int NB = first(NCOPY);  // B tiles per stage
+    static constexpr int PRODUCTS = (DMAX + 1) * (DMAX + 2) / 2 - (DMAX >= S ? (DMAX - S + 1) * (DMAX - S + 2) : 0);
     // table slice index of stage tile j
     __host__ __device__ static constexpr int bslice(int j) {
-        return j < U ? j : (j < U + N7 ? S + T7 + (j - U) : 2 * S + 1 + (j - U - N7));
+        if (j < U) return j;
+        int c = 1, r = j - U;
+        while (r >= cnt(c)) r -= cnt(c++);
+        return c * S + t0(c) + r;
     }
-    // stage tile of the B operand of product (s, t) at level d
-    __host__ __device__ static constexpr int btile(int d, int t) {
-        return d <= 4 ? t : (d == 5 ? U + (t - T7) : U + N7 + (t - 1));
-    }
+    // accumulator and stage tile of the B operand of product (s, t) at level d
+    __host__ __device__ static constexpr int acc(int d) { return d < MB ? d : MB; }
+    __host__ __device__ static constexpr int btile(int d, int t) { return d <= MB ? t : first(d - MB) + t - t0(d - MB); }
 };
+static_assert(Sched<6, 7>::NB == 16 && Sched<6, 7>::PRODUCTS == 26 && Sched<6, 7>::NACC == 5, "7-bit, 6 slices");
+static_assert(Sched<6, 8>::NB == 11 && Sched<6, 8>::PRODUCTS == 21 && Sched<6, 8>::NACC == 5, "8-bit, 6 slices");
+static_assert(Sched<5, 7>::NB == 9 && Sched<4, 8>::NB == 4 && Sched<4, 8>::NACC == 4 && Sched<5, 8>::NB == 5 &&
+                  Sched<4, 7>::NB == 4,
+              "schedules");
+static_assert(Sched<6, 7>::bslice(15) == 17 && Sched<6, 7>::btile(6, 5) == 15 && Sched<6, 8>::bslice(10) == 11 &&
+                  Sched<6, 8>::btile(5, 5) == 10 && Sched<6, 8>::btile(4, 4) == 4,
+              "tile maps");
 
-template <int S, int NT, class Epi>  // S slices, NT table rows per tile
+template <int S, int BITS>
+__host__ __device__ constexpr int stage_count() {
+    constexpr int st = S * 128 * 32 + Sched<S, BITS>::NB * 3072;
+    constexpr int n = (220 * 1024) / st;
+    return n > 6 ? 6 : n;
+}
+
+template <int S, int BITS, int NT, class Epi>  // S slices of BITS-bit digits, NT table rows per tile
 __global__ void __launch_bounds__(SP_THREADS, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUtensorMap mapA1,
                       const __grid_constant__ CUtensorMap mapB0, const __grid_constant__ CUtensorMap mapB1,
                       const SplitParams P, const Epi epi) {
-    using SC = Sched<S>;
-    constexpr int NST = S == 6 ? 3 : 4;
+    using SC = Sched<S, BITS>;
+    constexpr int NST = stage_count<S, BITS>();
     constexpr int A_TILE = SP_M * 32;                            // one slice, 16 K elements
     constexpr int B_TILE = ((NT * 32 + 1023) / 1024) * 1024;
     constexpr int STAGE = S * A_TILE + SC::NB * B_TILE;
@@ -631,7 +676,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             mbar_init(&empty[s], 1);
         }
         mbar_init(tfull, 1);
-        mbar_init(tempty, 8);
+        mbar_init(tempty, SP_EPI_WARPS);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -652,8 +697,8 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                 const SplitUnit u = P.units[ui];
                 const CUtensorMap* ma = (u.flags & 1) ? &mapA1 : &mapA0;
                 const CUtensorMap* mb = (u.flags & 2) ? &mapB1 : &mapB0;
-                const int arows = P.a_rows_total[u.flags & 1];
-                const int brows = P.b_rows_total[(u.flags >> 1) & 1];
+                const int arows = (u.flags & 1) ? P.a_rows_total[1] : P.a_rows_total[0];
+                const int brows = (u.flags & 2) ? P.b_rows_total[1] : P.b_rows_total[0];
                 for (int kb = 0; kb < u.ksteps; ++kb, ++it) {
                     const int st = it % NST;
                     const uint32_t ph = (it / NST) & 1;
@@ -703,8 +748,8 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
 #pragma unroll
                     for (int a = 0; a < SC::NACC; ++a) first[a] = (kb == 0);
 #pragma unroll
-                    for (int d = 0; d <= S; ++d) {
-                        const int acc = d < 4 ? d : 4;
+                    for (int d = 0; d <= SC::DMAX; ++d) {
+                        const int acc = SC::acc(d);
 #pragma unroll
                         for (int s = 0; s < S; ++s) {
                             const int t = d - s;
@@ -723,8 +768,10 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     } else {
         // ---------------- epilogue ----------------
         const int q = warp & 3;              // TMEM lane quarter of this warp
-        const int half = (warp - 2) >> 2;    // which half of the columns
-        const int col0 = half * (NT / 2);
+        constexpr int CW = NT / (SP_EPI_WARPS / 4);  // columns per epilogue warp
+        static_assert(CW % 4 == 0 && CW <= 64, "epilogue column split");
+        const int part = (warp - 2) >> 2;    // which column part
+        const int col0 = part * CW;
         int tile = 0;
         for (int ui = blockIdx.x; ui < P.nunits; ui += gridDim.x, ++tile) {
             const SplitUnit u = P.units[ui];
@@ -733,69 +780,85 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             const int row = u.a_row0 + (rv ? r : 0);
             const int amap = u.flags & 1, bmap = (u.flags >> 1) & 1;
             // exponents: the row's, and this warp's columns (one per lane, read by shuffles)
-            const int ea = P.ea[amap][row];
+            const int* __restrict__ eav = amap ? P.ea[1] : P.ea[0];
+            const int* __restrict__ ebv = bmap ? P.eb[1] : P.eb[0];
+            const int ea = eav[row];
             // NT/2 <= 64 columns per warp: lane l holds the exponents of columns col0 + l and col0 + 32 + l
             const int ca = col0 + lane, cb = col0 + 32 + lane;
-            const int eb_a = (ca < col0 + NT / 2 && ca < u.n) ? P.eb[bmap][u.b_row0 + ca] : 0;
-            const int eb_b = (cb < col0 + NT / 2 && cb < u.n) ? P.eb[bmap][u.b_row0 + cb] : 0;
+            const int eb_a = (ca < col0 + CW && ca < u.n) ? ebv[u.b_row0 + ca] : 0;
+            const int eb_b = (cb < col0 + CW && cb < u.n) ? ebv[u.b_row0 + cb] : 0;
             const typename Epi::Row R = epi.row(u, row);
             const long long w0 = clock64();
             const bool got = mbar_wait(tfull, tile & 1, P.err, 4);
             const long long w1 = clock64();
             if (!__all_sync(0xffffffffu, got)) break;
             tc_fence_after();
-            for (int c0 = col0; c0 < col0 + NT / 2; c0 += 8) {
-                double old[8][2];
-                if constexpr (Epi::RMW) {
-                    if (rv) {
+            // phase 1: drain the accumulators of this warp's columns into exact
+            // integers, then hand TMEM back to the MMA issuer
+            // 32-bit conversions only: exact levels are integers of at most 2^24 and
+            // the last accumulator times 2^6 stays below 2^31 within the K bounds;
+            // the top two levels combine in 32 bits (|acc_0| 2^BITS + |acc_1| < 2^31).
+            // T = sum_{a < NACC-1} acc_a 2^{BITS (NACC-1-a) + 6} + round(2^6 acc_last),
+            // in units of 2^-6 of a level-(NACC-1) product: 2^{eA + eB - BITS (NACC + 1) - 6}.
+            constexpr int TEXP = -BITS * (SC::NACC + 1) - 6;
+            static_assert(SC::NACC == 4 || SC::NACC == 5, "four or five accumulators");
+            long long T[CW];
 #pragma unroll
-                        for (int j = 0; j < 8; ++j)
-                            if (c0 + j < u.n) epi.load(R, c0 + j, old[j]);
-                    }
-                }
-                long long T[8];
+            for (int c = 0; c < CW / 4; ++c) {
+                uint32_t v[SC::NACC][4];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) T[j] = 0;
+                for (int a = 0; a < SC::NACC; ++a)
+                    tmem_ld4(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * NT + col0 + 4 * c), v[a]);
+                tmem_ld_wait();
 #pragma unroll
-                for (int a = 0; a < SC::NACC; ++a) {
-                    uint32_t v[8];
-                    tmem_ld8(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * NT + c0), v);
-                    tmem_ld_wait();
-                    // 32-bit conversions only: exact levels are integers below 2^24 and the
-                    // shared accumulator times 2^6 stays below 2^31 for K <= 992
-                    if (a < SC::NACC - 1) {  // exact levels 0..3
-#pragma unroll
-                        for (int j = 0; j < 8; ++j)
-                            T[j] = (T[j] << 7) + (long long)__float2int_rn(__uint_as_float(v[j]));
-                    } else {  // shared levels 4..S, kept to 2^-6 of a level-4 unit
-#pragma unroll
-                        for (int j = 0; j < 8; ++j)
-                            T[j] = (T[j] << 13) + (long long)__float2int_rn(64.0f * __uint_as_float(v[j]));
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const int n = c0 + j;
-                    const int idx = n - col0;
-                    const int e1 = __shfl_sync(0xffffffffu, eb_a, idx & 31);
-                    const int e2 = __shfl_sync(0xffffffffu, eb_b, idx & 31);
-                    const int eb = idx < 32 ? e1 : e2;
-                    if (rv && n < u.n) {
-                        const long long Tj = T[j];
-                        const double v = u64_ldexp(Tj < 0 ? (unsigned long long)(-Tj) : (unsigned long long)Tj,
-                                                   Tj < 0, ea + eb - 48);
-                        epi.store(R, u, n, v, old[j]);
+                for (int j = 0; j < 4; ++j) {
+                    const int u = (__float2int_rn(__uint_as_float(v[0][j])) << BITS) +
+                                  __float2int_rn(__uint_as_float(v[1][j]));
+                    const int i2 = __float2int_rn(__uint_as_float(v[2][j]));
+                    const int il = __float2int_rn(64.0f * __uint_as_float(v[SC::NACC - 1][j]));
+                    if constexpr (SC::NACC == 5) {
+                        const int i3 = __float2int_rn(__uint_as_float(v[3][j]));
+                        T[4 * c + j] = ((long long)u << (3 * BITS + 6)) + ((long long)i2 << (2 * BITS + 6)) +
+                                       ((long long)i3 << (BITS + 6)) + (long long)il;
+                    } else {
+                        T[4 * c + j] = ((long long)u << (2 * BITS + 6)) + ((long long)i2 << (BITS + 6)) + (long long)il;
                     }
                 }
             }
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) {
-                mbar_arrive(tempty);
-                if (P.dbg && warp == 2) {
-                    atomicAdd(&P.dbg[3], (unsigned long long)(w1 - w0));
-                    atomicAdd(&P.dbg[4], (unsigned long long)(clock64() - w1));
+            const long long w2 = clock64();
+            if (lane == 0) mbar_arrive(tempty);
+            // phase 2 (overlaps the next tile's MMAs): FP64 results and stores
+#pragma unroll
+            for (int c = 0; c < CW / 4; ++c) {
+                double old[4][2];
+                if constexpr (Epi::RMW) {
+                    if (rv) {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            if (col0 + 4 * c + j < u.n) epi.load(R, col0 + 4 * c + j, old[j]);
+                    }
                 }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int n = col0 + 4 * c + j;
+                    const int idx = 4 * c + j;
+                    const int e1 = __shfl_sync(0xffffffffu, eb_a, idx & 31);
+                    const int e2 = __shfl_sync(0xffffffffu, eb_b, idx & 31);
+                    const int eb = idx < 32 ? e1 : e2;
+                    if (rv && n < u.n) {
+                        const long long Tj = T[4 * c + j];
+                        const double v = u64_ldexp(Tj < 0 ? (unsigned long long)(-Tj) : (unsigned long long)Tj,
+                                                   Tj < 0, ea + eb + TEXP);
+                        epi.store(R, u, n, v, old[j]);
+                    }
+                }
+            }
+            if (P.dbg && warp == 2 && lane == 0) {
+                atomicAdd(&P.dbg[3], (unsigned long long)(w1 - w0));
+                atomicAdd(&P.dbg[4], (unsigned long long)(w2 - w1));
+                atomicAdd(&P.dbg[6], (unsigned long long)(clock64() - w2));
             }
         }
     }
@@ -808,10 +871,10 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     }
 }
 
-template <int S, int NT>
+template <int S, int BITS, int NT>
 constexpr size_t split_smem_bytes() {
-    constexpr int NST = S == 6 ? 3 : 4;
-    return (size_t)NST * (S * SP_M * 32 + Sched<S>::NB * (((NT * 32 + 1023) / 1024) * 1024)) + 1024 + 256;
+    constexpr int NST = stage_count<S, BITS>();
+    return (size_t)NST * (S * SP_M * 32 + Sched<S, BITS>::NB * (((NT * 32 + 1023) / 1024) * 1024)) + 1024 + 256;
 }
 
 }  // namespace
@@ -874,6 +937,7 @@ struct SliceArray {
     int Kp = 0;
     int S = 0;
     int copies = 1;
+    int bits = 7;  // digit width of the slices
     int ensure(long long r, int kp, int s, int c = 1) {
         rows = r;
         Kp = kp;
@@ -916,14 +980,16 @@ void destroy_split(SplitState* s) { delete s; }
 namespace {
 
 template <class Loader>
-int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S, int fold, SliceArray& out) {
+int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S, int bits, int fold, SliceArray& out) {
+    out.bits = bits;
     if (rows <= 0) return ZEST_GPU_OK;
     if (K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: K above 992");
+    if (bits != 7 && !(bits == 8 && K <= SL_K8MAX)) return fail(ZEST_GPU_ERR_INVALID, "split path: digit width");
     const int R = slice_rows_per_block(K);
     const size_t smem = (size_t)2 * R * K * sizeof(double);
     ZG_CUDA_TRY(cudaFuncSetAttribute(slice_kernel<Loader>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
     const long long blocks = (rows + R - 1) / R;
-    slice_kernel<Loader><<<(unsigned)blocks, 256, smem, s>>>(ld, rows, K, out.Kp, S, fold, R, out.copies, out.ptr(),
+    slice_kernel<Loader><<<(unsigned)blocks, 256, smem, s>>>(ld, rows, K, out.Kp, S, bits, fold, R, out.copies, out.ptr(),
                                                             rows * out.Kp, out.ex.as<int>());
     return launch_check("slice_kernel");
 }
@@ -971,9 +1037,10 @@ __global__ void transpose_blocks_kernel(const double* __restrict__ in, const lon
     out[((long long)blk * nrow + k) * ld + i] = (i < cnt[blk]) ? in[(off[blk] + i) * nrow + k] : 0.0;
 }
 
-int slice_table(zest_gpu_context* ctx, const double* src, long long rows, int K, int ld, int S, SliceArray& dst) {
+int slice_table(zest_gpu_context* ctx, const double* src, long long rows, int K, int ld, int S, int bits,
+                SliceArray& dst) {
     ZG_TRY(dst.ensure(rows, r16(K), S, 3));
-    return launch_slice(ctx->stream, RowMajorLoader{src, ld}, rows, K, S, 0, dst);
+    return launch_slice(ctx->stream, RowMajorLoader{src, ld}, rows, K, S, bits, 0, dst);
 }
 
 int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, ZtSplitTables** out) {
@@ -996,7 +1063,7 @@ int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, 
             dim3 grid((ld + 127) / 128, rows);
             dft_table_kernel<<<grid, 128, 0, s>>>(tmp, rows, K, ld, N, row_off, col_off, mode);
             ZG_TRY(launch_check("dft_table_kernel"));
-            return slice_table(ctx, tmp, rows, K, ld, S, dst);
+            return slice_table(ctx, tmp, rows, K, ld, S, digit_bits(L), dst);
         };
         // forward: cos rows m in [0,L), cols i in [0,L); sin rows m in [1,L), cols i in [1,L)
         ZG_TRY(gen(L, L, 0, 0, 0, t->dft_cos_f));
@@ -1007,8 +1074,9 @@ int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, 
         ZG_CUDA_TRY(cudaStreamSynchronize(s));
     }
     // forward Legendre and radial tables (FP64 tables of the plain form)
-    ZG_TRY(slice_table(ctx, plan.leg.Pf.as<double>(), plan.leg.off_h[2 * (size_t)L], kh, kh, S, t->leg_f));
-    ZG_TRY(slice_table(ctx, plan.rad.Rf.as<double>(), plan.rad.off_h[L], nr, nr, S, t->rad_f));
+    ZG_TRY(slice_table(ctx, plan.leg.Pf.as<double>(), plan.leg.off_h[2 * (size_t)L], kh, kh, S, digit_bits(kh),
+                       t->leg_f));
+    ZG_TRY(slice_table(ctx, plan.rad.Rf.as<double>(), plan.rad.off_h[L], nr, nr, S, digit_bits(nr), t->rad_f));
     // backward tables: transposed blocks
     {
         const int kl = r16((L + 1) / 2);
@@ -1023,7 +1091,8 @@ int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, 
         transpose_blocks_kernel<<<g1, 256, 0, s>>>(plan.leg.Pb.as<double>(), plan.leg.off.as<long long>(),
                                                    dcnt.as<int>(), kh, kl, st->tmp.as<double>());
         ZG_TRY(launch_check("transpose_blocks_kernel"));
-        ZG_TRY(slice_table(ctx, st->tmp.as<double>(), (long long)2 * L * kh, kl, kl, S, t->leg_bT));
+        ZG_TRY(slice_table(ctx, st->tmp.as<double>(), (long long)2 * L * kh, kl, kl, S, digit_bits((L + 1) / 2),
+                           t->leg_bT));
         ZG_CUDA_TRY(cudaStreamSynchronize(s));
         // radial: per l block [nr][cnt(l)] from Rb
         std::vector<int> rc((size_t)L);
@@ -1035,7 +1104,8 @@ int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, 
         transpose_blocks_kernel<<<g2, 256, 0, s>>>(plan.rad.Rb.as<double>(), plan.rad.off.as<long long>(),
                                                    drc.as<int>(), nr, kl, st->tmp.as<double>());
         ZG_TRY(launch_check("transpose_blocks_kernel"));
-        ZG_TRY(slice_table(ctx, st->tmp.as<double>(), (long long)L * nr, kl, kl, S, t->rad_bT));
+        ZG_TRY(slice_table(ctx, st->tmp.as<double>(), (long long)L * nr, kl, kl, S, digit_bits((L + 1) / 2),
+                           t->rad_bT));
         ZG_CUDA_TRY(cudaStreamSynchronize(s));
     }
     *out = t.get();
@@ -1043,7 +1113,7 @@ int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, 
     return ZEST_GPU_OK;
 }
 
-template <int S, int NT, class Epi>
+template <int S, int BITS, int NT, class Epi>
 int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const SliceArray& A1, const SliceArray& B0,
                const SliceArray& B1, const Epi& epi) {
     const std::vector<SplitUnit>& units = ul.v;
@@ -1084,15 +1154,15 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
         ZG_CUDA_TRY(cudaMemsetAsync(st->cycles.p, 0, 8 * sizeof(unsigned long long), s));
         P.dbg = st->cycles.as<unsigned long long>();
     }
-    const size_t smem = split_smem_bytes<S, NT>();
-    ZG_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<S, NT, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const size_t smem = split_smem_bytes<S, BITS, NT>();
+    ZG_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<S, BITS, NT, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
     int nsm = 0;
     ZG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
     const int grid = std::min<int>(int(units.size()), nsm);
     {
         StageScope sc(ctx, ST_SPLIT_GEMM);
-        split_gemm_kernel<S, NT, Epi><<<grid, SP_THREADS, smem, s>>>(ma0, ma1, mb0, mb1, P, epi);
+        split_gemm_kernel<S, BITS, NT, Epi><<<grid, SP_THREADS, smem, s>>>(ma0, ma1, mb0, mb1, P, epi);
         ZG_TRY(launch_check("split_gemm_kernel"));
     }
     // surface a bounded-wait timeout of this launch to the caller
@@ -1108,14 +1178,21 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
         ZG_CUDA_TRY(cudaMemcpy(c, P.dbg, sizeof(c), cudaMemcpyDeviceToHost));
         std::fprintf(stderr,
                      "split_gemm S=%d units=%zu grid=%d: total %.0f | producer waits %.0f | mma waits tmem %.0f, "
-                     "smem %.0f | epilogue waits %.0f, works %.0f (cycles per CTA)\n",
+                     "smem %.0f | epilogue waits %.0f, drains %.0f, stores %.0f (cycles per CTA)\n",
                      S, units.size(), grid, double(c[5]) / grid, double(c[0]) / grid, double(c[1]) / grid,
-                     double(c[2]) / grid, double(c[3]) / grid, double(c[4]) / grid);
+                     double(c[2]) / grid, double(c[3]) / grid, double(c[4]) / grid, double(c[6]) / grid);
     }
     return ZEST_GPU_OK;
 }
 
-inline int products(int S) { return S * (S + 1) / 2 + S - 1; }
+// slice products per K block: pairs (s, t) of S slices with s + t <= the kept top level
+inline int products(int S, int bits) {
+    const int dmax = bits == 8 ? S - 1 : S;
+    int n = 0;
+    for (int a = 0; a < S; ++a)
+        for (int b = 0; b < S; ++b) n += (a + b <= dmax);
+    return n;
+}
 
 // Returns the cached work list of `key`, built by `build` on first use.
 template <class Build>
@@ -1135,20 +1212,31 @@ int get_units(zest_gpu_context* ctx, std::tuple<int, int, int, int, int, int> ke
 template <class Epi>
 int run_gemm(zest_gpu_context* ctx, int S, UnitList& ul, const SliceArray& A0, const SliceArray& A1,
              const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
-    switch (S) {
-    case 4: return run_gemm_t<4, 96>(ctx, ul, A0, A1, B0, B1, epi);
-    case 5: return run_gemm_t<5, 96>(ctx, ul, A0, A1, B0, B1, epi);
-    case 6: return run_gemm_t<6, 96>(ctx, ul, A0, A1, B0, B1, epi);
+    const int bits = A0.bits;
+    if (A1.bits != bits || B0.bits != bits || B1.bits != bits)
+        return fail(ZEST_GPU_ERR_INVALID, "split GEMM: operands sliced with different digit widths");
+    if (bits == 8) {
+        switch (S) {
+        case 4: return run_gemm_t<4, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
+        case 5: return run_gemm_t<5, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
+        case 6: return run_gemm_t<6, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
+        }
+    } else {
+        switch (S) {
+        case 4: return run_gemm_t<4, 7, 96>(ctx, ul, A0, A1, B0, B1, epi);
+        case 5: return run_gemm_t<5, 7, 96>(ctx, ul, A0, A1, B0, B1, epi);
+        case 6: return run_gemm_t<6, 7, 96>(ctx, ul, A0, A1, B0, B1, epi);
+        }
     }
     return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path supports 4..6 slices");
 }
 
 // tiles of a group: operand rows [a0, a0 + arows) x table rows [b0, b0 + nrows), K = kk
-void add_units(UnitList& ul, int S, long long a0, long long arows, int b0, int nrows, int NT, int kk, int flags,
-               int g) {
+void add_units(UnitList& ul, int S, int bits, long long a0, long long arows, int b0, int nrows, int NT, int kk,
+               int flags, int g) {
     if (arows <= 0 || nrows <= 0 || kk <= 0) return;
     const int ksteps = r16(kk) / 16;
-    const double P = products(S);
+    const double P = products(S, bits);
     for (long long r = 0; r < arows; r += SP_M)
         for (int c = 0; c < nrows; c += NT) {
             SplitUnit u;
@@ -1208,25 +1296,28 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
 
     // ---- longitude DFT: folded cos/sin products ----
     {
+        const int bits = digit_bits(Lg);
         const long long rows = (long long)batch * C;
         ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
         ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, DftFwdLoader{grids, sh.size(), C, N, 0}, rows, Lg, S, 1, st->op[0]));
-            if (Lg > 1) ZG_TRY(launch_slice(s, DftFwdLoader{grids, sh.size(), C, N, 1}, rows, Lg - 1, S, 2, st->op[1]));
+            ZG_TRY(launch_slice(s, DftFwdLoader{grids, sh.size(), C, N, 0}, rows, Lg, S, bits, 1, st->op[0]));
+            if (Lg > 1)
+                ZG_TRY(launch_slice(s, DftFwdLoader{grids, sh.size(), C, N, 1}, rows, Lg - 1, S, bits, 2, st->op[1]));
         }
         UnitList* u;
         ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
             for (long long r = 0; r < rows; r += SP_M) {
-                add_units(ul, S, r, std::min<long long>(SP_M, rows - r), 0, Lm, NT, Lg, 0, 0);
-                if (Lm > 1) add_units(ul, S, r, std::min<long long>(SP_M, rows - r), 0, Lm - 1, NT, Lg - 1, 1 | 2, 0);
+                add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lm, NT, Lg, 0, 0);
+                if (Lm > 1) add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lm - 1, NT, Lg - 1, 1 | 2, 0);
             }
         }, &u));
         ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_f, tb->dft_sin_f, EpiDftFwd{G, C, Lg}));
     }
     // ---- Legendre (folded over the equator) ----
     {
+        const int bits = digit_bits(kh);
         const long long per_m = (long long)batch * nr2;
         const long long rows = (long long)Lm * per_m;
         ZG_TRY(st->op[0].ensure(rows, r16(kh), S));
@@ -1234,15 +1325,15 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
             LegFwdLoader ld{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d};
-            ZG_TRY(launch_slice(s, ld, rows, kh, S, 1, st->op[0]));
-            ZG_TRY(launch_slice(s, ld, rows, kh, S, 2, st->op[1]));
+            ZG_TRY(launch_slice(s, ld, rows, kh, S, bits, 1, st->op[0]));
+            ZG_TRY(launch_slice(s, ld, rows, kh, S, bits, 2, st->op[1]));
         }
         UnitList* u;
         ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
             for (int m = 0; m < Lm; ++m)
                 for (int p = 0; p < 2; ++p) {
                     const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
-                    add_units(ul, S, (long long)m * per_m, per_m, int(plan.leg.off_h[2 * m + p]), cnt, NT, kh,
+                    add_units(ul, S, bits, (long long)m * per_m, per_m, int(plan.leg.off_h[2 * m + p]), cnt, NT, kh,
                               p | (p << 2), m);
                 }
         }, &u));
@@ -1250,16 +1341,17 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
     }
     // ---- radial ----
     {
+        const int bits = digit_bits(nr);
         const long long rows = tri_size(Lm) * batch * 2;
         ZG_TRY(st->op[0].ensure(rows, r16(nr), S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, RadFwdLoader{flm, nr}, rows, nr, S, 0, st->op[0]));
+            ZG_TRY(launch_slice(s, RadFwdLoader{flm, nr}, rows, nr, S, bits, 0, st->op[0]));
         }
         UnitList* u;
         ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
             for (int l = 0; l < Lm; ++l)
-                add_units(ul, S, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, int(plan.rad.off_h[l]),
+                add_units(ul, S, bits, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, int(plan.rad.off_h[l]),
                           (Lm - l + 1) / 2, NT, nr, 0, l);
         }, &u));
         ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd{coeffs, batch, csz}));
@@ -1290,30 +1382,34 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
 
     // ---- radial: coefficients -> flm ----
     {
+        const int bits = digit_bits((Lg + 1) / 2);
         const long long rows = tri_size(Lm) * batch * 2;
         ZG_TRY(st->op[0].ensure(rows, kl, S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, RadBwdLoader{coeffs, csz, batch, Lm}, rows, (Lm + 1) / 2, S, 0, st->op[0]));
+            ZG_TRY(launch_slice(s, RadBwdLoader{coeffs, csz, batch, Lm}, rows, (Lm + 1) / 2, S, bits, 0,
+                                st->op[0]));
         }
         UnitList* u;
         ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_B), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
             for (int l = 0; l < Lm; ++l)
-                add_units(ul, S, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, l * nr, nr, NT,
+                add_units(ul, S, bits, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, l * nr, nr, NT,
                           (Lm - l + 1) / 2, 0, l);
         }, &u));
         ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd{flm, nr}));
     }
     // ---- Legendre: flm -> G (north/south unfold; parity 1 read-modify-write) ----
     {
+        const int bits = digit_bits((Lg + 1) / 2);
         const long long per_m = (long long)batch * nr2;
         const long long rows = (long long)Lm * per_m;
         ZG_TRY(st->op[0].ensure(rows, kl, S));
         ZG_TRY(st->op[1].ensure(rows, kl, S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, LegBwdLoader{flm, batch, nr2, 0, Lm}, rows, (Lm + 1) / 2, S, 0, st->op[0]));
-            ZG_TRY(launch_slice(s, LegBwdLoader{flm, batch, nr2, 1, Lm}, rows, Lm / 2, S, 0, st->op[1]));
+            ZG_TRY(launch_slice(s, LegBwdLoader{flm, batch, nr2, 0, Lm}, rows, (Lm + 1) / 2, S, bits, 0,
+                                st->op[0]));
+            ZG_TRY(launch_slice(s, LegBwdLoader{flm, batch, nr2, 1, Lm}, rows, Lm / 2, S, bits, 0, st->op[1]));
         }
         if (Lm < Lg) {
             StageScope sc(ctx, ST_MEMSET);
@@ -1326,7 +1422,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                 for (int m = 0; m < Lm; ++m) {
                     const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
                     if (cnt == 0) continue;
-                    add_units(ul, S, (long long)m * per_m, per_m, (2 * m + p) * kh, kh, NT, cnt, p | (p << 2), m);
+                    add_units(ul, S, bits, (long long)m * per_m, per_m, (2 * m + p) * kh, kh, NT, cnt, p | (p << 2), m);
                 }
             }, &u));
             ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
@@ -1335,18 +1431,20 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
     }
     // ---- longitude: inverse real DFT, cos pass then sin read-modify-write pass ----
     {
+        const int bits = digit_bits(Lg);
         const long long rows = (long long)batch * C;
         ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
         ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, DftBwdLoader{G, batch, Lg, C, 0}, rows, Lg, S, 0, st->op[0]));
-            if (Lg > 1) ZG_TRY(launch_slice(s, DftBwdLoader{G, batch, Lg, C, 1}, rows, Lg - 1, S, 0, st->op[1]));
+            ZG_TRY(launch_slice(s, DftBwdLoader{G, batch, Lg, C, 0}, rows, Lg, S, bits, 0, st->op[0]));
+            if (Lg > 1)
+                ZG_TRY(launch_slice(s, DftBwdLoader{G, batch, Lg, C, 1}, rows, Lg - 1, S, bits, 0, st->op[1]));
         }
         UnitList* u;
         ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
             for (long long r = 0; r < rows; r += SP_M)
-                add_units(ul, S, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, Lg, 0, 0);
+                add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, Lg, 0, 0);
         }, &u));
         ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
                         EpiDftBwd{grids, C, N, sh.size()}));
@@ -1354,7 +1452,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             UnitList* v;
             ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 1), [&](UnitList& ul) {
                 for (long long r = 0; r < rows; r += SP_M)
-                    add_units(ul, S, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT, Lg - 1, 1 | 2 | 4, 0);
+                    add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT, Lg - 1, 1 | 2 | 4, 0);
             }, &v));
             ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
                             EpiDftBwd{grids, C, N, sh.size()}));
@@ -1374,10 +1472,11 @@ int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A
     SliceArray a, b;
     ZG_TRY(a.ensure(M, r16(K), S));
     ZG_TRY(b.ensure(N, r16(K), S, 3));
-    ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{A, K}, M, K, S, 0, a));
-    ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{B, K}, N, K, S, 0, b));
+    const int bits = digit_bits(K);
+    ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{A, K}, M, K, S, bits, 0, a));
+    ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{B, K}, N, K, S, bits, 0, b));
     UnitList u;
-    add_units(u, S, 0, M, 0, N, NT, K, 0, 0);
+    add_units(u, S, bits, 0, M, 0, N, NT, K, 0, 0);
     return run_gemm(ctx, S, u, a, a, b, b, EpiDense{C, N});
 }
 
