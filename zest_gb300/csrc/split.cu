@@ -232,76 +232,81 @@ constexpr int SL_K8MAX = 256; // K bound of exact level sums with balanced 8-bit
 // digit width of a contraction of length K: 8 bits while the exact levels stay exact
 inline int digit_bits(int K) { return K <= SL_K8MAX ? 8 : 7; }
 
-inline int slice_rows_per_block(int K) {
-    int r = 4096 / (K > 0 ? K : 1);
-    return r < 2 ? 2 : (r > 16 ? 16 : r);
+// Rows per slicing block: a power of two (so that in row-fast loops every
+// thread stays on one row) with the staged FP64 rows within 32 KB.
+inline int slice_rows_per_block(int K, bool two) {
+    const int per_row = K * (two ? 16 : 8);
+    int r = 16;
+    while (r > 1 && r * per_row > 32 * 1024) r >>= 1;
+    return r;
 }
 
-// Loaders return the pair (up, dn) of operand element (row, k); the folded
-// operands are fix(up) + fix(dn) (fold = 1) or fix(up) - fix(dn) (fold = 2),
-// computed exactly in integers at the row's scale.
+// Loaders give the pair (up, dn) of operand element (row, k) through a per-row
+// handle computed once per block row.  ROW_FAST loaders read consecutive rows
+// at one k contiguously; the others read consecutive k of one row.  TWO
+// loaders produce both members of the pair (a fold or two interleaved
+// operands), the others only `up`.
 struct RowMajorLoader {  // tables and dense operands: p[r*ld + k]
-    static constexpr bool ROW_FAST = false;
+    static constexpr bool ROW_FAST = false, TWO = false;
     const double* p;
     long long ld;
-    __device__ void get(long long r, int k, double& up, double& dn) const {
-        up = p[r * ld + k];
-        dn = 0.0;
-    }
+    struct Row { const double* p; };
+    __device__ Row row(long long r) const { return Row{p + r * ld}; }
+    __device__ void get(const Row& R, int k, double& up, double&) const { up = R.p[k]; }
 };
 
-struct DftFwdLoader {  // rows (b, col) of the ball grid; cos: x_k (+ x_{N-k}); sin: x_{k+1} - x_{N-k-1}
-    static constexpr bool ROW_FAST = true;
+// rows (b, col) of the ball grids; k = longitude: (x_k, x_{N-k}), x_0 alone.
+// Folded: cos operand x_k + x_{N-k} (k < L), sin operand x_k - x_{N-k} at k - 1.
+struct DftFwdLoader {
+    static constexpr bool ROW_FAST = true, TWO = true;
     const double* grid;
     long long gsz;
-    int C, N, sin;
-    __device__ void get(long long r, int k, double& up, double& dn) const {
-        const long long b = r / C, col = r - b * C;
-        const double* x = grid + b * gsz + col;
-        if (sin) {
-            const int i = k + 1;
-            up = x[(long long)i * C];
-            dn = x[(long long)(N - i) * C];
-        } else if (k == 0) {
-            up = x[0];
-            dn = 0.0;
-        } else {
-            up = x[(long long)k * C];
-            dn = x[(long long)(N - k) * C];
-        }
+    int C, N;
+    struct Row { const double* x; };
+    __device__ Row row(long long r) const {
+        const long long b = r / C;
+        return Row{grid + b * gsz + (r - b * C)};
+    }
+    __device__ void get(const Row& R, int k, double& up, double& dn) const {
+        up = R.x[(long long)k * C];
+        dn = k ? R.x[(long long)(N - k) * C] : 0.0;
     }
 };
 
-struct LegFwdLoader {  // rows (m, b, kc); K = folded latitude node
-    static constexpr bool ROW_FAST = true;
+// rows (m, b, kc) of the spectra; k = folded latitude node (north, south).
+struct LegFwdLoader {
+    static constexpr bool ROW_FAST = true, TWO = true;
     const double* G;
     int B, L, Nt, nr2, j0u, j0d;
-    __device__ void get(long long r, int k, double& up, double& dn) const {
+    struct Row { const double* base; };
+    __device__ Row row(long long r) const {
         const long long mb = r / nr2;
         const int kc = int(r - mb * nr2);
         const int m = int(mb / B), b = int(mb - (long long)m * B);
-        const double* base = G + ((long long)b * L + m) * Nt * nr2 + kc;
-        up = base[(long long)(j0u + k) * nr2];
-        dn = base[(long long)(j0d - k) * nr2];
+        return Row{G + ((long long)b * L + m) * Nt * nr2 + kc};
+    }
+    __device__ void get(const Row& R, int k, double& up, double& dn) const {
+        up = R.base[(long long)(j0u + k) * nr2];
+        dn = R.base[(long long)(j0d - k) * nr2];
     }
 };
 
-struct RadFwdLoader {  // rows ((t B + b) 2 + c); K = radial node
-    static constexpr bool ROW_FAST = false;
+struct RadFwdLoader {  // rows ((t B + b) 2 + c); k = radial node
+    static constexpr bool ROW_FAST = false, TWO = false;
     const double* flm;
     int nr;
-    __device__ void get(long long r, int k, double& up, double& dn) const {
-        up = flm[((r >> 1) * nr + k) * 2 + (r & 1)];
-        dn = 0.0;
-    }
+    struct Row { const double* p; };
+    __device__ Row row(long long r) const { return Row{flm + (r >> 1) * nr * 2 + (r & 1)}; }
+    __device__ void get(const Row& R, int k, double& up, double&) const { up = R.p[(long long)k * 2]; }
 };
 
-struct RadBwdLoader {  // rows ((tri(l,m) B + b) 2 + c); K = i, n = l + 2i
-    static constexpr bool ROW_FAST = false;
+struct RadBwdLoader {  // rows ((tri(l,m) B + b) 2 + c); k = i, n = l + 2i
+    static constexpr bool ROW_FAST = false, TWO = false;
     const double* coeffs;
     long long cs;
     int B, Lm;
-    __device__ void get(long long r, int k, double& up, double& dn) const {
+    struct Row { const double* base; int l, m; };
+    __device__ Row row(long long r) const {
         const long long tb = r >> 1;
         const int c = int(r & 1);
         const long long t = tb / B;
@@ -310,111 +315,198 @@ struct RadBwdLoader {  // rows ((tri(l,m) B + b) 2 + c); K = i, n = l + 2i
         while ((long long)(l + 1) * (l + 2) / 2 <= t) ++l;
         while ((long long)l * (l + 1) / 2 > t) --l;
         const int m = int(t - (long long)l * (l + 1) / 2);
-        const int n = l + 2 * k;
-        up = (n < Lm) ? coeffs[b * cs + zidx(n, l, m) * 2 + c] : 0.0;
-        dn = 0.0;
+        return Row{coeffs + b * cs + c, l, m};
+    }
+    __device__ void get(const Row& R, int k, double& up, double&) const {
+        const int n = R.l + 2 * k;
+        up = (n < Lm) ? R.base[zidx(n, R.l, R.m) * 2] : 0.0;
     }
 };
 
-struct LegBwdLoader {  // rows (m, b, kc); K = i, l = m + p + 2i
-    static constexpr bool ROW_FAST = true;
+// rows (m, b, kc) of flm; k = i: up = flm(l = m + 2i), dn = flm(l = m + 1 + 2i)
+struct LegBwdLoader {
+    static constexpr bool ROW_FAST = true, TWO = true;
     const double* flm;
-    int B, nr2, p, Lm;
-    __device__ void get(long long r, int k, double& up, double& dn) const {
+    int B, nr2, Lm;
+    struct Row { const double* base; int m; };
+    __device__ Row row(long long r) const {
         const long long mb = r / nr2;
         const int kc = int(r - mb * nr2);
         const int m = int(mb / B), b = int(mb - (long long)m * B);
-        const int l = m + p + 2 * k;
-        up = (l < Lm) ? flm[(tri_idx(l, m) * B + b) * nr2 + kc] : 0.0;
-        dn = 0.0;
+        return Row{flm + (long long)b * nr2 + kc, m};
+    }
+    __device__ void get(const Row& R, int k, double& up, double& dn) const {
+        const int l = R.m + 2 * k;
+        const long long st = (long long)B * nr2;
+        up = (l < Lm) ? R.base[tri_idx(l, R.m) * st] : 0.0;
+        dn = (l + 1 < Lm) ? R.base[tri_idx(l + 1, R.m) * st] : 0.0;
     }
 };
 
-struct DftBwdLoader {  // rows (b, col); cos: Re F_m; sin: Im F_{k+1}
-    static constexpr bool ROW_FAST = true;
+// rows (b, col); k = m: (Re F_m, Im F_m); the sin operand is Im F_k at k - 1
+struct DftBwdLoader {
+    static constexpr bool ROW_FAST = true, TWO = true;
     const double* G;
-    int B, L, C, sin;
-    __device__ void get(long long r, int k, double& up, double& dn) const {
+    int L, C;
+    struct Row { const double* g; };
+    __device__ Row row(long long r) const {
         const long long b = r / C, col = r - b * C;
-        const int m = sin ? k + 1 : k;
-        up = G[((b * L + m) * C + col) * 2 + sin];
-        dn = 0.0;
+        return Row{G + ((b * L) * C + col) * 2};
+    }
+    __device__ void get(const Row& R, int k, double& up, double& dn) const {
+        const double2 v = *reinterpret_cast<const double2*>(R.g + (long long)k * C * 2);
+        up = v.x;
+        dn = v.y;
     }
 };
 
-// One CTA converts R rows (R = slice_rows_per_block(K)) of K values: the
-// FP64 values are staged in shared memory (dynamic: 2 R K doubles) while the
-// row maxima are found, then every value is rounded to the row's fixed-point
-// grid, folded exactly in integers where requested, and split into balanced
-// base-2^bits digits, written as S BF16 slices (and copies scaled by 2^-bits,
-// 2^-2bits).
+// One slicing job: one operand array (mode SL_ONE, optionally folded) or two
+// from one read of the input (SL_FOLD: up + dn and up - dn; SL_PAIR: up and
+// dn), the second at index k - shift.  Both share the row exponents.
+enum { SL_ONE = 0, SL_FOLD = 1, SL_PAIR = 2 };
+struct SliceJob {
+    long long rows;
+    int K;       // staged k range (K0, and K1 + shift for the second array)
+    int S, bits, mode, fold, R, copies;
+    int K0, Kp0, K1, Kp1, shift;
+    __nv_bfloat16* out0;
+    __nv_bfloat16* out1;
+    long long stride0, stride1;  // elements between slices
+    int* ex0;
+    int* ex1;
+};
+
+// BF16 bits of the small integer d (|d| <= 2^8) times 2^{-sh}: the float is
+// exact and has at most 8 significant bits, so its upper half is the BF16.
+__device__ __forceinline__ uint32_t digit_f32_bits(int d, float scale) {
+    const float f = (__int_as_float(0x4B400000 + d) - 12582912.0f) * scale;
+    return __float_as_uint(f);
+}
+
+__device__ __forceinline__ void write_pair(uint32_t* dst, long long stride2, int copies, int bits, int d0, int d1) {
+    for (int c = 0; c < copies; ++c) {
+        const float sc = __int_as_float((127 - bits * c) << 23);  // 2^{-bits c}, exact
+        dst[c * stride2] = __byte_perm(digit_f32_bits(d0, sc), digit_f32_bits(d1, sc), 0x7632);
+    }
+}
+
+// Digits of two neighbouring elements, least significant first, each slice
+// written as one BF16 pair (slice s of copy c at out + (c S + s) stride).
+__device__ __forceinline__ void write_digits(long long w0, long long w1, const SliceJob& J, __nv_bfloat16* out,
+                                             long long stride, long long off) {
+    const long long mask = (1ll << J.bits) - 1;
+    const int halfv = 1 << (J.bits - 1), base = 1 << J.bits;
+    uint32_t* o = reinterpret_cast<uint32_t*>(out + off);
+    const long long stride2 = stride >> 1;  // in BF16 pairs (slice strides are even)
+    for (int s = J.S - 1; s >= 1; --s) {
+        int r0 = int(w0 & mask), r1 = int(w1 & mask);
+        if (r0 >= halfv) r0 -= base;
+        if (r1 >= halfv) r1 -= base;
+        w0 = (w0 - r0) >> J.bits;
+        w1 = (w1 - r1) >> J.bits;
+        write_pair(o + s * stride2, (long long)J.S * stride2, J.copies, J.bits, r0, r1);
+    }
+    write_pair(o, (long long)J.S * stride2, J.copies, J.bits, int(w0), int(w1));
+}
+
+// One CTA converts R rows of K values: the FP64 values are staged in shared
+// memory while the row maxima are found (thread-local in row-fast loops, a
+// warp reduction otherwise), then every value is rounded to the row's
+// fixed-point grid, folded exactly in integers where requested, and split
+// into balanced base-2^bits digits, written as S BF16 slices per copy
+// (copies scaled by 2^-bits, 2^-2bits).
 template <class Loader>
-__global__ void __launch_bounds__(256) slice_kernel(Loader ld, long long rows, int K, int Kp, int S, int bits,
-                                                    int fold, int R, int copies, __nv_bfloat16* __restrict__ out,
-                                                    long long slice_stride, int* __restrict__ ex) {
+__global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
     extern __shared__ double sl_smem[];
+    const int R = J.R, K = J.K;
     double* vu = sl_smem;
     double* vd = sl_smem + (size_t)R * K;
     __shared__ int emax[16];
+    __shared__ typename Loader::Row rowh[16];
     const long long row0 = (long long)blockIdx.x * R;
     if (threadIdx.x < 16) emax[threadIdx.x] = 0;
+    if (threadIdx.x < R && row0 + threadIdx.x < J.rows) rowh[threadIdx.x] = ld.row(row0 + threadIdx.x);
     __syncthreads();
-    for (int e = threadIdx.x; e < R * K; e += blockDim.x) {
-        int r, k;
-        if (Loader::ROW_FAST) { r = e % R; k = e / R; }
+    int tmax = 0;
+    const int lane = threadIdx.x & 31;
+    // warp-uniform trip count, so that the warp-wide reductions see all lanes
+    for (int e0 = threadIdx.x - lane; e0 < R * K; e0 += blockDim.x) {
+        const int e = e0 + lane;
+        const bool valid = e < R * K;
+        int r = 0, k = 0;
+        if (Loader::ROW_FAST) { r = e & (R - 1); k = e / R; }
         else { k = e % K; r = e / K; }
-        double up = 0.0, dn = 0.0;
-        if (row0 + r < rows) ld.get(row0 + r, k, up, dn);
-        vu[r * K + k] = up;
-        vd[r * K + k] = dn;
-        const int ee = max(biased_exp(up), biased_exp(dn));
-        if (ee) atomicMax(&emax[r], ee);
+        int ee = 0;
+        if (valid) {
+            double up = 0.0, dn = 0.0;
+            if (row0 + r < J.rows) ld.get(rowh[r], k, up, dn);
+            vu[r * K + k] = up;
+            if (Loader::TWO) vd[r * K + k] = dn;
+            ee = Loader::TWO ? max(biased_exp(up), biased_exp(dn)) : biased_exp(up);
+        }
+        if (Loader::ROW_FAST) {
+            tmax = max(tmax, ee);  // R divides the block size: this thread's row is fixed
+        } else {
+            const unsigned same = __match_any_sync(0xffffffffu, valid ? r : -1);
+            const int m = __reduce_max_sync(same, ee);
+            if (valid && lane == __ffs(same) - 1 && m) atomicMax(&emax[r], m);
+        }
     }
+    if (Loader::ROW_FAST && tmax) atomicMax(&emax[threadIdx.x & (R - 1)], tmax);
     __syncthreads();
-    const int hk = Kp >> 1;  // pairs of k per row
-    for (int e = threadIdx.x; e < R * hk; e += blockDim.x) {
-        const int r = e / hk, k = (e - r * hk) * 2;
-        const long long row = row0 + r;
-        if (row >= rows) continue;
-        // |x| < 2^(E_max - 1022); one more bit of headroom for the balanced
-        // leading digit, and one for a folded sum
-        const int er = emax[r] - 1022 + 1 + (fold ? 1 : 0);
-        long long v[2];
+    const int fold_bit = (J.mode == SL_FOLD || (J.mode == SL_ONE && J.fold)) ? 1 : 0;
+    const int nbits = J.bits * J.S;
+    // first array
+    {
+        const int hk = J.Kp0 >> 1;
+        for (int e = threadIdx.x; e < R * hk; e += blockDim.x) {
+            const int r = e / hk, k = (e - r * hk) * 2;
+            const long long row = row0 + r;
+            if (row >= J.rows) continue;
+            // |x| < 2^(E_max - 1022); one more bit of headroom for the balanced
+            // leading digit, and one for a folded sum
+            const int er = emax[r] - 1022 + 1 + fold_bit;
+            long long w[2];
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const int kk = k + q;
-            long long x = 0;
-            if (kk < K) {
-                x = to_fixed(vu[r * K + kk], er, bits * S);
-                if (fold == 1) x += to_fixed(vd[r * K + kk], er, bits * S);
-                else if (fold == 2) x -= to_fixed(vd[r * K + kk], er, bits * S);
+            for (int q = 0; q < 2; ++q) {
+                const int kk = k + q;
+                long long x = 0;
+                if (kk < J.K0) {
+                    x = to_fixed(vu[r * K + kk], er, nbits);
+                    if (J.mode == SL_FOLD || (J.mode == SL_ONE && J.fold == 1)) x += to_fixed(vd[r * K + kk], er, nbits);
+                    else if (J.mode == SL_ONE && J.fold == 2) x -= to_fixed(vd[r * K + kk], er, nbits);
+                }
+                w[q] = x;
             }
-            v[q] = x;
+            write_digits(w[0], w[1], J, J.out0, J.stride0, row * J.Kp0 + k);
+            if (k == 0) J.ex0[row] = er;
         }
-        int dg[2][8];
-        const long long mask = (1ll << bits) - 1;
-        const int halfv = 1 << (bits - 1), base = 1 << bits;
+    }
+    if (J.mode == SL_ONE) return;
+    // second array: index k - shift
+    {
+        const int hk = J.Kp1 >> 1;
+        for (int e = threadIdx.x; e < R * hk; e += blockDim.x) {
+            const int r = e / hk, k = (e - r * hk) * 2;
+            const long long row = row0 + r;
+            if (row >= J.rows) continue;
+            const int er = emax[r] - 1022 + 1 + fold_bit;
+            long long w[2];
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            long long w = v[q];
-            for (int s = S - 1; s >= 1; --s) {
-                int rem = int(w & mask);
-                if (rem >= halfv) rem -= base;
-                dg[q][s] = rem;
-                w = (w - rem) >> bits;
+            for (int q = 0; q < 2; ++q) {
+                const int kk = k + q, src = kk + J.shift;
+                long long x = 0;
+                if (kk < J.K1) {
+                    if (J.mode == SL_FOLD)
+                        x = to_fixed(vu[r * K + src], er, nbits) - to_fixed(vd[r * K + src], er, nbits);
+                    else
+                        x = to_fixed(vd[r * K + src], er, nbits);
+                }
+                w[q] = x;
             }
-            dg[q][0] = int(w);
+            write_digits(w[0], w[1], J, J.out1, J.stride1, row * J.Kp1 + k);
+            if (k == 0) J.ex1[row] = er;
         }
-        for (int c = 0; c < copies; ++c) {
-            const float sc = __int_as_float((127 - bits * c) << 23);  // 2^{-bits c}, exact
-            for (int s = 0; s < S; ++s) {
-                __nv_bfloat162 pr;
-                pr.x = __float2bfloat16_rn(float(dg[0][s]) * sc);
-                pr.y = __float2bfloat16_rn(float(dg[1][s]) * sc);
-                *reinterpret_cast<__nv_bfloat162*>(out + (c * S + s) * slice_stride + row * Kp + k) = pr;
-            }
-        }
-        if (k == 0) ex[row] = er;
     }
 }
 
@@ -980,18 +1072,64 @@ void destroy_split(SplitState* s) { delete s; }
 namespace {
 
 template <class Loader>
+int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
+    if (J.rows <= 0) return ZEST_GPU_OK;
+    if (J.K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: K above 992");
+    if (J.bits != 7 && !(J.bits == 8 && J.K <= SL_K8MAX))
+        return fail(ZEST_GPU_ERR_INVALID, "split path: digit width");
+    J.R = slice_rows_per_block(J.K, Loader::TWO);
+    const size_t smem = (size_t)(Loader::TWO ? 2 : 1) * J.R * J.K * sizeof(double);
+    ZG_CUDA_TRY(cudaFuncSetAttribute(slice_kernel<Loader>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+    const long long blocks = (J.rows + J.R - 1) / J.R;
+    slice_kernel<Loader><<<(unsigned)blocks, 256, smem, s>>>(ld, J);
+    return launch_check("slice_kernel");
+}
+
+// One operand array from `up` (fold 0) or up +- dn (fold 1 / 2).
+template <class Loader>
 int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S, int bits, int fold, SliceArray& out) {
     out.bits = bits;
-    if (rows <= 0) return ZEST_GPU_OK;
-    if (K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: K above 992");
-    if (bits != 7 && !(bits == 8 && K <= SL_K8MAX)) return fail(ZEST_GPU_ERR_INVALID, "split path: digit width");
-    const int R = slice_rows_per_block(K);
-    const size_t smem = (size_t)2 * R * K * sizeof(double);
-    ZG_CUDA_TRY(cudaFuncSetAttribute(slice_kernel<Loader>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-    const long long blocks = (rows + R - 1) / R;
-    slice_kernel<Loader><<<(unsigned)blocks, 256, smem, s>>>(ld, rows, K, out.Kp, S, bits, fold, R, out.copies, out.ptr(),
-                                                            rows * out.Kp, out.ex.as<int>());
-    return launch_check("slice_kernel");
+    SliceJob J{};
+    J.rows = rows;
+    J.K = J.K0 = K;
+    J.Kp0 = out.Kp;
+    J.S = S;
+    J.bits = bits;
+    J.mode = SL_ONE;
+    J.fold = fold;
+    J.copies = out.copies;
+    J.out0 = out.ptr();
+    J.stride0 = out.rows * out.Kp;
+    J.ex0 = out.ex.as<int>();
+    return run_slice(s, ld, J);
+}
+
+// Two operand arrays from one read: SL_FOLD (up + dn, up - dn) or SL_PAIR
+// (up, dn); the second holds k in [shift, shift + K1) at k - shift.
+template <class Loader>
+int launch_slice2(cudaStream_t s, const Loader& ld, long long rows, int K0, int K1, int shift, int S, int bits,
+                  int mode, SliceArray& out0, SliceArray& out1) {
+    out0.bits = out1.bits = bits;
+    SliceJob J{};
+    J.rows = rows;
+    J.K0 = K0;
+    J.K1 = K1;
+    J.shift = shift;
+    J.K = std::max(K0, K1 + shift);
+    J.Kp0 = out0.Kp;
+    J.Kp1 = out1.Kp;
+    J.S = S;
+    J.bits = bits;
+    J.mode = mode;
+    J.copies = out0.copies;
+    if (out1.copies != out0.copies) return fail(ZEST_GPU_ERR_INVALID, "split path: slice copies differ");
+    J.out0 = out0.ptr();
+    J.out1 = out1.ptr();
+    J.stride0 = out0.rows * out0.Kp;
+    J.stride1 = out1.rows * out1.Kp;
+    J.ex0 = out0.ex.as<int>();
+    J.ex1 = out1.ex.as<int>();
+    return run_slice(s, ld, J);
 }
 
 int get_state(zest_gpu_context* ctx, SplitState** out) {
@@ -1302,9 +1440,8 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
         ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, DftFwdLoader{grids, sh.size(), C, N, 0}, rows, Lg, S, bits, 1, st->op[0]));
-            if (Lg > 1)
-                ZG_TRY(launch_slice(s, DftFwdLoader{grids, sh.size(), C, N, 1}, rows, Lg - 1, S, bits, 2, st->op[1]));
+            ZG_TRY(launch_slice2(s, DftFwdLoader{grids, sh.size(), C, N}, rows, Lg, Lg - 1, 1, S, bits, SL_FOLD,
+                                 st->op[0], st->op[1]));
         }
         UnitList* u;
         ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
@@ -1325,8 +1462,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
             LegFwdLoader ld{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d};
-            ZG_TRY(launch_slice(s, ld, rows, kh, S, bits, 1, st->op[0]));
-            ZG_TRY(launch_slice(s, ld, rows, kh, S, bits, 2, st->op[1]));
+            ZG_TRY(launch_slice2(s, ld, rows, kh, kh, 0, S, bits, SL_FOLD, st->op[0], st->op[1]));
         }
         UnitList* u;
         ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
@@ -1407,9 +1543,8 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
         ZG_TRY(st->op[1].ensure(rows, kl, S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, LegBwdLoader{flm, batch, nr2, 0, Lm}, rows, (Lm + 1) / 2, S, bits, 0,
-                                st->op[0]));
-            ZG_TRY(launch_slice(s, LegBwdLoader{flm, batch, nr2, 1, Lm}, rows, Lm / 2, S, bits, 0, st->op[1]));
+            ZG_TRY(launch_slice2(s, LegBwdLoader{flm, batch, nr2, Lm}, rows, (Lm + 1) / 2, Lm / 2, 0, S, bits,
+                                 SL_PAIR, st->op[0], st->op[1]));
         }
         if (Lm < Lg) {
             StageScope sc(ctx, ST_MEMSET);
@@ -1437,9 +1572,8 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
         ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, DftBwdLoader{G, batch, Lg, C, 0}, rows, Lg, S, bits, 0, st->op[0]));
-            if (Lg > 1)
-                ZG_TRY(launch_slice(s, DftBwdLoader{G, batch, Lg, C, 1}, rows, Lg - 1, S, bits, 0, st->op[1]));
+            ZG_TRY(launch_slice2(s, DftBwdLoader{G, Lg, C}, rows, Lg, Lg - 1, 1, S, bits, SL_PAIR, st->op[0],
+                                 st->op[1]));
         }
         UnitList* u;
         ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
