@@ -80,8 +80,9 @@ int zest_gpu_ctx_create(zest_gpu_context** ctx, int device, void* stream);
 int zest_gpu_ctx_destroy(zest_gpu_context* ctx);
 /* Message of the last failing call on this thread ("" if none). */
 const char* zest_gpu_last_error(void);
-/* Precision of the dense contractions; `slices` = number of 7-bit BF16
- * slices per operand for ZEST_PRECISION_SPLIT (4..8, 0 = default 6). */
+/* Precision of the dense contractions; `slices` = number of BF16 digit
+ * slices per operand for ZEST_PRECISION_SPLIT (4..6, 0 = default 6): 8-bit
+ * digits for contraction lengths up to 256, 7-bit digits above. */
 int zest_gpu_set_precision(zest_gpu_context* ctx, int precision, int slices);
 int zest_gpu_synchronize(zest_gpu_context* ctx);
 /* Releases cached tables and scratch (they are rebuilt on demand). */
@@ -114,7 +115,8 @@ size_t zest_gpu_st_coeff_size(size_t order);
  * forward: zt::GLQTransformer<...>::forward_transform(BallGLQGridSpan<const double>,
  *          RealZernikeSpan<std::array<double,2>,...>)  zernike_glq_transformer.hpp:640-655
  *          (and the container-returning overload :687-693).  The expansion is
- *          truncated to min(exp_order, grid_order); higher coefficients are zeroed.
+ *          truncated to min(exp_order, grid_order); as in the reference, coefficients of
+ *          higher orders are not written (the SH forward transform likewise).
  * backward: ::backward_transform(RealZernikeSpan<const ...>, BallGLQGridSpan<double>)
  *          zernike_glq_transformer.hpp:663-679 (and :701-707). */
 int zest_gpu_zt_forward(zest_gpu_context* ctx, int zernike_norm, int sh_norm, int sh_phase,

@@ -104,6 +104,23 @@ def test_zt_order_mismatch(ctx, golden):
     assert relmax(ctx.zt_backward(z["trunc_c6"].ravel(), 6, 9), z["trunc_g69"]) < TOL
 
 
+def test_forward_leaves_orders_above_the_grid_untouched(ctx):
+    # zernike_glq_transformer.hpp:640-655 / sh_glq_transformer.hpp:632-647 write
+    # only the coefficients below min(expansion order, grid order)
+    from zest_gb300 import zt_coeff_size, st_coeff_size, zt_grid_shape, st_grid_shape
+    rng = np.random.default_rng(11)
+    g = rng.normal(size=int(np.prod(zt_grid_shape(6))))
+    out = np.full(2 * zt_coeff_size(9), 7.5)
+    ctx.zt_forward(g, 6, 9, out=out)
+    assert np.all(out[2 * zt_coeff_size(6):] == 7.5)
+    assert np.array_equal(out[:2 * zt_coeff_size(6)], ctx.zt_forward(g, 6, 6))
+    gs = rng.normal(size=int(np.prod(st_grid_shape(6))))
+    outs = np.full(2 * st_coeff_size(9), -2.0)
+    ctx.st_forward(gs, 6, 9, out=outs)
+    assert np.all(outs[2 * st_coeff_size(6):] == -2.0)
+    assert np.array_equal(outs[:2 * st_coeff_size(6)], ctx.st_forward(gs, 6, 6))
+
+
 @pytest.mark.parametrize("L,batch", [(33, 3), (64, 2)])
 def test_zt_vs_oracle_batched(ctx, oracle, L, batch):
     rng = np.random.default_rng(L)

@@ -346,10 +346,12 @@ class Context:
 
     @staticmethod
     def _alloc_like(x, n):
+        # zero-filled like the reference's containers: a forward transform to a
+        # higher expansion order leaves the orders above the grid's untouched
         if _is_torch(x):
             import torch
-            return torch.empty(n, dtype=torch.float64, device=x.device)
-        return np.empty(n, dtype=np.float64)
+            return torch.zeros(n, dtype=torch.float64, device=x.device)
+        return np.zeros(n, dtype=np.float64)
 
 
 def gl_nodes_weights(n: int, packed: bool = False):

@@ -199,20 +199,18 @@ __device__ __forceinline__ double u64_ldexp(unsigned long long a, bool neg, int 
 // fixed point: round(x 2^{nbits-e}) as int64 (|x| < 2^(e-1)), ties to even
 __device__ __forceinline__ long long to_fixed(double x, int e, int nbits) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    const int E = int((bits >> 52) & 0x7FF);
-    if (E == 0) return 0;  // zero and subnormals
+    const int E = int(bits >> 52) & 0x7FF;
     const unsigned long long M = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     const int sh = 1075 + e - nbits - E;
-    long long v;
-    if (sh >= 63) {
+    unsigned long long v;
+    if (E == 0 || sh >= 63) {  // zero, subnormals, and values below half a unit
         v = 0;
-    } else if (sh > 0) {  // round to nearest, ties to even
-        const unsigned long long q = M >> sh, rem = M & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-        v = (long long)(q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull));
+    } else if (sh > 0) {  // round to nearest, ties to even: add half - 1 and the parity of the kept part
+        v = (M + ((1ull << (sh - 1)) - 1) + ((M >> sh) & 1ull)) >> sh;
     } else {
-        v = (long long)(M << (-sh));
+        v = M << (-sh);
     }
-    return (bits >> 63) ? -v : v;
+    return (bits >> 63) ? -(long long)v : (long long)v;
 }
 
 __device__ __forceinline__ int biased_exp(double x) {
@@ -383,30 +381,50 @@ __device__ __forceinline__ uint32_t digit_f32_bits(int d, float scale) {
     return __float_as_uint(f);
 }
 
-__device__ __forceinline__ void write_pair(uint32_t* dst, long long stride2, int copies, int bits, int d0, int d1) {
+// Balanced digits of four neighbouring elements (slice 0 most significant)
+// written as BF16: four elements per slice and copy in one 8-byte store.
+// 8-bit digits: adding 128 sum_{i<S-1} 256^i turns the lower balanced digits
+// into the plain bytes of the sum (digit = byte - 128) and leaves the leading
+// digit as the sum shifted down.
+template <int S>
+__device__ __forceinline__ void write_digits4(const long long (&w)[4], int bits, int copies, __nv_bfloat16* out,
+                                              long long stride, long long off) {
+    int d[4][S];
+    if (bits == 8) {
+        constexpr long long OFF = (long long)((0x8080808080808080ull) >> (8 * (9 - S)));  // 128 per lower byte
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const long long u = w[q] + OFF;
+#pragma unroll
+            for (int s = 1; s < S; ++s) d[q][s] = int((u >> (8 * (S - 1 - s))) & 255) - 128;
+            d[q][0] = int(u >> (8 * (S - 1)));
+        }
+    } else {
+        const long long mask = (1ll << bits) - 1;
+        const int halfv = 1 << (bits - 1), base = 1 << bits;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            long long x = w[q];
+#pragma unroll
+            for (int s = S - 1; s >= 1; --s) {
+                int r = int(x & mask);
+                if (r >= halfv) r -= base;
+                d[q][s] = r;
+                x = (x - r) >> bits;
+            }
+            d[q][0] = int(x);
+        }
+    }
     for (int c = 0; c < copies; ++c) {
         const float sc = __int_as_float((127 - bits * c) << 23);  // 2^{-bits c}, exact
-        dst[c * stride2] = __byte_perm(digit_f32_bits(d0, sc), digit_f32_bits(d1, sc), 0x7632);
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            uint2 v;
+            v.x = __byte_perm(digit_f32_bits(d[0][s], sc), digit_f32_bits(d[1][s], sc), 0x7632);
+            v.y = __byte_perm(digit_f32_bits(d[2][s], sc), digit_f32_bits(d[3][s], sc), 0x7632);
+            *reinterpret_cast<uint2*>(out + (c * S + s) * stride + off) = v;
+        }
     }
-}
-
-// Digits of two neighbouring elements, least significant first, each slice
-// written as one BF16 pair (slice s of copy c at out + (c S + s) stride).
-__device__ __forceinline__ void write_digits(long long w0, long long w1, const SliceJob& J, __nv_bfloat16* out,
-                                             long long stride, long long off) {
-    const long long mask = (1ll << J.bits) - 1;
-    const int halfv = 1 << (J.bits - 1), base = 1 << J.bits;
-    uint32_t* o = reinterpret_cast<uint32_t*>(out + off);
-    const long long stride2 = stride >> 1;  // in BF16 pairs (slice strides are even)
-    for (int s = J.S - 1; s >= 1; --s) {
-        int r0 = int(w0 & mask), r1 = int(w1 & mask);
-        if (r0 >= halfv) r0 -= base;
-        if (r1 >= halfv) r1 -= base;
-        w0 = (w0 - r0) >> J.bits;
-        w1 = (w1 - r1) >> J.bits;
-        write_pair(o + s * stride2, (long long)J.S * stride2, J.copies, J.bits, r0, r1);
-    }
-    write_pair(o, (long long)J.S * stride2, J.copies, J.bits, int(w0), int(w1));
 }
 
 // One CTA converts R rows of K values: the FP64 values are staged in shared
@@ -415,7 +433,7 @@ __device__ __forceinline__ void write_digits(long long w0, long long w1, const S
 // fixed-point grid, folded exactly in integers where requested, and split
 // into balanced base-2^bits digits, written as S BF16 slices per copy
 // (copies scaled by 2^-bits, 2^-2bits).
-template <class Loader>
+template <class Loader, int S>
 __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
     extern __shared__ double sl_smem[];
     const int R = J.R, K = J.K;
@@ -455,20 +473,20 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
     if (Loader::ROW_FAST && tmax) atomicMax(&emax[threadIdx.x & (R - 1)], tmax);
     __syncthreads();
     const int fold_bit = (J.mode == SL_FOLD || (J.mode == SL_ONE && J.fold)) ? 1 : 0;
-    const int nbits = J.bits * J.S;
-    // first array
+    const int nbits = J.bits * S;
+    // first array: four neighbouring k per thread
     {
-        const int hk = J.Kp0 >> 1;
-        for (int e = threadIdx.x; e < R * hk; e += blockDim.x) {
-            const int r = e / hk, k = (e - r * hk) * 2;
+        const int qk = J.Kp0 >> 2;
+        for (int e = threadIdx.x; e < R * qk; e += blockDim.x) {
+            const int r = e / qk, k = (e - r * qk) * 4;
             const long long row = row0 + r;
             if (row >= J.rows) continue;
             // |x| < 2^(E_max - 1022); one more bit of headroom for the balanced
             // leading digit, and one for a folded sum
             const int er = emax[r] - 1022 + 1 + fold_bit;
-            long long w[2];
+            long long w[4];
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
+            for (int q = 0; q < 4; ++q) {
                 const int kk = k + q;
                 long long x = 0;
                 if (kk < J.K0) {
@@ -478,22 +496,22 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
                 }
                 w[q] = x;
             }
-            write_digits(w[0], w[1], J, J.out0, J.stride0, row * J.Kp0 + k);
+            write_digits4<S>(w, J.bits, J.copies, J.out0, J.stride0, row * J.Kp0 + k);
             if (k == 0) J.ex0[row] = er;
         }
     }
     if (J.mode == SL_ONE) return;
     // second array: index k - shift
     {
-        const int hk = J.Kp1 >> 1;
-        for (int e = threadIdx.x; e < R * hk; e += blockDim.x) {
-            const int r = e / hk, k = (e - r * hk) * 2;
+        const int qk = J.Kp1 >> 2;
+        for (int e = threadIdx.x; e < R * qk; e += blockDim.x) {
+            const int r = e / qk, k = (e - r * qk) * 4;
             const long long row = row0 + r;
             if (row >= J.rows) continue;
             const int er = emax[r] - 1022 + 1 + fold_bit;
-            long long w[2];
+            long long w[4];
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
+            for (int q = 0; q < 4; ++q) {
                 const int kk = k + q, src = kk + J.shift;
                 long long x = 0;
                 if (kk < J.K1) {
@@ -504,7 +522,7 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
                 }
                 w[q] = x;
             }
-            write_digits(w[0], w[1], J, J.out1, J.stride1, row * J.Kp1 + k);
+            write_digits4<S>(w, J.bits, J.copies, J.out1, J.stride1, row * J.Kp1 + k);
             if (k == 0) J.ex1[row] = er;
         }
     }
@@ -1079,10 +1097,18 @@ int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
         return fail(ZEST_GPU_ERR_INVALID, "split path: digit width");
     J.R = slice_rows_per_block(J.K, Loader::TWO);
     const size_t smem = (size_t)(Loader::TWO ? 2 : 1) * J.R * J.K * sizeof(double);
-    ZG_CUDA_TRY(cudaFuncSetAttribute(slice_kernel<Loader>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
     const long long blocks = (J.rows + J.R - 1) / J.R;
-    slice_kernel<Loader><<<(unsigned)blocks, 256, smem, s>>>(ld, J);
-    return launch_check("slice_kernel");
+    auto go = [&](auto kern) -> int {
+        ZG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+        kern<<<(unsigned)blocks, 256, smem, s>>>(ld, J);
+        return launch_check("slice_kernel");
+    };
+    switch (J.S) {
+    case 4: return go(slice_kernel<Loader, 4>);
+    case 5: return go(slice_kernel<Loader, 5>);
+    case 6: return go(slice_kernel<Loader, 6>);
+    }
+    return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path supports 4..6 slices");
 }
 
 // One operand array from `up` (fold 0) or up +- dn (fold 1 / 2).

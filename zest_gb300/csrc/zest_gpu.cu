@@ -292,10 +292,12 @@ int zt_forward_dev(zest_gpu_context* ctx, int zn, int sn, int sp, int Lg, int Le
                    double* coeffs) {
     cudaStream_t s = ctx->stream;
     const long long csz = 2 * zsize(Le);
-    if (batch == 0 || Le == 0) return ZEST_GPU_OK;
-    ZG_CUDA_TRY(cudaMemsetAsync(coeffs, 0, (size_t)batch * csz * sizeof(double), s));
-    if (Lg == 0) return ZEST_GPU_OK;
+    if (batch == 0 || Le == 0 || Lg == 0) return ZEST_GPU_OK;
     const int Lm = Lg < Le ? Lg : Le;
+    // like the reference, only the coefficients of orders below min(Le, Lg) are
+    // written; the rest of each expansion is left as it was
+    ZG_CUDA_TRY(cudaMemset2DAsync(coeffs, (size_t)csz * sizeof(double), 0, (size_t)2 * zsize(Lm) * sizeof(double),
+                                  batch, s));
     ZtPlan* plan;
     ZG_TRY(get_zt_plan(ctx, Lg, zn, sn, sp, &plan));
     if (ctx->precision == ZEST_PRECISION_SPLIT)
@@ -387,10 +389,11 @@ int st_forward_dev(zest_gpu_context* ctx, int sn, int sp, int layout, int Lg, in
                    const double* grids, double* coeffs) {
     cudaStream_t s = ctx->stream;
     const long long csz = 2 * tri_size(Le);
-    if (batch == 0 || Le == 0) return ZEST_GPU_OK;
-    ZG_CUDA_TRY(cudaMemsetAsync(coeffs, 0, (size_t)batch * csz * sizeof(double), s));
-    if (Lg == 0) return ZEST_GPU_OK;
+    if (batch == 0 || Le == 0 || Lg == 0) return ZEST_GPU_OK;
     const int Lm = Lg < Le ? Lg : Le;
+    // only the coefficients of orders below min(Le, Lg) are written, as in the reference
+    ZG_CUDA_TRY(cudaMemset2DAsync(coeffs, (size_t)csz * sizeof(double), 0, (size_t)2 * tri_size(Lm) * sizeof(double),
+                                  batch, s));
     StPlan* plan;
     ZG_TRY(get_st_plan(ctx, Lg, sn, sp, layout, &plan));
     const StShape& sh = plan->sh;
@@ -529,8 +532,12 @@ int check_ctx(zest_gpu_context* ctx) {
 }
 
 // Runs `body(in_dev, out_dev)` on device pointers, staging host buffers.
+// With out_pitch > 0 only the first out_width of every out_pitch output
+// elements are written by `body` and copied back (the rest of a host output is
+// left as it was).
 template <class F>
-int with_staging(zest_gpu_context* ctx, int mem, const double* in, size_t in_n, double* out, size_t out_n, F&& body) {
+int with_staging(zest_gpu_context* ctx, int mem, const double* in, size_t in_n, double* out, size_t out_n, F&& body,
+                 size_t out_pitch = 0, size_t out_width = 0) {
     if (mem == ZEST_MEM_DEVICE) return body(in, out);
     if (mem != ZEST_MEM_HOST) return fail(ZEST_GPU_ERR_INVALID, "mem must be ZEST_MEM_HOST or ZEST_MEM_DEVICE");
     cudaStream_t s = ctx->stream;
@@ -541,7 +548,13 @@ int with_staging(zest_gpu_context* ctx, int mem, const double* in, size_t in_n, 
         ZG_CUDA_TRY(cudaMemcpyAsync(ctx->in_stage.p, in, in_n * sizeof(double), cudaMemcpyHostToDevice, s));
     }
     ZG_TRY(body(ctx->in_stage.as<double>(), ctx->out_stage.as<double>()));
-    if (out_n) {
+    if (out_n && out_pitch && out_width < out_pitch) {
+        if (out_width) {
+            StageScope sc(ctx, ST_COPY_D2H);
+            ZG_CUDA_TRY(cudaMemcpy2DAsync(out, out_pitch * sizeof(double), ctx->out_stage.p, out_pitch * sizeof(double),
+                                          out_width * sizeof(double), out_n / out_pitch, cudaMemcpyDeviceToHost, s));
+        }
+    } else if (out_n) {
         StageScope sc(ctx, ST_COPY_D2H);
         ZG_CUDA_TRY(cudaMemcpyAsync(out, ctx->out_stage.p, out_n * sizeof(double), cudaMemcpyDeviceToHost, s));
     }
@@ -680,9 +693,13 @@ int zest_gpu_zt_forward(zest_gpu_context* ctx, int zn, int sn, int sp, size_t gr
     if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
     const size_t gn = batch * zest_gpu_zt_grid_size(grid_order), cn = batch * 2 * zest_gpu_zt_coeff_size(exp_order);
     if ((gn && !grids) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
-    return with_staging(ctx, mem, grids, gn, coeffs, cn, [&](const double* in, double* out) {
-        return zt_forward_dev(ctx, zn, sn, sp, int(grid_order), int(exp_order), int(batch), in, out);
-    });
+    const size_t lm = grid_order < exp_order ? grid_order : exp_order;
+    return with_staging(
+        ctx, mem, grids, gn, coeffs, cn,
+        [&](const double* in, double* out) {
+            return zt_forward_dev(ctx, zn, sn, sp, int(grid_order), int(exp_order), int(batch), in, out);
+        },
+        2 * zest_gpu_zt_coeff_size(exp_order), 2 * zest_gpu_zt_coeff_size(lm));
 }
 
 int zest_gpu_zt_backward(zest_gpu_context* ctx, int zn, int sn, int sp, size_t exp_order, size_t grid_order,
@@ -706,9 +723,13 @@ int zest_gpu_st_forward(zest_gpu_context* ctx, int sn, int sp, int layout, size_
     if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
     const size_t gn = batch * zest_gpu_st_grid_size(grid_order, layout), cn = batch * 2 * zest_gpu_st_coeff_size(exp_order);
     if ((gn && !grids) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
-    return with_staging(ctx, mem, grids, gn, coeffs, cn, [&](const double* in, double* out) {
-        return st_forward_dev(ctx, sn, sp, layout, int(grid_order), int(exp_order), int(batch), in, out);
-    });
+    const size_t lm = grid_order < exp_order ? grid_order : exp_order;
+    return with_staging(
+        ctx, mem, grids, gn, coeffs, cn,
+        [&](const double* in, double* out) {
+            return st_forward_dev(ctx, sn, sp, layout, int(grid_order), int(exp_order), int(batch), in, out);
+        },
+        2 * zest_gpu_st_coeff_size(exp_order), 2 * zest_gpu_st_coeff_size(lm));
 }
 
 int zest_gpu_st_backward(zest_gpu_context* ctx, int sn, int sp, int layout, size_t exp_order, size_t grid_order,
