@@ -1,0 +1,831 @@
+// C++20 interface of zest_gb300 with the reference's API (sebsassi/zest):
+// the same namespaces, class templates, aliases and member functions for the
+// Gauss-Legendre-quadrature transforms and rotations, each call forwarded to
+// the C-ABI of libzest_gb300 (zest_gpu.h), which runs it on the GPU.
+//
+// Code written against the reference's
+//     zest::zt::GLQTransformerGeo<> transformer(order);
+//     transformer.forward_transform(grid, expansion);
+//     zest::Rotor rotor(order);
+//     rotor.rotate(expansion, wigner_d_pi2, euler_angles, zest::RotationType::object);
+// compiles unchanged against these headers.  The conventions are template
+// parameters, so a grid, an expansion and a transformer of different
+// conventions do not combine: the mismatch is a compile-time error, as in the
+// reference.
+//
+// Interfaces kept (reference file:line):
+//   zt::LonLatRadLayout, BallGLQGridSpan, BallGLQGrid     zernike_glq_transformer.hpp:50-501
+//   zt::GLQTransformer and its aliases                     zernike_glq_transformer.hpp:510-1025
+//   zt::RealZernikeSpan, RealZernikeExpansion + aliases    zernike_expansion.hpp:156-447
+//   st::LonLatLayout, LatLonLayout, SphereGLQGrid(Span)    sh_glq_transformer.hpp:48-504
+//   st::GLQTransformer and its aliases                     sh_glq_transformer.hpp:520-1240
+//   st::RealSHSpan, RealSHExpansion + aliases              real_sh_expansion.hpp:49-292
+//   WignerdPiHalfCollection                                wignerd_collection.hpp:66-110
+//   Rotor, RotationType, euler_angles_from_rotation_matrix rotor.hpp:38-395
+//
+// Additions of this implementation:
+//   * GPUContext: the device, stream and cached tables behind a transformer or
+//     rotor (zest_gpu_ctx_create).  Every transformer and rotor owns one; like
+//     the reference's transformers they are not thread-safe.
+//   * transformer.set_precision(Precision::split): the tensor-core form of the
+//     Zernike contractions.
+//   * *_batch member functions: many grids / expansions in one call, on host
+//     or device memory.
+// Errors throw zest::GPUError carrying the library's status code and message.
+#pragma once
+
+#include <algorithm>
+#include <array>
+#include <concepts>
+#include <cstddef>
+#include <cstdint>
+#include <new>
+#include <span>
+#include <stdexcept>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "../zest_gpu.h"
+
+namespace zest {
+
+// ---------------------------------------------------------------------------
+// Errors, device context, storage
+// ---------------------------------------------------------------------------
+class GPUError : public std::runtime_error {
+public:
+    GPUError(int code, const char* message) : std::runtime_error(message), m_code(code) {}
+    [[nodiscard]] int code() const noexcept { return m_code; }
+
+private:
+    int m_code;
+};
+
+namespace detail {
+inline void check(int status) {
+    if (status != ZEST_GPU_OK) throw GPUError(status, zest_gpu_last_error());
+}
+constexpr std::size_t pad8(std::size_t n) noexcept { return (n + 7) & ~std::size_t(7); }
+}  // namespace detail
+
+enum class Precision { fp64 = ZEST_PRECISION_FP64, split = ZEST_PRECISION_SPLIT };
+enum class MemoryKind { device = ZEST_MEM_DEVICE, host = ZEST_MEM_HOST };
+
+// Owner of one zest_gpu_context: a device, a stream (nullptr = the default
+// stream), cached tables and scratch.
+class GPUContext {
+public:
+    explicit GPUContext(int device = 0, void* stream = nullptr) {
+        detail::check(zest_gpu_ctx_create(&m_ctx, device, stream));
+    }
+    ~GPUContext() {
+        if (m_ctx) zest_gpu_ctx_destroy(m_ctx);
+    }
+    GPUContext(GPUContext&& other) noexcept : m_ctx(std::exchange(other.m_ctx, nullptr)) {}
+    GPUContext& operator=(GPUContext&& other) noexcept {
+        std::swap(m_ctx, other.m_ctx);
+        return *this;
+    }
+    GPUContext(const GPUContext&) = delete;
+    GPUContext& operator=(const GPUContext&) = delete;
+
+    [[nodiscard]] zest_gpu_context* get() const noexcept { return m_ctx; }
+    void set_precision(Precision precision, int slices = 0) {
+        detail::check(zest_gpu_set_precision(m_ctx, int(precision), slices));
+    }
+    void synchronize() { detail::check(zest_gpu_synchronize(m_ctx)); }
+
+private:
+    zest_gpu_context* m_ctx = nullptr;
+};
+
+// Containers are cache-line (64-byte) aligned, as the reference's.
+template <typename T>
+struct CacheLineAllocator {
+    using value_type = T;
+    CacheLineAllocator() noexcept = default;
+    template <typename U>
+    CacheLineAllocator(const CacheLineAllocator<U>&) noexcept {}
+    T* allocate(std::size_t n) { return static_cast<T*>(::operator new(n * sizeof(T), std::align_val_t(64))); }
+    void deallocate(T* p, std::size_t) noexcept { ::operator delete(p, std::align_val_t(64)); }
+    template <typename U>
+    bool operator==(const CacheLineAllocator<U>&) const noexcept { return true; }
+};
+template <typename T>
+using AlignedVector = std::vector<T, CacheLineAllocator<T>>;
+
+// Grid alignment policy of the layouts: the fastest axis padded to 8 doubles.
+struct CacheLineAlignment {};
+
+enum class RotationType { object, coordinate };
+
+// ---------------------------------------------------------------------------
+// Spherical harmonics
+// ---------------------------------------------------------------------------
+namespace st {
+
+enum class SHPhase { none = -1, cs = 1 };
+enum class SHNorm { geo, qm };
+
+namespace detail {
+constexpr int abi(SHNorm n) noexcept { return n == SHNorm::geo ? ZEST_SH_GEO : ZEST_SH_QM; }
+constexpr int abi(SHPhase p) noexcept { return p == SHPhase::none ? ZEST_SH_PHASE_NONE : ZEST_SH_PHASE_CS; }
+}  // namespace detail
+
+// [lon][lat]: (2L - 1, pad8(L))
+template <typename AlignmentType = CacheLineAlignment>
+struct LonLatLayout {
+    using Alignment = AlignmentType;
+    static constexpr int abi = ZEST_LAYOUT_LONLAT;
+    [[nodiscard]] static constexpr std::size_t lon_size(std::size_t order) noexcept {
+        return 2 * order - std::min<std::size_t>(1, order);
+    }
+    [[nodiscard]] static constexpr std::size_t lat_size(std::size_t order) noexcept { return zest::detail::pad8(order); }
+    [[nodiscard]] static constexpr std::array<std::size_t, 2> shape(std::size_t order) noexcept {
+        return {lon_size(order), lat_size(order)};
+    }
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept {
+        return lon_size(order) * lat_size(order);
+    }
+    static constexpr std::size_t lat_axis = 1;
+    static constexpr std::size_t lon_axis = 0;
+};
+
+// [lat][lon]: (L, pad8(2L - 1))
+template <typename AlignmentType = CacheLineAlignment>
+struct LatLonLayout {
+    using Alignment = AlignmentType;
+    static constexpr int abi = ZEST_LAYOUT_LATLON;
+    [[nodiscard]] static constexpr std::size_t lat_size(std::size_t order) noexcept { return order; }
+    [[nodiscard]] static constexpr std::size_t lon_size(std::size_t order) noexcept {
+        return zest::detail::pad8(2 * order - std::min<std::size_t>(1, order));
+    }
+    [[nodiscard]] static constexpr std::array<std::size_t, 2> shape(std::size_t order) noexcept {
+        return {lat_size(order), lon_size(order)};
+    }
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept {
+        return lon_size(order) * lat_size(order);
+    }
+    static constexpr std::size_t lat_axis = 0;
+    static constexpr std::size_t lon_axis = 1;
+};
+
+using DefaultLayout = LonLatLayout<>;
+
+// Non-owning view of grid values on the sphere.
+template <typename ElementType, typename LayoutType = DefaultLayout>
+class SphereGLQGridSpan {
+public:
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    using Layout = LayoutType;
+    using ConstView = SphereGLQGridSpan<const value_type, Layout>;
+
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept { return Layout::size(order); }
+    [[nodiscard]] static constexpr std::array<std::size_t, 2> shape(std::size_t order) noexcept {
+        return Layout::shape(order);
+    }
+
+    SphereGLQGridSpan() noexcept = default;
+    constexpr SphereGLQGridSpan(element_type* data, std::size_t order) noexcept : m_data(data), m_order(order) {}
+    constexpr SphereGLQGridSpan(std::span<element_type> buffer, std::size_t order) noexcept
+        : m_data(buffer.data()), m_order(order) {}
+
+    [[nodiscard]] constexpr std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] constexpr std::array<std::size_t, 2> shape() const noexcept { return Layout::shape(m_order); }
+    [[nodiscard]] constexpr std::size_t size() const noexcept { return Layout::size(m_order); }
+    [[nodiscard]] constexpr element_type* data() const noexcept { return m_data; }
+    [[nodiscard]] constexpr std::span<element_type> flatten() const noexcept { return {m_data, size()}; }
+    [[nodiscard]] constexpr element_type& operator()(std::size_t i, std::size_t j) const noexcept {
+        return m_data[i * shape()[1] + j];
+    }
+    [[nodiscard]] constexpr operator ConstView() const noexcept { return ConstView(m_data, m_order); }
+
+private:
+    element_type* m_data = nullptr;
+    std::size_t m_order = 0;
+};
+
+// Owning grid on the sphere.
+template <typename ElementType = double, typename LayoutType = DefaultLayout>
+class SphereGLQGrid {
+public:
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    using Layout = LayoutType;
+    using View = SphereGLQGridSpan<element_type, Layout>;
+    using ConstView = SphereGLQGridSpan<const element_type, Layout>;
+
+    SphereGLQGrid() = default;
+    explicit SphereGLQGrid(std::size_t order) : m_values(Layout::size(order)), m_order(order) {}
+
+    [[nodiscard]] std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] std::array<std::size_t, 2> shape() const noexcept { return Layout::shape(m_order); }
+    [[nodiscard]] std::size_t size() const noexcept { return m_values.size(); }
+    [[nodiscard]] element_type* data() noexcept { return m_values.data(); }
+    [[nodiscard]] const element_type* data() const noexcept { return m_values.data(); }
+    [[nodiscard]] std::span<element_type> flatten() noexcept { return m_values; }
+    [[nodiscard]] std::span<const element_type> flatten() const noexcept { return m_values; }
+    [[nodiscard]] element_type& operator()(std::size_t i, std::size_t j) noexcept {
+        return m_values[i * shape()[1] + j];
+    }
+    void resize(std::size_t order) {
+        m_values.resize(Layout::size(order));
+        m_order = order;
+    }
+    [[nodiscard]] operator View() noexcept { return View(m_values.data(), m_order); }
+    [[nodiscard]] operator ConstView() const noexcept { return ConstView(m_values.data(), m_order); }
+
+private:
+    AlignedVector<element_type> m_values;
+    std::size_t m_order = 0;
+};
+
+// Real SH coefficients {cos, sin} of degree l and order m at l(l+1)/2 + m.
+template <typename ElementType, SHNorm sh_norm_param, SHPhase sh_phase_param>
+class RealSHSpan {
+public:
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    using ConstView = RealSHSpan<const value_type, sh_norm_param, sh_phase_param>;
+    static constexpr SHNorm norm = sh_norm_param;
+    static constexpr SHPhase phase = sh_phase_param;
+
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept { return order * (order + 1) / 2; }
+    [[nodiscard]] static constexpr std::size_t idx(std::size_t l, std::size_t m) noexcept {
+        return l * (l + 1) / 2 + m;
+    }
+
+    RealSHSpan() noexcept = default;
+    constexpr RealSHSpan(element_type* data, std::size_t order) noexcept : m_data(data), m_order(order) {}
+    constexpr RealSHSpan(std::span<element_type> buffer, std::size_t order) noexcept
+        : m_data(buffer.data()), m_order(order) {}
+
+    [[nodiscard]] constexpr std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] constexpr std::size_t size() const noexcept { return size(m_order); }
+    [[nodiscard]] constexpr element_type* data() const noexcept { return m_data; }
+    [[nodiscard]] constexpr std::span<element_type> flatten() const noexcept { return {m_data, size()}; }
+    [[nodiscard]] constexpr element_type& operator()(std::size_t l, std::size_t m) const noexcept {
+        return m_data[idx(l, m)];
+    }
+    [[nodiscard]] constexpr operator ConstView() const noexcept { return ConstView(m_data, m_order); }
+
+private:
+    element_type* m_data = nullptr;
+    std::size_t m_order = 0;
+};
+
+template <SHNorm sh_norm_param, SHPhase sh_phase_param, typename ElementType = std::array<double, 2>>
+class RealSHExpansion {
+public:
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    using View = RealSHSpan<element_type, sh_norm_param, sh_phase_param>;
+    using ConstView = RealSHSpan<const element_type, sh_norm_param, sh_phase_param>;
+    static constexpr SHNorm norm = sh_norm_param;
+    static constexpr SHPhase phase = sh_phase_param;
+
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept { return order * (order + 1) / 2; }
+
+    RealSHExpansion() = default;
+    explicit RealSHExpansion(std::size_t order) : m_coeffs(size(order)), m_order(order) {}
+
+    [[nodiscard]] std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] std::size_t size() const noexcept { return m_coeffs.size(); }
+    [[nodiscard]] element_type* data() noexcept { return m_coeffs.data(); }
+    [[nodiscard]] const element_type* data() const noexcept { return m_coeffs.data(); }
+    [[nodiscard]] std::span<element_type> flatten() noexcept { return m_coeffs; }
+    [[nodiscard]] std::span<const element_type> flatten() const noexcept { return m_coeffs; }
+    [[nodiscard]] element_type& operator()(std::size_t l, std::size_t m) noexcept {
+        return m_coeffs[View::idx(l, m)];
+    }
+    [[nodiscard]] const element_type& operator()(std::size_t l, std::size_t m) const noexcept {
+        return m_coeffs[View::idx(l, m)];
+    }
+    void resize(std::size_t order) {
+        m_coeffs.resize(size(order));
+        m_order = order;
+    }
+    [[nodiscard]] operator View() noexcept { return View(m_coeffs.data(), m_order); }
+    [[nodiscard]] operator ConstView() const noexcept { return ConstView(m_coeffs.data(), m_order); }
+
+private:
+    AlignedVector<element_type> m_coeffs;
+    std::size_t m_order = 0;
+};
+
+template <typename ElementType>
+using RealSHSpanAcoustics = RealSHSpan<ElementType, SHNorm::qm, SHPhase::none>;
+template <typename ElementType>
+using RealSHSpanQM = RealSHSpan<ElementType, SHNorm::qm, SHPhase::cs>;
+template <typename ElementType>
+using RealSHSpanGeo = RealSHSpan<ElementType, SHNorm::geo, SHPhase::none>;
+using RealSHExpansionAcoustics = RealSHExpansion<SHNorm::qm, SHPhase::none>;
+using RealSHExpansionQM = RealSHExpansion<SHNorm::qm, SHPhase::cs>;
+using RealSHExpansionGeo = RealSHExpansion<SHNorm::geo, SHPhase::none>;
+
+// An SH expansion type: its conventions are static members and it converts
+// to the span of those conventions.
+template <typename T>
+concept real_sh_expansion = requires {
+    { std::remove_cvref_t<T>::norm } -> std::convertible_to<SHNorm>;
+    { std::remove_cvref_t<T>::phase } -> std::convertible_to<SHPhase>;
+} && std::convertible_to<T, RealSHSpan<typename std::remove_cvref_t<T>::element_type,
+                                       std::remove_cvref_t<T>::norm, std::remove_cvref_t<T>::phase>>;
+
+// Spherical-harmonic transforms on the GLQ grid, sh_glq_transformer.hpp:520-754.
+template <SHNorm sh_norm_param, SHPhase sh_phase_param, typename GridLayoutType = DefaultLayout>
+class GLQTransformer {
+public:
+    using GridLayout = GridLayoutType;
+    static constexpr SHNorm sh_norm = sh_norm_param;
+    static constexpr SHPhase phase = sh_phase_param;
+
+    GLQTransformer() : GLQTransformer(0) {}
+    explicit GLQTransformer(std::size_t order, int device = 0, void* stream = nullptr)
+        : m_ctx(device, stream), m_order(order) {}
+
+    [[nodiscard]] std::size_t order() const noexcept { return m_order; }
+    void resize(std::size_t order) { m_order = order; }
+    [[nodiscard]] GPUContext& context() noexcept { return m_ctx; }
+
+    void forward_transform(SphereGLQGridSpan<const double, GridLayout> values,
+                           RealSHSpan<std::array<double, 2>, sh_norm_param, sh_phase_param> expansion) {
+        resize(values.order());
+        forward_transform_batch(values.data(), values.order(), reinterpret_cast<double*>(expansion.data()),
+                                expansion.order(), 1, MemoryKind::host);
+    }
+    void backward_transform(RealSHSpan<const std::array<double, 2>, sh_norm_param, sh_phase_param> expansion,
+                            SphereGLQGridSpan<double, GridLayout> values) {
+        resize(values.order());
+        backward_transform_batch(reinterpret_cast<const double*>(expansion.data()), expansion.order(),
+                                 values.data(), values.order(), 1, MemoryKind::host);
+    }
+    [[nodiscard]] RealSHExpansion<sh_norm_param, sh_phase_param> forward_transform(
+        SphereGLQGridSpan<const double, GridLayout> values, std::size_t order) {
+        RealSHExpansion<sh_norm_param, sh_phase_param> expansion(order);
+        forward_transform(values, expansion);
+        return expansion;
+    }
+    [[nodiscard]] SphereGLQGrid<double, GridLayout> backward_transform(
+        RealSHSpan<const std::array<double, 2>, sh_norm_param, sh_phase_param> expansion, std::size_t order) {
+        SphereGLQGrid<double, GridLayout> grid(order);
+        backward_transform(expansion, grid);
+        return grid;
+    }
+
+    // `batch` contiguous grids of grid_order -> expansions of exp_order.
+    void forward_transform_batch(const double* grids, std::size_t grid_order, double* coeffs, std::size_t exp_order,
+                                 std::size_t batch, MemoryKind mem) {
+        zest::detail::check(zest_gpu_st_forward(m_ctx.get(), detail::abi(sh_norm_param), detail::abi(sh_phase_param),
+                                                GridLayout::abi, grid_order, exp_order, batch, grids, coeffs,
+                                                int(mem)));
+    }
+    void backward_transform_batch(const double* coeffs, std::size_t exp_order, double* grids, std::size_t grid_order,
+                                  std::size_t batch, MemoryKind mem) {
+        zest::detail::check(zest_gpu_st_backward(m_ctx.get(), detail::abi(sh_norm_param), detail::abi(sh_phase_param),
+                                                 GridLayout::abi, exp_order, grid_order, batch, coeffs, grids,
+                                                 int(mem)));
+    }
+
+private:
+    GPUContext m_ctx;
+    std::size_t m_order;
+};
+
+template <typename GridLayout = DefaultLayout>
+using GLQTransformerAcoustics = GLQTransformer<SHNorm::qm, SHPhase::none, GridLayout>;
+template <typename GridLayout = DefaultLayout>
+using GLQTransformerQM = GLQTransformer<SHNorm::qm, SHPhase::cs, GridLayout>;
+template <typename GridLayout = DefaultLayout>
+using GLQTransformerGeo = GLQTransformer<SHNorm::geo, SHPhase::none, GridLayout>;
+
+}  // namespace st
+
+// ---------------------------------------------------------------------------
+// 3D Zernike functions on the unit ball
+// ---------------------------------------------------------------------------
+namespace zt {
+
+enum class ZernikeNorm { normed, unnormed };
+
+namespace detail {
+constexpr int abi(ZernikeNorm n) noexcept {
+    return n == ZernikeNorm::normed ? ZEST_ZERNIKE_NORMED : ZEST_ZERNIKE_UNNORMED;
+}
+}  // namespace detail
+
+// [lon][lat][rad]: (2L - 1, L + 1, pad8(L + 1))
+template <typename AlignmentType = CacheLineAlignment>
+struct LonLatRadLayout {
+    using Alignment = AlignmentType;
+    [[nodiscard]] static constexpr std::size_t lon_size(std::size_t order) noexcept {
+        return 2 * order - std::min<std::size_t>(1, order);
+    }
+    [[nodiscard]] static constexpr std::size_t lat_size(std::size_t order) noexcept { return order + 1; }
+    [[nodiscard]] static constexpr std::size_t rad_size(std::size_t order) noexcept {
+        return zest::detail::pad8(order + 1);
+    }
+    [[nodiscard]] static constexpr std::array<std::size_t, 3> shape(std::size_t order) noexcept {
+        return {lon_size(order), lat_size(order), rad_size(order)};
+    }
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept {
+        return lon_size(order) * lat_size(order) * rad_size(order);
+    }
+};
+
+using DefaultLayout = LonLatRadLayout<>;
+
+template <typename ElementType, typename LayoutType = DefaultLayout>
+class BallGLQGridSpan {
+public:
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    using Layout = LayoutType;
+    using ConstView = BallGLQGridSpan<const value_type, Layout>;
+
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept { return Layout::size(order); }
+    [[nodiscard]] static constexpr std::array<std::size_t, 3> shape(std::size_t order) noexcept {
+        return Layout::shape(order);
+    }
+
+    BallGLQGridSpan() noexcept = default;
+    constexpr BallGLQGridSpan(element_type* data, std::size_t order) noexcept : m_data(data), m_order(order) {}
+    constexpr BallGLQGridSpan(std::span<element_type> buffer, std::size_t order) noexcept
+        : m_data(buffer.data()), m_order(order) {}
+
+    [[nodiscard]] constexpr std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] constexpr std::array<std::size_t, 3> shape() const noexcept { return Layout::shape(m_order); }
+    [[nodiscard]] constexpr std::size_t size() const noexcept { return Layout::size(m_order); }
+    [[nodiscard]] constexpr element_type* data() const noexcept { return m_data; }
+    [[nodiscard]] constexpr std::span<element_type> flatten() const noexcept { return {m_data, size()}; }
+    [[nodiscard]] constexpr element_type& operator()(std::size_t i, std::size_t j, std::size_t k) const noexcept {
+        const auto s = shape();
+        return m_data[(i * s[1] + j) * s[2] + k];
+    }
+    [[nodiscard]] constexpr operator ConstView() const noexcept { return ConstView(m_data, m_order); }
+
+private:
+    element_type* m_data = nullptr;
+    std::size_t m_order = 0;
+};
+
+template <typename ElementType = double, typename LayoutType = DefaultLayout>
+class BallGLQGrid {
+public:
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    using Layout = LayoutType;
+    using View = BallGLQGridSpan<element_type, Layout>;
+    using ConstView = BallGLQGridSpan<const element_type, Layout>;
+
+    BallGLQGrid() = default;
+    explicit BallGLQGrid(std::size_t order) : m_values(Layout::size(order)), m_order(order) {}
+
+    [[nodiscard]] std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] std::array<std::size_t, 3> shape() const noexcept { return Layout::shape(m_order); }
+    [[nodiscard]] std::size_t size() const noexcept { return m_values.size(); }
+    [[nodiscard]] element_type* data() noexcept { return m_values.data(); }
+    [[nodiscard]] const element_type* data() const noexcept { return m_values.data(); }
+    [[nodiscard]] std::span<element_type> flatten() noexcept { return m_values; }
+    [[nodiscard]] std::span<const element_type> flatten() const noexcept { return m_values; }
+    [[nodiscard]] element_type& operator()(std::size_t i, std::size_t j, std::size_t k) noexcept {
+        const auto s = shape();
+        return m_values[(i * s[1] + j) * s[2] + k];
+    }
+    void resize(std::size_t order) {
+        m_values.resize(Layout::size(order));
+        m_order = order;
+    }
+    [[nodiscard]] operator View() noexcept { return View(m_values.data(), m_order); }
+    [[nodiscard]] operator ConstView() const noexcept { return ConstView(m_values.data(), m_order); }
+
+private:
+    AlignedVector<element_type> m_values;
+    std::size_t m_order = 0;
+};
+
+// Real Zernike coefficients {cos, sin} of (n, l, m), n - l even, at
+// (n+1)(n+3)(2n+1)/24 + floor(l^2/4) + m.
+template <typename ElementType, ZernikeNorm zernike_norm_param, st::SHNorm sh_norm_param,
+          st::SHPhase sh_phase_param>
+class RealZernikeSpan {
+public:
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    using ConstView = RealZernikeSpan<const value_type, zernike_norm_param, sh_norm_param, sh_phase_param>;
+    static constexpr ZernikeNorm zernike_norm = zernike_norm_param;
+    static constexpr st::SHNorm sh_norm = sh_norm_param;
+    static constexpr st::SHPhase sh_phase = sh_phase_param;
+
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept {
+        return (order + 1) * (order + 3) * (2 * order + 1) / 24;
+    }
+    [[nodiscard]] static constexpr std::size_t idx(std::size_t n, std::size_t l, std::size_t m) noexcept {
+        return (n + 1) * (n + 3) * (2 * n + 1) / 24 + (l * l) / 4 + m;
+    }
+
+    RealZernikeSpan() noexcept = default;
+    constexpr RealZernikeSpan(element_type* data, std::size_t order) noexcept : m_data(data), m_order(order) {}
+    constexpr RealZernikeSpan(std::span<element_type> buffer, std::size_t order) noexcept
+        : m_data(buffer.data()), m_order(order) {}
+
+    [[nodiscard]] constexpr std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] constexpr std::size_t size() const noexcept { return size(m_order); }
+    [[nodiscard]] constexpr element_type* data() const noexcept { return m_data; }
+    [[nodiscard]] constexpr std::span<element_type> flatten() const noexcept { return {m_data, size()}; }
+    [[nodiscard]] constexpr element_type& operator()(std::size_t n, std::size_t l, std::size_t m) const noexcept {
+        return m_data[idx(n, l, m)];
+    }
+    [[nodiscard]] constexpr operator ConstView() const noexcept { return ConstView(m_data, m_order); }
+
+private:
+    element_type* m_data = nullptr;
+    std::size_t m_order = 0;
+};
+
+template <ZernikeNorm zernike_norm_param, st::SHNorm sh_norm_param, st::SHPhase sh_phase_param,
+          typename ElementType = std::array<double, 2>>
+class RealZernikeExpansion {
+public:
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    using View = RealZernikeSpan<element_type, zernike_norm_param, sh_norm_param, sh_phase_param>;
+    using ConstView = RealZernikeSpan<const element_type, zernike_norm_param, sh_norm_param, sh_phase_param>;
+    static constexpr ZernikeNorm zernike_norm = zernike_norm_param;
+    static constexpr st::SHNorm sh_norm = sh_norm_param;
+    static constexpr st::SHPhase sh_phase = sh_phase_param;
+
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept { return View::size(order); }
+
+    RealZernikeExpansion() = default;
+    explicit RealZernikeExpansion(std::size_t order) : m_coeffs(size(order)), m_order(order) {}
+
+    [[nodiscard]] std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] std::size_t size() const noexcept { return m_coeffs.size(); }
+    [[nodiscard]] element_type* data() noexcept { return m_coeffs.data(); }
+    [[nodiscard]] const element_type* data() const noexcept { return m_coeffs.data(); }
+    [[nodiscard]] std::span<element_type> flatten() noexcept { return m_coeffs; }
+    [[nodiscard]] std::span<const element_type> flatten() const noexcept { return m_coeffs; }
+    [[nodiscard]] element_type& operator()(std::size_t n, std::size_t l, std::size_t m) noexcept {
+        return m_coeffs[View::idx(n, l, m)];
+    }
+    [[nodiscard]] const element_type& operator()(std::size_t n, std::size_t l, std::size_t m) const noexcept {
+        return m_coeffs[View::idx(n, l, m)];
+    }
+    void resize(std::size_t order) {
+        m_coeffs.resize(size(order));
+        m_order = order;
+    }
+    [[nodiscard]] operator View() noexcept { return View(m_coeffs.data(), m_order); }
+    [[nodiscard]] operator ConstView() const noexcept { return ConstView(m_coeffs.data(), m_order); }
+
+private:
+    AlignedVector<element_type> m_coeffs;
+    std::size_t m_order = 0;
+};
+
+// Aliases of the reference, zernike_expansion.hpp:233-447 (its
+// RealZernikeSpanNormalAcoustics names ZernikeNorm::unnormed; kept so).
+template <typename ElementType>
+using RealZernikeSpanAcoustics = RealZernikeSpan<ElementType, ZernikeNorm::unnormed, st::SHNorm::qm, st::SHPhase::none>;
+template <typename ElementType>
+using RealZernikeSpanNormalAcoustics
+    = RealZernikeSpan<ElementType, ZernikeNorm::unnormed, st::SHNorm::qm, st::SHPhase::none>;
+template <typename ElementType>
+using RealZernikeSpanQM = RealZernikeSpan<ElementType, ZernikeNorm::unnormed, st::SHNorm::qm, st::SHPhase::cs>;
+template <typename ElementType>
+using RealZernikeSpanNormalQM = RealZernikeSpan<ElementType, ZernikeNorm::normed, st::SHNorm::qm, st::SHPhase::cs>;
+template <typename ElementType>
+using RealZernikeSpanGeo = RealZernikeSpan<ElementType, ZernikeNorm::unnormed, st::SHNorm::geo, st::SHPhase::none>;
+template <typename ElementType>
+using RealZernikeSpanNormalGeo = RealZernikeSpan<ElementType, ZernikeNorm::normed, st::SHNorm::geo, st::SHPhase::none>;
+using RealZernikeExpansionAcoustics = RealZernikeExpansion<ZernikeNorm::unnormed, st::SHNorm::qm, st::SHPhase::none>;
+using RealZernikeExpansionNormalAcoustics = RealZernikeExpansion<ZernikeNorm::normed, st::SHNorm::qm, st::SHPhase::none>;
+using RealZernikeExpansionQM = RealZernikeExpansion<ZernikeNorm::unnormed, st::SHNorm::qm, st::SHPhase::cs>;
+using RealZernikeExpansionNormalQM = RealZernikeExpansion<ZernikeNorm::normed, st::SHNorm::qm, st::SHPhase::cs>;
+using RealZernikeExpansionGeo = RealZernikeExpansion<ZernikeNorm::unnormed, st::SHNorm::geo, st::SHPhase::none>;
+using RealZernikeExpansionNormalGeo = RealZernikeExpansion<ZernikeNorm::normed, st::SHNorm::geo, st::SHPhase::none>;
+
+template <typename T>
+concept real_zernike_expansion = requires {
+    { std::remove_cvref_t<T>::zernike_norm } -> std::convertible_to<ZernikeNorm>;
+    { std::remove_cvref_t<T>::sh_norm } -> std::convertible_to<st::SHNorm>;
+    { std::remove_cvref_t<T>::sh_phase } -> std::convertible_to<st::SHPhase>;
+} && std::convertible_to<T, RealZernikeSpan<typename std::remove_cvref_t<T>::element_type,
+                                            std::remove_cvref_t<T>::zernike_norm, std::remove_cvref_t<T>::sh_norm,
+                                            std::remove_cvref_t<T>::sh_phase>>;
+
+// Zernike transforms on the GLQ grid of the ball, zernike_glq_transformer.hpp:510-707.
+template <ZernikeNorm zernike_norm_param, st::SHNorm sh_norm_param, st::SHPhase sh_phase_param,
+          typename GridLayoutType = DefaultLayout>
+class GLQTransformer {
+public:
+    using GridLayout = GridLayoutType;
+    static constexpr ZernikeNorm zernike_norm = zernike_norm_param;
+    static constexpr st::SHNorm sh_norm = sh_norm_param;
+    static constexpr st::SHPhase phase = sh_phase_param;
+    using Expansion = RealZernikeExpansion<zernike_norm_param, sh_norm_param, sh_phase_param>;
+
+    GLQTransformer() : GLQTransformer(0) {}
+    explicit GLQTransformer(std::size_t order, int device = 0, void* stream = nullptr)
+        : m_ctx(device, stream), m_order(order) {}
+
+    [[nodiscard]] std::size_t order() const noexcept { return m_order; }
+    void resize(std::size_t order) { m_order = order; }
+    [[nodiscard]] GPUContext& context() noexcept { return m_ctx; }
+    // the contractions' arithmetic: FP64 (default) or split precision on the tensor cores
+    void set_precision(Precision precision, int slices = 0) { m_ctx.set_precision(precision, slices); }
+
+    void forward_transform(
+        BallGLQGridSpan<const double, GridLayout> values,
+        RealZernikeSpan<std::array<double, 2>, zernike_norm_param, sh_norm_param, sh_phase_param> expansion) {
+        resize(values.order());
+        forward_transform_batch(values.data(), values.order(), reinterpret_cast<double*>(expansion.data()),
+                                expansion.order(), 1, MemoryKind::host);
+    }
+    void backward_transform(
+        RealZernikeSpan<const std::array<double, 2>, zernike_norm_param, sh_norm_param, sh_phase_param> expansion,
+        BallGLQGridSpan<double, GridLayout> values) {
+        resize(values.order());
+        backward_transform_batch(reinterpret_cast<const double*>(expansion.data()), expansion.order(),
+                                 values.data(), values.order(), 1, MemoryKind::host);
+    }
+    [[nodiscard]] Expansion forward_transform(BallGLQGridSpan<const double, GridLayout> values, std::size_t order) {
+        Expansion expansion(order);
+        forward_transform(values, expansion);
+        return expansion;
+    }
+    [[nodiscard]] BallGLQGrid<double, GridLayout> backward_transform(
+        RealZernikeSpan<const std::array<double, 2>, zernike_norm_param, sh_norm_param, sh_phase_param> expansion,
+        std::size_t order) {
+        BallGLQGrid<double, GridLayout> grid(order);
+        backward_transform(expansion, grid);
+        return grid;
+    }
+
+    // `batch` contiguous grids of grid_order -> expansions of exp_order.
+    void forward_transform_batch(const double* grids, std::size_t grid_order, double* coeffs, std::size_t exp_order,
+                                 std::size_t batch, MemoryKind mem) {
+        zest::detail::check(zest_gpu_zt_forward(m_ctx.get(), detail::abi(zernike_norm_param),
+                                                st::detail::abi(sh_norm_param), st::detail::abi(sh_phase_param),
+                                                grid_order, exp_order, batch, grids, coeffs, int(mem)));
+    }
+    void backward_transform_batch(const double* coeffs, std::size_t exp_order, double* grids, std::size_t grid_order,
+                                  std::size_t batch, MemoryKind mem) {
+        zest::detail::check(zest_gpu_zt_backward(m_ctx.get(), detail::abi(zernike_norm_param),
+                                                 st::detail::abi(sh_norm_param), st::detail::abi(sh_phase_param),
+                                                 exp_order, grid_order, batch, coeffs, grids, int(mem)));
+    }
+
+private:
+    GPUContext m_ctx;
+    std::size_t m_order;
+};
+
+template <typename GridLayout = DefaultLayout>
+using GLQTransformerAcoustics = GLQTransformer<ZernikeNorm::unnormed, st::SHNorm::qm, st::SHPhase::none, GridLayout>;
+template <typename GridLayout = DefaultLayout>
+using GLQTransformerNormalAcoustics
+    = GLQTransformer<ZernikeNorm::normed, st::SHNorm::qm, st::SHPhase::none, GridLayout>;
+template <typename GridLayout = DefaultLayout>
+using GLQTransformerQM = GLQTransformer<ZernikeNorm::unnormed, st::SHNorm::qm, st::SHPhase::cs, GridLayout>;
+template <typename GridLayout = DefaultLayout>
+using GLQTransformerNormalQM = GLQTransformer<ZernikeNorm::normed, st::SHNorm::qm, st::SHPhase::cs, GridLayout>;
+template <typename GridLayout = DefaultLayout>
+using GLQTransformerGeo = GLQTransformer<ZernikeNorm::unnormed, st::SHNorm::geo, st::SHPhase::none, GridLayout>;
+template <typename GridLayout = DefaultLayout>
+using GLQTransformerNormalGeo = GLQTransformer<ZernikeNorm::normed, st::SHNorm::geo, st::SHPhase::none, GridLayout>;
+
+}  // namespace zt
+
+// ---------------------------------------------------------------------------
+// Rotations
+// ---------------------------------------------------------------------------
+
+// Wigner d^l_{m1 m2}(pi/2) for 0 <= m1, m2 <= l < max_order, generated on the
+// device (wignerd_collection.hpp:66-110); block l at l(l+1)(2l+1)/6, row m1.
+class WignerdPiHalfCollection {
+public:
+    WignerdPiHalfCollection() = default;
+    explicit WignerdPiHalfCollection(std::size_t max_order, int device = 0) : m_device(device) { expand(max_order); }
+
+    void expand(std::size_t max_order) {
+        if (max_order <= m_max_order && !m_matrices.empty()) return;
+        GPUContext ctx(m_device);
+        m_matrices.assign(max_order * (max_order + 1) * (2 * max_order + 1) / 6, 0.0);
+        if (max_order) zest::detail::check(zest_gpu_wignerd_table(ctx.get(), max_order, m_matrices.data(), ZEST_MEM_HOST));
+        m_max_order = max_order;
+    }
+    [[nodiscard]] std::span<const double> matrices() const noexcept { return m_matrices; }
+    [[nodiscard]] std::size_t max_order() const noexcept { return m_max_order; }
+    [[nodiscard]] double operator()(std::size_t l, std::size_t m1, std::size_t m2) const noexcept {
+        return m_matrices[l * (l + 1) * (2 * l + 1) / 6 + (l + 1) * m1 + m2];
+    }
+
+private:
+    std::vector<double> m_matrices;
+    std::size_t m_max_order = 0;
+    int m_device = 0;
+};
+
+// Euler angles (intrinsic ZYZ) of a rotation matrix, rotor.hpp:53-63.
+[[nodiscard]] inline std::array<double, 3> euler_angles_from_rotation_matrix(
+    const std::array<std::array<double, 3>, 3>& matrix) {
+    double m[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) m[3 * i + j] = matrix[i][j];
+    std::array<double, 3> euler{};
+    zest::detail::check(zest_gpu_euler_from_matrix(m, euler.data()));
+    return euler;
+}
+
+// Rotations of real Zernike and SH expansions, rotor.hpp:95-395.  The rotor
+// owns a device context, which holds its own copy of the Wigner d(pi/2)
+// tables (the same values as `wigner_d_pi2`, generated by the same kernel).
+class Rotor {
+public:
+    Rotor() : Rotor(0) {}
+    explicit Rotor(std::size_t max_order, int device = 0, void* stream = nullptr)
+        : m_ctx(device, stream), m_max_order(max_order) {}
+
+    void expand(std::size_t max_order) { m_max_order = std::max(m_max_order, max_order); }
+    [[nodiscard]] std::size_t max_order() const noexcept { return m_max_order; }
+    [[nodiscard]] GPUContext& context() noexcept { return m_ctx; }
+
+    template <zt::real_zernike_expansion ExpansionType>
+        requires std::same_as<typename std::remove_cvref_t<ExpansionType>::value_type, std::array<double, 2>>
+    void rotate(ExpansionType&& expansion, const WignerdPiHalfCollection& wigner_d_pi2,
+                const std::array<double, 3>& euler_angles, RotationType type) {
+        auto span = as_zt_span(expansion);
+        check_wigner(wigner_d_pi2, span.order());
+        expand(span.order());
+        zest::detail::check(zest_gpu_zt_rotate(m_ctx.get(), span.order(), 1, reinterpret_cast<double*>(span.data()),
+                                               euler_angles.data(), abi(type), ZEST_MEM_HOST));
+    }
+    template <st::real_sh_expansion ExpansionType>
+        requires std::same_as<typename std::remove_cvref_t<ExpansionType>::value_type, std::array<double, 2>>
+    void rotate(ExpansionType&& expansion, const WignerdPiHalfCollection& wigner_d_pi2,
+                const std::array<double, 3>& euler_angles, RotationType type) {
+        auto span = as_st_span(expansion);
+        check_wigner(wigner_d_pi2, span.order());
+        expand(span.order());
+        zest::detail::check(zest_gpu_st_rotate(m_ctx.get(), span.order(), 1, reinterpret_cast<double*>(span.data()),
+                                               euler_angles.data(), abi(type), ZEST_MEM_HOST));
+    }
+    template <typename ExpansionType>
+        requires zt::real_zernike_expansion<ExpansionType> || st::real_sh_expansion<ExpansionType>
+    void rotate(ExpansionType&& expansion, const WignerdPiHalfCollection& wigner_d_pi2,
+                const std::array<std::array<double, 3>, 3>& matrix, RotationType type) {
+        rotate(std::forward<ExpansionType>(expansion), wigner_d_pi2, euler_angles_from_rotation_matrix(matrix), type);
+    }
+
+    template <zt::real_zernike_expansion ExpansionType>
+        requires std::same_as<typename std::remove_cvref_t<ExpansionType>::value_type, std::array<double, 2>>
+    void polar_rotate(ExpansionType&& expansion, double angle, RotationType type) {
+        auto span = as_zt_span(expansion);
+        zest::detail::check(zest_gpu_zt_polar_rotate(m_ctx.get(), span.order(), 1,
+                                                     reinterpret_cast<double*>(span.data()), &angle, abi(type),
+                                                     ZEST_MEM_HOST));
+    }
+    template <st::real_sh_expansion ExpansionType>
+        requires std::same_as<typename std::remove_cvref_t<ExpansionType>::value_type, std::array<double, 2>>
+    void polar_rotate(ExpansionType&& expansion, double angle, RotationType type) {
+        auto span = as_st_span(expansion);
+        zest::detail::check(zest_gpu_st_polar_rotate(m_ctx.get(), span.order(), 1,
+                                                     reinterpret_cast<double*>(span.data()), &angle, abi(type),
+                                                     ZEST_MEM_HOST));
+    }
+
+    // `batch` contiguous Zernike expansions of one order, one Euler triple each.
+    void rotate_batch(double* coeffs, std::size_t order, std::size_t batch, const double* euler_angles,
+                      RotationType type, MemoryKind mem) {
+        zest::detail::check(
+            zest_gpu_zt_rotate(m_ctx.get(), order, batch, coeffs, euler_angles, abi(type), int(mem)));
+    }
+
+private:
+    static constexpr int abi(RotationType t) noexcept {
+        return t == RotationType::object ? ZEST_ROTATION_OBJECT : ZEST_ROTATION_COORDINATE;
+    }
+    static void check_wigner(const WignerdPiHalfCollection& w, std::size_t order) {
+        if (w.max_order() < order)
+            throw GPUError(ZEST_GPU_ERR_INVALID, "WignerdPiHalfCollection is smaller than the expansion order");
+    }
+    template <typename E>
+    static auto as_zt_span(E& e) {
+        using T = std::remove_cvref_t<E>;
+        return zt::RealZernikeSpan<std::array<double, 2>, T::zernike_norm, T::sh_norm, T::sh_phase>(e);
+    }
+    template <typename E>
+    static auto as_st_span(E& e) {
+        using T = std::remove_cvref_t<E>;
+        return st::RealSHSpan<std::array<double, 2>, T::norm, T::phase>(e);
+    }
+
+    GPUContext m_ctx;
+    std::size_t m_max_order;
+};
+
+}  // namespace zest
