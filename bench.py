@@ -33,6 +33,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Zernike fwd+bwd transforms/s, order 200x64: split-prec vs FP64 GPU at 1e-11 err"
+# DRAM read + write bytes of the split GEMMs of one forward+backward step per
+# function at order 200 (ncu capture of all eight launches at batch 4: 8.89 GB)
+GEMM_DRAM_BYTES_PER_FUNCTION_ORDER200 = 8.889e9 / 4
 UNIT = "transforms/s"
 
 
@@ -184,6 +187,91 @@ def run_reference_arm(args, rank: int, world: int) -> None:
 
 
 # --------------------------------------------------------------------------
+def run_batching(args, rank: int, world: int, barrier) -> None:
+    """4096 expansions, orders drawn uniformly from [8, 128] (sorted), c_nlm ~
+    N(0, (n+1)^-2) with Im(m=0) = 0, Haar-uniform Euler angles; one step =
+    Rotor::rotate of every expansion then its backward transform, all through
+    zest_gpu_zt_rotate_backward_ragged (a CUDA graph replay after the first
+    call).  Reports expansions/s and the step's HBM traffic against the
+    measured copy bandwidth."""
+    import torch
+    import zest_gb300 as zg
+    ctx = zg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    precision = args.precision if args.precision != "auto" else "split"
+    ctx.set_precision(zg.PRECISION_SPLIT if precision == "split" else zg.PRECISION_FP64, args.slices)
+    ctx.set_autotune(True)
+    rng = np.random.default_rng(4096 + rank)
+    n = args.items
+    orders = np.sort(rng.integers(8, 129, size=n)).astype(np.int32)
+    csz = [2 * zg.zt_coeff_size(int(L)) for L in orders]
+    gsz = [int(np.prod(zg.zt_grid_shape(int(L)))) for L in orders]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    coeffs = torch.empty(sum(csz), dtype=torch.float64, device=dev)
+    grids = torch.empty(sum(gsz), dtype=torch.float64, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(4096 + rank)
+    scales = {}
+    off = 0
+    for L, c in zip(orders, csz):
+        L = int(L)
+        if L not in scales:
+            sc = np.zeros((c // 2, 2))
+            for nn in range(L):
+                for l in range(nn & 1, nn + 1, 2):
+                    base = (nn + 1) * (nn + 3) * (2 * nn + 1) // 24 + (l * l) // 4
+                    sc[base:base + l + 1] = (nn + 1) ** -1.0
+                    sc[base, 1] = 0.0
+            scales[L] = torch.from_numpy(sc.ravel()).to(dev)
+        coeffs[off:off + c] = torch.randn(c, dtype=torch.float64, device=dev, generator=gen) * scales[L]
+        off += c
+    e = np.stack([rng.uniform(0, 2 * np.pi, n), np.arccos(rng.uniform(-1, 1, n)), rng.uniform(0, 2 * np.pi, n)], 1)
+    euler = torch.from_numpy(np.ascontiguousarray(e).ravel()).to(dev)
+    ctx.zt_rotate_backward_ragged(orders, coeffs, euler, grids)  # eager run, autotuning, graph capture
+    for _ in range(args.warmup):
+        ctx.zt_rotate_backward_ragged(orders, coeffs, euler, grids)
+    ctx.synchronize()
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    stream = torch.cuda.current_stream()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    # the library works on its own stream: time with host-synchronised events around it
+    ctx.synchronize()
+    e0.record(stream)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.zt_rotate_backward_ragged(orders, coeffs, euler, grids)
+    ctx.synchronize()
+    t1 = time.perf_counter()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms = (t1 - t0) * 1e3 / args.steps
+    T = np.array([zg.zt_coeff_size(int(L)) for L in orders], dtype=np.float64)
+    G = np.array(gsz, dtype=np.float64)
+    bytes_step = float(np.sum(32 * T + 16 * T + 8 * G))
+    peaks = measured_peaks()
+    achieved = bytes_step / (ms * 1e-3) / 1e9
+    if rank == 0:
+        print(json.dumps({
+            "metric": "Zernike rotate + backward expansions/s, 4096 orders U{8..128}",
+            "value": world * n / (ms * 1e-3), "unit": "expansions/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "bf16-slices + f64",
+            "data": "synthetic", "config": {"workload": "zernike_ragged_rotate_backward", "items": n,
+                                            "orders": "U{8..128} sorted", "precision": precision,
+                                            "graph": "CUDA graph replay", "autotune": True},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                         "algorithmic": "32 T(L) rotate in place + 16 T(L) coefficient read + 8 G(L) grid write",
+                         "bytes_per_step": bytes_step},
+            "timing": "host wall clock around K graph launches, device synchronised on both sides",
+            "clocks": clocks}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -196,6 +284,10 @@ def main():
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["transforms", "batching"], default="transforms",
+                    help="transforms: the headline (order 200 x 64 forward+backward); batching: 4096 "
+                         "expansions of orders U{8..128}, rotate + backward in one graph")
+    ap.add_argument("--items", type=int, default=4096)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -219,6 +311,10 @@ def main():
     def barrier():
         if dist is not None:
             dist.barrier()
+
+    if args.workload == "batching":
+        run_batching(args, rank, world, barrier)
+        return
 
     L, B = args.order, args.batch
     ctx = zg.Context(local_rank)
@@ -321,12 +417,21 @@ def main():
         useful, issued = tflops[0] / steps_run, tflops[1] / steps_run
         achieved = useful / (gemm_ms * 1e-3) / 1e12 if gemm_ms == gemm_ms and gemm_ms > 0 else None
         peak = peaks["bf16_tflops_sustained"] or peaks["bf16_tflops"]
-        roofline = {"bound": "tensor", "kernel": "split_gemm_kernel (all launches of a step)", "achieved": achieved,
+        # DRAM bytes of the eight split_gemm_kernel launches of one step, from one
+        # ncu capture at order 200 x 4 (8.89 GB, proportional to the batch)
+        launches_per_step = stage_n.get("split_gemm", 8.0) or 8.0
+        traffic = GEMM_DRAM_BYTES_PER_FUNCTION_ORDER200 * B / launches_per_step if L == 200 else None
+        roofline = {"bound": "tensor", "kernel": "split_gemm_kernel (per launch, averaged over a step's launches)",
+                    "achieved": achieved,
                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if achieved else None,
-                    "traffic": None, "peak_source": peaks["source"] + " bf16 sustained",
-                    "algorithmic": "BF16 MMA flops of the slice products on valid rows per step",
+                    "traffic": traffic, "traffic_unit": "bytes per launch (ncu dram read + write)",
+                    "peak_source": peaks["source"] + " bf16 sustained",
+                    "algorithmic": "BF16 MMA flops of the slice products on valid rows",
                     "useful_tflop_per_step": useful / 1e12, "issued_tflop_per_step": issued / 1e12,
-                    "issued_rate": issued / (gemm_ms * 1e-3) / 1e12 if achieved else None}
+                    "issued_rate": issued / (gemm_ms * 1e-3) / 1e12 if achieved else None,
+                    "dram_rate_tbs": (traffic * launches_per_step / (gemm_ms * 1e-3) / 1e12
+                                      if traffic and gemm_ms == gemm_ms and gemm_ms > 0 else None),
+                    "hbm_peak_tbs": peaks["hbm_gbs"] / 1e3 if peaks.get("hbm_gbs") else None}
     else:
         # FP64 form: the dominant stage is the folded Legendre contraction, bound by
         # the FP64 pipe (1.20 TFLOP/s DFMA measured on this GPU model)

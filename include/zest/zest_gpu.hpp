@@ -389,6 +389,24 @@ public:
                                                  int(mem)));
     }
 
+    // Vector-Jacobian products (adjoints) of the two transforms: the grid
+    // cotangent of forward_transform from its coefficient cotangent, and the
+    // coefficient cotangent of backward_transform from its grid cotangent.
+    void forward_transform_vjp(RealSHSpan<const std::array<double, 2>, sh_norm_param, sh_phase_param> expansion_cot,
+                               SphereGLQGridSpan<double, GridLayout> values_cot) {
+        zest::detail::check(zest_gpu_st_forward_vjp(
+            m_ctx.get(), detail::abi(sh_norm_param), detail::abi(sh_phase_param), GridLayout::abi, values_cot.order(),
+            expansion_cot.order(), 1, reinterpret_cast<const double*>(expansion_cot.data()), values_cot.data(),
+            ZEST_MEM_HOST));
+    }
+    void backward_transform_vjp(SphereGLQGridSpan<const double, GridLayout> values_cot,
+                                RealSHSpan<std::array<double, 2>, sh_norm_param, sh_phase_param> expansion_cot) {
+        zest::detail::check(zest_gpu_st_backward_vjp(
+            m_ctx.get(), detail::abi(sh_norm_param), detail::abi(sh_phase_param), GridLayout::abi,
+            expansion_cot.order(), values_cot.order(), 1, values_cot.data(),
+            reinterpret_cast<double*>(expansion_cot.data()), ZEST_MEM_HOST));
+    }
+
 private:
     GPUContext m_ctx;
     std::size_t m_order;
@@ -679,6 +697,35 @@ public:
                                                  exp_order, grid_order, batch, coeffs, grids, int(mem)));
     }
 
+    // Vector-Jacobian products (adjoints): the grid cotangent of
+    // forward_transform, W B(G^+ c), and the coefficient cotangent of
+    // backward_transform, G F(W^-1 g) (W quadrature weights, G Gram diagonal).
+    void forward_transform_vjp(
+        RealZernikeSpan<const std::array<double, 2>, zernike_norm_param, sh_norm_param, sh_phase_param> expansion_cot,
+        BallGLQGridSpan<double, GridLayout> values_cot) {
+        forward_transform_vjp_batch(reinterpret_cast<const double*>(expansion_cot.data()), expansion_cot.order(),
+                                    values_cot.data(), values_cot.order(), 1, MemoryKind::host);
+    }
+    void backward_transform_vjp(
+        BallGLQGridSpan<const double, GridLayout> values_cot,
+        RealZernikeSpan<std::array<double, 2>, zernike_norm_param, sh_norm_param, sh_phase_param> expansion_cot) {
+        backward_transform_vjp_batch(values_cot.data(), values_cot.order(),
+                                     reinterpret_cast<double*>(expansion_cot.data()), expansion_cot.order(), 1,
+                                     MemoryKind::host);
+    }
+    void forward_transform_vjp_batch(const double* coeffs_cot, std::size_t exp_order, double* grids_cot,
+                                     std::size_t grid_order, std::size_t batch, MemoryKind mem) {
+        zest::detail::check(zest_gpu_zt_forward_vjp(m_ctx.get(), detail::abi(zernike_norm_param),
+                                                    st::detail::abi(sh_norm_param), st::detail::abi(sh_phase_param),
+                                                    grid_order, exp_order, batch, coeffs_cot, grids_cot, int(mem)));
+    }
+    void backward_transform_vjp_batch(const double* grids_cot, std::size_t grid_order, double* coeffs_cot,
+                                      std::size_t exp_order, std::size_t batch, MemoryKind mem) {
+        zest::detail::check(zest_gpu_zt_backward_vjp(m_ctx.get(), detail::abi(zernike_norm_param),
+                                                     st::detail::abi(sh_norm_param), st::detail::abi(sh_phase_param),
+                                                     exp_order, grid_order, batch, grids_cot, coeffs_cot, int(mem)));
+    }
+
 private:
     GPUContext m_ctx;
     std::size_t m_order;
@@ -796,6 +843,27 @@ public:
         zest::detail::check(zest_gpu_st_polar_rotate(m_ctx.get(), span.order(), 1,
                                                      reinterpret_cast<double*>(span.data()), &angle, abi(type),
                                                      ZEST_MEM_HOST));
+    }
+
+    // Vector-Jacobian product of y = rotate(expansion, euler_angles): writes
+    // D^T out_cot into expansion_cot (if non-empty) and returns the gradient
+    // of <out_cot, y> with respect to the three Euler angles.
+    template <typename ExpansionType, typename CotangentType>
+        requires(zt::real_zernike_expansion<ExpansionType> || st::real_sh_expansion<ExpansionType>)
+    std::array<double, 3> rotate_vjp(const ExpansionType& expansion, const WignerdPiHalfCollection& wigner_d_pi2,
+                                     const std::array<double, 3>& euler_angles, RotationType type,
+                                     const CotangentType& out_cot, double* expansion_cot = nullptr) {
+        std::array<double, 3> grad{};
+        const double* x = reinterpret_cast<const double*>(expansion.data());
+        const double* y = reinterpret_cast<const double*>(out_cot.data());
+        check_wigner(wigner_d_pi2, expansion.order());
+        if constexpr (zt::real_zernike_expansion<ExpansionType>)
+            zest::detail::check(zest_gpu_zt_rotate_vjp(m_ctx.get(), expansion.order(), 1, x, euler_angles.data(),
+                                                       abi(type), y, expansion_cot, grad.data(), ZEST_MEM_HOST));
+        else
+            zest::detail::check(zest_gpu_st_rotate_vjp(m_ctx.get(), expansion.order(), 1, x, euler_angles.data(),
+                                                       abi(type), y, expansion_cot, grad.data(), ZEST_MEM_HOST));
+        return grad;
     }
 
     // `batch` contiguous Zernike expansions of one order, one Euler triple each.

@@ -194,6 +194,60 @@ int zest_gpu_zt_rotate_noalloc(void* stream, size_t order, size_t batch, double*
                                const double* euler, int rotation_type,
                                const double* wignerd, size_t wignerd_order);
 
+/* ---- batches of expansions of different orders (no reference counterpart;
+ *      the reference runs one Rotor::rotate + backward_transform per expansion,
+ *      rotor.hpp:214-243, zernike_glq_transformer.hpp:663-679) ----
+ * Rotates expansion i by euler[3i..3i+2] (in place) and backward-transforms it
+ * to a grid of its own order, for n_items expansions.  `orders` (host) must be
+ * non-decreasing; `coeffs`, `euler` and `grids` are device buffers, expansions
+ * and grids packed back to back in item order.  The first call for a given
+ * (orders, buffers, conventions, precision) runs the work eagerly and records
+ * it into a CUDA graph on the context; a later identical call replays the
+ * graph.  Results are those of zest_gpu_zt_rotate + zest_gpu_zt_backward per
+ * item. */
+int zest_gpu_zt_rotate_backward_ragged(zest_gpu_context* ctx, int zernike_norm, int sh_norm, int sh_phase,
+                                       size_t n_items, const int* orders, double* coeffs, const double* euler,
+                                       int rotation_type, double* grids);
+/* Autotuning of the FP64 contraction tile shapes: when enabled, the first run
+ * of each Zernike stage at a new size times the candidate shapes on the
+ * context stream and keeps the fastest (default off: a size rule). */
+int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable);
+
+/* ---- adjoints: vector-Jacobian products (no reference counterpart; the
+ *      reference has no derivatives) ----
+ * The transforms are linear; these return the transpose applied to a
+ * cotangent, for gradients of losses through them.  With B the backward
+ * transform, W the grid's quadrature weights and G the Gram diagonal of the
+ * real basis, the reference's forward transform (zernike_glq_transformer.hpp:
+ * 640-655, sh_glq_transformer.hpp:632-647) is F = G^+ B^T W, so
+ *   forward_vjp:  grids_cot  = F^T coeffs_cot = W B (G^+ coeffs_cot)
+ *   backward_vjp: coeffs_cot = B^T grids_cot  = G F (W^-1 grids_cot)
+ * (the sin part of m = 0, and orders a transform does not use, get 0).
+ * Orders, batching and memory kinds as for the transforms. */
+int zest_gpu_zt_forward_vjp(zest_gpu_context* ctx, int zernike_norm, int sh_norm, int sh_phase,
+                            size_t grid_order, size_t exp_order, size_t batch,
+                            const double* coeffs_cot, double* grids_cot, int mem);
+int zest_gpu_zt_backward_vjp(zest_gpu_context* ctx, int zernike_norm, int sh_norm, int sh_phase,
+                             size_t exp_order, size_t grid_order, size_t batch,
+                             const double* grids_cot, double* coeffs_cot, int mem);
+int zest_gpu_st_forward_vjp(zest_gpu_context* ctx, int sh_norm, int sh_phase, int layout,
+                            size_t grid_order, size_t exp_order, size_t batch,
+                            const double* coeffs_cot, double* grids_cot, int mem);
+int zest_gpu_st_backward_vjp(zest_gpu_context* ctx, int sh_norm, int sh_phase, int layout,
+                             size_t exp_order, size_t grid_order, size_t batch,
+                             const double* grids_cot, double* coeffs_cot, int mem);
+/* Rotor::rotate (rotor.hpp:214-243 / 125-141) as y = D(euler) x, per batch
+ * item: coeffs_cot = D^T out_cot (the inverse rotation of out_cot) and
+ * euler_cot[3 b + k] = sum over coefficients of out_cot * d y / d euler_k.
+ * Either output may be NULL; `coeffs` (x) is needed only for euler_cot.
+ * The angle gradient supports orders up to 1024. */
+int zest_gpu_zt_rotate_vjp(zest_gpu_context* ctx, size_t order, size_t batch, const double* coeffs,
+                           const double* euler, int rotation_type, const double* out_cot,
+                           double* coeffs_cot, double* euler_cot, int mem);
+int zest_gpu_st_rotate_vjp(zest_gpu_context* ctx, size_t order, size_t batch, const double* coeffs,
+                           const double* euler, int rotation_type, const double* out_cot,
+                           double* coeffs_cot, double* euler_cot, int mem);
+
 /* ---- split-precision dense product (no reference counterpart) ----
  * C = A B^T for row-major FP64 A (M x K) and B (N x K), K <= 992, evaluated
  * with the context's slice count on the tcgen05 path used by

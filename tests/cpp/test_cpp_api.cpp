@@ -10,7 +10,10 @@
 //     <op> <conventions> <order> <input file> <output file> [extra file]
 // runs it through the C++ interface and writes the result as raw doubles.
 // The test harness compares the outputs with the golden fixtures.
+#include <algorithm>
 #include <array>
+#include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -170,6 +173,70 @@ void run_rot(const std::string& op, const std::string& conv, std::size_t order, 
     }
 }
 
+// Transpose identities through the C++ adjoints, written as relative
+// differences: <F g, c> vs <g, F^T c>, <B c, g> vs <c, B^T g>,
+// <rotate(x), y> vs <x, rotate^T y>.
+void run_vjp_checks(const std::string& out) {
+    const std::size_t L = 9;
+    zt::GLQTransformerGeo<> t(L);
+    zt::BallGLQGrid<double> g(L), gt(L), bc(L);
+    zt::RealZernikeExpansionGeo c(L), fg(L), ct(L), x(L), y(L), xt(L);
+    std::uint64_t s = 12345;
+    auto rnd = [&]() {
+        s = s * 6364136223846793005ull + 1442695040888963407ull;
+        return double(s >> 11) / double(1ull << 53) - 0.5;
+    };
+    for (auto& v : g.flatten()) v = rnd();
+    for (std::size_t n = 0; n < L; ++n)
+        for (std::size_t l = n & 1; l <= n; l += 2)
+            for (std::size_t m = 0; m <= l; ++m) {
+                c(n, l, m) = {rnd(), m ? rnd() : 0.0};
+                x(n, l, m) = {rnd(), m ? rnd() : 0.0};
+                y(n, l, m) = {rnd(), m ? rnd() : 0.0};
+            }
+    t.forward_transform(g, fg);
+    t.forward_transform_vjp(c, gt);
+    t.backward_transform(c, bc);
+    t.backward_transform_vjp(g, ct);
+    auto dot_c = [&](const auto& a, const auto& b) {
+        double d = 0.0;
+        for (std::size_t i = 0; i < a.size(); ++i) d += a.data()[i][0] * b.data()[i][0] + a.data()[i][1] * b.data()[i][1];
+        return d;
+    };
+    auto dot_g = [&](const auto& a, const auto& b) {
+        double d = 0.0;
+        for (std::size_t i = 0; i < a.size(); ++i) d += a.data()[i] * b.data()[i];
+        return d;
+    };
+    auto rel = [](double a, double b) { return std::abs(a - b) / std::max({std::abs(a), std::abs(b), 1e-300}); };
+    double r[4];
+    r[0] = rel(dot_c(fg, c), dot_g(g, gt));
+    r[1] = rel(dot_g(bc, g), dot_c(c, ct));
+    Rotor rotor(L);
+    WignerdPiHalfCollection w(L);
+    const std::array<double, 3> e{0.3, 1.1, -2.0};
+    zt::RealZernikeExpansionGeo rx = x;
+    rotor.rotate(rx, w, e, RotationType::object);
+    const std::array<double, 3> grad = rotor.rotate_vjp(x, w, e, RotationType::object, y,
+                                                        reinterpret_cast<double*>(xt.data()));
+    r[2] = rel(dot_c(rx, y), dot_c(x, xt));
+    // the angle gradient against a central difference of <rotate(x, e), y>
+    const double h = 1e-6;
+    double worst = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        std::array<double, 3> ep = e, em = e;
+        ep[k] += h;
+        em[k] -= h;
+        zt::RealZernikeExpansionGeo xp = x, xm = x;
+        rotor.rotate(xp, w, ep, RotationType::object);
+        rotor.rotate(xm, w, em, RotationType::object);
+        const double fd = (dot_c(xp, y) - dot_c(xm, y)) / (2 * h);
+        worst = std::max(worst, std::abs(fd - grad[k]) / std::max(std::abs(fd), 1e-3));
+    }
+    r[3] = worst;
+    write_doubles(out, r, 4);
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -189,6 +256,11 @@ int main(int argc, char** argv) {
             std::size_t order = 0;
             ss >> op >> conv >> order >> in >> out >> extra;
             const std::vector<double> x = read_doubles(dir + "/" + in);
+            if (op == "vjp_checks") {
+                run_vjp_checks(dir + "/" + out);
+                ++n;
+                continue;
+            }
             if (op == "zt_fwd" || op == "zt_bwd") run_zt(op, conv, order, x, dir + "/" + out);
             else if (op == "st_fwd" || op == "st_bwd") run_st(op, conv, order, x, dir + "/" + out);
             else run_rot(op, conv, order, x, dir + "/" + out, read_doubles(dir + "/" + extra));

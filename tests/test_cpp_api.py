@@ -89,6 +89,10 @@ def test_cpp_interface_matches_golden(binary, golden, tmp_path):
         job("st_rot", "0", L + 3, r[f"sc_{L}"], r[f"sobj_{L}"], r[f"ze_{L}"])
         job("st_rot", "1", L + 3, r[f"sc_{L}"], r[f"scoord_{L}"], r[f"ze_{L}"])
         job("st_polar", "1", L + 3, r[f"sc_{L}"], r[f"spolar_{L}"], r[f"ze_{L}"][1:2])
+    # transpose identities and the angle gradient through the C++ adjoints
+    _write(d, "unused.bin", np.zeros(1))
+    jobs.append(f"vjp_checks 0 0 unused.bin out{len(jobs)}.bin")
+    vjp_out = f"out{len(jobs) - 1}.bin"
     with open(os.path.join(d, "jobs.txt"), "w") as f:
         f.write("\n".join(jobs) + "\n")
     res = subprocess.run([binary, d], capture_output=True, text=True, timeout=300)
@@ -97,3 +101,6 @@ def test_cpp_interface_matches_golden(binary, golden, tmp_path):
         got = np.fromfile(os.path.join(d, name))
         assert got.size == want.size, what
         assert relmax(got, want) < TOL, what
+    r = np.fromfile(os.path.join(d, vjp_out))
+    assert np.all(r[:3] < 1e-12), r
+    assert r[3] < 1e-7, r

@@ -95,6 +95,14 @@ _SIGNATURES = {
     "zest_gpu_split_gemm": [_vp, _sz, _sz, _sz, _vp, _vp, _vp, _i],
     "zest_gpu_profile_flops": [_vp, _i, _vp, _vp],
     "zest_gpu_zt_rotate_noalloc": [_vp, _sz, _sz, _vp, _vp, _i, _vp, _sz],
+    "zest_gpu_zt_forward_vjp": [_vp, _i, _i, _i, _sz, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_zt_backward_vjp": [_vp, _i, _i, _i, _sz, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_st_forward_vjp": [_vp, _i, _i, _i, _sz, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_st_backward_vjp": [_vp, _i, _i, _i, _sz, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_zt_rotate_vjp": [_vp, _sz, _sz, _vp, _vp, _i, _vp, _vp, _vp, _i],
+    "zest_gpu_st_rotate_vjp": [_vp, _sz, _sz, _vp, _vp, _i, _vp, _vp, _vp, _i],
+    "zest_gpu_zt_rotate_backward_ragged": [_vp, _i, _i, _i, _sz, _vp, _vp, _vp, _i, _vp],
+    "zest_gpu_set_autotune": [_vp, _i],
 }
 _SIZE_FUNCS = {
     "zest_gpu_zt_grid_size": [_sz],
@@ -310,6 +318,99 @@ class Context:
         ap, am = _ptr(angles, batch)
         _check(self.lib.zest_gpu_st_polar_rotate(self._h, order, batch, cp, ap, rotation_type, cm))
         return coeffs
+
+    def set_autotune(self, enable: bool = True):
+        _check(self.lib.zest_gpu_set_autotune(self._h, int(enable)))
+
+    def zt_rotate_backward_ragged(self, orders, coeffs, euler, grids, conv=ZT_GEO,
+                                  rotation_type: int = ROTATION_OBJECT):
+        """Rotate each expansion (in place) and backward-transform it to its own
+        grid; orders non-decreasing, coeffs/euler/grids torch CUDA float64
+        tensors packed in item order."""
+        if not (_is_torch(coeffs) and _is_torch(euler) and _is_torch(grids)) or not coeffs.is_cuda:
+            raise ValueError("coeffs, euler and grids must be CUDA tensors")
+        o = np.ascontiguousarray(orders, dtype=np.int32)
+        csz = int(sum(2 * zt_coeff_size(int(L)) for L in o))
+        gsz = int(sum(int(np.prod(zt_grid_shape(int(L)))) for L in o))
+        cp, _ = _ptr(coeffs, csz)
+        ep, _ = _ptr(euler, 3 * o.size)
+        gp, _ = _ptr(grids, gsz)
+        _check(self.lib.zest_gpu_zt_rotate_backward_ragged(self._h, *conv, o.size, _vp(o.ctypes.data), cp, ep,
+                                                           rotation_type, gp))
+        return grids
+
+    # ---- adjoints (vector-Jacobian products) ----
+    def zt_forward_vjp(self, coeffs_cot, grid_order: int, exp_order: Optional[int] = None, batch: int = 1,
+                       conv=ZT_GEO, out=None):
+        """Grid cotangent of zt_forward(grids, grid_order, exp_order)."""
+        exp_order = grid_order if exp_order is None else exp_order
+        gsz = int(np.prod(zt_grid_shape(grid_order))) * batch
+        csz = 2 * zt_coeff_size(exp_order) * batch
+        cp, cm = _ptr(coeffs_cot, csz)
+        if out is None:
+            out = self._alloc_like(coeffs_cot, gsz)
+        gp, gm = _ptr(out, gsz)
+        _check(self.lib.zest_gpu_zt_forward_vjp(self._h, *conv, grid_order, exp_order, batch, cp, gp, cm))
+        return out
+
+    def zt_backward_vjp(self, grids_cot, exp_order: int, grid_order: Optional[int] = None, batch: int = 1,
+                        conv=ZT_GEO, out=None):
+        """Coefficient cotangent of zt_backward(coeffs, exp_order, grid_order)."""
+        grid_order = exp_order if grid_order is None else grid_order
+        gsz = int(np.prod(zt_grid_shape(grid_order))) * batch
+        csz = 2 * zt_coeff_size(exp_order) * batch
+        gp, gm = _ptr(grids_cot, gsz)
+        if out is None:
+            out = self._alloc_like(grids_cot, csz)
+        cp, cm = _ptr(out, csz)
+        _check(self.lib.zest_gpu_zt_backward_vjp(self._h, *conv, exp_order, grid_order, batch, gp, cp, gm))
+        return out
+
+    def st_forward_vjp(self, coeffs_cot, grid_order: int, exp_order: Optional[int] = None, batch: int = 1,
+                       conv=ST_GEO, layout: int = LAYOUT_LONLAT, out=None):
+        exp_order = grid_order if exp_order is None else exp_order
+        gsz = int(np.prod(st_grid_shape(grid_order, layout))) * batch
+        csz = 2 * st_coeff_size(exp_order) * batch
+        cp, cm = _ptr(coeffs_cot, csz)
+        if out is None:
+            out = self._alloc_like(coeffs_cot, gsz)
+        gp, gm = _ptr(out, gsz)
+        _check(self.lib.zest_gpu_st_forward_vjp(self._h, *conv, layout, grid_order, exp_order, batch, cp, gp, cm))
+        return out
+
+    def st_backward_vjp(self, grids_cot, exp_order: int, grid_order: Optional[int] = None, batch: int = 1,
+                        conv=ST_GEO, layout: int = LAYOUT_LONLAT, out=None):
+        grid_order = exp_order if grid_order is None else grid_order
+        gsz = int(np.prod(st_grid_shape(grid_order, layout))) * batch
+        csz = 2 * st_coeff_size(exp_order) * batch
+        gp, gm = _ptr(grids_cot, gsz)
+        if out is None:
+            out = self._alloc_like(grids_cot, csz)
+        cp, cm = _ptr(out, csz)
+        _check(self.lib.zest_gpu_st_backward_vjp(self._h, *conv, layout, exp_order, grid_order, batch, gp, cp, gm))
+        return out
+
+    def _rotate_vjp(self, fn, csize, coeffs, order, euler, out_cot, batch, rotation_type, want_coeffs, want_euler):
+        cp, cm = _ptr(coeffs, csize * batch)
+        ep, em = _ptr(euler, 3 * batch)
+        yp, ym = _ptr(out_cot, csize * batch)
+        xb = self._alloc_like(out_cot, csize * batch) if want_coeffs else None
+        eb = self._alloc_like(out_cot, 3 * batch) if want_euler else None
+        xbp = _ptr(xb, csize * batch)[0] if xb is not None else _vp(0)
+        ebp = _ptr(eb, 3 * batch)[0] if eb is not None else _vp(0)
+        _check(fn(self._h, order, batch, cp, ep, rotation_type, yp, xbp, ebp, ym))
+        return xb, eb
+
+    def zt_rotate_vjp(self, coeffs, order: int, euler, out_cot, batch: int = 1,
+                      rotation_type: int = ROTATION_OBJECT, want_coeffs: bool = True, want_euler: bool = True):
+        """(coeffs cotangent, euler cotangent) of y = zt_rotate(coeffs, order, euler)."""
+        return self._rotate_vjp(self.lib.zest_gpu_zt_rotate_vjp, 2 * zt_coeff_size(order), coeffs, order, euler,
+                                out_cot, batch, rotation_type, want_coeffs, want_euler)
+
+    def st_rotate_vjp(self, coeffs, order: int, euler, out_cot, batch: int = 1,
+                      rotation_type: int = ROTATION_OBJECT, want_coeffs: bool = True, want_euler: bool = True):
+        return self._rotate_vjp(self.lib.zest_gpu_st_rotate_vjp, 2 * st_coeff_size(order), coeffs, order, euler,
+                                out_cot, batch, rotation_type, want_coeffs, want_euler)
 
     def split_gemm(self, A: np.ndarray, B: np.ndarray) -> np.ndarray:
         """C = A B^T through the split-precision tensor-core path (host arrays)."""

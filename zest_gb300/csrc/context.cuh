@@ -85,6 +85,27 @@ struct StPlan {
     LegTables leg;
 };
 
+// A batch of expansions of different orders (rotate, then backward
+// transform), its device work lists and the CUDA graph that replays it.
+struct RaggedPlan {
+    std::vector<int> orders;
+    const void* coeffs = nullptr;
+    const void* euler = nullptr;
+    const void* grids = nullptr;
+    int zn = 0, sn = 0, sp = 0, type = 0, precision = 0, slices = 0;
+    int Lmax = 0;
+    long long nwork = 0;
+    DevBuf coff, work;                                         // per-item coefficient offsets, {item, n, l}
+    std::vector<long long> coff_h, goff_h;
+    std::vector<std::tuple<int, int, int>> buckets;            // {order, first item, count}
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~RaggedPlan() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
 struct TileEntry {
     DevBuf buf;
     int count = 0;
@@ -130,10 +151,17 @@ struct zest_gpu_context {
     std::map<int, std::unique_ptr<FftEntry>> ffts;
     std::map<int, std::unique_ptr<DevBuf>> wigner;
     std::map<std::tuple<int, int>, std::pair<std::unique_ptr<DevBuf>, int>> vec_lists;
-    std::map<std::tuple<int, int, int, int, int>, std::unique_ptr<TileEntry>> tiles;
+    std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<TileEntry>> tiles;
+    bool autotune = false;                                    // time the tile shapes on first use
+    std::unique_ptr<RaggedPlan> ragged;                       // last batch of uneven orders, with its graph
+    cudaStream_t graph_stream = nullptr;                      // own stream for graph capture and replay
+    cudaEvent_t graph_ev[2] = {nullptr, nullptr};             // ordering with the context stream
+    std::map<std::tuple<int, int, int, int>, int> tuned;      // chosen shape per (stage, L, Lm, batch)
     DevBuf s0, s1;          // transform scratch (spectra, flm)
     DevBuf in_stage, out_stage, aux_stage;  // host <-> device staging
     DevBuf phase;           // rotation phases
+    DevBuf adj0, adj1, adj2;  // adjoint scratch (scaled operands, inverse angles, angle partials)
+    std::map<std::tuple<int, int, int>, std::unique_ptr<DevBuf>> adj_w;  // quadrature weight slabs
     std::unique_ptr<SplitState, SplitDeleter> split;
     Profiler prof;
 };

@@ -258,8 +258,11 @@ struct StLegBwd {
 };
 
 // tile shapes: Zernike sums have few rows and many columns; SH sums have
-// many rows (or K) and 2*batch columns.
-constexpr int ZBM = 64, ZBN = 64, ZTM = 4, ZTN = 4, ZBK = 8;
+// many rows (or K) and 2*batch columns.  The Zernike sums come in three
+// shapes of 256 threads (the autotuner picks one per stage and size): groups
+// have (L - m)/2 or (L + 1)/2 rows, so small orders waste most of a 64-row tile.
+//   variant 0: 64 x 64 (4 x 4 per thread), 1: 32 x 128 (2 x 8), 2: 16 x 128 (1 x 8)
+constexpr int ZBK = 8;
 constexpr int SBM = 128, SBN = 16, STM = 4, STN = 2, SBK = 8;
 
 template <class Prob, int BM, int BN, int TM, int TN, int BK>
@@ -269,30 +272,42 @@ int run(cudaStream_t s, const Prob& p, const TileList& tl, const char* name) {
     return launch_check(name);
 }
 
+template <class Prob>
+int run_zt(cudaStream_t s, const Prob& p, const TileList& tl, const char* name) {
+    switch (tl.variant) {
+    case 1: return run<Prob, 32, 128, 2, 8, ZBK>(s, p, tl, name);
+    case 2: return run<Prob, 16, 128, 1, 8, ZBK>(s, p, tl, name);
+    default: return run<Prob, 64, 64, 4, 4, ZBK>(s, p, tl, name);
+    }
+}
+
 }  // namespace
 
-void zt_tile_shape(int& bm, int& bn) { bm = ZBM; bn = ZBN; }
+void zt_tile_shape(int variant, int& bm, int& bn) {
+    bm = variant == 1 ? 32 : (variant == 2 ? 16 : 64);
+    bn = variant == 0 ? 64 : 128;
+}
 void st_tile_shape(int& bm, int& bn) { bm = SBM; bn = SBN; }
 
 int launch_zt_leg_fwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* G, double* flm, int Lg,
                       int nlat, int nrad, int batch) {
     ZtLegFwd p{lm, G, flm, Lg, nlat, 2 * nrad, batch};
-    return run<ZtLegFwd, ZBM, ZBN, ZTM, ZTN, ZBK>(s, p, tl, "zt_leg_fwd");
+    return run_zt(s, p, tl, "zt_leg_fwd");
 }
 int launch_zt_leg_bwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* flm, double* G, int Lg,
                       int nlat, int nrad, int batch) {
     ZtLegBwd p{lm, flm, G, Lg, nlat, 2 * nrad, batch};
-    return run<ZtLegBwd, ZBM, ZBN, ZTM, ZTN, ZBK>(s, p, tl, "zt_leg_bwd");
+    return run_zt(s, p, tl, "zt_leg_bwd");
 }
 int launch_zt_rad_fwd(cudaStream_t s, const RadMeta& rm, const TileList& tl, const double* flm, double* coeffs,
                       int nrad, int batch, long long coeff_stride) {
     ZtRadFwd p{rm, flm, coeffs, nrad, batch, coeff_stride};
-    return run<ZtRadFwd, ZBM, ZBN, ZTM, ZTN, ZBK>(s, p, tl, "zt_rad_fwd");
+    return run_zt(s, p, tl, "zt_rad_fwd");
 }
 int launch_zt_rad_bwd(cudaStream_t s, const RadMeta& rm, const TileList& tl, const double* coeffs, double* flm,
                       int nrad, int batch, long long coeff_stride) {
     ZtRadBwd p{rm, coeffs, flm, nrad, batch, coeff_stride};
-    return run<ZtRadBwd, ZBM, ZBN, ZTM, ZTN, ZBK>(s, p, tl, "zt_rad_bwd");
+    return run_zt(s, p, tl, "zt_rad_bwd");
 }
 int launch_st_leg_fwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* X, double* coeffs, int Lg,
                       int nlat, int batch, long long coeff_stride) {

@@ -40,6 +40,7 @@ struct RadMeta {
 struct TileList {
     const int4* tiles = nullptr;    // {group, row0, col0, -}
     int count = 0;
+    int variant = 0;                // tile shape of the Zernike sums (zt_tile_shape)
 };
 
 // Zernike (G: [b][m][lat][rad][2], flm: [tri(l,m)][b][rad][2], coeffs: [b][zidx][2])
@@ -57,7 +58,8 @@ int launch_st_leg_fwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, con
 int launch_st_leg_bwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* coeffs, double* X,
                       int Lg, int nlat, int batch, long long coeff_stride);
 // tile shapes (rows x cols per CTA) of the launches above
-void zt_tile_shape(int& bm, int& bn);
+void zt_tile_shape(int variant, int& bm, int& bn);
+constexpr int kZtTileVariants = 3;
 void st_tile_shape(int& bm, int& bn);
 
 // ---- rotations ------------------------------------------------------------------
@@ -69,5 +71,29 @@ int launch_rotate_vectors(cudaStream_t s, int kind, int L, int batch, double* co
                           double* phase_scratch);
 int launch_polar_vectors(cudaStream_t s, int kind, int L, int batch, double* coeffs, long long cstride,
                          const int2* vec_list, int nvec, const double* angles, int type);
+// Gradient of <ybar, rotate(x, euler)> with respect to the Euler angles of each
+// batch item -> grad[3 * batch].  part: 3 * nvec * batch doubles of scratch.
+int launch_rotate_euler_grad(cudaStream_t s, int kind, int L, int batch, const double* x, const double* ybar,
+                             long long cstride, const int2* vec_list, int nvec, const double* wigner,
+                             const double* euler, int type, double* phase_scratch, double* part, double* grad);
+// Rotations of `items` expansions of different orders in one launch: work
+// entries {item, n, l, -}, item i's coefficients at coeffs + coff[i]; phase
+// scratch 6 * Lmax * items doubles.
+int launch_rotate_ragged(cudaStream_t s, int kind, int Lmax, int items, double* coeffs, const long long* coff,
+                         const int4* work, long long nwork, const double* wigner, const double* euler, int type,
+                         double* phase_scratch);
+// Euler angles (3 per item) of the inverse rotations.
+int launch_invert_euler(cudaStream_t s, int batch, const double* euler, double* out);
+
+// ---- adjoints of the transforms (adjoint.cu) --------------------------------------
+// c_out = G c_in (inverse = 0) or G^+ c_in (inverse = 1) for the Gram diagonal of
+// the real basis under the quadrature: G = S (1 if normed, 1/(2n+3) if unnormed)
+// for Zernike, S for SH, S = 4 pi (geo) or 1 (qm); 0 for the sin part of m = 0.
+int launch_zt_gram(cudaStream_t s, const double* in, double* out, int L, int batch, int sh_norm, int zernike_norm,
+                   int inverse);
+int launch_st_gram(cudaStream_t s, const double* in, double* out, int L, int batch, int sh_norm, int inverse);
+// out[i] = in[i] * w[i % slab] (divide = 0) or in[i] / w[i % slab] (divide = 1) over n values.
+int launch_grid_weights(cudaStream_t s, const double* in, double* out, long long n, const double* w, long long slab,
+                        int divide);
 
 }  // namespace zgpu

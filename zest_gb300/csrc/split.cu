@@ -1087,6 +1087,20 @@ struct SplitState {
 
 void destroy_split(SplitState* s) { delete s; }
 
+// Bounded-wait error flag of the split GEMMs launched so far (0 if none); clears it.
+int split_check_flag(zest_gpu_context* ctx) {
+    SplitState* st = ctx->split.get();
+    if (!st || !st->err.p) return ZEST_GPU_OK;
+    int herr = 0;
+    ZG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    ZG_CUDA_TRY(cudaMemcpy(&herr, st->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+        cudaMemset(st->err.p, 0, sizeof(int));
+        return fail(ZEST_GPU_ERR_TIMEOUT, "split GEMM: bounded wait expired (code " + std::to_string(herr) + ")");
+    }
+    return ZEST_GPU_OK;
+}
+
 namespace {
 
 template <class Loader>
@@ -1329,7 +1343,11 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
         split_gemm_kernel<S, BITS, NT, Epi><<<grid, SP_THREADS, smem, s>>>(ma0, ma1, mb0, mb1, P, epi);
         ZG_TRY(launch_check("split_gemm_kernel"));
     }
-    // surface a bounded-wait timeout of this launch to the caller
+    // surface a bounded-wait timeout of this launch to the caller (not while the
+    // stream is being captured into a graph: the graph's caller checks the flag)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    ZG_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+    if (cap != cudaStreamCaptureStatusNone) return ZEST_GPU_OK;
     ZG_CUDA_TRY(cudaStreamSynchronize(s));
     int herr = 0;
     ZG_CUDA_TRY(cudaMemcpy(&herr, st->err.p, sizeof(int), cudaMemcpyDeviceToHost));

@@ -25,5 +25,8 @@ int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A
 // (counted while profiling is enabled): useful = valid rows x table rows x K,
 // issued = whole 128-row tiles as executed.
 void split_flops(zest_gpu_context* ctx, bool reset, double* useful, double* issued);
+// Synchronizes the context stream and reports (and clears) a bounded-wait
+// timeout recorded by split GEMMs launched without a host check (graph replay).
+int split_check_flag(zest_gpu_context* ctx);
 
 }  // namespace zgpu

@@ -231,12 +231,14 @@ static int get_st_plan(zest_gpu_context* ctx, int L, int sn, int sp, int layout,
 
 // Tile lists of the grouped contractions, cached per (kind, L, Lm, batch).
 // kinds: 0 zt_leg_fwd, 1 zt_leg_bwd, 2 zt_rad_fwd, 3 zt_rad_bwd, 4 st_leg_fwd, 5 st_leg_bwd
-static int get_tiles(zest_gpu_context* ctx, int kind, int L, int Lm, int batch, int aux, TileList* tl) {
-    auto key = std::make_tuple(kind, L, Lm, batch, aux);
+static int get_tiles(zest_gpu_context* ctx, int kind, int L, int Lm, int batch, int aux, TileList* tl,
+                     int variant = 0) {
+    if (kind > 3) variant = 0;
+    auto key = std::make_tuple(kind, L, Lm, batch, aux, variant);
     auto it = ctx->tiles.find(key);
     if (it == ctx->tiles.end()) {
         int bm, bn;
-        if (kind <= 3) zt_tile_shape(bm, bn);
+        if (kind <= 3) zt_tile_shape(variant, bm, bn);
         else st_tile_shape(bm, bn);
         std::vector<int4> v;
         auto add = [&](int g, long long M, long long N) {
@@ -279,12 +281,70 @@ static int get_tiles(zest_gpu_context* ctx, int kind, int L, int Lm, int batch, 
         ZG_TRY(upload(e->buf, v, ctx->stream));
         it = ctx->tiles.emplace(key, std::move(e)).first;
     }
+    tl->variant = variant;
     tl->tiles = it->second->buf.as<int4>();
     tl->count = it->second->count;
     return ZEST_GPU_OK;
 }
 
 static bool valid01(int x) { return x == 0 || x == 1; }
+
+// ---------------------------------------------------------------------------
+// Autotuner of the tile shape of the Zernike FP64 sums.  When tuning is on,
+// the first run of a stage (kind 0..3) at a size (L, Lm, batch) times each
+// tile shape with CUDA events on the context stream (after one untimed run)
+// and keeps the fastest; the stages overwrite their outputs, so the extra runs
+// change nothing.  Without tuning, or while the stream is being captured, a
+// size rule picks the shape: small orders have few rows per group.
+template <class Run>
+static int zt_tile_variant(zest_gpu_context* ctx, int kind, int L, int Lm, int batch, int aux, Run&& run,
+                           int* variant) {
+    auto key = std::make_tuple(kind, L, Lm, batch);
+    auto it = ctx->tuned.find(key);
+    if (it != ctx->tuned.end()) {
+        *variant = it->second;
+        return ZEST_GPU_OK;
+    }
+    *variant = Lm < 48 ? 2 : (Lm < 96 ? 1 : 0);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    ZG_CUDA_TRY(cudaStreamIsCapturing(ctx->stream, &cap));
+    if (!ctx->autotune || cap != cudaStreamCaptureStatusNone) return ZEST_GPU_OK;
+    cudaEvent_t e0, e1;
+    ZG_CUDA_TRY(cudaEventCreate(&e0));
+    ZG_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 0.0f;
+    int rc = ZEST_GPU_OK;
+    for (int v = 0; v < kZtTileVariants && rc == ZEST_GPU_OK; ++v) {
+        TileList tl;
+        rc = get_tiles(ctx, kind, L, Lm, batch, aux, &tl, v);
+        if (rc == ZEST_GPU_OK) rc = run(tl);
+        if (rc == ZEST_GPU_OK && cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = fail(ZEST_GPU_ERR_CUDA, "event");
+        if (rc == ZEST_GPU_OK) rc = run(tl);
+        if (rc == ZEST_GPU_OK && cudaEventRecord(e1, ctx->stream) != cudaSuccess) rc = fail(ZEST_GPU_ERR_CUDA, "event");
+        float ms = 0.0f;
+        if (rc == ZEST_GPU_OK && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+            rc = fail(ZEST_GPU_ERR_CUDA, "autotuner timing failed");
+        if (rc == ZEST_GPU_OK && (v == 0 || ms < best)) {
+            best = ms;
+            *variant = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc == ZEST_GPU_OK) ctx->tuned.emplace(key, *variant);
+    return rc;
+}
+
+// Runs one Zernike FP64 stage with its tuned tile shape, profiled as `stage`.
+template <class Run>
+static int zt_stage(zest_gpu_context* ctx, int stage, int kind, int L, int Lm, int batch, int aux, Run&& run) {
+    int v = 0;
+    ZG_TRY(zt_tile_variant(ctx, kind, L, Lm, batch, aux, run, &v));
+    TileList tl;
+    ZG_TRY(get_tiles(ctx, kind, L, Lm, batch, aux, &tl, v));
+    StageScope sc(ctx, stage);
+    return run(tl);
+}
 
 // ---------------------------------------------------------------------------
 // Zernike transforms on device pointers.
@@ -321,19 +381,16 @@ int zt_forward_dev(zest_gpu_context* ctx, int zn, int sn, int sp, int Lg, int Le
     lm.ld = plan->leg.nnodes;
     lm.j0u = plan->leg.j0u;
     lm.j0d = plan->leg.j0d;
-    TileList tl;
-    ZG_TRY(get_tiles(ctx, 0, Lg, Lm, batch, 0, &tl));
-    {
-        StageScope sc(ctx, ST_LEG_FWD);
-        ZG_TRY(launch_zt_leg_fwd(s, lm, tl, G, flm, Lg, int(sh.nlat), int(sh.nrad), batch));
-    }
+    ZG_TRY(zt_stage(ctx, ST_LEG_FWD, 0, Lg, Lm, batch, 0, [&](const TileList& tl) {
+        return launch_zt_leg_fwd(s, lm, tl, G, flm, Lg, int(sh.nlat), int(sh.nrad), batch);
+    }));
     RadMeta rm;
     rm.R = plan->rad.Rf.as<double>();
     rm.off = plan->rad.off.as<long long>();
     ZG_TRY(rad_cnt(ctx, plan->rad, Lm, &rm.cnt));
-    ZG_TRY(get_tiles(ctx, 2, Lg, Lm, batch, 0, &tl));
-    StageScope sc(ctx, ST_RAD_FWD);
-    return launch_zt_rad_fwd(s, rm, tl, flm, coeffs, int(sh.nrad), batch, csz);
+    return zt_stage(ctx, ST_RAD_FWD, 2, Lg, Lm, batch, 0, [&](const TileList& tl) {
+        return launch_zt_rad_fwd(s, rm, tl, flm, coeffs, int(sh.nrad), batch, csz);
+    });
 }
 
 int zt_backward_dev(zest_gpu_context* ctx, int zn, int sn, int sp, int Le, int Lg, int batch, const double* coeffs,
@@ -363,12 +420,9 @@ int zt_backward_dev(zest_gpu_context* ctx, int zn, int sn, int sp, int Le, int L
     rm.R = plan->rad.Rb.as<double>();
     rm.off = plan->rad.off.as<long long>();
     ZG_TRY(rad_cnt(ctx, plan->rad, Lm, &rm.cnt));
-    TileList tl;
-    ZG_TRY(get_tiles(ctx, 3, Lg, Lm, batch, 0, &tl));
-    {
-        StageScope sc(ctx, ST_RAD_BWD);
-        ZG_TRY(launch_zt_rad_bwd(s, rm, tl, coeffs, flm, int(sh.nrad), batch, csz));
-    }
+    ZG_TRY(zt_stage(ctx, ST_RAD_BWD, 3, Lg, Lm, batch, 0, [&](const TileList& tl) {
+        return launch_zt_rad_bwd(s, rm, tl, coeffs, flm, int(sh.nrad), batch, csz);
+    }));
     LegMeta lm;
     lm.P = plan->leg.Pb.as<double>();
     lm.off = plan->leg.off.as<long long>();
@@ -376,11 +430,9 @@ int zt_backward_dev(zest_gpu_context* ctx, int zn, int sn, int sp, int Le, int L
     lm.ld = plan->leg.nnodes;
     lm.j0u = plan->leg.j0u;
     lm.j0d = plan->leg.j0d;
-    ZG_TRY(get_tiles(ctx, 1, Lg, Lm, batch, lm.ld, &tl));
-    {
-        StageScope sc(ctx, ST_LEG_BWD);
-        ZG_TRY(launch_zt_leg_bwd(s, lm, tl, flm, G, Lg, int(sh.nlat), int(sh.nrad), batch));
-    }
+    ZG_TRY(zt_stage(ctx, ST_LEG_BWD, 1, Lg, Lm, batch, lm.ld, [&](const TileList& tl) {
+        return launch_zt_leg_bwd(s, lm, tl, flm, G, Lg, int(sh.nlat), int(sh.nrad), batch);
+    }));
     StageScope sc(ctx, ST_FFT_INV);
     return launch_rfft_inv(s, *fft, G, int(cols), Lg, batch, 0, grids, sh.size(), cols, 1);
 }
@@ -517,6 +569,272 @@ int polar_dev(zest_gpu_context* ctx, int kind, int L, int batch, double* coeffs,
     return launch_polar_vectors(ctx->stream, kind, L, batch, coeffs, cstride, vl, nvec, angles, type);
 }
 
+// ---------------------------------------------------------------------------
+// Adjoints (vector-Jacobian products); the identities are in adjoint.cu.
+
+// Quadrature weights of one slab of the grid, cached: Zernike [lat][rad] of
+// (2 pi / nlon) w_lat w_rad r^2 / 2; SH LonLat [lat] and LatLon [lat][lon] of
+// (2 pi / nlon) w_lat, the middle latitude of an odd LatLon grid doubled.
+static int get_adj_weights(zest_gpu_context* ctx, int kind, int L, int layout, const double** out, long long* slab) {
+    const double pi = 3.14159265358979323846264338327950288;
+    auto key = std::make_tuple(kind, L, kind == 0 ? 0 : layout);
+    auto it = ctx->adj_w.find(key);
+    std::vector<double> w;
+    if (kind == 0) {
+        const ZtShape sh = zt_shape(L);
+        *slab = sh.nlat * sh.nrad;
+        if (it == ctx->adj_w.end()) {
+            std::vector<double> xl(sh.nlat), wl(sh.nlat), xr(sh.nrad), wr(sh.nrad);
+            gl_nodes_weights(long(sh.nlat), false, xl.data(), wl.data());
+            gl_nodes_weights(long(sh.nrad), false, xr.data(), wr.data());
+            w.resize((size_t)*slab);
+            const double cphi = 2.0 * pi / double(sh.nlon);
+            for (long long j = 0; j < sh.nlat; ++j)
+                for (long long k = 0; k < sh.nrad; ++k) {
+                    const double r = 0.5 * (1.0 + xr[k]);
+                    w[j * sh.nrad + k] = cphi * wl[j] * (wr[k] * r * r * 0.5);
+                }
+        }
+    } else {
+        const StShape sh = st_shape(L, layout);
+        *slab = layout == ZEST_LAYOUT_LATLON ? sh.nlat * sh.nlon : sh.nlat;
+        if (it == ctx->adj_w.end()) {
+            std::vector<double> xl(sh.nlat), wl(sh.nlat);
+            gl_nodes_weights(long(sh.nlat), false, xl.data(), wl.data());
+            const double cphi = 2.0 * pi / double(sh.nlon);
+            for (long long j = 0; j < sh.nlat; ++j) wl[j] *= cphi;
+            if ((sh.nlat & 1) && layout == ZEST_LAYOUT_LATLON) wl[sh.nlat / 2] *= 2.0;
+            if (layout == ZEST_LAYOUT_LATLON) {
+                w.resize((size_t)*slab);
+                for (long long j = 0; j < sh.nlat; ++j)
+                    for (long long i = 0; i < sh.nlon; ++i) w[j * sh.nlon + i] = wl[j];
+            } else {
+                w = wl;
+            }
+        }
+    }
+    if (it == ctx->adj_w.end()) {
+        auto buf = std::make_unique<DevBuf>();
+        ZG_TRY(upload(*buf, w, ctx->stream));
+        it = ctx->adj_w.emplace(key, std::move(buf)).first;
+    }
+    *out = it->second->as<double>();
+    return ZEST_GPU_OK;
+}
+
+// grid cotangent of a forward transform: W B (G^+ cbar)
+int zt_forward_vjp_dev(zest_gpu_context* ctx, int zn, int sn, int sp, int Lg, int Le, int batch, const double* cbar,
+                       double* gbar) {
+    if (batch == 0 || Lg == 0) return ZEST_GPU_OK;
+    const long long csz = 2 * zsize(Le), gsz = zt_shape(Lg).size();
+    ZG_TRY(ctx->adj0.ensure((size_t)batch * csz * sizeof(double) + 16));
+    ZG_TRY(launch_zt_gram(ctx->stream, cbar, ctx->adj0.as<double>(), Le, batch, sn, zn, 1));
+    ZG_TRY(zt_backward_dev(ctx, zn, sn, sp, Le, Lg, batch, ctx->adj0.as<double>(), gbar));
+    const double* w;
+    long long slab;
+    ZG_TRY(get_adj_weights(ctx, 0, Lg, 0, &w, &slab));
+    return launch_grid_weights(ctx->stream, gbar, gbar, (long long)batch * gsz, w, slab, 0);
+}
+
+// coefficient cotangent of a backward transform: G F (W^-1 gbar); orders not
+// used by the backward transform get 0
+int zt_backward_vjp_dev(zest_gpu_context* ctx, int zn, int sn, int sp, int Le, int Lg, int batch, const double* gbar,
+                        double* cbar) {
+    if (batch == 0 || Le == 0) return ZEST_GPU_OK;
+    const long long csz = 2 * zsize(Le), gsz = zt_shape(Lg).size();
+    ZG_CUDA_TRY(cudaMemsetAsync(cbar, 0, (size_t)batch * csz * sizeof(double), ctx->stream));
+    if (Lg == 0) return ZEST_GPU_OK;
+    const double* w;
+    long long slab;
+    ZG_TRY(get_adj_weights(ctx, 0, Lg, 0, &w, &slab));
+    ZG_TRY(ctx->adj0.ensure((size_t)batch * gsz * sizeof(double) + 16));
+    ZG_TRY(launch_grid_weights(ctx->stream, gbar, ctx->adj0.as<double>(), (long long)batch * gsz, w, slab, 1));
+    ZG_TRY(zt_forward_dev(ctx, zn, sn, sp, Lg, Le, batch, ctx->adj0.as<double>(), cbar));
+    return launch_zt_gram(ctx->stream, cbar, cbar, Le, batch, sn, zn, 0);
+}
+
+int st_forward_vjp_dev(zest_gpu_context* ctx, int sn, int sp, int layout, int Lg, int Le, int batch,
+                       const double* cbar, double* gbar) {
+    if (batch == 0 || Lg == 0) return ZEST_GPU_OK;
+    const long long csz = 2 * tri_size(Le), gsz = st_shape(Lg, layout).size();
+    ZG_TRY(ctx->adj0.ensure((size_t)batch * csz * sizeof(double) + 16));
+    ZG_TRY(launch_st_gram(ctx->stream, cbar, ctx->adj0.as<double>(), Le, batch, sn, 1));
+    ZG_TRY(st_backward_dev(ctx, sn, sp, layout, Le, Lg, batch, ctx->adj0.as<double>(), gbar));
+    const double* w;
+    long long slab;
+    ZG_TRY(get_adj_weights(ctx, 1, Lg, layout, &w, &slab));
+    return launch_grid_weights(ctx->stream, gbar, gbar, (long long)batch * gsz, w, slab, 0);
+}
+
+int st_backward_vjp_dev(zest_gpu_context* ctx, int sn, int sp, int layout, int Le, int Lg, int batch,
+                        const double* gbar, double* cbar) {
+    if (batch == 0 || Le == 0) return ZEST_GPU_OK;
+    const long long csz = 2 * tri_size(Le), gsz = st_shape(Lg, layout).size();
+    ZG_CUDA_TRY(cudaMemsetAsync(cbar, 0, (size_t)batch * csz * sizeof(double), ctx->stream));
+    if (Lg == 0) return ZEST_GPU_OK;
+    const double* w;
+    long long slab;
+    ZG_TRY(get_adj_weights(ctx, 1, Lg, layout, &w, &slab));
+    ZG_TRY(ctx->adj0.ensure((size_t)batch * gsz * sizeof(double) + 16));
+    ZG_TRY(launch_grid_weights(ctx->stream, gbar, ctx->adj0.as<double>(), (long long)batch * gsz, w, slab, 1));
+    ZG_TRY(st_forward_dev(ctx, sn, sp, layout, Lg, Le, batch, ctx->adj0.as<double>(), cbar));
+    return launch_st_gram(ctx->stream, cbar, cbar, Le, batch, sn, 0);
+}
+
+// y = rotate(x, euler): xbar = D^T ybar = rotate(ybar, inverse angles) (D is
+// orthogonal on the real coefficients), ebar = (dy/d euler)^T ybar.
+int rotate_vjp_dev(zest_gpu_context* ctx, int kind, int L, int batch, const double* x, const double* euler, int type,
+                   const double* ybar, double* xbar, double* ebar) {
+    if (batch == 0) return ZEST_GPU_OK;
+    cudaStream_t s = ctx->stream;
+    const long long cstride = kind == 0 ? 2 * zsize(L) : 2 * tri_size(L);
+    if (xbar) {
+        ZG_CUDA_TRY(cudaMemcpyAsync(xbar, ybar, (size_t)batch * cstride * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        ZG_TRY(ctx->adj1.ensure((size_t)batch * 3 * sizeof(double)));
+        ZG_TRY(launch_invert_euler(s, batch, euler, ctx->adj1.as<double>()));
+        ZG_TRY(rotate_dev(ctx, kind, L, batch, xbar, ctx->adj1.as<double>(), type));
+    }
+    if (ebar) {
+        if (L <= 1) {
+            ZG_CUDA_TRY(cudaMemsetAsync(ebar, 0, (size_t)batch * 3 * sizeof(double), s));
+            return ZEST_GPU_OK;
+        }
+        const double* wig;
+        ZG_TRY(get_wigner(ctx, L, &wig));
+        const int2* vl;
+        int nvec;
+        ZG_TRY(get_vectors(ctx, kind, L, &vl, &nvec));
+        ZG_TRY(ctx->phase.ensure((size_t)batch * 6 * L * sizeof(double)));
+        ZG_TRY(ctx->adj2.ensure((size_t)batch * nvec * 3 * sizeof(double) + 16));
+        StageScope sc(ctx, ST_ROTATE);
+        ZG_TRY(launch_rotate_euler_grad(s, kind, L, batch, x, ybar, cstride, vl, nvec, wig, euler, type,
+                                        ctx->phase.as<double>(), ctx->adj2.as<double>(), ebar));
+    }
+    return ZEST_GPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batches of expansions of different orders: rotate every expansion (one
+// launch over a ragged work list), then backward-transform each group of equal
+// order as one batch.  The first call for a given (orders, buffers,
+// conventions, precision) runs eagerly -- building tables, work lists and
+// scratch, and autotuning tile shapes -- and then records the same sequence
+// into a CUDA graph; later identical calls replay the graph (a single launch
+// from the host).
+static int ragged_sequence(zest_gpu_context* ctx, RaggedPlan& P, double* coeffs, const double* euler,
+                           double* grids) {
+    const double* wig;
+    ZG_TRY(get_wigner(ctx, P.Lmax, &wig));
+    {
+        StageScope sc(ctx, ST_ROTATE);
+        ZG_TRY(launch_rotate_ragged(ctx->stream, 0, P.Lmax, int(P.orders.size()), coeffs, P.coff.as<long long>(),
+                                    P.work.as<int4>(), P.nwork, wig, euler, P.type, ctx->phase.as<double>()));
+    }
+    for (const auto& bk : P.buckets) {
+        const int L = std::get<0>(bk), first = std::get<1>(bk), count = std::get<2>(bk);
+        ZG_TRY(zt_backward_dev(ctx, P.zn, P.sn, P.sp, L, L, count, coeffs + P.coff_h[first], grids + P.goff_h[first]));
+    }
+    return ZEST_GPU_OK;
+}
+
+// Runs `body` on the context's own capture stream (created on first use; the
+// legacy default stream cannot be captured), ordered after the work queued on
+// the context stream and before the work queued on it later.
+template <class F>
+static int on_graph_stream(zest_gpu_context* ctx, F&& body) {
+    if (!ctx->graph_stream) {
+        ZG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->graph_stream, cudaStreamNonBlocking));
+        ZG_CUDA_TRY(cudaEventCreateWithFlags(&ctx->graph_ev[0], cudaEventDisableTiming));
+        ZG_CUDA_TRY(cudaEventCreateWithFlags(&ctx->graph_ev[1], cudaEventDisableTiming));
+    }
+    cudaStream_t user = ctx->stream;
+    ZG_CUDA_TRY(cudaEventRecord(ctx->graph_ev[0], user));
+    ZG_CUDA_TRY(cudaStreamWaitEvent(ctx->graph_stream, ctx->graph_ev[0], 0));
+    ctx->stream = ctx->graph_stream;
+    const int rc = body();
+    ctx->stream = user;
+    ZG_CUDA_TRY(cudaEventRecord(ctx->graph_ev[1], ctx->graph_stream));
+    ZG_CUDA_TRY(cudaStreamWaitEvent(user, ctx->graph_ev[1], 0));
+    return rc;
+}
+
+static int ragged_on_graph_stream(zest_gpu_context* ctx, int zn, int sn, int sp, const std::vector<int>& orders,
+                                  double* coeffs, const double* euler, int type, double* grids);
+
+int zt_rotate_backward_ragged_dev(zest_gpu_context* ctx, int zn, int sn, int sp, const std::vector<int>& orders,
+                                  double* coeffs, const double* euler, int type, double* grids) {
+    return on_graph_stream(ctx, [&] { return ragged_on_graph_stream(ctx, zn, sn, sp, orders, coeffs, euler, type, grids); });
+}
+
+static int ragged_on_graph_stream(zest_gpu_context* ctx, int zn, int sn, int sp, const std::vector<int>& orders,
+                                  double* coeffs, const double* euler, int type, double* grids) {
+    RaggedPlan* P = ctx->ragged.get();
+    const bool same = P && P->orders == orders && P->coeffs == coeffs && P->euler == euler && P->grids == grids &&
+                      P->zn == zn && P->sn == sn && P->sp == sp && P->type == type &&
+                      P->precision == ctx->precision && P->slices == ctx->slices;
+    if (same && P->exec) {
+        ZG_CUDA_TRY(cudaGraphLaunch(P->exec, ctx->stream));
+        if (P->precision == ZEST_PRECISION_SPLIT) ZG_TRY(split_check_flag(ctx));
+        return ZEST_GPU_OK;
+    }
+    // new plan: offsets, buckets and the rotation work list
+    auto np = std::make_unique<RaggedPlan>();
+    np->orders = orders;
+    np->coeffs = coeffs;
+    np->euler = euler;
+    np->grids = grids;
+    np->zn = zn;
+    np->sn = sn;
+    np->sp = sp;
+    np->type = type;
+    np->precision = ctx->precision;
+    np->slices = ctx->slices;
+    const int n = int(orders.size());
+    np->coff_h.resize(n + 1);
+    np->goff_h.resize(n + 1);
+    std::vector<int4> work;
+    long long co = 0, go = 0;
+    for (int i = 0; i < n; ++i) {
+        const int L = orders[i];
+        np->coff_h[i] = co;
+        np->goff_h[i] = go;
+        co += 2 * zsize(L);
+        go += zt_shape(L).size();
+        np->Lmax = std::max(np->Lmax, L);
+        if (np->buckets.empty() || std::get<0>(np->buckets.back()) != L) np->buckets.emplace_back(L, i, 0);
+        ++std::get<2>(np->buckets.back());
+        for (int l = 0; l < L; ++l)  // the rotated (n, l) vectors, as get_vectors
+            for (int nn = (l == 0 ? 2 : l); nn < L; nn += 2) work.push_back(make_int4(i, nn, l, 0));
+    }
+    np->coff_h[n] = co;
+    np->goff_h[n] = go;
+    np->nwork = (long long)work.size();
+    ZG_TRY(upload(np->coff, np->coff_h, ctx->stream));
+    ZG_TRY(upload(np->work, work, ctx->stream));
+    ZG_TRY(ctx->phase.ensure((size_t)n * 6 * std::max(np->Lmax, 1) * sizeof(double)));
+    ctx->ragged = std::move(np);
+    P = ctx->ragged.get();
+    // eager run: the result of this call, and every table, list and buffer the graph needs
+    ZG_TRY(ragged_sequence(ctx, *P, coeffs, euler, grids));
+    ZG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    // record the same sequence (nothing executes during capture)
+    const bool prof = ctx->prof.on;
+    ctx->prof.on = false;
+    ZG_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+    const int rc = ragged_sequence(ctx, *P, coeffs, euler, grids);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->prof.on = prof;
+    if (rc != ZEST_GPU_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (ec != cudaSuccess) return fail(ZEST_GPU_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+    P->graph = g;
+    ZG_CUDA_TRY(cudaGraphInstantiate(&P->exec, g, 0));
+    return ZEST_GPU_OK;
+}
+
 }  // namespace zgpu
 
 // ===========================================================================
@@ -594,6 +912,13 @@ int zest_gpu_ctx_destroy(zest_gpu_context* ctx) {
     if (!ctx) return ZEST_GPU_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    ctx->ragged.reset();
+    if (ctx->graph_stream) {
+        cudaStreamSynchronize(ctx->graph_stream);
+        cudaStreamDestroy(ctx->graph_stream);
+        for (cudaEvent_t e : ctx->graph_ev)
+            if (e) cudaEventDestroy(e);
+    }
     delete ctx;
     return ZEST_GPU_OK;
 }
@@ -605,7 +930,7 @@ int zest_gpu_set_precision(zest_gpu_context* ctx, int precision, int slices) {
     if (precision != ZEST_PRECISION_FP64 && precision != ZEST_PRECISION_SPLIT)
         return fail(ZEST_GPU_ERR_INVALID, "unknown precision");
     if (slices == 0) slices = 6;
-    if (slices < 4 || slices > 8) return fail(ZEST_GPU_ERR_INVALID, "slices must be in 4..8");
+    if (slices < 4 || slices > 6) return fail(ZEST_GPU_ERR_INVALID, "slices must be in 4..6");
     if (precision == ZEST_PRECISION_SPLIT) ZG_TRY(split_available());
     ctx->precision = precision;
     ctx->slices = slices;
@@ -786,6 +1111,131 @@ int zest_gpu_zt_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch, 
 int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch, double* coeffs, const double* angles,
                              int rotation_type, int mem) {
     return rotate_common(ctx, 1, order, batch, coeffs, angles, 1, rotation_type, mem, true);
+}
+
+int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable) {
+    ZG_TRY(check_ctx(ctx));
+    ctx->autotune = enable != 0;
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_zt_rotate_backward_ragged(zest_gpu_context* ctx, int zn, int sn, int sp, size_t n_items,
+                                       const int* orders, double* coeffs, const double* euler, int rotation_type,
+                                       double* grids) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(zn) || !valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (!valid01(rotation_type)) return fail(ZEST_GPU_ERR_INVALID, "invalid rotation type");
+    if (n_items == 0) return ZEST_GPU_OK;
+    if (n_items > 65535) return fail(ZEST_GPU_ERR_INVALID, "too many expansions (max 65535)");
+    if (!orders || !coeffs || !euler || !grids) return fail(ZEST_GPU_ERR_INVALID, "null pointer");
+    std::vector<int> ord(orders, orders + n_items);
+    for (size_t i = 0; i < n_items; ++i) {
+        if (ord[i] < 1 || ord[i] > 2048) return fail(ZEST_GPU_ERR_INVALID, "orders must be in 1..2048");
+        if (i && ord[i] < ord[i - 1]) return fail(ZEST_GPU_ERR_INVALID, "orders must be non-decreasing");
+    }
+    return zt_rotate_backward_ragged_dev(ctx, zn, sn, sp, ord, coeffs, euler, rotation_type, grids);
+}
+
+// ---- adjoints ----
+int zest_gpu_zt_forward_vjp(zest_gpu_context* ctx, int zn, int sn, int sp, size_t grid_order, size_t exp_order,
+                            size_t batch, const double* coeffs_cot, double* grids_cot, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(zn) || !valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (grid_order > kMaxOrder || exp_order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t gn = batch * zest_gpu_zt_grid_size(grid_order), cn = batch * 2 * zest_gpu_zt_coeff_size(exp_order);
+    if ((gn && !grids_cot) || (cn && !coeffs_cot)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, coeffs_cot, cn, grids_cot, gn, [&](const double* in, double* out) {
+        return zt_forward_vjp_dev(ctx, zn, sn, sp, int(grid_order), int(exp_order), int(batch), in, out);
+    });
+}
+
+int zest_gpu_zt_backward_vjp(zest_gpu_context* ctx, int zn, int sn, int sp, size_t exp_order, size_t grid_order,
+                             size_t batch, const double* grids_cot, double* coeffs_cot, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(zn) || !valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (grid_order > kMaxOrder || exp_order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t gn = batch * zest_gpu_zt_grid_size(grid_order), cn = batch * 2 * zest_gpu_zt_coeff_size(exp_order);
+    if ((gn && !grids_cot) || (cn && !coeffs_cot)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, grids_cot, gn, coeffs_cot, cn, [&](const double* in, double* out) {
+        return zt_backward_vjp_dev(ctx, zn, sn, sp, int(exp_order), int(grid_order), int(batch), in, out);
+    });
+}
+
+int zest_gpu_st_forward_vjp(zest_gpu_context* ctx, int sn, int sp, int layout, size_t grid_order, size_t exp_order,
+                            size_t batch, const double* coeffs_cot, double* grids_cot, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn) || !valid01(sp) || !valid01(layout)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention/layout");
+    if (grid_order > kMaxOrder || exp_order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t gn = batch * zest_gpu_st_grid_size(grid_order, layout), cn = batch * 2 * zest_gpu_st_coeff_size(exp_order);
+    if ((gn && !grids_cot) || (cn && !coeffs_cot)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, coeffs_cot, cn, grids_cot, gn, [&](const double* in, double* out) {
+        return st_forward_vjp_dev(ctx, sn, sp, layout, int(grid_order), int(exp_order), int(batch), in, out);
+    });
+}
+
+int zest_gpu_st_backward_vjp(zest_gpu_context* ctx, int sn, int sp, int layout, size_t exp_order, size_t grid_order,
+                             size_t batch, const double* grids_cot, double* coeffs_cot, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn) || !valid01(sp) || !valid01(layout)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention/layout");
+    if (grid_order > kMaxOrder || exp_order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t gn = batch * zest_gpu_st_grid_size(grid_order, layout), cn = batch * 2 * zest_gpu_st_coeff_size(exp_order);
+    if ((gn && !grids_cot) || (cn && !coeffs_cot)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, grids_cot, gn, coeffs_cot, cn, [&](const double* in, double* out) {
+        return st_backward_vjp_dev(ctx, sn, sp, layout, int(exp_order), int(grid_order), int(batch), in, out);
+    });
+}
+
+static int rotate_vjp_common(zest_gpu_context* ctx, int kind, size_t order, size_t batch, const double* coeffs,
+                             const double* euler, int type, const double* out_cot, double* coeffs_cot,
+                             double* euler_cot, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(type)) return fail(ZEST_GPU_ERR_INVALID, "invalid rotation type");
+    if (order > 2048) return fail(ZEST_GPU_ERR_INVALID, "rotation order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t cn = batch * 2 * (kind == 0 ? zest_gpu_zt_coeff_size(order) : zest_gpu_st_coeff_size(order));
+    const size_t an = batch * 3;
+    if (!coeffs_cot && !euler_cot) return ZEST_GPU_OK;
+    if ((cn && !out_cot) || (an && !euler) || (euler_cot && cn && !coeffs))
+        return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    auto run = [&](const double* x, const double* e, const double* yb, double* xb, double* eb) {
+        return rotate_vjp_dev(ctx, kind, int(order), int(batch), x, e, type, yb, xb, eb);
+    };
+    if (mem == ZEST_MEM_DEVICE) return run(coeffs, euler, out_cot, coeffs_cot, euler_cot);
+    if (mem != ZEST_MEM_HOST) return fail(ZEST_GPU_ERR_INVALID, "mem must be ZEST_MEM_HOST or ZEST_MEM_DEVICE");
+    // staging: in_stage = [x | ybar], aux_stage = [euler | ebar], out_stage = xbar
+    cudaStream_t s = ctx->stream;
+    ZG_TRY(ctx->in_stage.ensure(2 * cn * sizeof(double) + 16));
+    ZG_TRY(ctx->aux_stage.ensure(2 * an * sizeof(double) + 16));
+    ZG_TRY(ctx->out_stage.ensure(cn * sizeof(double) + 16));
+    double* dx = ctx->in_stage.as<double>();
+    double* dy = dx + cn;
+    double* de = ctx->aux_stage.as<double>();
+    double* deb = de + an;
+    double* dxb = ctx->out_stage.as<double>();
+    if (cn && euler_cot) ZG_CUDA_TRY(cudaMemcpyAsync(dx, coeffs, cn * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (cn) ZG_CUDA_TRY(cudaMemcpyAsync(dy, out_cot, cn * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (an) ZG_CUDA_TRY(cudaMemcpyAsync(de, euler, an * sizeof(double), cudaMemcpyHostToDevice, s));
+    ZG_TRY(run(dx, de, dy, coeffs_cot ? dxb : nullptr, euler_cot ? deb : nullptr));
+    if (coeffs_cot && cn) ZG_CUDA_TRY(cudaMemcpyAsync(coeffs_cot, dxb, cn * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (euler_cot && an) ZG_CUDA_TRY(cudaMemcpyAsync(euler_cot, deb, an * sizeof(double), cudaMemcpyDeviceToHost, s));
+    ZG_CUDA_TRY(cudaStreamSynchronize(s));
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_zt_rotate_vjp(zest_gpu_context* ctx, size_t order, size_t batch, const double* coeffs,
+                           const double* euler, int rotation_type, const double* out_cot, double* coeffs_cot,
+                           double* euler_cot, int mem) {
+    return rotate_vjp_common(ctx, 0, order, batch, coeffs, euler, rotation_type, out_cot, coeffs_cot, euler_cot, mem);
+}
+
+int zest_gpu_st_rotate_vjp(zest_gpu_context* ctx, size_t order, size_t batch, const double* coeffs,
+                           const double* euler, int rotation_type, const double* out_cot, double* coeffs_cot,
+                           double* euler_cot, int mem) {
+    return rotate_vjp_common(ctx, 1, order, batch, coeffs, euler, rotation_type, out_cot, coeffs_cot, euler_cot, mem);
 }
 
 int zest_gpu_split_gemm(zest_gpu_context* ctx, size_t M, size_t N, size_t K, const double* A, const double* B,
