@@ -32,6 +32,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from zest_gb300.replicas import max_over_ranks, replica_seed0, whole_job_rate  # noqa: E402
+
 METRIC = "Zernike fwd+bwd transforms/s, order 200x64: split-prec vs FP64 GPU at 1e-11 err"
 # DRAM read + write bytes of the split GEMMs of one forward+backward step per
 # function at order 200 (ncu capture of all eight launches at batch 4: 8.89 GB)
@@ -187,6 +189,63 @@ def run_reference_arm(args, rank: int, world: int) -> None:
 
 
 # --------------------------------------------------------------------------
+def run_sh(args, rank: int, world: int, barrier) -> None:
+    """Spherical harmonics at lmax 1023 (order 1024), batch 8, FP64: real
+    coefficients N(0, (l+1)^-2) (4pi normalisation, no Condon-Shortley phase),
+    synthesised to the LonLat grid (2047 x 1024) and transformed back; one step
+    = backward then forward of the batch.  Error = max over items of
+    max|c - c_in| / max|c_in| (the round trip is exact in exact arithmetic)."""
+    import torch
+    import zest_gb300 as zg
+    ctx = zg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    L, B = 1024, 8
+    ncoef = zg.st_coeff_size(L)
+    rng = np.random.default_rng(1024 + rank)
+    l_of = np.zeros(ncoef, dtype=np.int64)
+    for l in range(L):
+        l_of[l * (l + 1) // 2:(l + 1) * (l + 2) // 2] = l
+    c = rng.normal(size=(B, ncoef, 2)) / (l_of[None, :, None] + 1.0)
+    c[:, [l * (l + 1) // 2 for l in range(L)], 1] = 0.0
+    dev = torch.device("cuda", torch.cuda.current_device())
+    cd = torch.from_numpy(c.ravel()).to(dev)
+    gd = torch.empty(B * int(np.prod(zg.st_grid_shape(L))), dtype=torch.float64, device=dev)
+    cout = torch.empty_like(cd)
+
+    def step():
+        ctx.st_backward(cd, L, batch=B, out=gd)
+        ctx.st_forward(gd, L, batch=B, out=cout)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    ctx.profile(True)
+    ctx.profile_read(reset=True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    prof = ctx.profile_read(reset=True)
+    ms = max_over_ranks(e0.elapsed_time(e1), None) / args.steps
+    err = max(float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
+              for x, y in zip(cout.cpu().numpy().reshape(B, -1), c.reshape(B, -1)))
+    if rank == 0:
+        print(json.dumps({
+            "metric": "SH backward+forward transforms/s, lmax 1023 x 8, FP64", "value": world * B / (ms * 1e-3),
+            "unit": "transforms/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "sh_glq_bwd_fwd", "order": 1024, "batch": B,
+                                            "layout": "LonLat", "conventions": "GLQTransformerGeo"},
+            "roundtrip_max_rel_err": err,
+            "stages_ms": {k: v[0] / args.steps for k, v in prof.items()}, "clocks": clocks}), flush=True)
+
+
 def run_batching(args, rank: int, world: int, barrier) -> None:
     """4096 expansions, orders drawn uniformly from [8, 128] (sorted), c_nlm ~
     N(0, (n+1)^-2) with Im(m=0) = 0, Haar-uniform Euler angles; one step =
@@ -284,7 +343,7 @@ def main():
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["transforms", "batching"], default="transforms",
+    ap.add_argument("--workload", choices=["transforms", "batching", "sh"], default="transforms",
                     help="transforms: the headline (order 200 x 64 forward+backward); batching: 4096 "
                          "expansions of orders U{8..128}, rotate + backward in one graph")
     ap.add_argument("--items", type=int, default=4096)
@@ -315,6 +374,9 @@ def main():
     if args.workload == "batching":
         run_batching(args, rank, world, barrier)
         return
+    if args.workload == "sh":
+        run_sh(args, rank, world, barrier)
+        return
 
     L, B = args.order, args.batch
     ctx = zg.Context(local_rank)
@@ -329,7 +391,7 @@ def main():
 
     gsz = int(np.prod(zg.zt_grid_shape(L)))
     csz = 2 * zg.zt_coeff_size(L)
-    coeffs_h = zt_coeffs(L, B, seed0=1 + rank * B)
+    coeffs_h = zt_coeffs(L, B, seed0=replica_seed0(rank, B))
     coeffs_d = torch.from_numpy(coeffs_h.ravel()).cuda()
     grids_d = ctx.zt_backward(coeffs_d, L, batch=B)          # FP64 synthesis of the inputs
     cbuf = torch.empty(B * csz, dtype=torch.float64, device="cuda")
@@ -364,11 +426,7 @@ def main():
         launches = zg.launch_count() - n0
         barrier()
         flops = ctx.profile_flops(reset=True)
-        ms = e0.elapsed_time(e1)
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(e0.elapsed_time(e1), dist, "cuda")
         return ms, prof, launches, clocks, flops
 
     # ---- plain FP64 form (always measured: it is the ratio's denominator) ----
@@ -406,7 +464,7 @@ def main():
     else:
         ms, prof, launches, clocks, tflops = ms64, prof64, launches64, clocks64, (0.0, 0.0)
         dtype = "f64"
-    value = world * B * args.steps / (ms * 1e-3)
+    value = whole_job_rate(B * args.steps, world, ms * 1e-3)
 
     # ---- roofline of the dominant stage, from the live CUDA-event stage timings ----
     steps_run = args.steps
@@ -464,12 +522,8 @@ def main():
         for _ in range(n_e2e):
             e2e_step()
         torch.cuda.synchronize()
-        secs = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([secs], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            secs = float(t.item())
-        e2e = {"value": world * B * n_e2e / secs, "unit": UNIT,
+        secs = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+        e2e = {"value": whole_job_rate(B * n_e2e, world, secs), "unit": UNIT,
                "h2d_bytes_per_step": B * (gsz + csz) * 8, "d2h_bytes_per_step": B * (csz + gsz) * 8,
                "host_buffers": "pinned", "steps": n_e2e}
         del gh, ch, go

@@ -624,30 +624,31 @@ struct EpiRadBwd {  // rows ((t B + b) 2 + c) -> flm[(t B + b)][k][c]
     }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double*) const { R.p[2 * n] = v; }
 };
-struct EpiLegBwd {  // rows (m, b, kc) -> G north/south pair (conjugated); parity 1 adds/subtracts
-    static constexpr bool RMW = true;
+// rows (m, b, kc) -> G north/south pair (conjugated).  Parity 0 writes both
+// nodes; parity 1 (RMW) adds to the north node and subtracts from the south.
+template <bool RMW_>
+struct EpiLegBwdT {
+    static constexpr bool RMW = RMW_;
     double* G;
     int B, L, Nt, nr2, j0u, j0d;
-    struct Row { double* up; double* dn; double sg; bool rmw; };
+    struct Row { double* up; double* dn; double sg; };
     __device__ Row row(const SplitUnit& u, int r) const {
         const int m = u.g;
         const long long local = r - (long long)m * B * nr2;
         const int b = int(local / nr2), kc = int(local - (long long)b * nr2);
         double* base = G + ((long long)b * L + m) * Nt * nr2 + kc;
         return Row{base + (long long)(j0u + u.aux) * nr2, base + (long long)(j0d - u.aux) * nr2,
-                   (kc & 1) ? -1.0 : 1.0, ((u.flags >> 2) & 1) != 0};
+                   (kc & 1) ? -1.0 : 1.0};
     }
     __device__ void load(const Row& R, int n, double* old) const {
-        if (R.rmw) {
-            old[0] = R.up[(long long)n * nr2];
-            old[1] = R.dn[-(long long)n * nr2];
-        }
+        old[0] = R.up[(long long)n * nr2];
+        old[1] = R.dn[-(long long)n * nr2];
     }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
         const double x = R.sg * v;
         double* up = R.up + (long long)n * nr2;
         double* dn = R.dn - (long long)n * nr2;
-        if (!R.rmw) {
+        if constexpr (!RMW) {
             *up = x;
             *dn = x;
         } else if (up == dn) {  // the equator node: its parity-1 contribution is zero
@@ -658,27 +659,30 @@ struct EpiLegBwd {  // rows (m, b, kc) -> G north/south pair (conjugated); parit
         }
     }
 };
-struct EpiDftBwd {  // rows (b, col) -> grid[b][i][col] and grid[b][N-i][col]
-    static constexpr bool RMW = true;
+using EpiLegBwd0 = EpiLegBwdT<false>;
+using EpiLegBwd1 = EpiLegBwdT<true>;
+
+// rows (b, col) -> grid[b][i][col] and grid[b][N-i][col]: the cos pass writes
+// both, the sin pass (RMW) adds to x_i and subtracts from x_{N-i}
+template <bool RMW_>
+struct EpiDftBwdT {
+    static constexpr bool RMW = RMW_;
     double* grid;
     int C, N;
     long long gsz;
-    struct Row { double* x; int i0; bool rmw; };
+    struct Row { double* x; int i0; };
     __device__ Row row(const SplitUnit& u, int r) const {
         const long long b = r / C, col = r - b * C;
-        const bool sin = ((u.flags >> 1) & 1) != 0;
-        return Row{grid + b * gsz + col, u.aux + (sin ? 1 : 0), sin};
+        return Row{grid + b * gsz + col, u.aux + (RMW ? 1 : 0)};
     }
     __device__ void load(const Row& R, int n, double* old) const {
-        if (R.rmw) {
-            const int i = R.i0 + n;
-            old[0] = R.x[(long long)i * C];
-            old[1] = R.x[(long long)(N - i) * C];
-        }
+        const int i = R.i0 + n;
+        old[0] = R.x[(long long)i * C];
+        old[1] = R.x[(long long)(N - i) * C];
     }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
         const int i = R.i0 + n;
-        if (!R.rmw) {
+        if constexpr (!RMW) {
             R.x[(long long)i * C] = v;
             if (i > 0) R.x[(long long)(N - i) * C] = v;
         } else {
@@ -687,6 +691,8 @@ struct EpiDftBwd {  // rows (b, col) -> grid[b][i][col] and grid[b][N-i][col]
         }
     }
 };
+using EpiDftBwd0 = EpiDftBwdT<false>;
+using EpiDftBwd1 = EpiDftBwdT<true>;
 
 struct SplitParams {
     const SplitUnit* units;
@@ -766,7 +772,8 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     constexpr int B_TILE = ((NT * 32 + 1023) / 1024) * 1024;
     constexpr int STAGE = S * A_TILE + SC::NB * B_TILE;
     constexpr uint32_t TX = S * (SP_M * 32) + SC::NB * (NT * 32);
-    constexpr uint32_t IDESC = idesc_bf16_f32(SP_M, NT);
+    // the MMA's N follows the unit's valid table rows, rounded up to 16
+    // (the B tile is always loaded whole; the MMA reads its first N rows)
     static_assert(SC::NACC * NT <= 512, "accumulators must fit in TMEM");
     static_assert(NT % 32 == 0, "each epilogue warp owns whole 16-column chunks");
 
@@ -840,6 +847,8 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             bool ok = true;
             for (int ui = blockIdx.x; ui < P.nunits && ok; ui += gridDim.x, ++tile) {
                 const SplitUnit u = P.units[ui];
+                const int nmma = min(NT, (u.n + 15) & ~15);
+                const uint32_t idesc = idesc_bf16_f32(SP_M, nmma);
                 const long long w0 = clock64();
                 if (!mbar_wait(tempty, (tile & 1) ^ 1, P.err, 2)) { ok = false; break; }
                 if (P.dbg) atomicAdd(&P.dbg[1], (unsigned long long)(clock64() - w0));
@@ -865,7 +874,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                             const int t = d - s;
                             if (t < 0 || t >= S) continue;
                             umma_bf16(tmem + acc * NT, da + (uint64_t)((s * A_TILE) >> 4),
-                                      db + (uint64_t)((SC::btile(d, t) * B_TILE) >> 4), IDESC, first[acc] ? 0u : 1u);
+                                      db + (uint64_t)((SC::btile(d, t) * B_TILE) >> 4), idesc, first[acc] ? 0u : 1u);
                             first[acc] = false;
                         }
                     }
@@ -913,6 +922,9 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             constexpr int TEXP = -BITS * (SC::NACC + 1) - 6;
             static_assert(SC::NACC == 4 || SC::NACC == 5, "four or five accumulators");
             long long T[CW];
+            // warps whose columns are all past the unit's valid rows skip the work
+            const bool active = col0 < u.n;
+            if (active) {
 #pragma unroll
             for (int c = 0; c < CW / 4; ++c) {
                 uint32_t v[SC::NACC][4];
@@ -935,11 +947,13 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                     }
                 }
             }
+            }
             tc_fence_before();
             __syncwarp();
             const long long w2 = clock64();
             if (lane == 0) mbar_arrive(tempty);
             // phase 2 (overlaps the next tile's MMAs): FP64 results and stores
+            if (active) {
 #pragma unroll
             for (int c = 0; c < CW / 4; ++c) {
                 double old[4][2];
@@ -964,6 +978,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                         epi.store(R, u, n, v, old[j]);
                     }
                 }
+            }
             }
             if (P.dbg && warp == 2 && lane == 0) {
                 atomicAdd(&P.dbg[3], (unsigned long long)(w1 - w0));
@@ -1404,11 +1419,9 @@ int run_gemm(zest_gpu_context* ctx, int S, UnitList& ul, const SliceArray& A0, c
         case 6: return run_gemm_t<6, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
         }
     } else {
-        switch (S) {
-        case 4: return run_gemm_t<4, 7, 96>(ctx, ul, A0, A1, B0, B1, epi);
-        case 5: return run_gemm_t<5, 7, 96>(ctx, ul, A0, A1, B0, B1, epi);
-        case 6: return run_gemm_t<6, 7, 96>(ctx, ul, A0, A1, B0, B1, epi);
-        }
+        // 7-bit digits (contractions longer than 256) come with 6 slices only
+        if (S == 6) return run_gemm_t<6, 7, 96>(ctx, ul, A0, A1, B0, B1, epi);
+        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: contractions longer than 256 need 6 slices");
     }
     return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path supports 4..6 slices");
 }
@@ -1604,8 +1617,12 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                     add_units(ul, S, bits, (long long)m * per_m, per_m, (2 * m + p) * kh, kh, NT, cnt, p | (p << 2), m);
                 }
             }, &u));
-            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
-                            EpiLegBwd{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d}));
+            if (p == 0)
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
+                                EpiLegBwd0{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d}));
+            else
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
+                                EpiLegBwd1{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d}));
         }
     }
     // ---- longitude: inverse real DFT, cos pass then sin read-modify-write pass ----
@@ -1625,7 +1642,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                 add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, Lg, 0, 0);
         }, &u));
         ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
-                        EpiDftBwd{grids, C, N, sh.size()}));
+                        EpiDftBwd0{grids, C, N, sh.size()}));
         if (Lg > 1) {
             UnitList* v;
             ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 1), [&](UnitList& ul) {
@@ -1633,7 +1650,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                     add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT, Lg - 1, 1 | 2 | 4, 0);
             }, &v));
             ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
-                            EpiDftBwd{grids, C, N, sh.size()}));
+                            EpiDftBwd1{grids, C, N, sh.size()}));
         }
     }
     return ZEST_GPU_OK;
