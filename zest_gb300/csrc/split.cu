@@ -231,11 +231,12 @@ constexpr int SL_K8MAX = 256; // K bound of exact level sums with balanced 8-bit
 inline int digit_bits(int K) { return K <= SL_K8MAX ? 8 : 7; }
 
 // Rows per slicing block: a power of two (so that in row-fast loops every
-// thread stays on one row) with the staged FP64 rows within 32 KB.
+// thread stays on one row), up to 32 rows (longer contiguous runs in the
+// row-fast loads), with the staged FP64 rows within 96 KB.
 inline int slice_rows_per_block(int K, bool two) {
     const int per_row = K * (two ? 16 : 8);
-    int r = 16;
-    while (r > 1 && r * per_row > 32 * 1024) r >>= 1;
+    int r = 32;
+    while (r > 1 && r * per_row > 96 * 1024) r >>= 1;
     return r;
 }
 
@@ -439,10 +440,10 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
     const int R = J.R, K = J.K;
     double* vu = sl_smem;
     double* vd = sl_smem + (size_t)R * K;
-    __shared__ int emax[16];
-    __shared__ typename Loader::Row rowh[16];
+    __shared__ int emax[32];
+    __shared__ typename Loader::Row rowh[32];
     const long long row0 = (long long)blockIdx.x * R;
-    if (threadIdx.x < 16) emax[threadIdx.x] = 0;
+    if (threadIdx.x < 32) emax[threadIdx.x] = 0;
     if (threadIdx.x < R && row0 + threadIdx.x < J.rows) rowh[threadIdx.x] = ld.row(row0 + threadIdx.x);
     __syncthreads();
     int tmax = 0;
@@ -1128,7 +1129,7 @@ int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
     const size_t smem = (size_t)(Loader::TWO ? 2 : 1) * J.R * J.K * sizeof(double);
     const long long blocks = (J.rows + J.R - 1) / J.R;
     auto go = [&](auto kern) -> int {
-        ZG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+        ZG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
         kern<<<(unsigned)blocks, 256, smem, s>>>(ld, J);
         return launch_check("slice_kernel");
     };
