@@ -181,8 +181,10 @@ def run_reference_arm(args, rank: int, world: int) -> None:
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "zernike_glq_fwd_bwd", "order": L, "batch": per_step, "threads": nthreads,
-                   "transformer": "GLQTransformerGeo", "build": "g++ -O3 (-mcpu=native on aarch64)"},
+        "config": {"workload": "zernike_glq_fwd_bwd", "order": L, "batch": args.batch, "precision": "fp64",
+                   "conventions": "GLQTransformerGeo (unnormed Zernike, 4pi SH, no CS phase)",
+                   "grid": [2 * L - 1, L + 1, (L + 1 + 7) // 8 * 8], "parallelism": f"{nthreads} host threads",
+                   "sample_per_step": per_step, "build": "g++ -O3 (-mcpu=native on aarch64)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "reference", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
@@ -460,7 +462,7 @@ def main():
         del g64
         errors = {"forward_coeffs": err_c, "backward_grid": err_g, "roundtrip_grid": err_rt,
                   "measure": "max over the batch of max|x - x_fp64| / max|x_fp64| per function"}
-        dtype = "bf16-slices (7-bit fixed point), fp32 exact partial sums, fp64 recombination"
+        dtype = "bf16 digit slices (8-bit fixed point, 6 per operand), fp32 exact level sums, fp64 recombination"
     else:
         ms, prof, launches, clocks, tflops = ms64, prof64, launches64, clocks64, (0.0, 0.0)
         dtype = "f64"
