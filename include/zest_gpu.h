@@ -47,7 +47,7 @@ extern "C" {
 #define ZEST_GPU_ERR_OOM 2         /* device allocation failed */
 #define ZEST_GPU_ERR_CUDA 3        /* a CUDA runtime call or kernel launch failed */
 #define ZEST_GPU_ERR_TIMEOUT 4     /* a bounded in-kernel wait gave up */
-#define ZEST_GPU_ERR_UNSUPPORTED 5 /* valid request this build does not support */
+#define ZEST_GPU_ERR_UNSUPPORTED 5 /* valid request the library does not support */
 
 /* ---- conventions: zest::zt::ZernikeNorm (zernike_conventions.hpp:35),
  *      zest::st::SHNorm, zest::st::SHPhase (sh_conventions.hpp:35-47) ---- */
