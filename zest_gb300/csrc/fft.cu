@@ -25,33 +25,101 @@ namespace zgpu {
 
 namespace {
 
-// One Stockham pass for all NC columns: src -> dst, twiddle table tw (size N),
-// conj_tw = inverse transform.
-__device__ __forceinline__ void stockham_stage(const double2* __restrict__ src, double2* __restrict__ dst,
+__device__ __forceinline__ double2 cmul_tw(double2 a, double2 w, bool conj) {
+    if (conj) w.y = -w.y;
+    return make_double2(fma(a.x, w.x, -a.y * w.y), fma(a.x, w.y, a.y * w.x));
+}
+
+// One Stockham pass for all NC columns: src -> dst, twiddle table tw (size N,
+// W_t = e^{-2 pi i t/N}; conjugated for the inverse transform).  Butterfly
+// (j, column) of radix R takes x_r = src[j + r N/R], twiddles it,
+// t_r = x_r W^{r jm step}, and forms the R-point DFT
+//     y_q = sum_r t_r W_R^{r q} -> dst[(j/Ns) Ns R + jm + q Ns].
+// Radix 2 and 4 are done per butterfly.  An odd radix pairs the outputs q and
+// R - q: with s_r = t_r + t_{R-r}, d_r = t_r - t_{R-r} (r = 1..(R-1)/2),
+//     y_q = a -+ i b,  y_{R-q} = a +- i b,  a = t_0 + sum_r s_r cos(2 pi r q/R),
+//     b = sum_r d_r sin(2 pi r q/R)
+// (upper signs forward): R - 1 multiply-adds per output instead of 4 R.
+// Phase A (per butterfly) twiddles and writes s_r, d_r back in place --
+// every src element belongs to exactly one butterfly -- and stores y_0;
+// phase B computes the output pairs, one (butterfly, q) per thread.
+__device__ __forceinline__ void stockham_stage(double2* __restrict__ src, double2* __restrict__ dst,
                                                const double2* __restrict__ tw, int N, int R, int Ns, int NC,
                                                bool inverse) {
     const int NR = N / R;
     const int step = N / (Ns * R);
-    const int total = N * NC;
-    for (int o = threadIdx.x; o < total; o += blockDim.x) {
+    const int wR = N / R;  // W_R^m = tw[wR m]
+    const size_t xs = (size_t)NR * NC;
+    const int nb = NR * NC;
+    for (int o = threadIdx.x; o < nb; o += blockDim.x) {
         const int cp = o % NC;
-        const int idx = o / NC;
-        const int j = idx % NR;
-        const int q = idx / NR;
+        const int j = o / NC;
         const int jm = j % Ns;
-        const int base = (jm + q * Ns) * step;
-        double2 acc = make_double2(0.0, 0.0);
-        int t = 0;
-        for (int r = 0; r < R; ++r) {
-            const double2 v = src[(j + r * NR) * NC + cp];
-            double2 w = tw[t];
-            if (inverse) w.y = -w.y;
-            acc.x = fma(v.x, w.x, fma(-v.y, w.y, acc.x));
-            acc.y = fma(v.x, w.y, fma(v.y, w.x, acc.y));
-            t += base;
+        const int obase = (j / Ns) * Ns * R + jm;
+        double2* x = src + (size_t)j * NC + cp;
+        const int tstep = jm * step;
+        int t = tstep;
+        for (int r = 1; r < R; ++r) {
+            x[r * xs] = cmul_tw(x[r * xs], tw[t], inverse);
+            t += tstep;
             if (t >= N) t -= N;
         }
-        dst[((j / Ns) * Ns * R + jm + q * Ns) * NC + cp] = acc;
+        if (R == 2) {
+            const double2 a = x[0], b = x[xs];
+            dst[(size_t)obase * NC + cp] = make_double2(a.x + b.x, a.y + b.y);
+            dst[(size_t)(obase + Ns) * NC + cp] = make_double2(a.x - b.x, a.y - b.y);
+        } else if (R == 4) {
+            const double2 a = x[0], b = x[xs], c = x[2 * xs], d = x[3 * xs];
+            const double2 s0 = make_double2(a.x + c.x, a.y + c.y), d0 = make_double2(a.x - c.x, a.y - c.y);
+            const double2 s1 = make_double2(b.x + d.x, b.y + d.y), d1 = make_double2(b.x - d.x, b.y - d.y);
+            // forward: y1 = d0 - i d1, y3 = d0 + i d1 (signs of i swapped for the inverse)
+            const double2 md1 = inverse ? make_double2(-d1.y, d1.x) : make_double2(d1.y, -d1.x);  // -+ i d1
+            dst[(size_t)obase * NC + cp] = make_double2(s0.x + s1.x, s0.y + s1.y);
+            dst[(size_t)(obase + Ns) * NC + cp] = make_double2(d0.x + md1.x, d0.y + md1.y);
+            dst[(size_t)(obase + 2 * Ns) * NC + cp] = make_double2(s0.x - s1.x, s0.y - s1.y);
+            dst[(size_t)(obase + 3 * Ns) * NC + cp] = make_double2(d0.x - md1.x, d0.y - md1.y);
+        } else {
+            const int h = R >> 1;
+            double2 y0 = x[0];
+            for (int r = 1; r <= h; ++r) {
+                const double2 a = x[r * xs], b = x[(R - r) * xs];
+                const double2 sr = make_double2(a.x + b.x, a.y + b.y);
+                x[r * xs] = sr;
+                x[(R - r) * xs] = make_double2(a.x - b.x, a.y - b.y);
+                y0.x += sr.x;
+                y0.y += sr.y;
+            }
+            dst[(size_t)obase * NC + cp] = y0;
+        }
+    }
+    if (R == 2 || R == 4) return;
+    __syncthreads();
+    const int h = R >> 1;
+    const int np = nb * h;
+    for (int o = threadIdx.x; o < np; o += blockDim.x) {
+        const int bq = o / h;
+        const int q = o - bq * h + 1;
+        const int cp = bq % NC;
+        const int j = bq / NC;
+        const int jm = j % Ns;
+        const int obase = (j / Ns) * Ns * R + jm;
+        const double2* x = src + (size_t)j * NC + cp;
+        double2 a = x[0], b = make_double2(0.0, 0.0);
+        int m = q;
+        for (int r = 1; r <= h; ++r) {
+            const double2 w = tw[wR * m];  // cos(2 pi m/R), -sin(2 pi m/R)
+            const double2 sr = x[r * xs], dr = x[(R - r) * xs];
+            a.x = fma(sr.x, w.x, a.x);
+            a.y = fma(sr.y, w.x, a.y);
+            b.x = fma(dr.x, -w.y, b.x);
+            b.y = fma(dr.y, -w.y, b.y);
+            m += q;
+            if (m >= R) m -= R;
+        }
+        // forward: y_q = a - i b, y_{R-q} = a + i b; inverse: the other way round
+        const double2 mib = inverse ? make_double2(-b.y, b.x) : make_double2(b.y, -b.x);  // -+ i b
+        dst[(size_t)(obase + q * Ns) * NC + cp] = make_double2(a.x + mib.x, a.y + mib.y);
+        dst[(size_t)(obase + (R - q) * Ns) * NC + cp] = make_double2(a.x - mib.x, a.y - mib.y);
     }
 }
 
