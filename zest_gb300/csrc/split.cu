@@ -226,6 +226,7 @@ namespace {
 
 constexpr int SL_KMAX = 992;  // K bound of exact level sums (balanced 7-bit digits)
 constexpr int SL_K8MAX = 256; // K bound of exact level sums with balanced 8-bit digits
+constexpr int SL_UNROLL = 8;  // independent loads per thread in the staging loops
 
 // digit width of a contraction of length K: 8 bits while the exact levels stay exact
 inline int digit_bits(int K) { return K <= SL_K8MAX ? 8 : 7; }
@@ -366,7 +367,7 @@ enum { SL_ONE = 0, SL_FOLD = 1, SL_PAIR = 2 };
 struct SliceJob {
     long long rows;
     int K;       // staged k range (K0, and K1 + shift for the second array)
-    int S, bits, mode, fold, R, copies;
+    int S, bits, mode, fold, R, lr, copies;  // lr = log2(R)
     int K0, Kp0, K1, Kp1, shift;
     __nv_bfloat16* out0;
     __nv_bfloat16* out1;
@@ -382,29 +383,30 @@ __device__ __forceinline__ uint32_t digit_f32_bits(int d, float scale) {
     return __float_as_uint(f);
 }
 
-// Balanced digits of four neighbouring elements (slice 0 most significant)
-// written as BF16: four elements per slice and copy in one 8-byte store.
+// Balanced digits of two neighbouring elements (slice 0 most significant)
+// written as BF16 pairs: one 4-byte store per slice and copy.
 // 8-bit digits: adding 128 sum_{i<S-1} 256^i turns the lower balanced digits
 // into the plain bytes of the sum (digit = byte - 128) and leaves the leading
 // digit as the sum shifted down.
 template <int S>
-__device__ __forceinline__ void write_digits4(const long long (&w)[4], int bits, int copies, __nv_bfloat16* out,
+__device__ __forceinline__ void write_digits2(long long w0, long long w1, int bits, int copies, __nv_bfloat16* out,
                                               long long stride, long long off) {
-    int d[4][S];
+    int d[2][S];
     if (bits == 8) {
         constexpr long long OFF = (long long)((0x8080808080808080ull) >> (8 * (9 - S)));  // 128 per lower byte
+        const long long u[2] = {w0 + OFF, w1 + OFF};
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const long long u = w[q] + OFF;
+        for (int q = 0; q < 2; ++q) {
 #pragma unroll
-            for (int s = 1; s < S; ++s) d[q][s] = int((u >> (8 * (S - 1 - s))) & 255) - 128;
-            d[q][0] = int(u >> (8 * (S - 1)));
+            for (int s = 1; s < S; ++s) d[q][s] = int((u[q] >> (8 * (S - 1 - s))) & 255) - 128;
+            d[q][0] = int(u[q] >> (8 * (S - 1)));
         }
     } else {
         const long long mask = (1ll << bits) - 1;
         const int halfv = 1 << (bits - 1), base = 1 << bits;
+        const long long w[2] = {w0, w1};
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < 2; ++q) {
             long long x = w[q];
 #pragma unroll
             for (int s = S - 1; s >= 1; --s) {
@@ -416,115 +418,165 @@ __device__ __forceinline__ void write_digits4(const long long (&w)[4], int bits,
             d[q][0] = int(x);
         }
     }
-    for (int c = 0; c < copies; ++c) {
-        const float sc = __int_as_float((127 - bits * c) << 23);  // 2^{-bits c}, exact
+    uint32_t* o = reinterpret_cast<uint32_t*>(out + off);
+    const long long s2 = stride >> 1;  // slice stride in BF16 pairs (slice strides are even)
+    if (copies == 1) {
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-            uint2 v;
-            v.x = __byte_perm(digit_f32_bits(d[0][s], sc), digit_f32_bits(d[1][s], sc), 0x7632);
-            v.y = __byte_perm(digit_f32_bits(d[2][s], sc), digit_f32_bits(d[3][s], sc), 0x7632);
-            *reinterpret_cast<uint2*>(out + (c * S + s) * stride + off) = v;
+        for (int s = 0; s < S; ++s)
+            o[s * s2] = __byte_perm(digit_f32_bits(d[0][s], 1.0f), digit_f32_bits(d[1][s], 1.0f), 0x7632);
+    } else {
+        for (int c = 0; c < copies; ++c) {
+            const float sc = __int_as_float((127 - bits * c) << 23);  // 2^{-bits c}, exact
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+                o[(c * S + s) * s2] = __byte_perm(digit_f32_bits(d[0][s], sc), digit_f32_bits(d[1][s], sc), 0x7632);
         }
     }
 }
 
-// One CTA converts R rows of K values: the FP64 values are staged in shared
-// memory while the row maxima are found (thread-local in row-fast loops, a
-// warp reduction otherwise), then every value is rounded to the row's
-// fixed-point grid, folded exactly in integers where requested, and split
-// into balanced base-2^bits digits, written as S BF16 slices per copy
-// (copies scaled by 2^-bits, 2^-2bits).
+// One CTA converts R rows (R a power of two, <= 32) of K values.  Phase 1
+// stages the FP64 values in shared memory and finds each row's largest
+// exponent: for row-fast operands lane l of a warp reads row l mod R (so a
+// warp reads R consecutive rows at 32/R neighbouring k), otherwise one warp
+// walks one row along k; the maxima are reduced with warp shuffles.
+// Phase 2 gives each row to one warp and each lane a pair of neighbouring k:
+// the pair (and, for a shifted second array, the next element, taken from the
+// neighbouring lane) is rounded to the row's fixed-point grid once, folded
+// exactly in integers where requested, split into balanced base-2^bits digits
+// and written as S BF16 slices per copy (copies scaled by 2^-bits, 2^-2bits).
 template <class Loader, int S>
 __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
     extern __shared__ double sl_smem[];
-    const int R = J.R, K = J.K;
+    const int R = J.R, K = J.K, lr = J.lr;
     double* vu = sl_smem;
     double* vd = sl_smem + (size_t)R * K;
     __shared__ int emax[32];
     __shared__ typename Loader::Row rowh[32];
     const long long row0 = (long long)blockIdx.x * R;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     if (threadIdx.x < 32) emax[threadIdx.x] = 0;
     if (threadIdx.x < R && row0 + threadIdx.x < J.rows) rowh[threadIdx.x] = ld.row(row0 + threadIdx.x);
     __syncthreads();
-    int tmax = 0;
-    const int lane = threadIdx.x & 31;
-    // warp-uniform trip count, so that the warp-wide reductions see all lanes
-    for (int e0 = threadIdx.x - lane; e0 < R * K; e0 += blockDim.x) {
-        const int e = e0 + lane;
-        const bool valid = e < R * K;
-        int r = 0, k = 0;
-        if (Loader::ROW_FAST) { r = e & (R - 1); k = e / R; }
-        else { k = e % K; r = e / K; }
-        int ee = 0;
-        if (valid) {
-            double up = 0.0, dn = 0.0;
-            if (row0 + r < J.rows) ld.get(rowh[r], k, up, dn);
-            vu[r * K + k] = up;
-            if (Loader::TWO) vd[r * K + k] = dn;
-            ee = Loader::TWO ? max(biased_exp(up), biased_exp(dn)) : biased_exp(up);
+    if (Loader::ROW_FAST) {
+        const int r = lane & (R - 1), kl = lane >> lr, kstep = 32 >> lr;
+        const bool rv = row0 + r < J.rows;
+        int tmax = 0;
+        // SL_UNROLL independent loads in flight per thread before any store
+        const int kst = nw * kstep;
+        for (int k0 = warp * kstep + kl; k0 < K; k0 += SL_UNROLL * kst) {
+            double up[SL_UNROLL], dn[SL_UNROLL];
+#pragma unroll
+            for (int u = 0; u < SL_UNROLL; ++u) {
+                up[u] = 0.0;
+                dn[u] = 0.0;
+                const int k = k0 + u * kst;
+                if (rv && k < K) ld.get(rowh[r], k, up[u], dn[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < SL_UNROLL; ++u) {
+                const int k = k0 + u * kst;
+                if (k < K) {
+                    vu[r * K + k] = up[u];
+                    if (Loader::TWO) vd[r * K + k] = dn[u];
+                }
+                tmax = max(tmax, Loader::TWO ? max(biased_exp(up[u]), biased_exp(dn[u])) : biased_exp(up[u]));
+            }
         }
-        if (Loader::ROW_FAST) {
-            tmax = max(tmax, ee);  // R divides the block size: this thread's row is fixed
-        } else {
-            const unsigned same = __match_any_sync(0xffffffffu, valid ? r : -1);
-            const int m = __reduce_max_sync(same, ee);
-            if (valid && lane == __ffs(same) - 1 && m) atomicMax(&emax[r], m);
+        for (int o = R; o < 32; o <<= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+        if (lane < R && tmax) atomicMax(&emax[lane], tmax);
+    } else {
+        for (int r = warp; r < R; r += nw) {
+            int tmax = 0;
+            if (row0 + r < J.rows) {
+                for (int k0 = lane; k0 < K; k0 += 32 * SL_UNROLL) {
+                    double up[SL_UNROLL], dn[SL_UNROLL];
+#pragma unroll
+                    for (int u = 0; u < SL_UNROLL; ++u) {
+                        up[u] = 0.0;
+                        dn[u] = 0.0;
+                        if (k0 + 32 * u < K) ld.get(rowh[r], k0 + 32 * u, up[u], dn[u]);
+                    }
+#pragma unroll
+                    for (int u = 0; u < SL_UNROLL; ++u) {
+                        const int k = k0 + 32 * u;
+                        if (k < K) {
+                            vu[r * K + k] = up[u];
+                            if (Loader::TWO) vd[r * K + k] = dn[u];
+                        }
+                        tmax = max(tmax, Loader::TWO ? max(biased_exp(up[u]), biased_exp(dn[u])) : biased_exp(up[u]));
+                    }
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
+            if (lane == 0) emax[r] = tmax;
         }
     }
-    if (Loader::ROW_FAST && tmax) atomicMax(&emax[threadIdx.x & (R - 1)], tmax);
     __syncthreads();
+    const bool two = J.mode != SL_ONE;
     const int fold_bit = (J.mode == SL_FOLD || (J.mode == SL_ONE && J.fold)) ? 1 : 0;
     const int nbits = J.bits * S;
-    // first array: four neighbouring k per thread
-    {
-        const int qk = J.Kp0 >> 2;
-        for (int e = threadIdx.x; e < R * qk; e += blockDim.x) {
-            const int r = e / qk, k = (e - r * qk) * 4;
-            const long long row = row0 + r;
-            if (row >= J.rows) continue;
-            // |x| < 2^(E_max - 1022); one more bit of headroom for the balanced
-            // leading digit, and one for a folded sum
-            const int er = emax[r] - 1022 + 1 + fold_bit;
-            long long w[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int kk = k + q;
-                long long x = 0;
-                if (kk < J.K0) {
-                    x = to_fixed(vu[r * K + kk], er, nbits);
-                    if (J.mode == SL_FOLD || (J.mode == SL_ONE && J.fold == 1)) x += to_fixed(vd[r * K + kk], er, nbits);
-                    else if (J.mode == SL_ONE && J.fold == 2) x -= to_fixed(vd[r * K + kk], er, nbits);
-                }
-                w[q] = x;
-            }
-            write_digits4<S>(w, J.bits, J.copies, J.out0, J.stride0, row * J.Kp0 + k);
-            if (k == 0) J.ex0[row] = er;
+    const int np = (two ? max(J.Kp0, J.Kp1) : J.Kp0) >> 1;  // pairs per row
+    for (int r = warp; r < R; r += nw) {
+        const long long row = row0 + r;
+        if (row >= J.rows) continue;  // warp-uniform
+        // |x| < 2^(E_max - 1022); one more bit of headroom for the balanced
+        // leading digit, and one for a folded sum
+        const int er = emax[r] - 1022 + 1 + fold_bit;
+        if (lane == 0) {
+            J.ex0[row] = er;
+            if (two) J.ex1[row] = er;
         }
-    }
-    if (J.mode == SL_ONE) return;
-    // second array: index k - shift
-    {
-        const int qk = J.Kp1 >> 2;
-        for (int e = threadIdx.x; e < R * qk; e += blockDim.x) {
-            const int r = e / qk, k = (e - r * qk) * 4;
-            const long long row = row0 + r;
-            if (row >= J.rows) continue;
-            const int er = emax[r] - 1022 + 1 + fold_bit;
-            long long w[4];
+        const double* ru = vu + r * K;
+        const double* rd = vd + r * K;
+        for (int g0 = 0; g0 < np; g0 += 32) {
+            const int g = g0 + lane;
+            const int k = 2 * g;
+            // fixed-point values of elements k, k+1 (and k+2 for a shifted second array)
+            long long fu[3] = {0, 0, 0}, fd[3] = {0, 0, 0};
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int kk = k + q, src = kk + J.shift;
-                long long x = 0;
-                if (kk < J.K1) {
-                    if (J.mode == SL_FOLD)
-                        x = to_fixed(vu[r * K + src], er, nbits) - to_fixed(vd[r * K + src], er, nbits);
-                    else
-                        x = to_fixed(vd[r * K + src], er, nbits);
+            for (int q = 0; q < 2; ++q) {
+                if (k + q < K) {
+                    fu[q] = to_fixed(ru[k + q], er, nbits);
+                    if (Loader::TWO) fd[q] = to_fixed(rd[k + q], er, nbits);
                 }
-                w[q] = x;
             }
-            write_digits4<S>(w, J.bits, J.copies, J.out1, J.stride1, row * J.Kp1 + k);
-            if (k == 0) J.ex1[row] = er;
+            if (two && J.shift) {  // element k + 2: the next lane's first, or read for the last lane
+                fu[2] = __shfl_down_sync(0xffffffffu, fu[0], 1);
+                fd[2] = __shfl_down_sync(0xffffffffu, fd[0], 1);
+                if (lane == 31 && k + 2 < K) {
+                    fu[2] = to_fixed(ru[k + 2], er, nbits);
+                    if (Loader::TWO) fd[2] = to_fixed(rd[k + 2], er, nbits);
+                }
+            }
+            if (k < J.Kp0) {
+                long long w[2];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    long long x = 0;
+                    if (k + q < J.K0) {
+                        x = fu[q];
+                        if (J.mode == SL_FOLD || (J.mode == SL_ONE && J.fold == 1)) x += fd[q];
+                        else if (J.mode == SL_ONE && J.fold == 2) x -= fd[q];
+                    }
+                    w[q] = x;
+                }
+                write_digits2<S>(w[0], w[1], J.bits, J.copies, J.out0, J.stride0, row * J.Kp0 + k);
+            }
+            if (two && k < J.Kp1) {
+                long long w[2];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    long long x = 0;
+                    if (k + q < J.K1) {
+                        const int src = q + J.shift;  // shift is 0 or 1
+                        const long long a = src == 0 ? fu[0] : (src == 1 ? fu[1] : fu[2]);
+                        const long long b = src == 0 ? fd[0] : (src == 1 ? fd[1] : fd[2]);
+                        x = J.mode == SL_FOLD ? a - b : b;
+                    }
+                    w[q] = x;
+                }
+                write_digits2<S>(w[0], w[1], J.bits, J.copies, J.out1, J.stride1, row * J.Kp1 + k);
+            }
         }
     }
 }
@@ -1126,6 +1178,9 @@ int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
     if (J.bits != 7 && !(J.bits == 8 && J.K <= SL_K8MAX))
         return fail(ZEST_GPU_ERR_INVALID, "split path: digit width");
     J.R = slice_rows_per_block(J.K, Loader::TWO);
+    J.lr = 0;
+    while ((1 << J.lr) < J.R) ++J.lr;
+    if (J.shift < 0 || J.shift > 1) return fail(ZEST_GPU_ERR_INVALID, "split path: slice shift");
     const size_t smem = (size_t)(Loader::TWO ? 2 : 1) * J.R * J.K * sizeof(double);
     const long long blocks = (J.rows + J.R - 1) / J.R;
     auto go = [&](auto kern) -> int {
