@@ -344,19 +344,29 @@ struct LegBwdLoader {
 };
 
 // rows (b, col); k = m: (Re F_m, Im F_m); the sin operand is Im F_k at k - 1
+// rows (b, col = (lat, rad)); k = m: the spectrum at latitude lat, formed
+// from the two parity sums E_p[b][m][j'][2 rad + {re, im}] of the Legendre
+// stage: E_0 + E_1 at the north node lat = j0u + j', E_0 - E_1 at the south
+// node lat = j0d - j' (the equator, j0u = j0d, is north).
 struct DftBwdLoader {
     static constexpr bool ROW_FAST = true, TWO = true;
-    const double* G;
-    int L, C;
-    struct Row { const double* g; };
+    const double* E;
+    int L, C, nrad, kh, j0u, j0d, B;
+    struct Row { const double* e0; double sg; };
     __device__ Row row(long long r) const {
-        const long long b = r / C, col = r - b * C;
-        return Row{G + ((b * L) * C + col) * 2};
+        const long long b = r / C;
+        const int col = int(r - b * C);
+        const int lat = col / nrad, rad = col - lat * nrad;
+        const bool north = lat >= j0u;
+        const int jf = north ? lat - j0u : j0d - lat;
+        return Row{E + ((b * L) * kh + jf) * (2LL * nrad) + 2 * rad, north ? 1.0 : -1.0};
     }
     __device__ void get(const Row& R, int k, double& up, double& dn) const {
-        const double2 v = *reinterpret_cast<const double2*>(R.g + (long long)k * C * 2);
-        up = v.x;
-        dn = v.y;
+        const long long mo = (long long)k * kh * 2 * nrad;
+        const double2 a = *reinterpret_cast<const double2*>(R.e0 + mo);
+        const double2 c = *reinterpret_cast<const double2*>(R.e0 + mo + (long long)B * L * kh * 2 * nrad);
+        up = a.x + R.sg * c.x;
+        dn = a.y + R.sg * c.y;
     }
 };
 
@@ -677,75 +687,65 @@ struct EpiRadBwd {  // rows ((t B + b) 2 + c) -> flm[(t B + b)][k][c]
     }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double*) const { R.p[2 * n] = v; }
 };
-// rows (m, b, kc) -> G north/south pair (conjugated).  Parity 0 writes both
-// nodes; parity 1 (RMW) adds to the north node and subtracts from the south.
-template <bool RMW_>
-struct EpiLegBwdT {
-    static constexpr bool RMW = RMW_;
-    double* G;
-    int B, L, Nt, nr2, j0u, j0d;
-    struct Row { double* up; double* dn; double sg; };
+// rows (m, b, kc) -> E_p[b][m][j'][kc] (conjugated): the parity-p Legendre
+// sum at folded node j'; the north node j0u + j' of the spectrum is E_0 + E_1
+// and the south node j0d - j' is E_0 - E_1, formed by the DFT slicing that
+// reads them (no read-modify-write here).
+struct EpiLegBwdE {
+    static constexpr bool RMW = false;
+    double* E;
+    int B, L, kh, nr2;
+    struct Row { double* p; double sg; };
     __device__ Row row(const SplitUnit& u, int r) const {
-        const int m = u.g;
+        const int m = u.g, par = (u.flags >> 2) & 1;
         const long long local = r - (long long)m * B * nr2;
         const int b = int(local / nr2), kc = int(local - (long long)b * nr2);
-        double* base = G + ((long long)b * L + m) * Nt * nr2 + kc;
-        return Row{base + (long long)(j0u + u.aux) * nr2, base + (long long)(j0d - u.aux) * nr2,
-                   (kc & 1) ? -1.0 : 1.0};
+        return Row{E + ((((long long)par * B + b) * L + m) * kh + u.aux) * nr2 + kc, (kc & 1) ? -1.0 : 1.0};
     }
-    __device__ void load(const Row& R, int n, double* old) const {
-        old[0] = R.up[(long long)n * nr2];
-        old[1] = R.dn[-(long long)n * nr2];
-    }
-    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
-        const double x = R.sg * v;
-        double* up = R.up + (long long)n * nr2;
-        double* dn = R.dn - (long long)n * nr2;
-        if constexpr (!RMW) {
-            *up = x;
-            *dn = x;
-        } else if (up == dn) {  // the equator node: its parity-1 contribution is zero
-            *up = old[0] + x;
-        } else {
-            *up = old[0] + x;
-            *dn = old[1] - x;
-        }
+    __device__ void load(const Row&, int, double*) const {}
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double*) const {
+        R.p[(long long)n * nr2] = R.sg * v;
     }
 };
-using EpiLegBwd0 = EpiLegBwdT<false>;
-using EpiLegBwd1 = EpiLegBwdT<true>;
 
-// rows (b, col) -> grid[b][i][col] and grid[b][N-i][col]: the cos pass writes
-// both, the sin pass (RMW) adds to x_i and subtracts from x_{N-i}
-template <bool RMW_>
-struct EpiDftBwdT {
-    static constexpr bool RMW = RMW_;
+// Inverse DFT, rows (b, col).  The cos pass writes x_0 = C_0 to the grid and
+// C_i (i >= 1) to the scratch Cs[b][i][col]; the sin pass reads C_i once and
+// writes x_i = C_i + S_i and x_{N-i} = C_i - S_i.
+struct EpiDftBwdCos {
+    static constexpr bool RMW = false;
     double* grid;
-    int C, N;
+    double* Cs;
+    int C, N, L;
     long long gsz;
-    struct Row { double* x; int i0; };
+    struct Row { double* x; double* c; };
     __device__ Row row(const SplitUnit& u, int r) const {
         const long long b = r / C, col = r - b * C;
-        return Row{grid + b * gsz + col, u.aux + (RMW ? 1 : 0)};
+        return Row{grid + b * gsz + col, Cs + (b * L + u.aux) * C + col};
     }
-    __device__ void load(const Row& R, int n, double* old) const {
-        const int i = R.i0 + n;
-        old[0] = R.x[(long long)i * C];
-        old[1] = R.x[(long long)(N - i) * C];
-    }
-    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
-        const int i = R.i0 + n;
-        if constexpr (!RMW) {
-            R.x[(long long)i * C] = v;
-            if (i > 0) R.x[(long long)(N - i) * C] = v;
-        } else {
-            R.x[(long long)i * C] = old[0] + v;
-            R.x[(long long)(N - i) * C] = old[1] - v;
-        }
+    __device__ void load(const Row&, int, double*) const {}
+    __device__ void store(const Row& R, const SplitUnit& u, int n, double v, const double*) const {
+        if (u.aux + n == 0) R.x[0] = v;
+        else R.c[(long long)n * C] = v;
     }
 };
-using EpiDftBwd0 = EpiDftBwdT<false>;
-using EpiDftBwd1 = EpiDftBwdT<true>;
+struct EpiDftBwdSin {
+    static constexpr bool RMW = true;
+    double* grid;
+    const double* Cs;
+    int C, N, L;
+    long long gsz;
+    struct Row { double* x; const double* c; int i0; };
+    __device__ Row row(const SplitUnit& u, int r) const {
+        const long long b = r / C, col = r - b * C;
+        return Row{grid + b * gsz + col, Cs + (b * L + u.aux + 1) * C + col, u.aux + 1};
+    }
+    __device__ void load(const Row& R, int n, double* old) const { old[0] = R.c[(long long)n * C]; }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        const int i = R.i0 + n;
+        R.x[(long long)i * C] = old[0] + v;
+        R.x[(long long)(N - i) * C] = old[0] - v;
+    }
+};
 
 struct SplitParams {
     const SplitUnit* units;
@@ -1620,13 +1620,15 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
     ZtSplitTables* tb;
     ZG_TRY(build_zt_tables(ctx, st, plan, S, &tb));
     const ZtShape& sh = plan.sh;
-    const int C = int(sh.nlat * sh.nrad), N = int(sh.nlon), nt = int(sh.nlat), nr = int(sh.nrad), nr2 = 2 * nr;
+    const int C = int(sh.nlat * sh.nrad), N = int(sh.nlon), nr = int(sh.nrad), nr2 = 2 * nr;
     const int kh = plan.leg.nnodes;
     const int kl = r16((Lg + 1) / 2);
     const long long csz = 2 * zsize(Le);
-    ZG_TRY(ctx->s0.ensure((size_t)batch * Lg * C * 2 * sizeof(double)));
+    // the two parity sums E_p[b][m][folded node][kc] of the Legendre stage
+    const long long eblock = (long long)Lg * kh * nr2;  // one (p, b)
+    ZG_TRY(ctx->s0.ensure((size_t)2 * batch * eblock * sizeof(double)));
     ZG_TRY(ctx->s1.ensure((size_t)tri_size(Lm) * batch * nr2 * sizeof(double)));
-    double* G = ctx->s0.as<double>();
+    double* E = ctx->s0.as<double>();
     double* flm = ctx->s1.as<double>();
 
     // ---- radial: coefficients -> flm ----
@@ -1659,10 +1661,16 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             ZG_TRY(launch_slice2(s, LegBwdLoader{flm, batch, nr2, Lm}, rows, (Lm + 1) / 2, Lm / 2, 0, S, bits,
                                  SL_PAIR, st->op[0], st->op[1]));
         }
-        if (Lm < Lg) {
+        {
+            // orders the Legendre products do not write: E_0 for m >= Lm, E_1 for
+            // m >= Lm - 1 (its last group is empty)
             StageScope sc(ctx, ST_MEMSET);
-            ZG_CUDA_TRY(cudaMemset2DAsync(G + (size_t)Lm * C * 2, (size_t)Lg * C * 2 * sizeof(double), 0,
-                                          (size_t)(Lg - Lm) * C * 2 * sizeof(double), batch, s));
+            const size_t row = (size_t)kh * nr2 * sizeof(double);
+            if (Lm < Lg)
+                ZG_CUDA_TRY(cudaMemset2DAsync(E + (size_t)Lm * kh * nr2, eblock * sizeof(double), 0,
+                                              (size_t)(Lg - Lm) * row, batch, s));
+            ZG_CUDA_TRY(cudaMemset2DAsync(E + (size_t)batch * eblock + (size_t)(Lm - 1) * kh * nr2,
+                                          eblock * sizeof(double), 0, (size_t)(Lg - Lm + 1) * row, batch, s));
         }
         for (int p = 0; p < 2; ++p) {
             UnitList* u;
@@ -1673,12 +1681,8 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                     add_units(ul, S, bits, (long long)m * per_m, per_m, (2 * m + p) * kh, kh, NT, cnt, p | (p << 2), m);
                 }
             }, &u));
-            if (p == 0)
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
-                                EpiLegBwd0{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d}));
-            else
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
-                                EpiLegBwd1{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d}));
+            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
+                            EpiLegBwdE{E, batch, Lg, kh, nr2}));
         }
     }
     // ---- longitude: inverse real DFT, cos pass then sin read-modify-write pass ----
@@ -1689,16 +1693,18 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
         ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice2(s, DftBwdLoader{G, Lg, C}, rows, Lg, Lg - 1, 1, S, bits, SL_PAIR, st->op[0],
-                                 st->op[1]));
+            ZG_TRY(launch_slice2(s, DftBwdLoader{E, Lg, C, nr, kh, plan.leg.j0u, plan.leg.j0d, batch}, rows, Lg,
+                                 Lg - 1, 1, S, bits, SL_PAIR, st->op[0], st->op[1]));
         }
         UnitList* u;
         ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
             for (long long r = 0; r < rows; r += SP_M)
                 add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, Lg, 0, 0);
         }, &u));
+        // the cos sums C_i go to the scratch of the (already consumed) parity sums
+        double* Cs = E;
         ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
-                        EpiDftBwd0{grids, C, N, sh.size()}));
+                        EpiDftBwdCos{grids, Cs, C, N, Lg, sh.size()}));
         if (Lg > 1) {
             UnitList* v;
             ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 1), [&](UnitList& ul) {
@@ -1706,7 +1712,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                     add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT, Lg - 1, 1 | 2 | 4, 0);
             }, &v));
             ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
-                            EpiDftBwd1{grids, C, N, sh.size()}));
+                            EpiDftBwdSin{grids, Cs, C, N, Lg, sh.size()}));
         }
     }
     return ZEST_GPU_OK;
