@@ -349,8 +349,8 @@ def main():
                     help="transforms: the headline (order 200 x 64 forward+backward); batching: 4096 "
                          "expansions of orders U{8..128}, rotate + backward in one graph")
     ap.add_argument("--items", type=int, default=4096)
-    ap.add_argument("--autotune", action="store_true",
-                    help="let the context time the FP64 tile shapes on first use")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="use the size rule for the FP64 tile shapes instead of timing them on first use")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -384,8 +384,8 @@ def main():
 
     L, B = args.order, args.batch
     ctx = zg.Context(local_rank)
-    if args.autotune:
-        ctx.set_autotune(True)
+    if args.no_autotune:
+        ctx.set_autotune(False)
     precision = args.precision
     if precision == "auto":
         try:

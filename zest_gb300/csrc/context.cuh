@@ -152,7 +152,7 @@ struct zest_gpu_context {
     std::map<int, std::unique_ptr<DevBuf>> wigner;
     std::map<std::tuple<int, int>, std::pair<std::unique_ptr<DevBuf>, int>> vec_lists;
     std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<TileEntry>> tiles;
-    bool autotune = false;                                    // time the tile shapes on first use
+    bool autotune = true;                                     // time the tile shapes on first use
     std::unique_ptr<RaggedPlan> ragged;                       // last batch of uneven orders, with its graph
     cudaStream_t graph_stream = nullptr;                      // own stream for graph capture and replay
     cudaEvent_t graph_ev[2] = {nullptr, nullptr};             // ordering with the context stream
