@@ -95,6 +95,8 @@ public:
         detail::check(zest_gpu_set_precision(m_ctx, int(precision), slices));
     }
     void synchronize() { detail::check(zest_gpu_synchronize(m_ctx)); }
+    void set_autotune(bool enable) { detail::check(zest_gpu_set_autotune(m_ctx, int(enable))); }
+    void set_host_chunk_bytes(std::size_t bytes) { detail::check(zest_gpu_set_host_chunk_bytes(m_ctx, bytes)); }
 
 private:
     zest_gpu_context* m_ctx = nullptr;

@@ -213,6 +213,14 @@ int zest_gpu_zt_rotate_backward_ragged(zest_gpu_context* ctx, int zernike_norm, 
  * on the context stream and keeps the fastest; disabled, a size rule picks
  * them.  The shapes change only how the output is tiled, not any result. */
 int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable);
+/* Pipelining of host-memory Zernike transforms (mem = ZEST_MEM_HOST): a
+ * batch whose per-item input or output exceeds `bytes` in total is cut into
+ * chunks of about `bytes`, and the upload of one chunk, the transform of the
+ * previous one and the download of the one before run at the same time (two
+ * copy streams of the context and two device slots per direction).  The
+ * default is 512 MiB; 0 turns the pipelining off.  Results do not depend on it.
+ * Host buffers should be pinned for the copies to overlap. */
+int zest_gpu_set_host_chunk_bytes(zest_gpu_context* ctx, size_t bytes);
 
 /* ---- adjoints: vector-Jacobian products (no reference counterpart; the
  *      reference has no derivatives) ----

@@ -103,6 +103,7 @@ _SIGNATURES = {
     "zest_gpu_st_rotate_vjp": [_vp, _sz, _sz, _vp, _vp, _i, _vp, _vp, _vp, _i],
     "zest_gpu_zt_rotate_backward_ragged": [_vp, _i, _i, _i, _sz, _vp, _vp, _vp, _i, _vp],
     "zest_gpu_set_autotune": [_vp, _i],
+    "zest_gpu_set_host_chunk_bytes": [_vp, _sz],
 }
 _SIZE_FUNCS = {
     "zest_gpu_zt_grid_size": [_sz],
@@ -321,6 +322,11 @@ class Context:
 
     def set_autotune(self, enable: bool = True):
         _check(self.lib.zest_gpu_set_autotune(self._h, int(enable)))
+
+    def set_host_chunk_bytes(self, nbytes: int):
+        """Chunk size of the copy/compute pipeline of host-memory Zernike
+        transforms (default 512 MiB; 0 turns it off)."""
+        _check(self.lib.zest_gpu_set_host_chunk_bytes(self._h, int(nbytes)))
 
     def zt_rotate_backward_ragged(self, orders, coeffs, euler, grids, conv=ZT_GEO,
                                   rotation_type: int = ROTATION_OBJECT):

@@ -153,8 +153,11 @@ struct zest_gpu_context {
     std::map<std::tuple<int, int>, std::pair<std::unique_ptr<DevBuf>, int>> vec_lists;
     std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<TileEntry>> tiles;
     bool autotune = true;                                     // time the tile shapes on first use
+    size_t host_chunk_bytes = size_t(1) << 29;                // pipelined host calls: input bytes per chunk
     std::unique_ptr<RaggedPlan> ragged;                       // last batch of uneven orders, with its graph
     cudaStream_t graph_stream = nullptr;                      // own stream for graph capture and replay
+    cudaStream_t copy_stream[2] = {nullptr, nullptr};         // host->device, device->host of pipelined calls
+    cudaEvent_t pipe_ev[3][2] = {};                           // uploaded, computed, downloaded per slot
     cudaEvent_t graph_ev[2] = {nullptr, nullptr};             // ordering with the context stream
     std::map<std::tuple<int, int, int, int>, int> tuned;      // chosen shape per (stage, L, Lm, batch)
     DevBuf s0, s1;          // transform scratch (spectra, flm)
@@ -171,17 +174,18 @@ namespace zgpu {
 struct StageScope {
     zest_gpu_context* ctx;
     int stage;
+    cudaStream_t stream;
     cudaEvent_t e0 = nullptr;
-    StageScope(zest_gpu_context* c, int st) : ctx(c), stage(st) {
+    StageScope(zest_gpu_context* c, int st, cudaStream_t s = nullptr) : ctx(c), stage(st), stream(s ? s : c->stream) {
         if (ctx->prof.on) {
             e0 = ctx->prof.get();
-            cudaEventRecord(e0, ctx->stream);
+            cudaEventRecord(e0, stream);
         }
     }
     ~StageScope() {
         if (e0) {
             cudaEvent_t e1 = ctx->prof.get();
-            cudaEventRecord(e1, ctx->stream);
+            cudaEventRecord(e1, stream);
             ctx->prof.pending.emplace_back(stage, e0, e1);
         }
     }

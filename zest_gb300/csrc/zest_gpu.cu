@@ -880,6 +880,78 @@ int with_staging(zest_gpu_context* ctx, int mem, const double* in, size_t in_n, 
     return ZEST_GPU_OK;
 }
 
+// Host buffers of a batch larger than ctx->host_chunk_bytes of input: the
+// batch is cut into chunks of about that size whose uploads, computation and
+// downloads overlap -- uploads and downloads on two copy streams of the
+// context, the computation on the context stream, two device slots per
+// direction ordered by events.  `body(in_dev, out_dev, nb)` transforms nb
+// items; item sizes are in doubles; with out_pitch > 0 only the first
+// out_width of every out_pitch output doubles of an item are written and
+// copied back.  Device buffers and smaller batches go through with_staging.
+template <class F>
+int with_staging_batched(zest_gpu_context* ctx, int mem, const double* in, size_t in_item, double* out,
+                         size_t out_item, int batch, F&& body, size_t out_pitch = 0, size_t out_width = 0) {
+    auto whole = [&](const double* i, double* o) { return body(i, o, batch); };
+    const size_t item_bytes = std::max(in_item, out_item) * sizeof(double);
+    const size_t chunk = ctx->host_chunk_bytes;
+    if (mem != ZEST_MEM_HOST || batch < 2 || chunk == 0 || (size_t)batch * item_bytes <= chunk)
+        return with_staging(ctx, mem, in, (size_t)batch * in_item, out, (size_t)batch * out_item, whole,
+                            out_pitch, out_width);
+    const int per = (int)std::max<size_t>(1, chunk / item_bytes);
+    if (!ctx->copy_stream[0]) {
+        for (int k = 0; k < 2; ++k) ZG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->copy_stream[k], cudaStreamNonBlocking));
+        for (auto& ev : ctx->pipe_ev)
+            for (auto& e : ev) ZG_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const size_t in_slot = (size_t)per * in_item, out_slot = (size_t)per * out_item;
+    ZG_TRY(ctx->in_stage.ensure(2 * in_slot * sizeof(double)));
+    ZG_TRY(ctx->out_stage.ensure(2 * out_slot * sizeof(double)));
+    cudaStream_t cs = ctx->stream, up = ctx->copy_stream[0], down = ctx->copy_stream[1];
+    cudaEvent_t(&ev)[3][2] = ctx->pipe_ev;  // [0] uploaded, [1] computed, [2] downloaded
+    const int nch = (batch + per - 1) / per;
+    auto dev_in = [&](int c) { return ctx->in_stage.as<double>() + (size_t)(c & 1) * in_slot; };
+    auto dev_out = [&](int c) { return ctx->out_stage.as<double>() + (size_t)(c & 1) * out_slot; };
+    auto count = [&](int c) { return std::min(per, batch - c * per); };
+    auto upload_chunk = [&](int c) -> int {
+        if (c >= 2) ZG_CUDA_TRY(cudaStreamWaitEvent(up, ev[1][c & 1], 0));  // slot free: chunk c-2 computed
+        StageScope sc(ctx, ST_COPY_H2D, up);
+        ZG_CUDA_TRY(cudaMemcpyAsync(dev_in(c), in + (size_t)c * per * in_item,
+                                    (size_t)count(c) * in_item * sizeof(double), cudaMemcpyHostToDevice, up));
+        ZG_CUDA_TRY(cudaEventRecord(ev[0][c & 1], up));
+        return ZEST_GPU_OK;
+    };
+    // the context stream must not run ahead of work queued on it before this call
+    ZG_CUDA_TRY(cudaEventRecord(ev[2][0], cs));
+    ZG_CUDA_TRY(cudaStreamWaitEvent(up, ev[2][0], 0));
+    ZG_CUDA_TRY(cudaStreamWaitEvent(down, ev[2][0], 0));
+    ZG_TRY(upload_chunk(0));
+    for (int c = 0; c < nch; ++c) {
+        if (c + 1 < nch) ZG_TRY(upload_chunk(c + 1));
+        ZG_CUDA_TRY(cudaStreamWaitEvent(cs, ev[0][c & 1], 0));
+        if (c >= 2) ZG_CUDA_TRY(cudaStreamWaitEvent(cs, ev[2][c & 1], 0));  // output slot downloaded
+        ZG_TRY(body(dev_in(c), dev_out(c), count(c)));
+        ZG_CUDA_TRY(cudaEventRecord(ev[1][c & 1], cs));
+        ZG_CUDA_TRY(cudaStreamWaitEvent(down, ev[1][c & 1], 0));
+        {
+            StageScope sc(ctx, ST_COPY_D2H, down);
+            double* h = out + (size_t)c * per * out_item;
+            if (out_pitch && out_width < out_pitch) {
+                if (out_width)
+                    ZG_CUDA_TRY(cudaMemcpy2DAsync(h, out_pitch * sizeof(double), dev_out(c), out_pitch * sizeof(double),
+                                                  out_width * sizeof(double), (size_t)count(c) * out_item / out_pitch,
+                                                  cudaMemcpyDeviceToHost, down));
+            } else {
+                ZG_CUDA_TRY(cudaMemcpyAsync(h, dev_out(c), (size_t)count(c) * out_item * sizeof(double),
+                                            cudaMemcpyDeviceToHost, down));
+            }
+        }
+        ZG_CUDA_TRY(cudaEventRecord(ev[2][c & 1], down));
+    }
+    ZG_CUDA_TRY(cudaStreamSynchronize(down));
+    ZG_CUDA_TRY(cudaStreamSynchronize(cs));
+    return ZEST_GPU_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -919,6 +991,14 @@ int zest_gpu_ctx_destroy(zest_gpu_context* ctx) {
         for (cudaEvent_t e : ctx->graph_ev)
             if (e) cudaEventDestroy(e);
     }
+    for (cudaStream_t st : ctx->copy_stream)
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+    for (auto& ev : ctx->pipe_ev)
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
     delete ctx;
     return ZEST_GPU_OK;
 }
@@ -1019,10 +1099,10 @@ int zest_gpu_zt_forward(zest_gpu_context* ctx, int zn, int sn, int sp, size_t gr
     const size_t gn = batch * zest_gpu_zt_grid_size(grid_order), cn = batch * 2 * zest_gpu_zt_coeff_size(exp_order);
     if ((gn && !grids) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
     const size_t lm = grid_order < exp_order ? grid_order : exp_order;
-    return with_staging(
-        ctx, mem, grids, gn, coeffs, cn,
-        [&](const double* in, double* out) {
-            return zt_forward_dev(ctx, zn, sn, sp, int(grid_order), int(exp_order), int(batch), in, out);
+    return with_staging_batched(
+        ctx, mem, grids, zest_gpu_zt_grid_size(grid_order), coeffs, 2 * zest_gpu_zt_coeff_size(exp_order), int(batch),
+        [&](const double* in, double* out, int nb) {
+            return zt_forward_dev(ctx, zn, sn, sp, int(grid_order), int(exp_order), nb, in, out);
         },
         2 * zest_gpu_zt_coeff_size(exp_order), 2 * zest_gpu_zt_coeff_size(lm));
 }
@@ -1035,9 +1115,12 @@ int zest_gpu_zt_backward(zest_gpu_context* ctx, int zn, int sn, int sp, size_t e
     if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
     const size_t gn = batch * zest_gpu_zt_grid_size(grid_order), cn = batch * 2 * zest_gpu_zt_coeff_size(exp_order);
     if ((gn && !grids) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
-    return with_staging(ctx, mem, coeffs, cn, grids, gn, [&](const double* in, double* out) {
-        return zt_backward_dev(ctx, zn, sn, sp, int(exp_order), int(grid_order), int(batch), in, out);
-    });
+    return with_staging_batched(ctx, mem, coeffs, 2 * zest_gpu_zt_coeff_size(exp_order), grids,
+                                zest_gpu_zt_grid_size(grid_order), int(batch),
+                                [&](const double* in, double* out, int nb) {
+                                    return zt_backward_dev(ctx, zn, sn, sp, int(exp_order), int(grid_order), nb, in,
+                                                           out);
+                                });
 }
 
 int zest_gpu_st_forward(zest_gpu_context* ctx, int sn, int sp, int layout, size_t grid_order, size_t exp_order,
@@ -1116,6 +1199,12 @@ int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch, 
 int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable) {
     ZG_TRY(check_ctx(ctx));
     ctx->autotune = enable != 0;
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_set_host_chunk_bytes(zest_gpu_context* ctx, size_t bytes) {
+    ZG_TRY(check_ctx(ctx));
+    ctx->host_chunk_bytes = bytes;
     return ZEST_GPU_OK;
 }
 
