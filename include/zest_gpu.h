@@ -221,6 +221,13 @@ int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable);
  * default is 512 MiB; 0 turns the pipelining off.  Results do not depend on it.
  * Host buffers should be pinned for the copies to overlap. */
 int zest_gpu_set_host_chunk_bytes(zest_gpu_context* ctx, size_t bytes);
+/* Self-test of the failure path of the split GEMMs' bounded waits: one
+ * kernel waits, for `seconds` (1 ms .. 2 s), on an mbarrier that nothing
+ * arrives on, and a second wait in the same kernel gives up as soon as the
+ * first has set the error flag.  Returns ZEST_GPU_ERR_TIMEOUT, reported
+ * exactly as a timed-out GEMM is; the flag is cleared and the context stays
+ * usable. */
+int zest_gpu_selftest_wait_timeout(zest_gpu_context* ctx, double seconds);
 
 /* ---- adjoints: vector-Jacobian products (no reference counterpart; the
  *      reference has no derivatives) ----

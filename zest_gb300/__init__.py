@@ -104,6 +104,7 @@ _SIGNATURES = {
     "zest_gpu_zt_rotate_backward_ragged": [_vp, _i, _i, _i, _sz, _vp, _vp, _vp, _i, _vp],
     "zest_gpu_set_autotune": [_vp, _i],
     "zest_gpu_set_host_chunk_bytes": [_vp, _sz],
+    "zest_gpu_selftest_wait_timeout": [_vp, ctypes.c_double],
 }
 _SIZE_FUNCS = {
     "zest_gpu_zt_grid_size": [_sz],

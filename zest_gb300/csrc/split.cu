@@ -98,14 +98,15 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
 }
 // Bounded wait on an mbarrier phase; false (and the error flag set) on timeout
 // or when another role already gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code,
+                                          long long limit_ns = SP_TIMEOUT_NS) {
     if (mbar_try(bar, parity)) return true;
     const unsigned long long t0 = gtime();
     for (unsigned it = 1;; ++it) {
         if (mbar_try(bar, parity)) return true;
         if ((it & 255) == 0) {
             if (*(volatile int*)err) return false;
-            if (gtime() - t0 > (unsigned long long)SP_TIMEOUT_NS) {
+            if (gtime() - t0 > (unsigned long long)limit_ns) {
                 atomicCAS(err, 0, code);
                 return false;
             }
@@ -1054,6 +1055,29 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     }
 }
 
+// Self-test of the failure path: warp 0 waits, with a limit of limit_ns, on an
+// mbarrier that nothing arrives on; warp 1 waits on another one with the
+// GEMMs' own limit and must give up as soon as warp 0 has set the flag.  The
+// flag reaches the host as in split_gemm_kernel.
+__global__ void wait_expiry_kernel(int* err, int* host_err, long long limit_ns) {
+    __shared__ __align__(8) uint64_t bar[2];
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+    }
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) {
+        const int w = threadIdx.x >> 5;
+        if (w == 0) mbar_wait(&bar[0], 0, err, 6, limit_ns);
+        else mbar_wait(&bar[1], 0, err, 7);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int e = *(volatile int*)err;
+        if (e) *(volatile int*)host_err = e;
+    }
+}
+
 template <int S, int BITS, int NT>
 constexpr size_t split_smem_bytes() {
     constexpr int NST = stage_count<S, BITS>();
@@ -1754,6 +1778,14 @@ int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A
     add_units(u, S, bits, 0, M, 0, N, NT, K, 0, 0);
     ZG_TRY(run_gemm(ctx, S, u, a, a, b, b, EpiDense{C, N}));
     return split_finish(ctx);  // also keeps the local operands alive until the product is done
+}
+
+int split_wait_selftest(zest_gpu_context* ctx, long long limit_ns) {
+    SplitState* st;
+    ZG_TRY(get_state(ctx, &st));
+    wait_expiry_kernel<<<1, 64, 0, ctx->stream>>>(st->err.as<int>(), st->host_err_dev, limit_ns);
+    ZG_TRY(launch_check("wait_expiry_kernel"));
+    return split_finish(ctx);
 }
 
 void split_flops(zest_gpu_context* ctx, bool reset, double* useful, double* issued) {

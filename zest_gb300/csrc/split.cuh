@@ -26,7 +26,10 @@ int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A
 // issued = whole 128-row tiles as executed.
 void split_flops(zest_gpu_context* ctx, bool reset, double* useful, double* issued);
 // Synchronizes the context stream and reports (and clears) a bounded-wait
-// timeout recorded by split GEMMs launched without a host check (graph replay).
+// timeout recorded by the split GEMMs launched since the last check.
 int split_check_flag(zest_gpu_context* ctx);
+// Makes one bounded mbarrier wait run out after limit_ns (nothing arrives on
+// it) and reports it as the GEMMs' timeouts are reported: ZEST_GPU_ERR_TIMEOUT.
+int split_wait_selftest(zest_gpu_context* ctx, long long limit_ns);
 
 }  // namespace zgpu

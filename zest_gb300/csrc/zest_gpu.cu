@@ -1202,6 +1202,12 @@ int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable) {
     return ZEST_GPU_OK;
 }
 
+int zest_gpu_selftest_wait_timeout(zest_gpu_context* ctx, double seconds) {
+    ZG_TRY(check_ctx(ctx));
+    if (!(seconds >= 1e-3 && seconds <= 2.0)) return fail(ZEST_GPU_ERR_INVALID, "wait limit outside [1 ms, 2 s]");
+    return split_wait_selftest(ctx, (long long)(seconds * 1e9));
+}
+
 int zest_gpu_set_host_chunk_bytes(zest_gpu_context* ctx, size_t bytes) {
     ZG_TRY(check_ctx(ctx));
     ctx->host_chunk_bytes = bytes;
