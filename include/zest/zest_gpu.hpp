@@ -22,6 +22,9 @@
 //   st::RealSHSpan, RealSHExpansion + aliases              real_sh_expansion.hpp:49-292
 //   WignerdPiHalfCollection                                wignerd_collection.hpp:66-110
 //   Rotor, RotationType, euler_angles_from_rotation_matrix rotor.hpp:38-395
+//   st::GridEvaluator, zt::GridEvaluator                   grid_evaluator.hpp:52-325
+//   st::power_spectrum, cross_power_spectrum, zt::power_spectrum, zt::RadialZernikeSpan
+//                                                          power_spectra.hpp:38-163
 //
 // Additions of this implementation:
 //   * GPUContext: the device, stream and cached tables behind a transformer or
@@ -897,5 +900,212 @@ private:
     GPUContext m_ctx;
     std::size_t m_max_order;
 };
+
+// ---------------------------------------------------------------------------
+// Evaluation at arbitrary points and power spectra
+// ---------------------------------------------------------------------------
+
+namespace detail {
+// The reference's spectra are free functions; they run on a context per thread.
+inline GPUContext& thread_context() {
+    thread_local GPUContext ctx(0);
+    return ctx;
+}
+}  // namespace detail
+
+namespace st {
+
+// Evaluation of SH expansions on the product grid of arbitrary longitudes and
+// colatitudes, grid_evaluator.hpp:52-133.  Values [lon][lat], row-major.
+class GridEvaluator {
+public:
+    GridEvaluator() : GridEvaluator(0) {}
+    explicit GridEvaluator(std::size_t max_order, int device = 0, void* stream = nullptr)
+        : m_ctx(device, stream), m_max_order(max_order) {}
+    GridEvaluator(std::size_t max_order, std::size_t lon_size, std::size_t lat_size) : GridEvaluator(max_order) {
+        resize(max_order, lon_size, lat_size);
+    }
+    void resize(std::size_t max_order, std::size_t lon_size, std::size_t lat_size) {
+        m_max_order = max_order;
+        m_lon_size = lon_size;
+        m_lat_size = lat_size;
+    }
+    [[nodiscard]] GPUContext& context() noexcept { return m_ctx; }
+
+    template <real_sh_expansion ExpansionType>
+    [[nodiscard]] std::vector<double> evaluate(ExpansionType&& expansion, std::span<const double> longitudes,
+                                               std::span<const double> colatitudes) {
+        using E = std::remove_cvref_t<ExpansionType>;
+        if (longitudes.empty() || colatitudes.empty()) return {};
+        resize(expansion.order(), longitudes.size(), colatitudes.size());
+        std::vector<double> res(longitudes.size() * colatitudes.size());
+        evaluate_batch<E::norm, E::phase>(reinterpret_cast<const double*>(expansion.data()), expansion.order(), 1,
+                                          longitudes.data(), longitudes.size(), colatitudes.data(),
+                                          colatitudes.size(), res.data(), MemoryKind::host);
+        return res;
+    }
+    // `batch` contiguous expansions; coefficients, points and values all host or all device memory
+    template <SHNorm sh_norm, SHPhase sh_phase>
+    void evaluate_batch(const double* coeffs, std::size_t order, std::size_t batch, const double* lon,
+                        std::size_t nlon, const double* colat, std::size_t nlat, double* values, MemoryKind mem) {
+        zest::detail::check(zest_gpu_st_evaluate(m_ctx.get(), detail::abi(sh_norm), detail::abi(sh_phase), order,
+                                                 batch, coeffs, nlon, lon, nlat, colat, values, int(mem)));
+    }
+
+private:
+    GPUContext m_ctx;
+    std::size_t m_max_order = 0, m_lon_size = 0, m_lat_size = 0;
+};
+
+// power_spectra.hpp:38-104.  (The reference's own SH spectra name the
+// convention ExpansionType::sh_norm, which its SH spans do not define; here
+// they read the span's `norm`, which is what they mean.)
+template <real_sh_expansion ExpansionType>
+void cross_power_spectrum(ExpansionType&& a, ExpansionType&& b, std::span<double> out) {
+    using E = std::remove_cvref_t<ExpansionType>;
+    if (a.order() != b.order())
+        throw GPUError(ZEST_GPU_ERR_INVALID, "cross_power_spectrum: expansions of different orders");
+    zest::detail::check(zest_gpu_st_cross_power_spectrum(
+        zest::detail::thread_context().get(), detail::abi(E::norm), a.order(), 1,
+        reinterpret_cast<const double*>(a.data()), reinterpret_cast<const double*>(b.data()), out.size(), out.data(),
+        ZEST_MEM_HOST));
+}
+template <real_sh_expansion ExpansionType>
+[[nodiscard]] std::vector<double> cross_power_spectrum(ExpansionType&& a, ExpansionType&& b) {
+    std::vector<double> out(std::min(a.order(), b.order()));
+    cross_power_spectrum(std::forward<ExpansionType>(a), std::forward<ExpansionType>(b), out);
+    return out;
+}
+template <real_sh_expansion ExpansionType>
+void power_spectrum(ExpansionType&& expansion, std::span<double> out) {
+    using E = std::remove_cvref_t<ExpansionType>;
+    if (out.size() < expansion.order()) throw GPUError(ZEST_GPU_ERR_INVALID, "power_spectrum: output too small");
+    zest::detail::check(zest_gpu_st_power_spectrum(zest::detail::thread_context().get(), detail::abi(E::norm),
+                                                   expansion.order(), 1,
+                                                   reinterpret_cast<const double*>(expansion.data()), out.data(),
+                                                   ZEST_MEM_HOST));
+}
+template <real_sh_expansion ExpansionType>
+[[nodiscard]] std::vector<double> power_spectrum(ExpansionType&& expansion) {
+    std::vector<double> out(expansion.order());
+    power_spectrum(std::forward<ExpansionType>(expansion), out);
+    return out;
+}
+
+}  // namespace st
+
+namespace zt {
+
+// Values R_nl of one radial index (n, l), n - l even, at floor((n+1)^2/4) + l/2
+// (RadialZernikeSpan over RadialZernikeLayout, zernike_expansion.hpp:43-75,
+// layout.hpp:254-289).
+template <typename ElementType, ZernikeNorm zernike_norm_param>
+class RadialZernikeSpan {
+public:
+    using element_type = ElementType;
+    static constexpr ZernikeNorm zernike_norm = zernike_norm_param;
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept { return ((order + 1) * (order + 1)) >> 2; }
+    [[nodiscard]] static constexpr std::size_t idx(std::size_t n, std::size_t l) noexcept {
+        return (((n + 1) * (n + 1)) >> 2) + (l >> 1);
+    }
+    RadialZernikeSpan() noexcept = default;
+    constexpr RadialZernikeSpan(element_type* data, std::size_t order) noexcept : m_data(data), m_order(order) {}
+    constexpr RadialZernikeSpan(std::span<element_type> buffer, std::size_t order) noexcept
+        : m_data(buffer.data()), m_order(order) {}
+    [[nodiscard]] constexpr std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] constexpr std::size_t size() const noexcept { return size(m_order); }
+    [[nodiscard]] constexpr element_type* data() const noexcept { return m_data; }
+    [[nodiscard]] constexpr element_type& operator()(std::size_t n, std::size_t l) const noexcept {
+        return m_data[idx(n, l)];
+    }
+
+private:
+    element_type* m_data = nullptr;
+    std::size_t m_order = 0;
+};
+
+// Evaluation of Zernike expansions on the product grid of arbitrary
+// longitudes, colatitudes and radii, grid_evaluator.hpp:147-325.
+// Values [lon][lat][rad], row-major.
+class GridEvaluator {
+public:
+    GridEvaluator() : GridEvaluator(0) {}
+    explicit GridEvaluator(std::size_t max_order, int device = 0, void* stream = nullptr)
+        : m_ctx(device, stream), m_max_order(max_order) {}
+    GridEvaluator(std::size_t max_order, std::size_t lon_size, std::size_t lat_size, std::size_t rad_size)
+        : GridEvaluator(max_order) {
+        resize(max_order, lon_size, lat_size, rad_size);
+    }
+    void resize(std::size_t max_order, std::size_t lon_size, std::size_t lat_size, std::size_t rad_size) {
+        m_max_order = max_order;
+        m_lon_size = lon_size;
+        m_lat_size = lat_size;
+        m_rad_size = rad_size;
+    }
+    [[nodiscard]] GPUContext& context() noexcept { return m_ctx; }
+
+    template <real_zernike_expansion ExpansionType>
+    [[nodiscard]] std::vector<double> evaluate(ExpansionType&& expansion, std::span<const double> longitudes,
+                                               std::span<const double> colatitudes, std::span<const double> radii) {
+        using E = std::remove_cvref_t<ExpansionType>;
+        if (longitudes.empty() || colatitudes.empty() || radii.empty()) return {};
+        resize(expansion.order(), longitudes.size(), colatitudes.size(), radii.size());
+        std::vector<double> res(longitudes.size() * colatitudes.size() * radii.size());
+        evaluate_batch<E::zernike_norm, E::sh_norm, E::sh_phase>(
+            reinterpret_cast<const double*>(expansion.data()), expansion.order(), 1, longitudes.data(),
+            longitudes.size(), colatitudes.data(), colatitudes.size(), radii.data(), radii.size(), res.data(),
+            MemoryKind::host);
+        return res;
+    }
+    template <ZernikeNorm zernike_norm, st::SHNorm sh_norm, st::SHPhase sh_phase>
+    void evaluate_batch(const double* coeffs, std::size_t order, std::size_t batch, const double* lon,
+                        std::size_t nlon, const double* colat, std::size_t nlat, const double* rad, std::size_t nrad,
+                        double* values, MemoryKind mem) {
+        zest::detail::check(zest_gpu_zt_evaluate(m_ctx.get(), detail::abi(zernike_norm), st::detail::abi(sh_norm),
+                                                 st::detail::abi(sh_phase), order, batch, coeffs, nlon, lon, nlat,
+                                                 colat, nrad, rad, values, int(mem)));
+    }
+
+private:
+    GPUContext m_ctx;
+    std::size_t m_max_order = 0, m_lon_size = 0, m_lat_size = 0, m_rad_size = 0;
+};
+
+// power_spectra.hpp:124-163: out(n, l) = norm sum_m |c_nlm|^2 for l = n&1, .. < n
+// (the reference's bound: the l = n entries are not written).
+template <real_zernike_expansion ExpansionType>
+void power_spectrum(ExpansionType&& expansion,
+                    RadialZernikeSpan<double, std::remove_cvref_t<ExpansionType>::zernike_norm> out) {
+    using E = std::remove_cvref_t<ExpansionType>;
+    const std::size_t order = std::min(out.order(), expansion.order());
+    if (order == 0) return;
+    if (order == expansion.order()) {
+        zest::detail::check(zest_gpu_zt_power_spectrum(zest::detail::thread_context().get(),
+                                                       st::detail::abi(E::sh_norm), order, 1,
+                                                       reinterpret_cast<const double*>(expansion.data()),
+                                                       out.data(), ZEST_MEM_HOST));
+        return;
+    }
+    // a smaller output: the leading orders of the expansion, copied contiguously
+    using Span = RealZernikeSpan<const std::array<double, 2>, E::zernike_norm, E::sh_norm, E::sh_phase>;
+    const Span full(reinterpret_cast<const std::array<double, 2>*>(expansion.data()), expansion.order());
+    std::vector<std::array<double, 2>> head(Span::size(order));
+    for (std::size_t n = 0; n < order; ++n)
+        for (std::size_t l = n & 1; l <= n; l += 2)
+            for (std::size_t m = 0; m <= l; ++m) head[Span::idx(n, l, m)] = full(n, l, m);
+    zest::detail::check(zest_gpu_zt_power_spectrum(zest::detail::thread_context().get(), st::detail::abi(E::sh_norm),
+                                                   order, 1, reinterpret_cast<const double*>(head.data()),
+                                                   out.data(), ZEST_MEM_HOST));
+}
+template <real_zernike_expansion ExpansionType>
+[[nodiscard]] std::vector<double> power_spectrum(ExpansionType&& expansion) {
+    using E = std::remove_cvref_t<ExpansionType>;
+    std::vector<double> res(RadialZernikeSpan<double, E::zernike_norm>::size(expansion.order()));
+    power_spectrum(std::forward<ExpansionType>(expansion),
+                   RadialZernikeSpan<double, E::zernike_norm>(res, expansion.order()));
+    return res;
+}
+
+}  // namespace zt
 
 }  // namespace zest

@@ -154,6 +154,42 @@ int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
 /* euler_angles_from_rotation_matrix, rotor.hpp:53-63 (row-major 3x3, host). */
 int zest_gpu_euler_from_matrix(const double* matrix, double* euler);
 
+/* ---- evaluation at arbitrary points ----
+ * zt::GridEvaluator::evaluate, grid_evaluator.hpp:228-266 (sums in
+ * src/grid_evaluator.cpp:180-257): the values of `batch` Zernike expansions of
+ * `order` on the product grid of nlon longitudes, nlat colatitudes and nrad
+ * radii, values[b][i][j][k] row-major, item b at b * nlon * nlat * nrad.
+ * `coeffs`, `values` and the three point arrays are all host or all device
+ * memory (`mem`).  Like the reference, cos(colatitude), cos(longitude) and
+ * sin(longitude) are taken with the host's std::cos and std::sin, and the
+ * multiples cos/sin(m lon) by its recurrence (src/grid_evaluator.cpp:43-66).
+ * Unlike the reference, whose st::GridEvaluator keeps adding into a buffer it
+ * never clears (src/grid_evaluator.cpp:95-151), every call starts afresh. */
+int zest_gpu_zt_evaluate(zest_gpu_context* ctx, int zernike_norm, int sh_norm, int sh_phase, size_t order,
+                         size_t batch, const double* coeffs, size_t nlon, const double* lon, size_t nlat,
+                         const double* colat, size_t nrad, const double* rad, double* values, int mem);
+/* st::GridEvaluator::evaluate, grid_evaluator.hpp:84-133: values[b][i][j],
+ * nlon x nlat per item. */
+int zest_gpu_st_evaluate(zest_gpu_context* ctx, int sh_norm, int sh_phase, size_t order, size_t batch,
+                         const double* coeffs, size_t nlon, const double* lon, size_t nlat, const double* colat,
+                         double* values, int mem);
+
+/* ---- power spectra (power_spectra.hpp) ----
+ * norm = 1/(4 pi) for ZEST_SH_GEO, 1 for ZEST_SH_QM (sh_conventions.hpp). */
+/* st::power_spectrum, :88-104: out[b * order + l] = norm sum_m |c_lm|^2, l < order. */
+int zest_gpu_st_power_spectrum(zest_gpu_context* ctx, int sh_norm, size_t order, size_t batch,
+                               const double* coeffs, double* out, int mem);
+/* st::cross_power_spectrum, :38-52: out[b * out_len + l] = norm sum_m a_lm . b_lm
+ * for l < min(order, out_len - 1), as the reference; other entries untouched
+ * (its vector overload, :62-69, passes out_len = order). */
+int zest_gpu_st_cross_power_spectrum(zest_gpu_context* ctx, int sh_norm, size_t order, size_t batch,
+                                     const double* a, const double* b, size_t out_len, double* out, int mem);
+/* zt::power_spectrum, :124-146: out[b * floor((order+1)^2/4) + floor((n+1)^2/4) + l/2]
+ * = norm sum_m |c_nlm|^2.  As in the reference, l runs over n&1, n&1+2, .. < n,
+ * so the l = n entries are not written. */
+int zest_gpu_zt_power_spectrum(zest_gpu_context* ctx, int sh_norm, size_t order, size_t batch,
+                               const double* coeffs, double* out, int mem);
+
 /* ---- Zernike rotation that allocates no device memory ----
  * No counterpart in the reference: its rotations run on the host.  Same
  * operation and result as zest_gpu_zt_rotate with ZEST_MEM_DEVICE (the same

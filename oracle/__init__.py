@@ -193,6 +193,30 @@ class _Lib:
         self._st_polar(sn, sp, L, c, angle, rtype)
         return c
 
+    # -- evaluation at arbitrary points, power spectra --
+    def zt_evaluate(self, coeffs, L, lon, colat, rad, zn=1, sn=0, sp=0):
+        lon = np.ascontiguousarray(lon, dtype=np.float64)
+        colat = np.ascontiguousarray(colat, dtype=np.float64)
+        rad = np.ascontiguousarray(rad, dtype=np.float64)
+        c = np.ascontiguousarray(coeffs, dtype=np.float64)
+        out = np.zeros((lon.size, colat.size, rad.size))
+        self._zt_eval(zn, sn, sp, L, c, lon, colat, rad, out)
+        return out
+
+    def st_evaluate(self, coeffs, L, lon, colat, sn=0, sp=0):
+        lon = np.ascontiguousarray(lon, dtype=np.float64)
+        colat = np.ascontiguousarray(colat, dtype=np.float64)
+        c = np.ascontiguousarray(coeffs, dtype=np.float64)
+        out = np.zeros((lon.size, colat.size))
+        self._st_eval(sn, sp, L, c, lon, colat, out)
+        return out
+
+    def zt_power_spectrum(self, coeffs, L, sn=0, out=None):
+        c = np.ascontiguousarray(coeffs, dtype=np.float64)
+        out = np.zeros(rad_size(L)) if out is None else np.array(out, dtype=np.float64, copy=True)
+        self._zt_ps(sn, L, c, out)
+        return out
+
 
 class Oracle(_Lib):
     """The C restatement (oracle/zest_oracle.c)."""
@@ -246,6 +270,33 @@ class Oracle(_Lib):
 
     def _st_polar(self, sn, sp, L, c, angle, rtype):
         self._f("st_polar_rotate", [_c_sz, _p_dbl, _c_dbl, _c_int], None)(L, _ptr(c), angle, rtype)
+
+    def _zt_eval(self, zn, sn, sp, L, c, lon, colat, rad, out):
+        self._f("zt_evaluate", [_c_sz, _c_int, _c_int, _c_int, _p_dbl, _c_sz, _p_dbl, _c_sz, _p_dbl, _c_sz, _p_dbl,
+                                _p_dbl], None)(L, zn, sn, sp, _ptr(c), lon.size, _ptr(lon), colat.size, _ptr(colat),
+                                               rad.size, _ptr(rad), _ptr(out))
+
+    def _st_eval(self, sn, sp, L, c, lon, colat, out):
+        self._f("st_evaluate", [_c_sz, _c_int, _c_int, _p_dbl, _c_sz, _p_dbl, _c_sz, _p_dbl, _p_dbl], None)(
+            L, sn, sp, _ptr(c), lon.size, _ptr(lon), colat.size, _ptr(colat), _ptr(out))
+
+    def _zt_ps(self, sn, L, c, out):
+        self._f("zt_power_spectrum", [_c_sz, _c_int, _p_dbl, _p_dbl], None)(L, sn, _ptr(c), _ptr(out))
+
+    def st_power_spectrum(self, coeffs, L, sn=0):
+        c = np.ascontiguousarray(coeffs, dtype=np.float64)
+        out = np.zeros(L)
+        self._f("st_power_spectrum", [_c_sz, _c_int, _p_dbl, _p_dbl], None)(L, sn, _ptr(c), _ptr(out))
+        return out
+
+    def st_cross_power_spectrum(self, a, b, L, sn=0, out_len=None, out=None):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        out_len = L if out_len is None else out_len
+        out = np.zeros(out_len) if out is None else np.array(out, dtype=np.float64, copy=True)
+        self._f("st_cross_power_spectrum", [_c_sz, _c_int, _p_dbl, _p_dbl, _c_sz, _p_dbl], None)(
+            L, sn, _ptr(a), _ptr(b), out_len, _ptr(out))
+        return out
 
     def euler_from_matrix(self, mat):
         m = np.ascontiguousarray(mat, dtype=np.float64).reshape(9)
@@ -306,15 +357,16 @@ class Reference(_Lib):
         self._f("zt_rotate_matrix", [_c_int, _c_int, _c_int, _c_sz, _p_dbl, _p_dbl, _c_int])(zn, sn, sp, L, _ptr(c), _ptr(m), rtype)
         return c
 
-    def zt_evaluate(self, coeffs, L, lon, colat, rad, zn=1, sn=0, sp=0):
-        lon = np.ascontiguousarray(lon, dtype=np.float64)
-        colat = np.ascontiguousarray(colat, dtype=np.float64)
-        rad = np.ascontiguousarray(rad, dtype=np.float64)
-        c = np.ascontiguousarray(coeffs, dtype=np.float64)
-        out = np.zeros((lon.size, colat.size, rad.size))
+    def _zt_eval(self, zn, sn, sp, L, c, lon, colat, rad, out):
         self._f("zt_evaluate", [_c_int, _c_int, _c_int, _c_sz, _p_dbl, _c_sz, _p_dbl, _c_sz, _p_dbl, _c_sz, _p_dbl, _p_dbl])(
             zn, sn, sp, L, _ptr(c), lon.size, _ptr(lon), colat.size, _ptr(colat), rad.size, _ptr(rad), _ptr(out))
-        return out
+
+    def _st_eval(self, sn, sp, L, c, lon, colat, out):
+        self._f("st_evaluate", [_c_int, _c_int, _c_sz, _p_dbl, _c_sz, _p_dbl, _c_sz, _p_dbl, _p_dbl])(
+            sn, sp, L, _ptr(c), lon.size, _ptr(lon), colat.size, _ptr(colat), _ptr(out))
+
+    def _zt_ps(self, sn, L, c, out):
+        self._f("zt_power_spectrum", [_c_int, _c_sz, _p_dbl, _p_dbl])(sn, L, _ptr(c), _ptr(out))
 
     def zt_fwd_bwd_batch(self, grids, L, nthreads, zn=1, sn=0, sp=0):
         grids = np.ascontiguousarray(grids, dtype=np.float64)

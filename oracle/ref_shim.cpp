@@ -13,6 +13,7 @@
 //   zest::zt::RadialZernikeRecursion include/radial_zernike_recursion.hpp:38-297
 //   zest::gl::gl_nodes_and_weights  include/gauss_legendre.hpp:1549-1565
 //   zest::{zt,st}::GridEvaluator    include/grid_evaluator.hpp:52-325
+//   zest::zt::power_spectrum        include/power_spectra.hpp:124-146
 #include <array>
 #include <chrono>
 #include <cstddef>
@@ -25,6 +26,7 @@
 #include "rotor.hpp"
 #include "wignerd_collection.hpp"
 #include "grid_evaluator.hpp"
+#include "power_spectra.hpp"
 
 using zest::zt::ZernikeNorm;
 using zest::st::SHNorm;
@@ -258,6 +260,30 @@ int ref_zt_evaluate(int zn, int sn, int sp, std::size_t order, const double* coe
         auto res = ev.evaluate(e, std::span<const double>(lon, nlon), std::span<const double>(colat, nlat),
                                std::span<const double>(rad, nrad));
         std::memcpy(out, res.data(), res.size() * sizeof(double));
+    });
+}
+
+int ref_st_evaluate(int sn, int sp, std::size_t order, const double* coeffs, std::size_t nlon, const double* lon,
+                    std::size_t nlat, const double* colat, double* out) {
+    return dispatch_st(sn, sp, [&]<SHNorm N, SHPhase P>() {
+        zest::st::GridEvaluator ev(order, nlon, nlat);
+        zest::st::RealSHSpan<const std::array<double, 2>, N, P> e(
+            reinterpret_cast<const std::array<double, 2>*>(coeffs), order);
+        auto res = ev.evaluate(e, std::span<const double>(lon, nlon), std::span<const double>(colat, nlat));
+        std::memcpy(out, res.data(), res.size() * sizeof(double));
+    });
+}
+
+// zt::power_spectrum takes its expansion as a forwarding reference and reads
+// ExpansionType::sh_norm, so the span is passed as a prvalue.  (The SH
+// spectra, power_spectra.hpp:38-104, read ExpansionType::sh_norm too, which
+// the SH spans do not have -- they name it `norm` -- so they do not compile
+// and are not wrapped here.)
+int ref_zt_power_spectrum(int sn, std::size_t order, const double* coeffs, double* out) {
+    return dispatch_zt(1, sn, 0, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
+        using Span = zest::zt::RealZernikeSpan<const std::array<double, 2>, Z, N, P>;
+        zest::zt::power_spectrum(Span(reinterpret_cast<const std::array<double, 2>*>(coeffs), order),
+                                 zest::zt::RadialZernikeSpan<double, Z>(out, order));
     });
 }
 

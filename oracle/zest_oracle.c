@@ -868,3 +868,136 @@ void oracle_euler_from_matrix(const double* r, double* e) {
     e[1] = atan2(by, r[8]);
     e[2] = atan2(r[7], -r[6]);
 }
+
+/* ---------------------------------------------------------------------------
+ * Evaluation at arbitrary points: zt::GridEvaluator::evaluate
+ * (include/grid_evaluator.hpp:228-266; sum_n :275-306, sum_l and sum_m
+ * src/grid_evaluator.cpp:195-257) and st::GridEvaluator::evaluate
+ * (include/grid_evaluator.hpp:84-133; sum_m src/grid_evaluator.cpp:126-151),
+ * with the reference's loop orders.  cos/sin(m lon) by the recurrence of
+ * detail::recursive_trig (src/grid_evaluator.cpp:43-66).  Values are laid out
+ * [lon][lat][rad] (Zernike) and [lon][lat] (SH), row-major.
+ */
+static double* eval_trig(sz L, sz nlon, const double* lon) {
+    double* t = (double*)calloc(2 * L * nlon + 2, sizeof(double));
+    for (sz i = 0; i < nlon; ++i) { t[2 * i] = 1.0; t[2 * i + 1] = 0.0; }
+    if (L < 2) return t;
+    double* t1 = t + 2 * nlon;
+    for (sz i = 0; i < nlon; ++i) { t1[2 * i] = cos(lon[i]); t1[2 * i + 1] = sin(lon[i]); }
+    for (sz m = 2; m < L; ++m) {
+        const double* p = t + 2 * (m - 1) * nlon;
+        double* q = t + 2 * m * nlon;
+        for (sz i = 0; i < nlon; ++i) {
+            q[2 * i] = p[2 * i] * t1[2 * i] - p[2 * i + 1] * t1[2 * i + 1];
+            q[2 * i + 1] = p[2 * i] * t1[2 * i + 1] + p[2 * i + 1] * t1[2 * i];
+        }
+    }
+    return t;
+}
+
+void oracle_zt_evaluate(sz L, int zernike_norm, int sh_norm, int sh_phase, const double* c, sz nlon,
+                        const double* lon, sz nlat, const double* colat, sz nrad, const double* rad, double* out) {
+    memset(out, 0, sizeof(double) * nlon * nlat * nrad);
+    if (L == 0 || nlon == 0 || nlat == 0 || nrad == 0) return;
+    double* R = (double*)calloc(rad_size(L) * nrad, sizeof(double));
+    oracle_radial_zernike(L, zernike_norm, nrad, rad, R);
+    double* z = (double*)malloc(sizeof(double) * nlat);
+    for (sz j = 0; j < nlat; ++j) z[j] = cos(colat[j]);
+    double* P = (double*)calloc(tri_size(L) * nlat, sizeof(double));
+    oracle_plm_real(L, sh_norm, sh_phase, nlat, z, P);
+    double* T = eval_trig(L, nlon, lon);
+    /* sum_n: flm[tri(l,m)][k][2] */
+    double* flm = (double*)calloc(tri_size(L) * nrad * 2, sizeof(double));
+    for (sz n = 0; n < L; ++n)
+        for (sz l = n & 1; l <= n; l += 2)
+            for (sz m = 0; m <= l; ++m) {
+                const double c0 = c[2 * zidx(n, l, m)], c1 = c[2 * zidx(n, l, m) + 1];
+                const double* Rnl = R + rad_idx(n, l) * nrad;
+                double* f = flm + tri_idx(l, m) * nrad * 2;
+                for (sz k = 0; k < nrad; ++k) { f[2 * k] += Rnl[k] * c0; f[2 * k + 1] += Rnl[k] * c1; }
+            }
+    /* sum_l: fm[m][j][k][2] */
+    double* fm = (double*)calloc(L * nlat * nrad * 2, sizeof(double));
+    for (sz l = 0; l < L; ++l)
+        for (sz m = 0; m <= l; ++m) {
+            const double* f = flm + tri_idx(l, m) * nrad * 2;
+            const double* Plm = P + tri_idx(l, m) * nlat;
+            for (sz j = 0; j < nlat; ++j) {
+                const double w = Plm[j];
+                double* g = fm + (m * nlat + j) * nrad * 2;
+                for (sz k = 0; k < nrad; ++k) { g[2 * k] += w * f[2 * k]; g[2 * k + 1] += w * f[2 * k + 1]; }
+            }
+        }
+    /* sum_m */
+    for (sz m = 0; m < L; ++m)
+        for (sz i = 0; i < nlon; ++i) {
+            const double cl = T[2 * (m * nlon + i)], sl = T[2 * (m * nlon + i) + 1];
+            for (sz j = 0; j < nlat; ++j) {
+                const double* g = fm + (m * nlat + j) * nrad * 2;
+                double* v = out + (i * nlat + j) * nrad;
+                for (sz k = 0; k < nrad; ++k) v[k] += g[2 * k] * cl + g[2 * k + 1] * sl;
+            }
+        }
+    free(R); free(z); free(P); free(T); free(flm); free(fm);
+}
+
+void oracle_st_evaluate(sz L, int sh_norm, int sh_phase, const double* c, sz nlon, const double* lon, sz nlat,
+                        const double* colat, double* out) {
+    memset(out, 0, sizeof(double) * nlon * nlat);
+    if (L == 0 || nlon == 0 || nlat == 0) return;
+    double* z = (double*)malloc(sizeof(double) * nlat);
+    for (sz j = 0; j < nlat; ++j) z[j] = cos(colat[j]);
+    double* P = (double*)calloc(tri_size(L) * nlat, sizeof(double));
+    oracle_plm_real(L, sh_norm, sh_phase, nlat, z, P);
+    double* T = eval_trig(L, nlon, lon);
+    double* fm = (double*)calloc(L * nlat * 2, sizeof(double));
+    for (sz l = 0; l < L; ++l)
+        for (sz m = 0; m <= l; ++m) {
+            const double c0 = c[2 * tri_idx(l, m)], c1 = c[2 * tri_idx(l, m) + 1];
+            const double* Plm = P + tri_idx(l, m) * nlat;
+            for (sz j = 0; j < nlat; ++j) { fm[2 * (m * nlat + j)] += Plm[j] * c0; fm[2 * (m * nlat + j) + 1] += Plm[j] * c1; }
+        }
+    for (sz m = 0; m < L; ++m)
+        for (sz i = 0; i < nlon; ++i) {
+            const double cl = T[2 * (m * nlon + i)], sl = T[2 * (m * nlon + i) + 1];
+            for (sz j = 0; j < nlat; ++j) out[i * nlat + j] += fm[2 * (m * nlat + j)] * cl + fm[2 * (m * nlat + j) + 1] * sl;
+        }
+    free(z); free(P); free(T); free(fm);
+}
+
+/* ---------------------------------------------------------------------------
+ * Power spectra (include/power_spectra.hpp).  norm = 1/(4 pi) (geo) or 1 (qm),
+ * st::normalization (include/sh_conventions.hpp).
+ */
+static double sh_norm_const(int sh_norm) { return sh_norm ? 1.0 : 0.07957747154594766788444188168625718; }
+
+/* st::cross_power_spectrum (:38-52): l < min(L, out_len - 1); other entries untouched. */
+void oracle_st_cross_power_spectrum(sz L, int sh_norm, const double* a, const double* b, sz out_len, double* out) {
+    const double norm = sh_norm_const(sh_norm);
+    const sz nl = out_len ? (L < out_len - 1 ? L : out_len - 1) : 0;
+    for (sz l = 0; l < nl; ++l) {
+        out[l] = a[2 * tri_idx(l, 0)] * b[2 * tri_idx(l, 0)];
+        for (sz m = 1; m <= l; ++m)
+            out[l] += a[2 * tri_idx(l, m)] * b[2 * tri_idx(l, m)] + a[2 * tri_idx(l, m) + 1] * b[2 * tri_idx(l, m) + 1];
+        out[l] *= norm;
+    }
+}
+
+/* st::power_spectrum (:88-104): l < L. */
+void oracle_st_power_spectrum(sz L, int sh_norm, const double* a, double* out) {
+    oracle_st_cross_power_spectrum(L, sh_norm, a, a, L + 1, out);
+}
+
+/* zt::power_spectrum (:124-146): out[floor((n+1)^2/4) + l/2], l = n&1, .. < n
+ * (the reference's bound; the l = n entries are not written). */
+void oracle_zt_power_spectrum(sz L, int sh_norm, const double* c, double* out) {
+    const double norm = sh_norm_const(sh_norm);
+    for (sz n = 0; n < L; ++n)
+        for (sz l = n & 1; l < n; l += 2) {
+            double* o = out + rad_idx(n, l);
+            *o = c[2 * zidx(n, l, 0)] * c[2 * zidx(n, l, 0)];
+            for (sz m = 1; m <= l; ++m)
+                *o += c[2 * zidx(n, l, m)] * c[2 * zidx(n, l, m)] + c[2 * zidx(n, l, m) + 1] * c[2 * zidx(n, l, m) + 1];
+            *o *= norm;
+        }
+}

@@ -21,6 +21,8 @@
 #include <string>
 #include <vector>
 
+#include "zest/grid_evaluator.hpp"
+#include "zest/power_spectra.hpp"
 #include "zest/rotor.hpp"
 #include "zest/sh_glq_transformer.hpp"
 #include "zest/zernike_glq_transformer.hpp"
@@ -59,6 +61,8 @@ static_assert(st::LonLatLayout<>::shape(1024) == std::array<std::size_t, 2>{2047
 static_assert(st::LatLonLayout<>::shape(7) == std::array<std::size_t, 2>{7, 16});
 static_assert(zt::RealZernikeExpansionGeo::size(20) == 825);
 static_assert(int(st::SHPhase::none) == -1 && int(st::SHPhase::cs) == 1);
+static_assert(zt::RadialZernikeSpan<double, zt::ZernikeNorm::unnormed>::size(4) == 6);
+static_assert(zt::RadialZernikeSpan<double, zt::ZernikeNorm::unnormed>::idx(3, 3) == 5);
 
 std::vector<double> read_doubles(const std::string& path) {
     std::ifstream f(path, std::ios::binary);
@@ -143,6 +147,58 @@ void run_st(const std::string& op, const std::string& conv, std::size_t order, c
     else if (conv == "101") st_job<st::GLQTransformer<SN::geo, SP::cs, TL>>(op, order, in, out);
     else if (conv == "111") st_job<st::GLQTransformer<SN::qm, SP::cs, TL>>(op, order, in, out);
     else throw std::runtime_error("bad conventions " + conv);
+}
+
+// conventions "zn sn sp" -> f.template operator()<ZN, SN, SP>()
+template <typename F>
+void dispatch_zt_conv(const std::string& conv, F&& f) {
+    using ZN = zt::ZernikeNorm;
+    using SN = st::SHNorm;
+    using SP = st::SHPhase;
+    if (conv == "000") f.template operator()<ZN::normed, SN::geo, SP::none>();
+    else if (conv == "100") f.template operator()<ZN::unnormed, SN::geo, SP::none>();
+    else if (conv == "010") f.template operator()<ZN::normed, SN::qm, SP::none>();
+    else if (conv == "110") f.template operator()<ZN::unnormed, SN::qm, SP::none>();
+    else if (conv == "001") f.template operator()<ZN::normed, SN::geo, SP::cs>();
+    else if (conv == "101") f.template operator()<ZN::unnormed, SN::geo, SP::cs>();
+    else if (conv == "011") f.template operator()<ZN::normed, SN::qm, SP::cs>();
+    else if (conv == "111") f.template operator()<ZN::unnormed, SN::qm, SP::cs>();
+    else throw std::runtime_error("bad conventions " + conv);
+}
+
+// zt::GridEvaluator / st::GridEvaluator on the points of `pts` =
+// [nlon, nlat, nrad, lon..., colat..., rad...]; zt::power_spectrum
+void run_eval(const std::string& op, const std::string& conv, std::size_t order, const std::vector<double>& in,
+              const std::string& out, const std::vector<double>& pts) {
+    const std::size_t nlon = std::size_t(pts[0]), nlat = std::size_t(pts[1]), nrad = std::size_t(pts[2]);
+    const std::span<const double> lon(pts.data() + 3, nlon), colat(lon.data() + nlon, nlat),
+        rad(colat.data() + nlat, nrad);
+    if (op == "zt_eval") {
+        dispatch_zt_conv(conv, [&]<zt::ZernikeNorm Z, st::SHNorm N, st::SHPhase P>() {
+            zt::RealZernikeExpansion<Z, N, P> e(order);
+            std::copy(in.begin(), in.end(), reinterpret_cast<double*>(e.data()));
+            zt::GridEvaluator ev(order, nlon, nlat, nrad);
+            const std::vector<double> v = ev.evaluate(e, lon, colat, rad);
+            write_doubles(out, v.data(), v.size());
+        });
+    } else if (op == "st_eval") {
+        dispatch_zt_conv("0" + conv, [&]<zt::ZernikeNorm Z, st::SHNorm N, st::SHPhase P>() {
+            st::RealSHExpansion<N, P> e(order);
+            std::copy(in.begin(), in.end(), reinterpret_cast<double*>(e.data()));
+            st::GridEvaluator ev(order, nlon, nlat);
+            const std::vector<double> v = ev.evaluate(e, lon, colat);
+            write_doubles(out, v.data(), v.size());
+        });
+    } else if (op == "zt_ps") {
+        dispatch_zt_conv("1" + conv + "0", [&]<zt::ZernikeNorm Z, st::SHNorm N, st::SHPhase P>() {
+            zt::RealZernikeExpansion<Z, N, P> e(order);
+            std::copy(in.begin(), in.end(), reinterpret_cast<double*>(e.data()));
+            const std::vector<double> v = zt::power_spectrum(e);
+            write_doubles(out, v.data(), v.size());
+        });
+    } else {
+        throw std::runtime_error("bad op " + op);
+    }
 }
 
 // rotations of GLQTransformerGeo-convention expansions; conv = rotation type digit
@@ -263,6 +319,8 @@ int main(int argc, char** argv) {
             }
             if (op == "zt_fwd" || op == "zt_bwd") run_zt(op, conv, order, x, dir + "/" + out);
             else if (op == "st_fwd" || op == "st_bwd") run_st(op, conv, order, x, dir + "/" + out);
+            else if (op == "zt_eval" || op == "st_eval" || op == "zt_ps")
+                run_eval(op, conv, order, x, dir + "/" + out, read_doubles(dir + "/" + extra));
             else run_rot(op, conv, order, x, dir + "/" + out, read_doubles(dir + "/" + extra));
             ++n;
         }

@@ -143,6 +143,36 @@ def main():
         rot[f"spolar_{L}"] = ref.st_polar_rotate(s, L + 3, e[1], 1)
     np.savez_compressed(os.path.join(HERE, "rotation.npz"), **rot)
 
+    # Evaluation at arbitrary points (zt/st GridEvaluator) and the Zernike power
+    # spectrum.  The reference's SH spectra do not compile against its SH spans
+    # (they read ExpansionType::sh_norm), so they have no fixture.
+    rng2 = np.random.default_rng(20240611)
+    ev = {}
+    for L, nlon, nlat, nrad in [(1, 3, 2, 2), (6, 7, 5, 4), (13, 11, 9, 6), (24, 5, 17, 3)]:
+        lon = rng2.uniform(-np.pi, 3 * np.pi, nlon)
+        colat = rng2.uniform(0.0, np.pi, nlat)
+        rad = rng2.uniform(0.0, 1.0, nrad)
+        ev[f"lon_{L}"], ev[f"colat_{L}"], ev[f"rad_{L}"] = lon, colat, rad
+        c = rand_zt(rng2, L, power=1.0)
+        ev[f"zc_{L}"] = c
+        for conv in CONVS_ZT:
+            key = "".join(map(str, conv))
+            ev[f"zv_{L}_{key}"] = ref.zt_evaluate(c, L, lon, colat, rad, *conv)
+        s = rand_st(rng2, L + 2)
+        ev[f"sc_{L}"] = s
+        for conv in CONVS_ST:
+            key = "".join(map(str, conv))
+            ev[f"sv_{L}_{key}"] = ref.st_evaluate(s, L + 2, lon, colat, *conv)
+    np.savez_compressed(os.path.join(HERE, "evaluate.npz"), **ev)
+
+    ps = {}
+    for L in [1, 2, 7, 16, 31]:
+        c = rand_zt(rng2, L, power=1.0)
+        ps[f"zc_{L}"] = c
+        for sn in (0, 1):
+            ps[f"zp_{L}_{sn}"] = ref.zt_power_spectrum(c, L, sn)
+    np.savez_compressed(os.path.join(HERE, "spectra.npz"), **ps)
+
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

@@ -89,6 +89,19 @@ def test_cpp_interface_matches_golden(binary, golden, tmp_path):
         job("st_rot", "0", L + 3, r[f"sc_{L}"], r[f"sobj_{L}"], r[f"ze_{L}"])
         job("st_rot", "1", L + 3, r[f"sc_{L}"], r[f"scoord_{L}"], r[f"ze_{L}"])
         job("st_polar", "1", L + 3, r[f"sc_{L}"], r[f"spolar_{L}"], r[f"ze_{L}"][1:2])
+    # GridEvaluator and power spectra (extra file: [nlon, nlat, nrad, lon, colat, rad])
+    e = golden("evaluate")
+    for L in (6, 13):
+        pts = np.concatenate([[e[f"lon_{L}"].size, e[f"colat_{L}"].size, e[f"rad_{L}"].size],
+                              e[f"lon_{L}"], e[f"colat_{L}"], e[f"rad_{L}"]])
+        for conv in ["100", "011"]:
+            job("zt_eval", conv, L, e[f"zc_{L}"], e[f"zv_{L}_{conv}"], pts)
+        for conv in ["00", "11"]:
+            job("st_eval", conv, L + 2, e[f"sc_{L}"], e[f"sv_{L}_{conv}"], pts)
+    p = golden("spectra")
+    for L in (7, 16):
+        for sn in (0, 1):
+            job("zt_ps", str(sn), L, p[f"zc_{L}"], p[f"zp_{L}_{sn}"], np.zeros(3))
     # transpose identities and the angle gradient through the C++ adjoints
     _write(d, "unused.bin", np.zeros(1))
     jobs.append(f"vjp_checks 0 0 unused.bin out{len(jobs)}.bin")

@@ -105,6 +105,11 @@ _SIGNATURES = {
     "zest_gpu_set_autotune": [_vp, _i],
     "zest_gpu_set_host_chunk_bytes": [_vp, _sz],
     "zest_gpu_selftest_wait_timeout": [_vp, ctypes.c_double],
+    "zest_gpu_zt_evaluate": [_vp, _i, _i, _i, _sz, _sz, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _i],
+    "zest_gpu_st_evaluate": [_vp, _i, _i, _sz, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _i],
+    "zest_gpu_st_power_spectrum": [_vp, _i, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_st_cross_power_spectrum": [_vp, _i, _sz, _sz, _vp, _vp, _sz, _vp, _i],
+    "zest_gpu_zt_power_spectrum": [_vp, _i, _sz, _sz, _vp, _vp, _i],
 }
 _SIZE_FUNCS = {
     "zest_gpu_zt_grid_size": [_sz],
@@ -450,6 +455,87 @@ class Context:
     def wignerd_table(self, order: int) -> np.ndarray:
         out = np.zeros(order * (order + 1) * (2 * order + 1) // 6)
         _check(self.lib.zest_gpu_wignerd_table(self._h, order, _vp(out.ctypes.data), MEM_HOST))
+        return out
+
+    # ---- evaluation at arbitrary points (zt/st GridEvaluator) ----
+    def _points(self, x, like):
+        """A point array in the memory kind of `like` (numpy for host data,
+        a CUDA float64 tensor for device data)."""
+        if _is_torch(like):
+            import torch
+            if _is_torch(x):
+                return x.to(dtype=torch.float64, device=like.device).contiguous()
+            return torch.as_tensor(np.ascontiguousarray(x, dtype=np.float64), device=like.device)
+        if _is_torch(x):
+            return x.detach().cpu().numpy().astype(np.float64)
+        return np.ascontiguousarray(x, dtype=np.float64)
+
+    def zt_evaluate(self, coeffs, order: int, lon, colat, rad, batch: int = 1, conv=ZT_GEO, out=None):
+        """Values [batch][lon][lat][rad] of Zernike expansions on the product
+        grid of the given longitudes, colatitudes and radii."""
+        lon, colat, rad = (self._points(v, coeffs) for v in (lon, colat, rad))
+        nlon, nlat, nrad = (int(v.numel() if _is_torch(v) else v.size) for v in (lon, colat, rad))
+        cp, cm = _ptr(coeffs, 2 * zt_coeff_size(order) * batch)
+        n = batch * nlon * nlat * nrad
+        if out is None:
+            out = self._alloc_like(coeffs, n)
+        vp, vm = _ptr(out, n)
+        if vm != cm:
+            raise ValueError("coefficients and values must both be host or both be device memory")
+        lp, _ = _ptr(lon, nlon)
+        tp, _ = _ptr(colat, nlat)
+        rp, _ = _ptr(rad, nrad)
+        _check(self.lib.zest_gpu_zt_evaluate(self._h, *conv, order, batch, cp, nlon, lp, nlat, tp, nrad, rp, vp, cm))
+        return out
+
+    def st_evaluate(self, coeffs, order: int, lon, colat, batch: int = 1, conv=ST_GEO, out=None):
+        """Values [batch][lon][lat] of SH expansions on the product grid."""
+        lon, colat = (self._points(v, coeffs) for v in (lon, colat))
+        nlon, nlat = (int(v.numel() if _is_torch(v) else v.size) for v in (lon, colat))
+        cp, cm = _ptr(coeffs, 2 * st_coeff_size(order) * batch)
+        n = batch * nlon * nlat
+        if out is None:
+            out = self._alloc_like(coeffs, n)
+        vp, vm = _ptr(out, n)
+        if vm != cm:
+            raise ValueError("coefficients and values must both be host or both be device memory")
+        lp, _ = _ptr(lon, nlon)
+        tp, _ = _ptr(colat, nlat)
+        _check(self.lib.zest_gpu_st_evaluate(self._h, *conv, order, batch, cp, nlon, lp, nlat, tp, vp, cm))
+        return out
+
+    # ---- power spectra ----
+    def st_power_spectrum(self, coeffs, order: int, batch: int = 1, sh_norm: int = 0, out=None):
+        cp, cm = _ptr(coeffs, 2 * st_coeff_size(order) * batch)
+        if out is None:
+            out = self._alloc_like(coeffs, batch * order)
+        op, om = _ptr(out, batch * order)
+        if om != cm:
+            raise ValueError("coefficients and spectrum must both be host or both be device memory")
+        _check(self.lib.zest_gpu_st_power_spectrum(self._h, sh_norm, order, batch, cp, op, cm))
+        return out
+
+    def st_cross_power_spectrum(self, a, b, order: int, batch: int = 1, sh_norm: int = 0, out_len=None, out=None):
+        out_len = order if out_len is None else out_len
+        ap, am = _ptr(a, 2 * st_coeff_size(order) * batch)
+        bp, bm = _ptr(b, 2 * st_coeff_size(order) * batch)
+        if out is None:
+            out = self._alloc_like(a, batch * out_len)
+        op, om = _ptr(out, batch * out_len)
+        if not (am == bm == om):
+            raise ValueError("inputs and spectrum must all be host or all be device memory")
+        _check(self.lib.zest_gpu_st_cross_power_spectrum(self._h, sh_norm, order, batch, ap, bp, out_len, op, am))
+        return out
+
+    def zt_power_spectrum(self, coeffs, order: int, batch: int = 1, sh_norm: int = 0, out=None):
+        n = batch * (((order + 1) * (order + 1)) >> 2)
+        cp, cm = _ptr(coeffs, 2 * zt_coeff_size(order) * batch)
+        if out is None:
+            out = self._alloc_like(coeffs, n)
+        op, om = _ptr(out, n)
+        if om != cm:
+            raise ValueError("coefficients and spectrum must both be host or both be device memory")
+        _check(self.lib.zest_gpu_zt_power_spectrum(self._h, sh_norm, order, batch, cp, op, cm))
         return out
 
     @staticmethod

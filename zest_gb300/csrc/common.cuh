@@ -80,12 +80,14 @@ int launch_check(const char* what);
 // pipeline stages timed by the context profiler (zest_gpu_profile_*)
 enum Stage {
     ST_FFT_FWD = 0, ST_FFT_INV, ST_LEG_FWD, ST_LEG_BWD, ST_RAD_FWD, ST_RAD_BWD, ST_ROTATE,
-    ST_SPLIT_SLICE, ST_SPLIT_GEMM, ST_COPY_H2D, ST_COPY_D2H, ST_MEMSET, ST_COUNT
+    ST_SPLIT_SLICE, ST_SPLIT_GEMM, ST_COPY_H2D, ST_COPY_D2H, ST_MEMSET, ST_EVAL_TABLES, ST_EVAL_RAD, ST_EVAL_LEG,
+    ST_EVAL_LON, ST_SPECTRUM, ST_COUNT
 };
 inline const char* stage_name(int s) {
     static const char* names[ST_COUNT] = {"fft_fwd", "fft_inv", "legendre_fwd", "legendre_bwd", "radial_fwd",
                                           "radial_bwd", "rotate", "split_slice", "split_gemm", "copy_h2d",
-                                          "copy_d2h", "memset"};
+                                          "copy_d2h", "memset", "eval_tables", "eval_radial", "eval_legendre",
+                                          "eval_longitude", "spectrum"};
     return (s >= 0 && s < ST_COUNT) ? names[s] : "?";
 }
 }  // namespace zgpu

@@ -51,6 +51,15 @@ inline int upload(DevBuf& buf, const std::vector<T>& v, cudaStream_t s) {
     return ZEST_GPU_OK;
 }
 
+// Device buffers of the evaluation at arbitrary points (evaluate.cu).
+struct EvalBufs {
+    DevBuf z, r, cs, trig;            // points: cos(colat), radii, (cos, sin)(lon), trig table
+    DevBuf P, offP, cntP;             // Legendre table at the colatitudes, groups (m, parity)
+    DevBuf R, offR, cntR;             // radial table at the radii, groups l
+    DevBuf flm, G;                    // radial and Legendre sums
+    DevBuf tiles[3];                  // tile lists of the three sums
+};
+
 struct FftEntry {
     FftPlan plan;
     DevBuf tw;
@@ -166,6 +175,7 @@ struct zest_gpu_context {
     DevBuf adj0, adj1, adj2;  // adjoint scratch (scaled operands, inverse angles, angle partials)
     std::map<std::tuple<int, int, int>, std::unique_ptr<DevBuf>> adj_w;  // quadrature weight slabs
     std::unique_ptr<SplitState, SplitDeleter> split;
+    EvalBufs eval;          // evaluation at arbitrary points
     Profiler prof;
 };
 

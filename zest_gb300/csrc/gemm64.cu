@@ -257,6 +257,83 @@ struct StLegBwd {
     }
 };
 
+// ---------------------------------------------------------------------------
+// Evaluation at arbitrary points (zt::GridEvaluator, st::GridEvaluator,
+// grid_evaluator.hpp:52-325, src/grid_evaluator.cpp:95-257).  The colatitudes
+// have no equatorial symmetry, so the Legendre sums run over every node: one
+// group per m, rows = nodes, the two parities of l - m accumulated apart and
+// added (f_m = sum_l P_lm(z_j) flm, sum_l of the reference, no conjugation).
+
+// Zernike: flm [tri(l,m)][b][rad][2] -> G [b][m][lat][rad][2]
+struct EvZtLeg {
+    static constexpr int NACC = 2;
+    static constexpr bool A_K_FAST = false;
+    LegMeta lm;
+    const double* flm;
+    double* G;
+    int L, nlat, nr2, batch;
+    __device__ int M(int) const { return lm.ld; }
+    __device__ int N(int) const { return batch * nr2; }
+    __device__ int K(int g, int p) const { return lm.cnt[2 * g + p]; }
+    __device__ double a(int g, int p, int i, int k) const { return lm.P[(lm.off[2 * g + p] + k) * lm.ld + i]; }
+    __device__ double b(int g, int p, int k, int n) const {
+        const int l = g + p + 2 * k;
+        const int bb = n / nr2, kc = n - bb * nr2;
+        return flm[(tri_idx(l, g) * batch + bb) * nr2 + kc];
+    }
+    __device__ void store(int g, int i, int n, const double* v) const {
+        const int bb = n / nr2, kc = n - bb * nr2;
+        G[(((long long)bb * L + g) * nlat + i) * nr2 + kc] = v[0] + v[1];
+    }
+};
+
+// SH: coeffs [b][tri][2] -> G [b][m][lat][2]
+struct EvStLeg {
+    static constexpr int NACC = 2;
+    static constexpr bool A_K_FAST = false;
+    LegMeta lm;
+    const double* coeffs;
+    double* G;
+    int L, nlat, batch;
+    long long cstride;
+    __device__ int M(int) const { return lm.ld; }
+    __device__ int N(int) const { return batch * 2; }
+    __device__ int K(int g, int p) const { return lm.cnt[2 * g + p]; }
+    __device__ double a(int g, int p, int i, int k) const { return lm.P[(lm.off[2 * g + p] + k) * lm.ld + i]; }
+    __device__ double b(int g, int p, int k, int n) const {
+        const int l = g + p + 2 * k;
+        const int bb = n >> 1, c = n & 1;
+        return coeffs[bb * cstride + tri_idx(l, g) * 2 + c];
+    }
+    __device__ void store(int g, int i, int n, const double* v) const {
+        const int bb = n >> 1, c = n & 1;
+        G[(((long long)bb * L + g) * nlat + i) * 2 + c] = v[0] + v[1];
+    }
+};
+
+// Longitude sum (sum_m of the reference): group = item b, rows = longitudes i,
+// K = 2L pairs (m, cos/sin), columns = (lat, rad) points:
+// values[b][i][j][k] = sum_m G[b][m][j][k].re cos(m phi_i) + G[b][m][j][k].im sin(m phi_i).
+struct EvLon {
+    static constexpr int NACC = 1;
+    static constexpr bool A_K_FAST = true;
+    const double* trig;  // [i][m][cos, sin]
+    const double* G;     // [b][m][lat * rad][2]
+    double* values;      // [b][i][lat * rad]
+    int L, nlon, npts;
+    __device__ int M(int) const { return nlon; }
+    __device__ int N(int) const { return npts; }
+    __device__ int K(int, int) const { return 2 * L; }
+    __device__ double a(int, int, int i, int k) const { return trig[(long long)i * 2 * L + k]; }
+    __device__ double b(int g, int, int k, int n) const {
+        const int m = k >> 1, c = k & 1;
+        return G[(((long long)g * L + m) * npts + n) * 2 + c];
+    }
+    __device__ void store(int g, int i, int n, const double* v) const {
+        values[((long long)g * nlon + i) * npts + n] = v[0];
+    }
+};
+
 // tile shapes: Zernike sums have few rows and many columns; SH sums have
 // many rows (or K) and 2*batch columns.  The Zernike sums come in three
 // shapes of 256 threads (the autotuner picks one per stage and size): groups
@@ -282,6 +359,22 @@ int run_zt(cudaStream_t s, const Prob& p, const TileList& tl, const char* name) 
 }
 
 }  // namespace
+
+int launch_ev_zt_leg(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* flm, double* G, int L,
+                     int nlat, int nrad, int batch) {
+    EvZtLeg p{lm, flm, G, L, nlat, 2 * nrad, batch};
+    return run_zt(s, p, tl, "ev_zt_leg");
+}
+int launch_ev_st_leg(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* coeffs, double* G, int L,
+                     int nlat, int batch, long long coeff_stride) {
+    EvStLeg p{lm, coeffs, G, L, nlat, batch, coeff_stride};
+    return run<EvStLeg, SBM, SBN, STM, STN, SBK>(s, p, tl, "ev_st_leg");
+}
+int launch_ev_lon(cudaStream_t s, const TileList& tl, const double* trig, const double* G, double* values, int L,
+                  int nlon, int npts) {
+    EvLon p{trig, G, values, L, nlon, npts};
+    return run_zt(s, p, tl, "ev_lon");
+}
 
 void zt_tile_shape(int variant, int& bm, int& bn) {
     bm = variant == 1 ? 32 : (variant == 2 ? 16 : 64);

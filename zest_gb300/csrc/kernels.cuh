@@ -57,6 +57,17 @@ int launch_st_leg_fwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, con
                       int Lg, int nlat, int batch, long long coeff_stride);
 int launch_st_leg_bwd(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* coeffs, double* X,
                       int Lg, int nlat, int batch, long long coeff_stride);
+// Evaluation at arbitrary points: unfolded Legendre sums over all nlat nodes
+// (lm.ld = nlat) into G [b][m][lat][rad][2] (Zernike) or G [b][m][lat][2]
+// (SH); then the longitude sum into values [b][lon][lat * rad] with
+// trig [lon][m][cos, sin].  Zernike tile shapes (variant) for ev_zt_leg and
+// ev_lon, SH shapes for ev_st_leg.
+int launch_ev_zt_leg(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* flm, double* G, int L,
+                     int nlat, int nrad, int batch);
+int launch_ev_st_leg(cudaStream_t s, const LegMeta& lm, const TileList& tl, const double* coeffs, double* G, int L,
+                     int nlat, int batch, long long coeff_stride);
+int launch_ev_lon(cudaStream_t s, const TileList& tl, const double* trig, const double* G, double* values, int L,
+                  int nlon, int npts);
 // tile shapes (rows x cols per CTA) of the launches above
 void zt_tile_shape(int variant, int& bm, int& bn);
 constexpr int kZtTileVariants = 3;

@@ -16,6 +16,7 @@
 
 #include "common.cuh"
 #include "context.cuh"
+#include "evaluate.cuh"
 #include "kernels.cuh"
 #include "split.cuh"
 #include "tables.cuh"
@@ -1200,6 +1201,142 @@ int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable) {
     ZG_TRY(check_ctx(ctx));
     ctx->autotune = enable != 0;
     return ZEST_GPU_OK;
+}
+
+// ---- evaluation at arbitrary points, power spectra -------------------------------
+namespace {
+
+// points of an evaluation: host copies of the caller's arrays (device arrays are
+// copied back), since cos/sin of the angles are taken on the host with std::cos
+// and std::sin as in the reference (grid_evaluator.hpp:112-113, 251-252).
+int points_to_host(int mem, const double* p, size_t n, std::vector<double>& out) {
+    out.resize(n);
+    if (!n) return ZEST_GPU_OK;
+    if (!p) return fail(ZEST_GPU_ERR_INVALID, "null point array");
+    if (mem == ZEST_MEM_DEVICE) {
+        ZG_CUDA_TRY(cudaMemcpy(out.data(), p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+        std::copy(p, p + n, out.begin());
+    }
+    return ZEST_GPU_OK;
+}
+
+int eval_points(int mem, const double* lon, size_t nlon, const double* colat, size_t nlat, std::vector<double>& z,
+                std::vector<double>& cs) {
+    std::vector<double> a, c;
+    ZG_TRY(points_to_host(mem, lon, nlon, a));
+    ZG_TRY(points_to_host(mem, colat, nlat, c));
+    z.resize(nlat);
+    for (size_t j = 0; j < nlat; ++j) z[j] = std::cos(c[j]);
+    cs.resize(2 * nlon);
+    for (size_t i = 0; i < nlon; ++i) {
+        cs[2 * i] = std::cos(a[i]);
+        cs[2 * i + 1] = std::sin(a[i]);
+    }
+    return ZEST_GPU_OK;
+}
+
+}  // namespace
+
+int zest_gpu_zt_evaluate(zest_gpu_context* ctx, int zn, int sn, int sp, size_t order, size_t batch,
+                         const double* coeffs, size_t nlon, const double* lon, size_t nlat, const double* colat,
+                         size_t nrad, const double* rad, double* values, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(zn) || !valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    if (nlon > 0x7fffffff || nlat > 0x7fffffff || nrad > 0x7fffffff || nlat * nrad > 0x7fffffff)
+        return fail(ZEST_GPU_ERR_INVALID, "too many points");
+    if (mem != ZEST_MEM_HOST && mem != ZEST_MEM_DEVICE)
+        return fail(ZEST_GPU_ERR_INVALID, "mem must be ZEST_MEM_HOST or ZEST_MEM_DEVICE");
+    const size_t cn = batch * 2 * zest_gpu_zt_coeff_size(order), vn = batch * nlon * nlat * nrad;
+    if ((cn && !coeffs) || (vn && !values)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    if (vn == 0) return ZEST_GPU_OK;
+    std::vector<double> z, cs, r;
+    ZG_TRY(eval_points(mem, lon, nlon, colat, nlat, z, cs));
+    ZG_TRY(points_to_host(mem, rad, nrad, r));
+    return with_staging(ctx, mem, coeffs, cn, values, vn, [&](const double* in, double* out) {
+        return zt_evaluate_dev(ctx, zn, sn, sp, int(order), int(batch), in, z, cs, r, out);
+    });
+}
+
+int zest_gpu_st_evaluate(zest_gpu_context* ctx, int sn, int sp, size_t order, size_t batch, const double* coeffs,
+                         size_t nlon, const double* lon, size_t nlat, const double* colat, double* values, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    if (nlon > 0x7fffffff || nlat > 0x7fffffff) return fail(ZEST_GPU_ERR_INVALID, "too many points");
+    if (mem != ZEST_MEM_HOST && mem != ZEST_MEM_DEVICE)
+        return fail(ZEST_GPU_ERR_INVALID, "mem must be ZEST_MEM_HOST or ZEST_MEM_DEVICE");
+    const size_t cn = batch * 2 * zest_gpu_st_coeff_size(order), vn = batch * nlon * nlat;
+    if ((cn && !coeffs) || (vn && !values)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    if (vn == 0) return ZEST_GPU_OK;
+    std::vector<double> z, cs;
+    ZG_TRY(eval_points(mem, lon, nlon, colat, nlat, z, cs));
+    return with_staging(ctx, mem, coeffs, cn, values, vn, [&](const double* in, double* out) {
+        return st_evaluate_dev(ctx, sn, sp, int(order), int(batch), in, z, cs, out);
+    });
+}
+
+int zest_gpu_st_power_spectrum(zest_gpu_context* ctx, int sn, size_t order, size_t batch, const double* coeffs,
+                               double* out, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t cn = batch * 2 * zest_gpu_st_coeff_size(order), on = batch * order;
+    if ((cn && !coeffs) || (on && !out)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    if (on == 0) return ZEST_GPU_OK;
+    return with_staging(ctx, mem, coeffs, cn, out, on, [&](const double* in, double* o) {
+        return st_spectrum_dev(ctx, sn, int(order), int(batch), in, in, int(order), (long long)order, o);
+    });
+}
+
+int zest_gpu_st_cross_power_spectrum(zest_gpu_context* ctx, int sn, size_t order, size_t batch, const double* a,
+                                     const double* b, size_t out_len, double* out, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (order > kMaxOrder || out_len > kMaxOrder + 1) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t cn = batch * 2 * zest_gpu_st_coeff_size(order), on = batch * out_len;
+    if ((cn && (!a || !b)) || (on && !out)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    // entries l < min(order, out_len - 1) are written (power_spectra.hpp:42-43)
+    const size_t nl = out_len ? std::min(order, out_len - 1) : 0;
+    if (on == 0 || nl == 0) return ZEST_GPU_OK;
+    const double* bd = b;
+    if (mem == ZEST_MEM_HOST) {
+        ZG_TRY(ctx->aux_stage.ensure(cn * sizeof(double)));
+        StageScope sc(ctx, ST_COPY_H2D);
+        ZG_CUDA_TRY(cudaMemcpyAsync(ctx->aux_stage.p, b, cn * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        bd = ctx->aux_stage.as<double>();
+    }
+    return with_staging(
+        ctx, mem, a, cn, out, on,
+        [&](const double* in, double* o) {
+            return st_spectrum_dev(ctx, sn, int(order), int(batch), in, bd, int(nl), (long long)out_len, o);
+        },
+        out_len, nl);
+}
+
+int zest_gpu_zt_power_spectrum(zest_gpu_context* ctx, int sn, size_t order, size_t batch, const double* coeffs,
+                               double* out, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const size_t nidx = ((order + 1) * (order + 1)) >> 2;
+    const size_t cn = batch * 2 * zest_gpu_zt_coeff_size(order), on = batch * nidx;
+    if ((cn && !coeffs) || (on && !out)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    if (on == 0) return ZEST_GPU_OK;
+    if (mem == ZEST_MEM_HOST) {
+        // the entries the reference leaves alone (l = n) keep the caller's values
+        ZG_TRY(ctx->out_stage.ensure(on * sizeof(double)));
+        ZG_CUDA_TRY(cudaMemcpyAsync(ctx->out_stage.p, out, on * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    return with_staging(ctx, mem, coeffs, cn, out, on, [&](const double* in, double* o) {
+        return zt_spectrum_dev(ctx, sn, int(order), int(batch), in, o);
+    });
 }
 
 int zest_gpu_selftest_wait_timeout(zest_gpu_context* ctx, double seconds) {
