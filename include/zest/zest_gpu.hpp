@@ -39,6 +39,7 @@
 
 #include <algorithm>
 #include <array>
+#include <cmath>
 #include <concepts>
 #include <cstddef>
 #include <cstdint>
@@ -205,7 +206,11 @@ public:
     [[nodiscard]] constexpr element_type& operator()(std::size_t i, std::size_t j) const noexcept {
         return m_data[i * shape()[1] + j];
     }
-    [[nodiscard]] constexpr operator ConstView() const noexcept { return ConstView(m_data, m_order); }
+    [[nodiscard]] constexpr operator ConstView() const noexcept
+        requires(!std::is_const_v<ElementType>)
+    {
+        return ConstView(m_data, m_order);
+    }
 
 private:
     element_type* m_data = nullptr;
@@ -274,7 +279,11 @@ public:
     [[nodiscard]] constexpr element_type& operator()(std::size_t l, std::size_t m) const noexcept {
         return m_data[idx(l, m)];
     }
-    [[nodiscard]] constexpr operator ConstView() const noexcept { return ConstView(m_data, m_order); }
+    [[nodiscard]] constexpr operator ConstView() const noexcept
+        requires(!std::is_const_v<ElementType>)
+    {
+        return ConstView(m_data, m_order);
+    }
 
 private:
     element_type* m_data = nullptr;
@@ -487,7 +496,11 @@ public:
         const auto s = shape();
         return m_data[(i * s[1] + j) * s[2] + k];
     }
-    [[nodiscard]] constexpr operator ConstView() const noexcept { return ConstView(m_data, m_order); }
+    [[nodiscard]] constexpr operator ConstView() const noexcept
+        requires(!std::is_const_v<ElementType>)
+    {
+        return ConstView(m_data, m_order);
+    }
 
 private:
     element_type* m_data = nullptr;
@@ -561,7 +574,11 @@ public:
     [[nodiscard]] constexpr element_type& operator()(std::size_t n, std::size_t l, std::size_t m) const noexcept {
         return m_data[idx(n, l, m)];
     }
-    [[nodiscard]] constexpr operator ConstView() const noexcept { return ConstView(m_data, m_order); }
+    [[nodiscard]] constexpr operator ConstView() const noexcept
+        requires(!std::is_const_v<ElementType>)
+    {
+        return ConstView(m_data, m_order);
+    }
 
 private:
     element_type* m_data = nullptr;
@@ -1105,6 +1122,236 @@ template <real_zernike_expansion ExpansionType>
                    RadialZernikeSpan<double, E::zernike_norm>(res, expansion.order()));
     return res;
 }
+
+}  // namespace zt
+
+// ---------------------------------------------------------------------------
+// Sampling front-ends: the quadrature points, generate_values, and the
+// transformers of functions (zernike_glq_transformer.hpp:336-501, 1027-1178;
+// sh_glq_transformer.hpp:385-504, 1242-1351).  Functions are host callables
+// here, sampled on the host as in the reference; zest_gpu_sampling.cuh samples
+// device functors on the GPU instead.
+// ---------------------------------------------------------------------------
+
+namespace st {
+
+template <typename Func>
+concept spherical_function = requires(Func f, double lon, double colat) {
+    { f(lon, colat) } -> std::same_as<double>;
+};
+template <typename Func>
+concept cartesian_function = requires(Func f, std::array<double, 3> x) {
+    { f(x) } -> std::same_as<double>;
+};
+
+// Longitudes and GL colatitudes of the grid of a layout (counts from the
+// layout's shape, padding included, as the reference).
+template <typename LayoutType = DefaultLayout>
+class SphereGLQGridPoints {
+public:
+    using GridLayout = LayoutType;
+    SphereGLQGridPoints() = default;
+    explicit SphereGLQGridPoints(std::size_t order) { resize(order); }
+    void resize(std::size_t order) {
+        if (order == m_order && !m_longitudes.empty()) return;
+        const auto shape = GridLayout::shape(order);
+        m_longitudes.assign(shape[GridLayout::lon_axis], 0.0);
+        m_glq_nodes.assign(shape[GridLayout::lat_axis], 0.0);
+        zest::detail::check(zest_gpu_st_grid_points(order, GridLayout::abi, m_longitudes.data(), m_glq_nodes.data()));
+        m_order = order;
+    }
+    [[nodiscard]] std::array<std::size_t, 2> shape() const noexcept { return {m_glq_nodes.size(), m_longitudes.size()}; }
+    [[nodiscard]] std::span<const double> longitudes() const noexcept { return m_longitudes; }
+    [[nodiscard]] std::span<const double> glq_nodes() const noexcept { return m_glq_nodes; }
+
+    template <typename GridType, typename FuncType>
+        requires std::same_as<typename std::remove_cvref_t<GridType>::Layout, GridLayout>
+    void generate_values(GridType&& grid, FuncType&& f) {
+        resize(grid.order());
+        for (std::size_t i = 0; i < m_longitudes.size(); ++i)
+            for (std::size_t j = 0; j < m_glq_nodes.size(); ++j) {
+                const double v = f(m_longitudes[i], m_glq_nodes[j]);
+                if constexpr (GridLayout::lon_axis == 0) grid(i, j) = v;
+                else grid(j, i) = v;
+            }
+    }
+    template <typename FuncType>
+    [[nodiscard]] auto generate_values(FuncType&& f, std::size_t order) {
+        SphereGLQGrid<double, GridLayout> grid(order);
+        generate_values(grid, f);
+        return grid;
+    }
+
+private:
+    std::vector<double> m_longitudes, m_glq_nodes;
+    std::size_t m_order = 0;
+};
+
+// SH expansions of functions on the sphere (sh_glq_transformer.hpp:1257-1351).
+template <SHNorm sh_norm_param, SHPhase sh_phase_param, typename GridLayoutType = DefaultLayout>
+class SHTransformer {
+public:
+    using GridLayout = GridLayoutType;
+    SHTransformer() = default;
+    explicit SHTransformer(std::size_t order) : m_grid(order), m_points(order), m_transformer(order) {}
+    void resize(std::size_t order) {
+        m_points.resize(order);
+        if (m_grid.order() != order) m_grid = SphereGLQGrid<double, GridLayout>(order);
+        m_transformer.resize(order);
+    }
+    [[nodiscard]] GLQTransformer<sh_norm_param, sh_phase_param, GridLayout>& transformer() noexcept {
+        return m_transformer;
+    }
+
+    template <spherical_function FuncType>
+    void transform(FuncType&& f, RealSHSpan<std::array<double, 2>, sh_norm_param, sh_phase_param> expansion) {
+        resize(expansion.order());
+        m_points.generate_values(m_grid, f);
+        m_transformer.forward_transform(m_grid, expansion);
+    }
+    template <spherical_function FuncType>
+    [[nodiscard]] RealSHExpansion<sh_norm_param, sh_phase_param> transform(FuncType&& f, std::size_t order) {
+        RealSHExpansion<sh_norm_param, sh_phase_param> expansion(order);
+        transform(std::forward<FuncType>(f), expansion);
+        return expansion;
+    }
+    template <cartesian_function FuncType>
+    void transform(FuncType&& f, RealSHSpan<std::array<double, 2>, sh_norm_param, sh_phase_param> expansion) {
+        transform(spherical(f), expansion);
+    }
+    template <cartesian_function FuncType>
+    [[nodiscard]] RealSHExpansion<sh_norm_param, sh_phase_param> transform(FuncType&& f, std::size_t order) {
+        return transform(spherical(f), order);
+    }
+
+private:
+    template <typename F>
+    static auto spherical(F& f) {
+        return [&f](double lon, double colat) -> double {
+            const double scolat = std::sin(colat);
+            const std::array<double, 3> x = {scolat * std::cos(lon), scolat * std::sin(lon), std::cos(colat)};
+            return f(x);
+        };
+    }
+    SphereGLQGrid<double, GridLayout> m_grid;
+    SphereGLQGridPoints<GridLayout> m_points;
+    GLQTransformer<sh_norm_param, sh_phase_param, GridLayout> m_transformer;
+};
+
+}  // namespace st
+
+namespace zt {
+
+template <typename Func>
+concept spherical_function = requires(Func f, double lon, double colat, double r) {
+    { f(lon, colat, r) } -> std::same_as<double>;
+};
+template <typename Func>
+concept cartesian_function = requires(Func f, std::array<double, 3> x) {
+    { f(x) } -> std::same_as<double>;
+};
+
+// Longitudes, GL colatitudes and GL radii of the ball grid.
+template <typename LayoutType = DefaultLayout>
+class BallGLQGridPoints {
+public:
+    using GridLayout = LayoutType;
+    BallGLQGridPoints() = default;
+    explicit BallGLQGridPoints(std::size_t order) { resize(order); }
+    void resize(std::size_t order) {
+        if (order == m_order && !m_longitudes.empty()) return;
+        const auto shape = GridLayout::shape(order);
+        m_longitudes.assign(shape[0], 0.0);
+        m_lat_glq_nodes.assign(shape[1], 0.0);
+        m_rad_glq_nodes.assign(shape[2], 0.0);
+        zest::detail::check(
+            zest_gpu_zt_grid_points(order, m_longitudes.data(), m_lat_glq_nodes.data(), m_rad_glq_nodes.data()));
+        m_order = order;
+    }
+    [[nodiscard]] std::span<const double> longitudes() const noexcept { return m_longitudes; }
+    [[nodiscard]] std::span<const double> lat_glq_nodes() const noexcept { return m_lat_glq_nodes; }
+    [[nodiscard]] std::span<const double> rad_glq_nodes() const noexcept { return m_rad_glq_nodes; }
+
+    template <typename GridType, typename FuncType>
+        requires std::same_as<typename std::remove_cvref_t<GridType>::Layout, GridLayout>
+    void generate_values(GridType&& grid, FuncType&& f) {
+        resize(grid.order());
+        for (std::size_t i = 0; i < m_longitudes.size(); ++i)
+            for (std::size_t j = 0; j < m_lat_glq_nodes.size(); ++j)
+                for (std::size_t k = 0; k < m_rad_glq_nodes.size(); ++k)
+                    grid(i, j, k) = f(m_longitudes[i], m_lat_glq_nodes[j], m_rad_glq_nodes[k]);
+    }
+    template <typename FuncType>
+    [[nodiscard]] auto generate_values(FuncType&& f, std::size_t order) {
+        BallGLQGrid<double, GridLayout> grid(order);
+        generate_values(grid, f);
+        return grid;
+    }
+
+private:
+    std::vector<double> m_longitudes, m_lat_glq_nodes, m_rad_glq_nodes;
+    std::size_t m_order = 0;
+};
+
+// Zernike expansions of functions on balls of any radius
+// (zernike_glq_transformer.hpp:1054-1178).
+template <ZernikeNorm zernike_norm_param, st::SHNorm sh_norm_param, st::SHPhase sh_phase_param,
+          typename GridLayoutType = DefaultLayout>
+class ZernikeTransformer {
+public:
+    using GridLayout = GridLayoutType;
+    using Expansion = RealZernikeExpansion<zernike_norm_param, sh_norm_param, sh_phase_param>;
+    ZernikeTransformer() = default;
+    explicit ZernikeTransformer(std::size_t order) : m_grid(order), m_points(order), m_transformer(order) {}
+    void resize(std::size_t order) {
+        m_points.resize(order);
+        if (m_grid.order() != order) m_grid = BallGLQGrid<double, GridLayout>(order);
+        m_transformer.resize(order);
+    }
+    [[nodiscard]] GLQTransformer<zernike_norm_param, sh_norm_param, sh_phase_param, GridLayout>& transformer() noexcept {
+        return m_transformer;
+    }
+
+    template <spherical_function FuncType>
+    void transform(FuncType&& f, double radius,
+                   RealZernikeSpan<std::array<double, 2>, zernike_norm_param, sh_norm_param, sh_phase_param> expansion) {
+        auto f_scaled = [&](double lon, double colat, double r) { return f(lon, colat, r * radius); };
+        resize(expansion.order());
+        m_points.generate_values(m_grid, f_scaled);
+        m_transformer.forward_transform(m_grid, expansion);
+    }
+    template <spherical_function FuncType>
+    [[nodiscard]] Expansion transform(FuncType&& f, double radius, std::size_t order) {
+        Expansion expansion(order);
+        transform(std::forward<FuncType>(f), radius, expansion);
+        return expansion;
+    }
+    template <cartesian_function FuncType>
+    void transform(FuncType&& f, double radius,
+                   RealZernikeSpan<std::array<double, 2>, zernike_norm_param, sh_norm_param, sh_phase_param> expansion) {
+        auto f_spherical = [&](double lon, double colat, double r) -> double {
+            const double rad = r * radius;
+            const double scolat = std::sin(colat);
+            const std::array<double, 3> x = {rad * scolat * std::cos(lon), rad * scolat * std::sin(lon),
+                                             rad * std::cos(colat)};
+            return f(x);
+        };
+        resize(expansion.order());
+        m_points.generate_values(m_grid, f_spherical);
+        m_transformer.forward_transform(m_grid, expansion);
+    }
+    template <cartesian_function FuncType>
+    [[nodiscard]] Expansion transform(FuncType&& f, double radius, std::size_t order) {
+        Expansion expansion(order);
+        transform(std::forward<FuncType>(f), radius, expansion);
+        return expansion;
+    }
+
+private:
+    BallGLQGrid<double, GridLayout> m_grid;
+    BallGLQGridPoints<GridLayout> m_points;
+    GLQTransformer<zernike_norm_param, sh_norm_param, sh_phase_param, GridLayout> m_transformer;
+};
 
 }  // namespace zt
 

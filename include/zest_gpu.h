@@ -154,6 +154,16 @@ int zest_gpu_st_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
 /* euler_angles_from_rotation_matrix, rotor.hpp:53-63 (row-major 3x3, host). */
 int zest_gpu_euler_from_matrix(const double* matrix, double* euler);
 
+/* ---- points of the quadrature grids (host arrays, no context) ----
+ * BallGLQGridPoints (zernike_glq_transformer.hpp:336-501): 2L-1 longitudes
+ * 2 pi i / (2L-1), L+1 colatitudes (the GL nodes in angle style, descending
+ * from near pi) and pad8(L+1) radii (1 + x_k)/2.  SphereGLQGridPoints
+ * (sh_glq_transformer.hpp:385-504): the longitudes and colatitudes of the
+ * layout's shape, padding included, as the reference (LonLat: 2L-1 and
+ * pad8(L); LatLon: pad8(2L-1) and L). */
+int zest_gpu_zt_grid_points(size_t order, double* lon, double* colat, double* rad);
+int zest_gpu_st_grid_points(size_t order, int layout, double* lon, double* colat);
+
 /* ---- evaluation at arbitrary points ----
  * zt::GridEvaluator::evaluate, grid_evaluator.hpp:228-266 (sums in
  * src/grid_evaluator.cpp:180-257): the values of `batch` Zernike expansions of

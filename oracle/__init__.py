@@ -351,6 +351,15 @@ class Reference(_Lib):
         self._f("zt_grid_points", [_c_sz, _p_dbl, _p_dbl, _p_dbl])(L, _ptr(lon), _ptr(colat), _ptr(r))
         return lon, colat, r
 
+    def st_grid_points(self, L: int, latlon: int = 0):
+        nlon, nlat = st_grid_shape(L, bool(latlon))
+        if latlon:
+            nlon, nlat = nlat, nlon
+        lon = np.zeros(nlon)
+        colat = np.zeros(nlat)
+        self._f("st_grid_points", [_c_sz, _c_int, _p_dbl, _p_dbl])(L, int(latlon), _ptr(lon), _ptr(colat))
+        return lon, colat
+
     def zt_rotate_matrix(self, coeffs, L, mat, rtype=0, zn=1, sn=0, sp=0):
         c = np.array(coeffs, dtype=np.float64, copy=True, order="C")
         m = np.ascontiguousarray(mat, dtype=np.float64).reshape(9)

@@ -173,6 +173,15 @@ def main():
             ps[f"zp_{L}_{sn}"] = ref.zt_power_spectrum(c, L, sn)
     np.savez_compressed(os.path.join(HERE, "spectra.npz"), **ps)
 
+    # Points of the quadrature grids (BallGLQGridPoints, SphereGLQGridPoints).
+    pts = {}
+    for L in [1, 2, 5, 20, 64, 201]:
+        pts[f"zlon_{L}"], pts[f"zcolat_{L}"], pts[f"zrad_{L}"] = ref.zt_grid_points(L)
+    for L in [1, 3, 8, 12, 100]:
+        for latlon in (0, 1):
+            pts[f"slon_{L}_{latlon}"], pts[f"scolat_{L}_{latlon}"] = ref.st_grid_points(L, latlon)
+    np.savez_compressed(os.path.join(HERE, "points.npz"), **pts)
+
     for name in sorted(os.listdir(HERE)):
         if name.endswith(".npz"):
             print(name, os.path.getsize(os.path.join(HERE, name)))

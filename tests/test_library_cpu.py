@@ -80,3 +80,21 @@ def test_no_cpu_fallback_path(zlib):
             if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp", ".hpp")):
                 txt = open(os.path.join(dirpath, f)).read()
                 assert "import oracle" not in txt and "from oracle" not in txt and "zest_oracle" not in txt, f
+
+
+def test_grid_points_match_reference(zlib, golden):
+    # BallGLQGridPoints / SphereGLQGridPoints of the reference (points.npz):
+    # longitudes bit for bit; colatitudes and radii within 2 ulp (the
+    # reference's nodes come from Bogaert's asymptotic formulas, these from a
+    # double-double Newton solve)
+    p = golden("points")
+    for L in [1, 2, 5, 20, 64, 201]:
+        lon, colat, rad = zlib.zt_grid_points(L)
+        np.testing.assert_array_equal(lon, p[f"zlon_{L}"])
+        np.testing.assert_allclose(colat, p[f"zcolat_{L}"], rtol=0, atol=5e-16)
+        np.testing.assert_allclose(rad, p[f"zrad_{L}"], rtol=0, atol=2.5e-16)
+    for L in [1, 3, 8, 12, 100]:
+        for layout in (0, 1):
+            lon, colat = zlib.st_grid_points(L, layout)
+            np.testing.assert_array_equal(lon, p[f"slon_{L}_{layout}"])
+            np.testing.assert_allclose(colat, p[f"scolat_{L}_{layout}"], rtol=0, atol=5e-16)

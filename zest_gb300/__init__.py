@@ -105,6 +105,8 @@ _SIGNATURES = {
     "zest_gpu_set_autotune": [_vp, _i],
     "zest_gpu_set_host_chunk_bytes": [_vp, _sz],
     "zest_gpu_selftest_wait_timeout": [_vp, ctypes.c_double],
+    "zest_gpu_zt_grid_points": [_sz, _vp, _vp, _vp],
+    "zest_gpu_st_grid_points": [_sz, _i, _vp, _vp],
     "zest_gpu_zt_evaluate": [_vp, _i, _i, _i, _sz, _sz, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _i],
     "zest_gpu_st_evaluate": [_vp, _i, _i, _sz, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _i],
     "zest_gpu_st_power_spectrum": [_vp, _i, _sz, _sz, _vp, _vp, _i],
@@ -546,6 +548,25 @@ class Context:
             import torch
             return torch.zeros(n, dtype=torch.float64, device=x.device)
         return np.zeros(n, dtype=np.float64)
+
+
+def zt_grid_points(order: int):
+    """(lon, colat, rad) of the Zernike GLQ grid, as BallGLQGridPoints."""
+    nlon, nlat, nrad = zt_grid_shape(order)
+    lon, colat, rad = np.zeros(nlon), np.zeros(nlat), np.zeros(nrad)
+    _check(library().zest_gpu_zt_grid_points(order, _vp(lon.ctypes.data), _vp(colat.ctypes.data),
+                                             _vp(rad.ctypes.data)))
+    return lon, colat, rad
+
+
+def st_grid_points(order: int, layout: int = 0):
+    """(lon, colat) of the SH GLQ grid of a layout, as SphereGLQGridPoints
+    (counts from the layout's shape, padding included)."""
+    shape = st_grid_shape(order, layout)
+    nlon, nlat = (shape[1], shape[0]) if layout else shape
+    lon, colat = np.zeros(nlon), np.zeros(nlat)
+    _check(library().zest_gpu_st_grid_points(order, layout, _vp(lon.ctypes.data), _vp(colat.ctypes.data)))
+    return lon, colat
 
 
 def gl_nodes_weights(n: int, packed: bool = False):

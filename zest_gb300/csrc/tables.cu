@@ -95,25 +95,12 @@ void legendre_pair(long n, DD x, DD& pn, DD& pnm1) {
     pnm1 = p0;
 }
 
+// k-th node counted from +1 (k = 1 .. ceil(n/2)) in double-double
+DD node_dd(long n, long k);
+
 // k-th node counted from +1 (k = 1 .. ceil(n/2)) and its weight
 void node_weight(long n, long k, double& node, double& weight) {
-    const double pi = 3.14159265358979323846264338327950288;
-    DD x;
-    if ((n & 1) && k == (n + 1) / 2) {
-        x = dd(0.0);
-    } else {
-        const double theta = pi * (double(k) - 0.25) / (double(n) + 0.5);
-        x = dd(std::cos(theta + 1.0 / (8.0 * double(n) * double(n) * std::tan(theta))));
-        for (int it = 0; it < 60; ++it) {
-            DD pn, pnm1;
-            legendre_pair(n, x, pn, pnm1);
-            DD omx2 = mul(add(dd(1.0), neg(x)), add(dd(1.0), x));
-            DD dp = div(mul_d(add(pnm1, neg(mul(x, pn))), double(n)), omx2);
-            DD dx = div(pn, dp);
-            x = add(x, neg(dx));
-            if (std::fabs(dx.hi) < 1e-30 * (std::fabs(x.hi) + 1e-300) || dx.hi == 0.0) break;
-        }
-    }
+    const DD x = node_dd(n, k);
     DD pn, pnm1;
     legendre_pair(n, x, pn, pnm1);
     DD omx2 = mul(add(dd(1.0), neg(x)), add(dd(1.0), x));
@@ -122,7 +109,39 @@ void node_weight(long n, long k, double& node, double& weight) {
     node = x.hi + x.lo;
     weight = w.hi + w.lo;
 }
+DD node_dd(long n, long k) {
+    const double pi = 3.14159265358979323846264338327950288;
+    DD x;
+    if ((n & 1) && k == (n + 1) / 2) return dd(0.0);
+    const double theta = pi * (double(k) - 0.25) / (double(n) + 0.5);
+    x = dd(std::cos(theta + 1.0 / (8.0 * double(n) * double(n) * std::tan(theta))));
+    for (int it = 0; it < 60; ++it) {
+        DD pn, pnm1;
+        legendre_pair(n, x, pn, pnm1);
+        DD omx2 = mul(add(dd(1.0), neg(x)), add(dd(1.0), x));
+        DD dp = div(mul_d(add(pnm1, neg(mul(x, pn))), double(n)), omx2);
+        DD dx = div(pn, dp);
+        x = add(x, neg(dx));
+        if (std::fabs(dx.hi) < 1e-30 * (std::fabs(x.hi) + 1e-300) || dx.hi == 0.0) break;
+    }
+    return x;
+}
+
+// arccos of a double-double cosine: acos(hi) corrected to first order in lo
+double acos_dd(DD x) {
+    if (x.hi == 0.0 && x.lo == 0.0) return std::acos(0.0);
+    return std::acos(x.hi) - x.lo / std::sqrt((1.0 - x.hi) * (1.0 + x.hi));
+}
 }  // namespace
+
+void gl_colatitudes(long n, double* theta) {
+    const long nu = (n + 1) >> 1;
+    for (long k = 1; k <= nu; ++k) {
+        const DD x = node_dd(n, k);
+        theta[k - 1] = acos_dd(neg(x));
+        theta[n - k] = acos_dd(x);
+    }
+}
 
 void gl_nodes_weights(long n, bool packed, double* nodes, double* weights) {
     const long nu = (n + 1) >> 1;

@@ -9,6 +9,9 @@ namespace zgpu {
 // include/gauss_legendre.hpp:32-66 (unpacked ascending from -1; packed =
 // non-negative nodes ascending from 0).
 void gl_nodes_weights(long n, bool packed, double* nodes, double* weights);
+// The same nodes as colatitudes theta = arccos(x) (angle style), ordered as
+// the unpacked nodes (x ascending, theta descending from near pi).
+void gl_colatitudes(long n, double* theta);
 
 // P_lm(z_i) in the reference vector layout out[idx(l,m) * nz + i].
 int launch_plm_ref(cudaStream_t s, int L, int sh_norm, int sh_phase, int nz, const double* z, double* out);

@@ -1203,6 +1203,44 @@ int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable) {
     return ZEST_GPU_OK;
 }
 
+// ---- points of the quadrature grids ----------------------------------------------
+// BallGLQGridPoints::resize (zernike_glq_transformer.hpp:472-495) and
+// SphereGLQGridPoints::resize (sh_glq_transformer.hpp:483-500): longitudes
+// dlon * i with dlon = 2 pi / nlon, colatitudes the GL nodes in angle style,
+// radii (1 + x) / 2 of the cos-style nodes.  Counts from the layout's shape,
+// padding included.
+namespace {
+void longitudes(size_t nlon, double* lon) {
+    const double pi = 3.14159265358979323846264338327950288;
+    const double dlon = (2.0 * pi) / double(nlon);
+    for (size_t i = 0; i < nlon; ++i) lon[i] = dlon * double(i);
+}
+}  // namespace
+
+int zest_gpu_zt_grid_points(size_t order, double* lon, double* colat, double* rad) {
+    if (order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (order == 0) return ZEST_GPU_OK;
+    if (!lon || !colat || !rad) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    const ZtShape sh = zt_shape(long(order));
+    longitudes(size_t(sh.nlon), lon);
+    gl_colatitudes(long(sh.nlat), colat);
+    std::vector<double> w(size_t(sh.nrad));
+    gl_nodes_weights(long(sh.nrad), false, rad, w.data());
+    for (long k = 0; k < sh.nrad; ++k) rad[k] = 0.5 * (1.0 + rad[k]);
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_st_grid_points(size_t order, int layout, double* lon, double* colat) {
+    if (order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (layout != ZEST_LAYOUT_LONLAT && layout != ZEST_LAYOUT_LATLON) return fail(ZEST_GPU_ERR_INVALID, "bad layout");
+    if (order == 0) return ZEST_GPU_OK;
+    if (!lon || !colat) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    const StShape sh = st_shape(long(order), layout == ZEST_LAYOUT_LATLON);
+    longitudes(size_t(sh.nlon), lon);
+    gl_colatitudes(long(sh.nlat), colat);
+    return ZEST_GPU_OK;
+}
+
 // ---- evaluation at arbitrary points, power spectra -------------------------------
 namespace {
 
