@@ -248,6 +248,82 @@ def run_sh(args, rank: int, world: int, barrier) -> None:
             "stages_ms": {k: v[0] / args.steps for k, v in prof.items()}, "clocks": clocks}), flush=True)
 
 
+def run_evaluate(args, rank: int, world: int, barrier) -> None:
+    """Zernike expansions evaluated at arbitrary points (zt::GridEvaluator):
+    order 100, batch 8, c_nlm ~ N(0, (n+1)^-2), on the product grid of 200
+    longitudes, 100 colatitudes and 100 radii drawn uniformly (seeded).  One
+    step = the evaluation of the batch (tables, radial, Legendre and longitude
+    sums), FP64.  The dominant stage is the longitude sum, a dense FP64
+    product of 2 * nlon * (nlat * nrad) * 2L flops per item, reported against
+    the FP64 pipe's 1.20 TFLOP/s.  The reference's evaluator (one thread per
+    item) is timed on one item for the CPU baseline."""
+    import torch
+    import zest_gb300 as zg
+    ctx = zg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    L, B, nlon, nlat, nrad = 100, 8, 200, 100, 100
+    rng = np.random.default_rng(4242 + rank)
+    c = zt_coeffs(L, B, seed0=replica_seed0(rank, B))
+    lon = rng.uniform(0.0, 2.0 * np.pi, nlon)
+    colat = rng.uniform(0.0, np.pi, nlat)
+    rad = rng.uniform(0.0, 1.0, nrad)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    cd = torch.from_numpy(c.ravel()).to(dev)
+    lon_d, colat_d, rad_d = (torch.from_numpy(v).to(dev) for v in (lon, colat, rad))
+    vd = torch.empty(B * nlon * nlat * nrad, dtype=torch.float64, device=dev)
+
+    def step():
+        ctx.zt_evaluate(cd, L, lon_d, colat_d, rad_d, batch=B, out=vd)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    ctx.profile(True)
+    ctx.profile_read(reset=True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    prof = ctx.profile_read(reset=True)
+    ms = max_over_ranks(e0.elapsed_time(e1), None) / args.steps
+    stages = {k: v[0] / args.steps for k, v in prof.items()}
+    lon_flops = 2.0 * nlon * nlat * nrad * 2 * L * B
+    lon_ms = stages.get("eval_longitude")
+    achieved = lon_flops / (lon_ms * 1e-3) / 1e12 if lon_ms else None
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            from oracle import Reference
+            ref = Reference()
+            t0 = time.perf_counter()
+            want = ref.zt_evaluate(c[0], L, lon, colat, rad)
+            secs = time.perf_counter() - t0
+            got = vd[: nlon * nlat * nrad].cpu().numpy()
+            cpu = {"value": 1.0 / secs, "unit": "expansions/s", "cores": 1, "kind": "reference",
+                   "sample": "one order-100 expansion on the 200 x 100 x 100 points, zt::GridEvaluator",
+                   "max_rel_err_vs_reference": float(np.max(np.abs(got - want.ravel())) / np.max(np.abs(want)))}
+        except (FileNotFoundError, OSError) as exc:
+            cpu = {"unavailable": str(exc)}
+    if rank == 0:
+        print(json.dumps({
+            "metric": "Zernike expansions evaluated at arbitrary points per second, order 100, 2e6 points",
+            "value": world * B / (ms * 1e-3), "unit": "expansions/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "zernike_grid_evaluator", "order": L, "batch": B,
+                       "points": [nlon, nlat, nrad], "conventions": "GLQTransformerGeo"},
+            "roofline": {"bound": "fp64", "kernel": "gemm64_kernel<EvLon> (longitude sum)", "achieved": achieved,
+                         "peak": 1.20, "unit": "TFLOP/s", "frac": achieved / 1.20 if achieved else None,
+                         "peak_source": "DFMA microbenchmark on GB300 (1.20 TFLOP/s)"},
+            "stages_ms": stages, "cpu_baseline": cpu, "clocks": clocks}), flush=True)
+
+
 def run_batching(args, rank: int, world: int, barrier) -> None:
     """4096 expansions, orders drawn uniformly from [8, 128] (sorted), c_nlm ~
     N(0, (n+1)^-2) with Im(m=0) = 0, Haar-uniform Euler angles; one step =
@@ -345,7 +421,7 @@ def main():
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["transforms", "batching", "sh"], default="transforms",
+    ap.add_argument("--workload", choices=["transforms", "batching", "sh", "evaluate"], default="transforms",
                     help="transforms: the headline (order 200 x 64 forward+backward); batching: 4096 "
                          "expansions of orders U{8..128}, rotate + backward in one graph")
     ap.add_argument("--items", type=int, default=4096)
@@ -380,6 +456,9 @@ def main():
         return
     if args.workload == "sh":
         run_sh(args, rank, world, barrier)
+        return
+    if args.workload == "evaluate":
+        run_evaluate(args, rank, world, barrier)
         return
 
     L, B = args.order, args.batch
