@@ -192,10 +192,12 @@ def run_reference_arm(args, rank: int, world: int) -> None:
 
 # --------------------------------------------------------------------------
 def run_sh(args, rank: int, world: int, barrier) -> None:
-    """Spherical harmonics at lmax 1023 (order 1024), batch 8, FP64: real
+    """Spherical harmonics at lmax 1023 (order 1024), batch 8: real
     coefficients N(0, (l+1)^-2) (4pi normalisation, no Condon-Shortley phase),
     synthesised to the LonLat grid (2047 x 1024) and transformed back; one step
-    = backward then forward of the batch.  Error = max over items of
+    = backward then forward of the batch.  Timed in FP64 and, unless
+    --precision fp64, with the Legendre sums in split precision on the tensor
+    cores (the value reported).  Error = max over items of
     max|c - c_in| / max|c_in| (the round trip is exact in exact arithmetic)."""
     import torch
     import zest_gb300 as zg
@@ -217,35 +219,58 @@ def run_sh(args, rank: int, world: int, barrier) -> None:
         ctx.st_backward(cd, L, batch=B, out=gd)
         ctx.st_forward(gd, L, batch=B, out=cout)
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    barrier()
-    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-    sampler.start()
-    ctx.profile(True)
-    ctx.profile_read(reset=True)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        step()
-    e1.record()
-    torch.cuda.synchronize()
-    clocks = sampler.stop()
-    prof = ctx.profile_read(reset=True)
-    ms = max_over_ranks(e0.elapsed_time(e1), None) / args.steps
-    err = max(float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
-              for x, y in zip(cout.cpu().numpy().reshape(B, -1), c.reshape(B, -1)))
+    def timed(nsteps, nwarm):
+        for _ in range(nwarm):
+            step()
+        torch.cuda.synchronize()
+        barrier()
+        sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+        sampler.start()
+        ctx.profile(True)
+        ctx.profile_read(reset=True)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(nsteps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        clocks = sampler.stop()
+        prof = ctx.profile_read(reset=True)
+        ctx.profile(False)
+        ms = max_over_ranks(e0.elapsed_time(e1), None) / nsteps
+        err = max(float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
+                  for x, y in zip(cout.cpu().numpy().reshape(B, -1), c.reshape(B, -1)))
+        return ms, {k: v[0] / nsteps for k, v in prof.items()}, clocks, err
+
+    ms64, st64, clocks64, err64 = timed(args.steps, args.warmup)
+    split = args.precision != "fp64"
+    if split:
+        g64 = gd.clone()
+        ctx.set_precision(zg.PRECISION_SPLIT, 6)
+        ms, stages, clocks, err = timed(args.steps, args.warmup)
+        ctx.st_backward(cd, L, batch=B, out=gd)
+        torch.cuda.synchronize()
+        d_grid = float(((gd - g64).abs().reshape(B, -1).amax(1) / g64.abs().reshape(B, -1).amax(1)).max())
+        ctx.set_precision(zg.PRECISION_FP64)
+    else:
+        ms, stages, clocks, err, d_grid = ms64, st64, clocks64, err64, None
     if rank == 0:
         print(json.dumps({
-            "metric": "SH backward+forward transforms/s, lmax 1023 x 8, FP64", "value": world * B / (ms * 1e-3),
-            "unit": "transforms/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "metric": "SH backward+forward transforms/s, lmax 1023 x 8" + (", split-precision Legendre sums"
+                                                                             if split else ", FP64"),
+            "value": world * B / (ms * 1e-3), "unit": "transforms/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 digit slices, fp64 recombination" if split else "f64",
             "data": "synthetic", "config": {"workload": "sh_glq_bwd_fwd", "order": 1024, "batch": B,
-                                            "layout": "LonLat", "conventions": "GLQTransformerGeo"},
+                                            "layout": "LonLat", "conventions": "GLQTransformerGeo",
+                                            "precision": "split" if split else "fp64"},
             "roundtrip_max_rel_err": err,
-            "stages_ms": {k: v[0] / args.steps for k, v in prof.items()}, "clocks": clocks}), flush=True)
+            "backward_grid_max_rel_err_vs_fp64": d_grid,
+            "fp64_gpu": {"value": world * B / (ms64 * 1e-3), "ms_per_step": ms64, "stages_ms": st64,
+                         "roundtrip_max_rel_err": err64},
+            "split_vs_fp64": (ms64 / ms) if split else None,
+            "stages_ms": stages, "clocks": clocks}), flush=True)
 
 
 def run_evaluate(args, rank: int, world: int, barrier) -> None:

@@ -344,6 +344,26 @@ struct LegBwdLoader {
     }
 };
 
+// SH coefficients [b][tri(l,m)][c], rows (m, b, c); k = i: the pair
+// (l = m + 2i, l + 1), zero from Lm on (the two parity operands).
+struct StLegBwdLoader {
+    static constexpr bool ROW_FAST = true, TWO = true;
+    const double* c;
+    long long cs;
+    int B, Lm;
+    struct Row { const double* base; int m; };
+    __device__ Row row(long long r) const {
+        const long long mb = r >> 1;
+        const int m = int(mb / B), b = int(mb - (long long)m * B);
+        return Row{c + b * cs + (r & 1), m};
+    }
+    __device__ void get(const Row& R, int k, double& up, double& dn) const {
+        const int l = R.m + 2 * k;
+        up = (l < Lm) ? R.base[2 * tri_idx(l, R.m)] : 0.0;
+        dn = (l + 1 < Lm) ? R.base[2 * tri_idx(l + 1, R.m)] : 0.0;
+    }
+};
+
 // rows (b, col); k = m: (Re F_m, Im F_m); the sin operand is Im F_k at k - 1
 // rows (b, col = (lat, rad)); k = m: the spectrum at latitude lat, formed
 // from the two parity sums E_p[b][m][j'][2 rad + {re, im}] of the Legendre
@@ -606,6 +626,7 @@ struct SplitUnit {
     int flags;    // bit 0: A map, bit 1: B map, bit 2: parity / RMW
     int g;        // group (m or l)
     int aux;      // group-relative index of the first table row
+    int k0;       // first 16-wide K block (sums split into chunks of at most 256)
 };
 
 namespace {
@@ -709,6 +730,51 @@ struct EpiLegBwdE {
     }
 };
 
+// SH sums: the table is the 128-row operand (rows = table rows of a group), the
+// 2 x batch data rows (b, c) are the columns.
+// Forward: table row r of group (m, p) holds l = m + p + 2 (r - off(m, p)),
+// off(m, 0) = m L - m (m - 1) / 2 and off(m, 1) = off(m, 0) + (L - m + 1) / 2
+// (the group offsets of the Legendre tables of order L); column n -> (b, c).
+// ACC: a later K-chunk of the sum, added to the earlier chunks' result.
+template <bool ACC>
+struct EpiStLegFwd {
+    static constexpr bool RMW = ACC;
+    double* coeffs;
+    long long cs;
+    int L;
+    struct Row { double* p; };
+    __device__ Row row(const SplitUnit& u, int r) const {
+        const int m = u.g, p = (u.flags >> 2) & 1;
+        const long long off = (long long)m * L - (long long)m * (m - 1) / 2 + (p ? (L - m + 1) / 2 : 0);
+        const long long l = m + p + 2 * (r - off);
+        return Row{coeffs + 2 * tri_idx(l, m) + (u.aux >> 1) * cs};  // the unit's first column (b, c) = (aux/2, 0)
+    }
+    __device__ void load(const Row& R, int n, double* old) const { old[0] = R.p[(n >> 1) * cs + (n & 1)]; }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        R.p[(n >> 1) * cs + (n & 1)] = ACC ? old[0] + v : v;
+    }
+};
+// Backward: table row r of group (m, p) is folded node j = r - (2m + p) kh;
+// the parity sums go to E[p][b][m][j][c].
+template <bool ACC>
+struct EpiStLegBwdE {
+    static constexpr bool RMW = ACC;
+    double* E;
+    int B, L, kh;
+    struct Row { double* p; };
+    __device__ Row row(const SplitUnit& u, int r) const {
+        const int m = u.g, par = (u.flags >> 2) & 1;
+        const long long j = r - (long long)(2 * m + par) * kh;
+        return Row{E + (((long long)par * B * L + m) * kh + j) * 2 + (long long)(u.aux >> 1) * L * kh * 2};
+    }
+    __device__ void load(const Row& R, int n, double* old) const {
+        old[0] = R.p[(long long)(n >> 1) * L * kh * 2 + (n & 1)];
+    }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        R.p[(long long)(n >> 1) * L * kh * 2 + (n & 1)] = ACC ? old[0] + v : v;
+    }
+};
+
 // Inverse DFT, rows (b, col).  The cos pass writes x_0 = C_0 to the grid and
 // C_i (i >= 1) to the scratch Cs[b][i][col]; the sin pass reads C_i once and
 // writes x_i = C_i + S_i and x_{N-i} = C_i - S_i.
@@ -809,9 +875,9 @@ static_assert(Sched<6, 7>::bslice(15) == 17 && Sched<6, 7>::btile(6, 5) == 15 &&
                   Sched<6, 8>::btile(5, 5) == 10 && Sched<6, 8>::btile(4, 4) == 4,
               "tile maps");
 
-template <int S, int BITS>
+template <int S, int BITS, int NT>
 __host__ __device__ constexpr int stage_count() {
-    constexpr int st = S * 128 * 32 + Sched<S, BITS>::NB * 3072;
+    constexpr int st = S * 128 * 32 + Sched<S, BITS>::NB * (((NT * 32 + 1023) / 1024) * 1024);
     constexpr int n = (220 * 1024) / st;
     return n > 6 ? 6 : n;
 }
@@ -822,7 +888,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                       const __grid_constant__ CUtensorMap mapB0, const __grid_constant__ CUtensorMap mapB1,
                       const SplitParams P, const Epi epi) {
     using SC = Sched<S, BITS>;
-    constexpr int NST = stage_count<S, BITS>();
+    constexpr int NST = stage_count<S, BITS, NT>();
     constexpr int A_TILE = SP_M * 32;                            // one slice, 16 K elements
     constexpr int B_TILE = ((NT * 32 + 1023) / 1024) * 1024;
     constexpr int STAGE = S * A_TILE + SC::NB * B_TILE;
@@ -830,7 +896,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     // the MMA's N follows the unit's valid table rows, rounded up to 16
     // (the B tile is always loaded whole; the MMA reads its first N rows)
     static_assert(SC::NACC * NT <= 512, "accumulators must fit in TMEM");
-    static_assert(NT % 32 == 0, "each epilogue warp owns whole 16-column chunks");
+    static_assert(NT % 48 == 0, "each epilogue warp owns whole 16-column chunks");
 
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -881,10 +947,12 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                     unsigned char* sa = smem + st * STAGE;
                     unsigned char* sb = sa + S * A_TILE;
 #pragma unroll
-                    for (int s = 0; s < S; ++s) tma_load_2d(sa + s * A_TILE, ma, &full[st], kb * SP_KB, s * arows + u.a_row0);
+                    for (int s = 0; s < S; ++s)
+                        tma_load_2d(sa + s * A_TILE, ma, &full[st], (u.k0 + kb) * SP_KB, s * arows + u.a_row0);
 #pragma unroll
                     for (int j = 0; j < SC::NB; ++j)
-                        tma_load_2d(sb + j * B_TILE, mb, &full[st], kb * SP_KB, SC::bslice(j) * brows + u.b_row0);
+                        tma_load_2d(sb + j * B_TILE, mb, &full[st], (u.k0 + kb) * SP_KB,
+                                    SC::bslice(j) * brows + u.b_row0);
                 }
             }
             // drain: wait (bounded) for the copies this thread issued
@@ -1080,7 +1148,7 @@ __global__ void wait_expiry_kernel(int* err, int* host_err, long long limit_ns) 
 
 template <int S, int BITS, int NT>
 constexpr size_t split_smem_bytes() {
-    constexpr int NST = stage_count<S, BITS>();
+    constexpr int NST = stage_count<S, BITS, NT>();
     return (size_t)NST * (S * SP_M * 32 + Sched<S, BITS>::NB * (((NT * 32 + 1023) / 1024) * 1024)) + 1024 + 256;
 }
 
@@ -1163,9 +1231,16 @@ struct ZtSplitTables {
     SliceArray dft_cos_f, dft_sin_f, leg_f, rad_f, rad_bT, leg_bT, dft_cos_b, dft_sin_b;
 };
 
+// Sliced Legendre tables of one SH plan (the 128-row operand: no scaled copies).
+struct StSplitTables {
+    int S = 0;
+    SliceArray leg_f, leg_bT;
+};
+
 // Work list of one GEMM launch, with its tensor-core work.
 struct UnitList {
     std::vector<SplitUnit> v;
+    int max_ksteps = 0;   // longest sum of a unit, in 16-wide K blocks
     double useful = 0.0;  // 2 * rows * table rows * K * products, valid tiles only
     double issued = 0.0;  // the same for full 128 x NT x 16k tiles
     DevBuf dev;
@@ -1180,6 +1255,7 @@ struct SplitState {
     }
     SliceArray op[2];           // data operands of the current stage
     std::map<std::tuple<const void*, int>, std::unique_ptr<ZtSplitTables>> zt_tables;  // per (plan, S)
+    std::map<std::tuple<const void*, int>, std::unique_ptr<StSplitTables>> st_tables;  // per (plan, S)
     std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<UnitList>> units;  // cached work lists
     DevBuf tmp;                 // FP64 staging of generated tables
     DevBuf cycles;              // role wait counters, kept when ZEST_GPU_SPLIT_CYCLES is set
@@ -1212,7 +1288,7 @@ template <class Loader>
 int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
     if (J.rows <= 0) return ZEST_GPU_OK;
     if (J.K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: K above 992");
-    if (J.bits != 7 && !(J.bits == 8 && J.K <= SL_K8MAX))
+    if (J.bits != 7 && J.bits != 8)
         return fail(ZEST_GPU_ERR_INVALID, "split path: digit width");
     J.R = slice_rows_per_block(J.K, Loader::TWO);
     J.lr = 0;
@@ -1294,6 +1370,29 @@ int get_state(zest_gpu_context* ctx, SplitState** out) {
     return ZEST_GPU_OK;
 }
 
+// SH backward: the parity sums E[p][b][m][j][c] (groups with no degree below Lm
+// read as 0) unfolded to X[b][m][lat][c], conjugated as the reference's sum_l
+// writes them: north lat = j0u + j gets E_0 + E_1, south lat = j0d - j gets
+// E_0 - E_1 (the equator of an odd grid, j0u = j0d, where E_1 = 0, is written
+// twice with the same value).
+__global__ void st_unfold_kernel(const double* __restrict__ E, double* __restrict__ X, int B, int L, int Lm, int kh,
+                                 int nlat, int j0u, int j0d) {
+    const long long n = (long long)B * L * kh * 2;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int c = int(t & 1);
+    const long long q = t >> 1;
+    const int j = int(q % kh);
+    const long long bm = q / kh;
+    const int m = int(bm % L), b = int(bm / L);
+    const double e0 = (Lm - m > 0) ? E[(((long long)b * L + m) * kh + j) * 2 + c] : 0.0;
+    const double e1 = (Lm - m - 1 > 0) ? E[((((long long)B + b) * L + m) * kh + j) * 2 + c] : 0.0;
+    const double sg = c ? -1.0 : 1.0;
+    double* x = X + (((long long)b * L + m) * nlat) * 2 + c;
+    x[(long long)(j0u + j) * 2] = sg * (e0 + e1);
+    x[(long long)(j0d - j) * 2] = sg * (e0 - e1);
+}
+
 // FP64 table generators
 __global__ void dft_table_kernel(double* __restrict__ out, int rows, int K, int ld, int N, int row_off, int col_off,
                                  int mode) {
@@ -1327,8 +1426,8 @@ __global__ void transpose_blocks_kernel(const double* __restrict__ in, const lon
 }
 
 int slice_table(zest_gpu_context* ctx, const double* src, long long rows, int K, int ld, int S, int bits,
-                SliceArray& dst) {
-    ZG_TRY(dst.ensure(rows, r16(K), S, 3));
+                SliceArray& dst, int copies = 3) {
+    ZG_TRY(dst.ensure(rows, r16(K), S, copies));
     return launch_slice(ctx->stream, RowMajorLoader{src, ld}, rows, K, S, bits, 0, dst);
 }
 
@@ -1412,6 +1511,9 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
     cudaStream_t s = ctx->stream;
     CUtensorMap ma0, ma1, mb0, mb1;
     if (B0.copies != 3 || B1.copies != 3) return fail(ZEST_GPU_ERR_INVALID, "split GEMM: table slices lack scaled copies");
+    // the FP32 level sums stay exact only up to these lengths
+    if (ul.max_ksteps * SP_KB > (BITS == 8 ? SL_K8MAX : SL_KMAX))
+        return fail(ZEST_GPU_ERR_INVALID, "split GEMM: sum too long for exact level sums");
     ZG_TRY(make_map(&ma0, A0.ptr(), A0.rows, A0.Kp, S * A0.copies, SP_M));
     ZG_TRY(make_map(&ma1, A1.ptr(), A1.rows, A1.Kp, S * A1.copies, SP_M));
     ZG_TRY(make_map(&mb0, B0.ptr(), B0.rows, B0.Kp, S * 3, NT));
@@ -1495,12 +1597,18 @@ int get_units(zest_gpu_context* ctx, std::tuple<int, int, int, int, int, int> ke
     return ZEST_GPU_OK;
 }
 
-template <class Epi>
+template <int NT = 96, class Epi>
 int run_gemm(zest_gpu_context* ctx, int S, UnitList& ul, const SliceArray& A0, const SliceArray& A1,
              const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
     const int bits = A0.bits;
     if (A1.bits != bits || B0.bits != bits || B1.bits != bits)
         return fail(ZEST_GPU_ERR_INVALID, "split GEMM: operands sliced with different digit widths");
+    if constexpr (NT != 96) {
+        // narrow tiles (SH sums: 2 x batch columns) come with 6 slices only
+        if (S != 6) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: this contraction needs 6 slices");
+        return bits == 8 ? run_gemm_t<6, 8, NT>(ctx, ul, A0, A1, B0, B1, epi)
+                         : run_gemm_t<6, 7, NT>(ctx, ul, A0, A1, B0, B1, epi);
+    }
     if (bits == 8) {
         switch (S) {
         case 4: return run_gemm_t<4, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
@@ -1517,9 +1625,10 @@ int run_gemm(zest_gpu_context* ctx, int S, UnitList& ul, const SliceArray& A0, c
 
 // tiles of a group: operand rows [a0, a0 + arows) x table rows [b0, b0 + nrows), K = kk
 void add_units(UnitList& ul, int S, int bits, long long a0, long long arows, int b0, int nrows, int NT, int kk,
-               int flags, int g) {
+               int flags, int g, int k0 = 0) {
     if (arows <= 0 || nrows <= 0 || kk <= 0) return;
     const int ksteps = r16(kk) / 16;
+    ul.max_ksteps = std::max(ul.max_ksteps, ksteps);
     const double P = products(S, bits);
     for (long long r = 0; r < arows; r += SP_M)
         for (int c = 0; c < nrows; c += NT) {
@@ -1532,6 +1641,7 @@ void add_units(UnitList& ul, int S, int bits, long long a0, long long arows, int
             u.flags = flags;
             u.g = g;
             u.aux = c;
+            u.k0 = k0 / 16;
             ul.v.push_back(u);
             ul.useful += 2.0 * u.a_rows * u.n * kk * P;
             ul.issued += 2.0 * SP_M * NT * 16.0 * ksteps * P;
@@ -1539,7 +1649,43 @@ void add_units(UnitList& ul, int S, int bits, long long a0, long long arows, int
 }
 
 // work-list keys: (stage, Lg, Lm, batch, S, pass)
-enum { WK_DFT_F = 0, WK_LEG_F, WK_RAD_F, WK_RAD_B, WK_LEG_B, WK_DFT_B, WK_DENSE };
+enum { WK_DFT_F = 0, WK_LEG_F, WK_RAD_F, WK_RAD_B, WK_LEG_B, WK_DFT_B, WK_DENSE, WK_ST_LEG_F, WK_ST_LEG_B };
+
+// SH Legendre tables in digit slices: the forward table (weights and the
+// quadrature prefactor folded in, rows (m, p, l), K = folded nodes) and the
+// backward table transposed per group (m, p) to rows = folded nodes,
+// K = degrees l = m + p + 2i.
+int build_st_tables(zest_gpu_context* ctx, SplitState* st, StPlan& plan, int S, StSplitTables** out) {
+    auto key = std::make_tuple((const void*)&plan, S);
+    auto it = st->st_tables.find(key);
+    if (it != st->st_tables.end()) {
+        *out = it->second.get();
+        return ZEST_GPU_OK;
+    }
+    cudaStream_t s = ctx->stream;
+    auto t = std::make_unique<StSplitTables>();
+    t->S = S;
+    LegTables& lg = plan.leg;
+    const int L = lg.L, kh = lg.nnodes, kl = r16((L + 1) / 2);
+    // 8-bit digits at any length: the sums are cut into K-chunks of at most 256
+    ZG_TRY(slice_table(ctx, lg.Pf.as<double>(), lg.off_h[2 * (size_t)L], kh, kh, S, 8, t->leg_f, 1));
+    std::vector<int> cnt(2 * (size_t)L);
+    for (int m = 0; m < L; ++m)
+        for (int p = 0; p < 2; ++p) cnt[2 * m + p] = (L - m - p > 0) ? (L - m - p + 1) / 2 : 0;
+    DevBuf dcnt;
+    ZG_TRY(upload(dcnt, cnt, s));
+    ZG_TRY(st->tmp.ensure((size_t)2 * L * kh * kl * sizeof(double)));
+    dim3 g1((kh * kl + 255) / 256, 2 * L);
+    transpose_blocks_kernel<<<g1, 256, 0, s>>>(lg.Pb.as<double>(), lg.off.as<long long>(), dcnt.as<int>(), kh, kl,
+                                               st->tmp.as<double>());
+    ZG_TRY(launch_check("transpose_blocks_kernel"));
+    ZG_TRY(slice_table(ctx, st->tmp.as<double>(), (long long)2 * L * kh, kl, kl, S, 8, t->leg_bT, 1));
+    ZG_CUDA_TRY(cudaStreamSynchronize(s));
+    st->tmp.release();  // several GB at high orders; rebuilt on demand
+    *out = t.get();
+    st->st_tables.emplace(key, std::move(t));
+    return ZEST_GPU_OK;
+}
 
 }  // namespace
 
@@ -1756,6 +1902,135 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
                             EpiDftBwdSin{grids, Cs, C, N, Lg, sh.size()}));
         }
+    }
+    return split_finish(ctx);
+}
+
+// ===========================================================================
+// Split-precision SH Legendre sums.  The table is the 128-row operand: with
+// 2 x batch data rows per order m the data could not fill a row tile.  The
+// data (the folded spectra, or the coefficients) is the scaled-copy operand,
+// sliced per call; its 2 x batch rows are the columns, in tiles of 48 (or 96
+// for batches above 24).
+// ===========================================================================
+namespace {
+template <class F>
+int st_with_nt(int batch, F&& f) {
+    return 2 * batch <= 48 ? f(std::integral_constant<int, 48>{}) : f(std::integral_constant<int, 96>{});
+}
+// SH sums always use 8-bit digits and 6 slices; sums longer than 256 run as
+// K-chunks of at most 256 whose FP64 results are added (the later chunks
+// through the read-modify-write epilogues).
+constexpr int ST_KCHUNK = SL_K8MAX;
+template <int NT, class Epi>
+int run_gemm_st(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A, const SliceArray& B0, const SliceArray& B1,
+                const Epi& epi) {
+    if (A.bits != 8 || B0.bits != 8 || B1.bits != 8)
+        return fail(ZEST_GPU_ERR_INVALID, "split SH sums: operands must have 8-bit digits");
+    return run_gemm_t<6, 8, NT>(ctx, ul, A, A, B0, B1, epi);
+}
+}  // namespace
+
+int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* X,
+                     double* coeffs, long long csz) {
+    const int S = ctx->slices;
+    if (S != 6) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split SH transforms need 6 slices");
+    cudaStream_t s = ctx->stream;
+    SplitState* st;
+    ZG_TRY(get_state(ctx, &st));
+    const int kh = plan.leg.nnodes, nlat = int(plan.sh.nlat);
+    if (kh > SL_KMAX || (Lg + 1) / 2 > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: order too high");
+    StSplitTables* tb;
+    ZG_TRY(build_st_tables(ctx, st, plan, S, &tb));
+    const int bits = 8;
+    const long long per_m = 2LL * batch, rows = (long long)Lm * per_m;
+    ZG_TRY(st->op[0].ensure(rows, r16(kh), S, 3));
+    ZG_TRY(st->op[1].ensure(rows, r16(kh), S, 3));
+    {
+        StageScope sc(ctx, ST_SPLIT_SLICE);
+        LegFwdLoader ld{X, batch, Lg, nlat, 2, plan.leg.j0u, plan.leg.j0d};
+        ZG_TRY(launch_slice2(s, ld, rows, kh, kh, 0, S, bits, SL_FOLD, st->op[0], st->op[1]));
+    }
+    const int nchunk = (kh + ST_KCHUNK - 1) / ST_KCHUNK;
+    for (int ch = 0; ch < nchunk; ++ch) {
+        const int k0 = ch * ST_KCHUNK, kk = std::min(ST_KCHUNK, kh - k0);
+        ZG_TRY(st_with_nt(batch, [&](auto nt) -> int {
+            constexpr int NT = decltype(nt)::value;
+            UnitList* u;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_ST_LEG_F), Lg, Lm, batch, S, int(plan.sh.latlon) + 2 * ch),
+                             [&](UnitList& ul) {
+                                 for (int m = 0; m < Lm; ++m)
+                                     for (int p = 0; p < 2; ++p) {
+                                         const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
+                                         add_units(ul, S, bits, plan.leg.off_h[2 * m + p], cnt, int(m * per_m),
+                                                   int(per_m), NT, kk, (p << 1) | (p << 2), m, k0);
+                                     }
+                             },
+                             &u));
+            if (ch == 0)
+                return run_gemm_st<NT>(ctx, *u, tb->leg_f, st->op[0], st->op[1],
+                                       EpiStLegFwd<false>{coeffs, csz, plan.leg.L});
+            return run_gemm_st<NT>(ctx, *u, tb->leg_f, st->op[0], st->op[1],
+                                   EpiStLegFwd<true>{coeffs, csz, plan.leg.L});
+        }));
+    }
+    return split_finish(ctx);
+}
+
+int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* coeffs,
+                      long long csz, double* X) {
+    const int S = ctx->slices;
+    if (S != 6) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split SH transforms need 6 slices");
+    cudaStream_t s = ctx->stream;
+    SplitState* st;
+    ZG_TRY(get_state(ctx, &st));
+    const int kh = plan.leg.nnodes, nlat = int(plan.sh.nlat), kl = r16((Lg + 1) / 2);
+    if (kh > SL_KMAX || kl > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: order too high");
+    StSplitTables* tb;
+    ZG_TRY(build_st_tables(ctx, st, plan, S, &tb));
+    const int bits = 8;
+    const long long per_m = 2LL * batch, rows = (long long)Lm * per_m;
+    ZG_TRY(st->op[0].ensure(rows, kl, S, 3));
+    ZG_TRY(st->op[1].ensure(rows, kl, S, 3));
+    {
+        StageScope sc(ctx, ST_SPLIT_SLICE);
+        ZG_TRY(launch_slice2(s, StLegBwdLoader{coeffs, csz, batch, Lm}, rows, (Lm + 1) / 2, Lm / 2, 0, S, bits,
+                             SL_PAIR, st->op[0], st->op[1]));
+    }
+    // parity sums E[p][b][m][j][c]; groups with no degree below Lm are not
+    // written and the unfolding reads them as 0
+    ZG_TRY(ctx->s1.ensure((size_t)2 * batch * Lg * kh * 2 * sizeof(double)));
+    double* E = ctx->s1.as<double>();
+    const int nchunk = ((Lm + 1) / 2 + ST_KCHUNK - 1) / ST_KCHUNK;
+    for (int ch = 0; ch < nchunk; ++ch) {
+        const int k0 = ch * ST_KCHUNK;
+        ZG_TRY(st_with_nt(batch, [&](auto nt) -> int {
+            constexpr int NT = decltype(nt)::value;
+            UnitList* u;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_ST_LEG_B), Lg, Lm, batch, S, int(plan.sh.latlon) + 2 * ch),
+                             [&](UnitList& ul) {
+                                 for (int m = 0; m < Lm; ++m)
+                                     for (int p = 0; p < 2; ++p) {
+                                         const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
+                                         // the degrees of this chunk: i in [k0, min(cnt, k0 + 256))
+                                         const int kk = std::min(cnt - k0, ST_KCHUNK);
+                                         add_units(ul, S, bits, (long long)(2 * m + p) * kh, kh, int(m * per_m),
+                                                   int(per_m), NT, kk, (p << 1) | (p << 2), m, k0);
+                                     }
+                             },
+                             &u));
+            if (ch == 0)
+                return run_gemm_st<NT>(ctx, *u, tb->leg_bT, st->op[0], st->op[1],
+                                       EpiStLegBwdE<false>{E, batch, Lg, kh});
+            return run_gemm_st<NT>(ctx, *u, tb->leg_bT, st->op[0], st->op[1], EpiStLegBwdE<true>{E, batch, Lg, kh});
+        }));
+    }
+    {
+        StageScope sc(ctx, ST_SPLIT_SLICE);
+        const long long n = (long long)batch * Lg * kh * 2;
+        st_unfold_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(E, X, batch, Lg, Lm, kh, nlat, plan.leg.j0u,
+                                                                  plan.leg.j0d);
+        ZG_TRY(launch_check("st_unfold_kernel"));
     }
     return split_finish(ctx);
 }

@@ -1,5 +1,5 @@
 // Split-precision (BF16 fixed-point slices on tcgen05) form of the Zernike
-// contractions; see split.cu.
+// contractions and of the SH Legendre sums; see split.cu.
 #pragma once
 
 struct zest_gpu_context;
@@ -7,6 +7,7 @@ struct zest_gpu_context;
 namespace zgpu {
 
 struct ZtPlan;
+struct StPlan;
 struct SplitState;  // per-context state of the split path, defined in split.cu
 void destroy_split(SplitState* s);
 struct SplitDeleter {
@@ -19,6 +20,13 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
                      double* coeffs);
 int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int Lm, int batch, const double* coeffs,
                       double* grids);
+// SH Legendre sums in split precision (6 slices): the folded spectra X
+// [b][m][lat][2] (after the forward FFT) -> coefficients of degrees < Lm, and
+// coefficients -> X (before the inverse FFT), as the FP64 sums do.
+int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* X,
+                     double* coeffs, long long csz);
+int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* coeffs,
+                      long long csz, double* X);
 // C = A B^T (A: M x K, B: N x K, C: M x N, row-major FP64 device buffers)
 int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A, const double* B, double* C);
 // BF16 tensor-core flops of the split GEMM launches since the last reset

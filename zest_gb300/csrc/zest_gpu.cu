@@ -461,6 +461,7 @@ int st_forward_dev(zest_gpu_context* ctx, int sn, int sp, int layout, int Lg, in
         else
             ZG_TRY(launch_rfft_fwd(s, *fft, grids, sh.size(), sh.nlat, 1, int(sh.nlat), Lg, batch, 0, X));
     }
+    if (ctx->precision == ZEST_PRECISION_SPLIT) return split_st_forward(ctx, *plan, Lg, Lm, batch, X, coeffs, csz);
     LegMeta lm;
     lm.P = plan->leg.Pf.as<double>();
     lm.off = plan->leg.off.as<long long>();
@@ -492,6 +493,13 @@ int st_backward_dev(zest_gpu_context* ctx, int sn, int sp, int layout, int Le, i
     ZG_TRY(get_fft(ctx, int(sh.nlon), &fft));
     ZG_TRY(ctx->s0.ensure((size_t)batch * Lg * sh.nlat * 2 * sizeof(double)));
     double* X = ctx->s0.as<double>();
+    if (ctx->precision == ZEST_PRECISION_SPLIT) {
+        ZG_TRY(split_st_backward(ctx, *plan, Lg, Lm, batch, coeffs, csz, X));
+        StageScope sc(ctx, ST_FFT_INV);
+        if (layout == ZEST_LAYOUT_LATLON)
+            return launch_rfft_inv(s, *fft, X, int(sh.nlat), Lg, batch, 1, grids, sh.size(), 1, sh.nlon);
+        return launch_rfft_inv(s, *fft, X, int(sh.nlat), Lg, batch, 0, grids, sh.size(), sh.nlat, 1);
+    }
     LegMeta lm;
     lm.P = plan->leg.Pb.as<double>();
     lm.off = plan->leg.off.as<long long>();
