@@ -53,8 +53,9 @@ def rand_zt(rng, L, power=1.5, batch=1):
 
 @pytest.mark.parametrize("M,N,K", [(128, 80, 16), (1, 1, 1), (129, 81, 17), (300, 200, 208), (1000, 37, 256)])
 def test_split_gemm_exact_on_integers(split, M, N, K):
-    # integers with |x| < 2^20 are represented exactly by 6 slices of 7 bits,
-    # and the level sums are exact: the product must be exact
+    # integers with |x| < 2^20 are represented exactly by 6 slices of 8 bits
+    # (the dropped products involve only zero digits), and the level sums are
+    # exact: the product must be exact
     rng = np.random.default_rng(M + N + K)
     A = rng.integers(-(1 << 19), 1 << 19, size=(M, K)).astype(np.float64)
     B = rng.integers(-(1 << 19), 1 << 19, size=(N, K)).astype(np.float64)
@@ -81,13 +82,12 @@ def test_split_gemm_random(ctx, S):
 
 
 def split_model(A, B, S):
-    """Integer model of the split product: balanced base-2^bits digits of the
-    row-scaled operands (8-bit digits for K <= 256, 7-bit above), the levels
-    kept by the kernel (0..S-1 with 8-bit digits, 0..S with 7-bit) summed
-    exactly, scaled by 2^(eA + eB - bits (top level + 2))."""
+    """Integer model of the split product: balanced base-256 digits of the
+    row-scaled operands, levels 0..S-1 summed exactly over K-chunks of at most
+    256 terms, each chunk scaled by 2^(eA + eB - 8 (S + 1)) and the chunks
+    added in FP64, first to last."""
     K = A.shape[1]
-    bits = 8 if K <= 256 else 7
-    top = S - 1 if bits == 8 else S
+    bits, top = 8, S - 1
     base = 1 << bits
 
     def digits(X):
@@ -105,23 +105,28 @@ def split_model(A, B, S):
         return d, e
     da, ea = digits(A)
     db, eb = digits(B)
-    T = np.zeros((A.shape[0], B.shape[0]), dtype=object)
-    for lev in range(top + 1):
-        acc = np.zeros((A.shape[0], B.shape[0]), dtype=np.int64)
-        for s in range(S):
-            t = lev - s
-            if 0 <= t < S:
-                acc += da[s] @ db[t].T
-        T = T * base + acc.astype(object)
-    return T.astype(float) * np.exp2(ea[:, None] + eb[None, :] - bits * (top + 2))
+    scale = np.exp2(ea[:, None] + eb[None, :] - bits * (top + 2))
+    out = np.zeros((A.shape[0], B.shape[0]))
+    for k0 in range(0, K, 256):
+        ks = slice(k0, min(K, k0 + 256))
+        T = np.zeros((A.shape[0], B.shape[0]), dtype=object)
+        for lev in range(top + 1):
+            acc = np.zeros((A.shape[0], B.shape[0]), dtype=np.int64)
+            for s in range(S):
+                t = lev - s
+                if 0 <= t < S:
+                    acc += da[s][:, ks] @ db[t][:, ks].T
+            T = T * base + acc.astype(object)
+        out = out + T.astype(float) * scale
+    return out
 
 
-@pytest.mark.parametrize("K", [1, 16, 33, 64, 208, 256, 257, 400])
+@pytest.mark.parametrize("K", [1, 16, 33, 64, 208, 256, 257, 400, 992])
 def test_split_gemm_matches_integer_model(split, K):
     # The kernel sums levels 0..3 exactly and levels 4 and up in one shared
     # FP32 accumulator, whose products weigh at most 2^-28 of level 0: the
     # kernel must agree with the all-integer model to 1e-13 of the largest
-    # entry, on both sides of the 8-bit/7-bit digit switch at K = 256.
+    # entry, with one K-chunk (K <= 256) and with several (257, 400, 992).
     rng = np.random.default_rng(100 + K)
     A = rng.normal(size=(130, K)) * np.exp(rng.normal(size=(130, 1)))
     B = rng.normal(size=(70, K))
@@ -199,3 +204,22 @@ def test_split_zt_full_size_error_budget(ctx):
         assert relmax(gs[b * n:(b + 1) * n], g64[b * n:(b + 1) * n]) < SPLIT_TOL
         k = f64.size // batch
         assert relmax(fs[b * k:(b + 1) * k], f64[b * k:(b + 1) * k]) < SPLIT_TOL
+
+
+@pytest.mark.parametrize("L", [300, 520])
+def test_split_zt_long_sums_in_chunks(ctx, L):
+    # orders above 254: the DFT and radial sums (and above 510 the Legendre
+    # sums) exceed 256 terms and run as K-chunks; the 1e-11 bound must hold
+    import zest_gb300
+    rng = np.random.default_rng(L)
+    c = rand_zt(rng, L, batch=1).ravel()
+    g64 = ctx.zt_backward(c, L)
+    f64 = ctx.zt_forward(g64, L)
+    ctx.set_precision(zest_gb300.PRECISION_SPLIT, 6)
+    try:
+        gs = ctx.zt_backward(c, L)
+        fs = ctx.zt_forward(g64, L)
+    finally:
+        ctx.set_precision(zest_gb300.PRECISION_FP64)
+    assert relmax(gs, g64) < SPLIT_TOL
+    assert relmax(fs, f64) < SPLIT_TOL

@@ -4,8 +4,8 @@
 Tolerance: 1e-11 relative max-norm per item, the bound the split form is
 built to.  Covered: both layouts (including an odd LatLon grid, whose middle
 latitude the reference counts twice), all four conventions, truncation in
-both directions, 8-bit digits (short sums) and 7-bit digits (folded node
-counts above 256, order 600), narrow column tiles (2 x batch <= 48) and wide
+both directions, single sums (up to 256 terms) and K-chunked ones (folded
+node counts above 256, order 600), narrow column tiles (2 x batch <= 48) and wide
 ones (batch 30), and the round trip at order 1024 (the C2 configuration's
 order) against the input coefficients."""
 import numpy as np

@@ -225,12 +225,16 @@ __device__ __forceinline__ int biased_exp(double x) {
 // ===========================================================================
 namespace {
 
-constexpr int SL_KMAX = 992;  // K bound of exact level sums (balanced 7-bit digits)
+constexpr int SL_KMAX = 992;  // longest operand row the slicing stages (and longest sum)
 constexpr int SL_K8MAX = 256; // K bound of exact level sums with balanced 8-bit digits
 constexpr int SL_UNROLL = 8;  // independent loads per thread in the staging loops
 
 // digit width of a contraction of length K: 8 bits while the exact levels stay exact
-inline int digit_bits(int K) { return K <= SL_K8MAX ? 8 : 7; }
+// Digits are 8 bits wide at any length: sums longer than SL_K8MAX terms run
+// as K-chunks of at most SL_K8MAX whose FP64 results are added.
+inline int digit_bits(int) { return 8; }
+constexpr int KCHUNK = SL_K8MAX;
+inline int nchunks(int K) { return (K + KCHUNK - 1) / KCHUNK; }
 
 // Rows per slicing block: a power of two (so that in row-fast loops every
 // thread stays on one row), up to 32 rows (longer contiguous runs in the
@@ -633,18 +637,27 @@ namespace {
 
 // Epilogues map (operand row, table row) of a tile to an output location.
 // row(u, r) is evaluated once per row and tile; store() once per element.
+// ACC = true: a later K-chunk of the sum, whose value is added to what the
+// earlier chunks stored (load() reads it back; every epilogue is linear in v).
 // RMW epilogues expose load() so that the old values are fetched before the
 // accumulators are read (hiding the memory latency).
+template <bool ACC = false>
 struct EpiDense {  // C[row][b_row0 + n] (utility GEMM)
-    static constexpr bool RMW = false;
+    static constexpr bool RMW = ACC;
+    static constexpr bool CHUNK = ACC;
     double* C;
     long long ldc;
     struct Row { double* p; };
     __device__ Row row(const SplitUnit& u, int r) const { return Row{C + (long long)r * ldc + u.b_row0}; }
-    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double*) const { R.p[n] = v; }
+    __device__ void load(const Row& R, int n, double* old) const { old[0] = R.p[n]; }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        R.p[n] = ACC ? old[0] + v : v;
+    }
 };
+template <bool ACC = false>
 struct EpiDftFwd {  // rows (b, col): conj X_m -> G[b][m][col][re, im]
-    static constexpr bool RMW = false;
+    static constexpr bool RMW = ACC;
+    static constexpr bool CHUNK = ACC;
     double* G;
     int C, L;
     struct Row { double* p; };  // &G[b][m0][col][re or im]
@@ -654,67 +667,83 @@ struct EpiDftFwd {  // rows (b, col): conj X_m -> G[b][m][col][re, im]
         const int m0 = u.aux + sin;
         return Row{G + (((long long)b * L + m0) * C + col) * 2 + sin};
     }
-    __device__ void store(const Row& R, const SplitUnit& u, int n, double v, const double*) const {
+    __device__ void load(const Row& R, int n, double* old) const { old[0] = R.p[(long long)n * C * 2]; }
+    __device__ void store(const Row& R, const SplitUnit& u, int n, double v, const double* old) const {
         double* g = R.p + (long long)n * C * 2;
-        g[0] = v;
-        if (((u.flags >> 1) & 1) == 0 && u.aux + n == 0) g[1] = 0.0;  // Im X_0 = 0
+        g[0] = ACC ? old[0] + v : v;
+        if (!ACC && ((u.flags >> 1) & 1) == 0 && u.aux + n == 0) g[1] = 0.0;  // Im X_0 = 0
     }
 };
+template <bool ACC = false>
 struct EpiLegFwd {  // rows (m, b, kc) -> flm[tri(l,m)][b][kc], l = m + p + 2 (aux + n)
-    static constexpr bool RMW = false;
+    static constexpr bool RMW = ACC;
+    static constexpr bool CHUNK = ACC;
     double* flm;
     int B, nr2;
-    struct Row { double* p; int m; };
+    struct Row { double* p; int l0; };
     __device__ Row row(const SplitUnit& u, int r) const {
         const int m = u.g, p = (u.flags >> 2) & 1;
         const long long local = r - (long long)m * B * nr2;
         const int l0 = m + p + 2 * u.aux;
-        return Row{flm + (tri_idx(l0, m) * B) * nr2 + local, m};
+        return Row{flm + (tri_idx(l0, m) * B) * nr2 + local, l0};
     }
-    __device__ void store(const Row& R, const SplitUnit& u, int n, double v, const double*) const {
-        // tri(l + 2n, m) - tri(l, m) = n (2 l + 2 n + 1), l = l0
-        const int p = (u.flags >> 2) & 1;
-        const long long l0 = R.m + p + 2 * u.aux;
-        const long long dt = (long long)n * (2 * l0 + 2 * n + 1);
-        R.p[dt * B * nr2] = v;
+    // tri(l0 + 2n, m) - tri(l0, m) = n (2 l0 + 2 n + 1)
+    __device__ double* at(const Row& R, int n) const {
+        return R.p + (long long)n * (2LL * R.l0 + 2 * n + 1) * B * nr2;
+    }
+    __device__ void load(const Row& R, int n, double* old) const { old[0] = *at(R, n); }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        *at(R, n) = ACC ? old[0] + v : v;
     }
 };
+template <bool ACC = false>
 struct EpiRadFwd {  // rows ((tri(l,m) B + b) 2 + c) -> coeffs[b][zidx(n,l,m)][c]
-    static constexpr bool RMW = false;
+    static constexpr bool RMW = ACC;
+    static constexpr bool CHUNK = ACC;
     double* coeffs;
     int B;
     long long cs;
-    struct Row { double* p; long long zl0; };
+    struct Row { double* p; long long zl0; int l; };
     __device__ Row row(const SplitUnit& u, int r) const {
         const int l = u.g;
         const int tb = r >> 1, c = r & 1;
         const int t = tb / B, b = tb - t * B;
         const int m = t - int(tri_idx(l, 0));
         const long long n0 = l + 2 * u.aux;
-        return Row{coeffs + b * cs + 2 * m + c, n0};
+        return Row{coeffs + b * cs + 2 * m + c, n0, l};
     }
-    __device__ void store(const Row& R, const SplitUnit& u, int n, double v, const double*) const {
+    __device__ double* at(const Row& R, int n) const {
         const long long nn = R.zl0 + 2 * n;
-        const int l = u.g;
-        R.p[2 * ((nn + 1) * (nn + 3) * (2 * nn + 1) / 24 + ((l * l) >> 2))] = v;
+        return R.p + 2 * ((nn + 1) * (nn + 3) * (2 * nn + 1) / 24 + ((R.l * R.l) >> 2));
+    }
+    __device__ void load(const Row& R, int n, double* old) const { old[0] = *at(R, n); }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        *at(R, n) = ACC ? old[0] + v : v;
     }
 };
+template <bool ACC = false>
 struct EpiRadBwd {  // rows ((t B + b) 2 + c) -> flm[(t B + b)][k][c]
-    static constexpr bool RMW = false;
+    static constexpr bool RMW = ACC;
+    static constexpr bool CHUNK = ACC;
     double* flm;
     int nr;
     struct Row { double* p; };
     __device__ Row row(const SplitUnit& u, int r) const {
         return Row{flm + ((long long)(r >> 1) * nr + u.aux) * 2 + (r & 1)};
     }
-    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double*) const { R.p[2 * n] = v; }
+    __device__ void load(const Row& R, int n, double* old) const { old[0] = R.p[2 * n]; }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        R.p[2 * n] = ACC ? old[0] + v : v;
+    }
 };
 // rows (m, b, kc) -> E_p[b][m][j'][kc] (conjugated): the parity-p Legendre
 // sum at folded node j'; the north node j0u + j' of the spectrum is E_0 + E_1
 // and the south node j0d - j' is E_0 - E_1, formed by the DFT slicing that
 // reads them (no read-modify-write here).
+template <bool ACC = false>
 struct EpiLegBwdE {
-    static constexpr bool RMW = false;
+    static constexpr bool RMW = ACC;
+    static constexpr bool CHUNK = ACC;
     double* E;
     int B, L, kh, nr2;
     struct Row { double* p; double sg; };
@@ -724,9 +753,9 @@ struct EpiLegBwdE {
         const int b = int(local / nr2), kc = int(local - (long long)b * nr2);
         return Row{E + ((((long long)par * B + b) * L + m) * kh + u.aux) * nr2 + kc, (kc & 1) ? -1.0 : 1.0};
     }
-    __device__ void load(const Row&, int, double*) const {}
-    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double*) const {
-        R.p[(long long)n * nr2] = R.sg * v;
+    __device__ void load(const Row& R, int n, double* old) const { old[0] = R.p[(long long)n * nr2]; }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        R.p[(long long)n * nr2] = ACC ? old[0] + R.sg * v : R.sg * v;
     }
 };
 
@@ -739,6 +768,7 @@ struct EpiLegBwdE {
 template <bool ACC>
 struct EpiStLegFwd {
     static constexpr bool RMW = ACC;
+    static constexpr bool CHUNK = ACC;
     double* coeffs;
     long long cs;
     int L;
@@ -759,6 +789,7 @@ struct EpiStLegFwd {
 template <bool ACC>
 struct EpiStLegBwdE {
     static constexpr bool RMW = ACC;
+    static constexpr bool CHUNK = ACC;
     double* E;
     int B, L, kh;
     struct Row { double* p; };
@@ -778,25 +809,31 @@ struct EpiStLegBwdE {
 // Inverse DFT, rows (b, col).  The cos pass writes x_0 = C_0 to the grid and
 // C_i (i >= 1) to the scratch Cs[b][i][col]; the sin pass reads C_i once and
 // writes x_i = C_i + S_i and x_{N-i} = C_i - S_i.
+template <bool ACC = false>
 struct EpiDftBwdCos {
-    static constexpr bool RMW = false;
+    static constexpr bool RMW = ACC;
+    static constexpr bool CHUNK = ACC;
     double* grid;
     double* Cs;
     int C, N, L;
     long long gsz;
-    struct Row { double* x; double* c; };
+    struct Row { double* x; double* c; int aux; };
     __device__ Row row(const SplitUnit& u, int r) const {
         const long long b = r / C, col = r - b * C;
-        return Row{grid + b * gsz + col, Cs + (b * L + u.aux) * C + col};
+        return Row{grid + b * gsz + col, Cs + (b * L + u.aux) * C + col, u.aux};
     }
-    __device__ void load(const Row&, int, double*) const {}
-    __device__ void store(const Row& R, const SplitUnit& u, int n, double v, const double*) const {
-        if (u.aux + n == 0) R.x[0] = v;
-        else R.c[(long long)n * C] = v;
+    __device__ double* at(const Row& R, int n) const { return R.aux + n == 0 ? R.x : R.c + (long long)n * C; }
+    __device__ void load(const Row& R, int n, double* old) const { old[0] = *at(R, n); }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
+        *at(R, n) = ACC ? old[0] + v : v;
     }
 };
+// The first chunk reads the finished cos sums C_i and writes x_i = C_i + S_i,
+// x_{N-i} = C_i - S_i; later chunks add their S_i to x_i and subtract it from x_{N-i}.
+template <bool ACC = false>
 struct EpiDftBwdSin {
     static constexpr bool RMW = true;
+    static constexpr bool CHUNK = ACC;
     double* grid;
     const double* Cs;
     int C, N, L;
@@ -806,11 +843,19 @@ struct EpiDftBwdSin {
         const long long b = r / C, col = r - b * C;
         return Row{grid + b * gsz + col, Cs + (b * L + u.aux + 1) * C + col, u.aux + 1};
     }
-    __device__ void load(const Row& R, int n, double* old) const { old[0] = R.c[(long long)n * C]; }
+    __device__ void load(const Row& R, int n, double* old) const {
+        if (ACC) {
+            const int i = R.i0 + n;
+            old[0] = R.x[(long long)i * C];
+            old[1] = R.x[(long long)(N - i) * C];
+        } else {
+            old[0] = old[1] = R.c[(long long)n * C];
+        }
+    }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
         const int i = R.i0 + n;
         R.x[(long long)i * C] = old[0] + v;
-        R.x[(long long)(N - i) * C] = old[0] - v;
+        R.x[(long long)(N - i) * C] = old[1] - v;
     }
 };
 
@@ -1603,22 +1648,17 @@ int run_gemm(zest_gpu_context* ctx, int S, UnitList& ul, const SliceArray& A0, c
     const int bits = A0.bits;
     if (A1.bits != bits || B0.bits != bits || B1.bits != bits)
         return fail(ZEST_GPU_ERR_INVALID, "split GEMM: operands sliced with different digit widths");
-    if constexpr (NT != 96) {
-        // narrow tiles (SH sums: 2 x batch columns) come with 6 slices only
-        if (S != 6) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: this contraction needs 6 slices");
-        return bits == 8 ? run_gemm_t<6, 8, NT>(ctx, ul, A0, A1, B0, B1, epi)
-                         : run_gemm_t<6, 7, NT>(ctx, ul, A0, A1, B0, B1, epi);
-    }
-    if (bits == 8) {
+    if (bits != 8) return fail(ZEST_GPU_ERR_INVALID, "split GEMM: operands need 8-bit digits");
+    if constexpr (NT != 96 || Epi::CHUNK) {
+        // narrow tiles (SH sums) and the later K-chunks of long sums come with 6 slices only
+        if (S != 6) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: sums longer than 256 terms need 6 slices");
+        return run_gemm_t<6, 8, NT>(ctx, ul, A0, A1, B0, B1, epi);
+    } else {
         switch (S) {
         case 4: return run_gemm_t<4, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
         case 5: return run_gemm_t<5, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
         case 6: return run_gemm_t<6, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
         }
-    } else {
-        // 7-bit digits (contractions longer than 256) come with 6 slices only
-        if (S == 6) return run_gemm_t<6, 7, 96>(ctx, ul, A0, A1, B0, B1, epi);
-        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: contractions longer than 256 need 6 slices");
     }
     return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path supports 4..6 slices");
 }
@@ -1744,14 +1784,21 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
             ZG_TRY(launch_slice2(s, DftFwdLoader{grids, sh.size(), C, N}, rows, Lg, Lg - 1, 1, S, bits, SL_FOLD,
                                  st->op[0], st->op[1]));
         }
-        UnitList* u;
-        ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
-            for (long long r = 0; r < rows; r += SP_M) {
-                add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lm, NT, Lg, 0, 0);
-                if (Lm > 1) add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lm - 1, NT, Lg - 1, 1 | 2, 0);
-            }
-        }, &u));
-        ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_f, tb->dft_sin_f, EpiDftFwd{G, C, Lg}));
+        for (int ch = 0; ch < nchunks(Lg); ++ch) {
+            const int k0 = ch * KCHUNK;
+            UnitList* u;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_F), Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+                for (long long r = 0; r < rows; r += SP_M) {
+                    const long long rr = std::min<long long>(SP_M, rows - r);
+                    add_units(ul, S, bits, r, rr, 0, Lm, NT, std::min(KCHUNK, Lg - k0), 0, 0, k0);
+                    if (Lm > 1) add_units(ul, S, bits, r, rr, 0, Lm - 1, NT, std::min(KCHUNK, Lg - 1 - k0), 1 | 2, 0, k0);
+                }
+            }, &u));
+            if (ch == 0)
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_f, tb->dft_sin_f, EpiDftFwd<false>{G, C, Lg}));
+            else
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_f, tb->dft_sin_f, EpiDftFwd<true>{G, C, Lg}));
+        }
     }
     // ---- Legendre (folded over the equator) ----
     {
@@ -1765,16 +1812,22 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
             LegFwdLoader ld{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d};
             ZG_TRY(launch_slice2(s, ld, rows, kh, kh, 0, S, bits, SL_FOLD, st->op[0], st->op[1]));
         }
-        UnitList* u;
-        ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
-            for (int m = 0; m < Lm; ++m)
-                for (int p = 0; p < 2; ++p) {
-                    const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
-                    add_units(ul, S, bits, (long long)m * per_m, per_m, int(plan.leg.off_h[2 * m + p]), cnt, NT, kh,
-                              p | (p << 2), m);
-                }
-        }, &u));
-        ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd{flm, batch, nr2}));
+        for (int ch = 0; ch < nchunks(kh); ++ch) {
+            const int k0 = ch * KCHUNK;
+            UnitList* u;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_F), Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+                for (int m = 0; m < Lm; ++m)
+                    for (int p = 0; p < 2; ++p) {
+                        const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
+                        add_units(ul, S, bits, (long long)m * per_m, per_m, int(plan.leg.off_h[2 * m + p]), cnt, NT,
+                                  std::min(KCHUNK, kh - k0), p | (p << 2), m, k0);
+                    }
+            }, &u));
+            if (ch == 0)
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd<false>{flm, batch, nr2}));
+            else
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd<true>{flm, batch, nr2}));
+        }
     }
     // ---- radial ----
     {
@@ -1785,13 +1838,19 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
             StageScope sc(ctx, ST_SPLIT_SLICE);
             ZG_TRY(launch_slice(s, RadFwdLoader{flm, nr}, rows, nr, S, bits, 0, st->op[0]));
         }
-        UnitList* u;
-        ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_F), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
-            for (int l = 0; l < Lm; ++l)
-                add_units(ul, S, bits, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, int(plan.rad.off_h[l]),
-                          (Lm - l + 1) / 2, NT, nr, 0, l);
-        }, &u));
-        ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd{coeffs, batch, csz}));
+        for (int ch = 0; ch < nchunks(nr); ++ch) {
+            const int k0 = ch * KCHUNK;
+            UnitList* u;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_F), Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+                for (int l = 0; l < Lm; ++l)
+                    add_units(ul, S, bits, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2,
+                              int(plan.rad.off_h[l]), (Lm - l + 1) / 2, NT, std::min(KCHUNK, nr - k0), 0, l, k0);
+            }, &u));
+            if (ch == 0)
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd<false>{coeffs, batch, csz}));
+            else
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd<true>{coeffs, batch, csz}));
+        }
     }
     return split_finish(ctx);
 }
@@ -1829,13 +1888,19 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             ZG_TRY(launch_slice(s, RadBwdLoader{coeffs, csz, batch, Lm}, rows, (Lm + 1) / 2, S, bits, 0,
                                 st->op[0]));
         }
-        UnitList* u;
-        ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_B), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
-            for (int l = 0; l < Lm; ++l)
-                add_units(ul, S, bits, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, l * nr, nr, NT,
-                          (Lm - l + 1) / 2, 0, l);
-        }, &u));
-        ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd{flm, nr}));
+        for (int ch = 0; ch < nchunks((Lm + 1) / 2); ++ch) {
+            const int k0 = ch * KCHUNK;
+            UnitList* u;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_B), Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+                for (int l = 0; l < Lm; ++l)
+                    add_units(ul, S, bits, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, l * nr, nr, NT,
+                              std::min(KCHUNK, (Lm - l + 1) / 2 - k0), 0, l, k0);
+            }, &u));
+            if (ch == 0)
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<false>{flm, nr}));
+            else
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<true>{flm, nr}));
+        }
     }
     // ---- Legendre: flm -> G (north/south unfold; parity 1 read-modify-write) ----
     {
@@ -1860,17 +1925,24 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             ZG_CUDA_TRY(cudaMemset2DAsync(E + (size_t)batch * eblock + (size_t)(Lm - 1) * kh * nr2,
                                           eblock * sizeof(double), 0, (size_t)(Lg - Lm + 1) * row, batch, s));
         }
-        for (int p = 0; p < 2; ++p) {
+        for (int p = 0; p < 2; ++p)
+            for (int ch = 0; ch < nchunks((Lm + 1) / 2); ++ch) {
+            const int k0 = ch * KCHUNK;
             UnitList* u;
-            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_B), Lg, Lm, batch, S, p), [&](UnitList& ul) {
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_B), Lg, Lm, batch, S, p + 8 * ch), [&](UnitList& ul) {
                 for (int m = 0; m < Lm; ++m) {
                     const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
                     if (cnt == 0) continue;
-                    add_units(ul, S, bits, (long long)m * per_m, per_m, (2 * m + p) * kh, kh, NT, cnt, p | (p << 2), m);
+                    add_units(ul, S, bits, (long long)m * per_m, per_m, (2 * m + p) * kh, kh, NT,
+                              std::min(KCHUNK, cnt - k0), p | (p << 2), m, k0);
                 }
             }, &u));
-            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
-                            EpiLegBwdE{E, batch, Lg, kh, nr2}));
+            if (ch == 0)
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
+                                EpiLegBwdE<false>{E, batch, Lg, kh, nr2}));
+            else
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
+                                EpiLegBwdE<true>{E, batch, Lg, kh, nr2}));
         }
     }
     // ---- longitude: inverse real DFT, cos pass then sin read-modify-write pass ----
@@ -1884,23 +1956,38 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             ZG_TRY(launch_slice2(s, DftBwdLoader{E, Lg, C, nr, kh, plan.leg.j0u, plan.leg.j0d, batch}, rows, Lg,
                                  Lg - 1, 1, S, bits, SL_PAIR, st->op[0], st->op[1]));
         }
-        UnitList* u;
-        ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 0), [&](UnitList& ul) {
-            for (long long r = 0; r < rows; r += SP_M)
-                add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, Lg, 0, 0);
-        }, &u));
         // the cos sums C_i go to the scratch of the (already consumed) parity sums
         double* Cs = E;
-        ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
-                        EpiDftBwdCos{grids, Cs, C, N, Lg, sh.size()}));
-        if (Lg > 1) {
-            UnitList* v;
-            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 1), [&](UnitList& ul) {
+        for (int ch = 0; ch < nchunks(Lg); ++ch) {
+            const int k0 = ch * KCHUNK;
+            UnitList* u;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
                 for (long long r = 0; r < rows; r += SP_M)
-                    add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT, Lg - 1, 1 | 2 | 4, 0);
+                    add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, std::min(KCHUNK, Lg - k0),
+                              0, 0, k0);
+            }, &u));
+            if (ch == 0)
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
+                                EpiDftBwdCos<false>{grids, Cs, C, N, Lg, sh.size()}));
+            else
+                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
+                                EpiDftBwdCos<true>{grids, Cs, C, N, Lg, sh.size()}));
+        }
+        // the sin pass after every cos chunk: its first chunk reads the finished C_i
+        for (int ch = 0; Lg > 1 && ch < nchunks(Lg - 1); ++ch) {
+            const int k0 = ch * KCHUNK;
+            UnitList* v;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 1 + 8 * ch), [&](UnitList& ul) {
+                for (long long r = 0; r < rows; r += SP_M)
+                    add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT,
+                              std::min(KCHUNK, Lg - 1 - k0), 1 | 2 | 4, 0, k0);
             }, &v));
-            ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
-                            EpiDftBwdSin{grids, Cs, C, N, Lg, sh.size()}));
+            if (ch == 0)
+                ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
+                                EpiDftBwdSin<false>{grids, Cs, C, N, Lg, sh.size()}));
+            else
+                ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
+                                EpiDftBwdSin<true>{grids, Cs, C, N, Lg, sh.size()}));
         }
     }
     return split_finish(ctx);
@@ -2049,10 +2136,15 @@ int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A
     const int bits = digit_bits(K);
     ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{A, K}, M, K, S, bits, 0, a));
     ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{B, K}, N, K, S, bits, 0, b));
-    UnitList u;
-    add_units(u, S, bits, 0, M, 0, N, NT, K, 0, 0);
-    ZG_TRY(run_gemm(ctx, S, u, a, a, b, b, EpiDense{C, N}));
-    return split_finish(ctx);  // also keeps the local operands alive until the product is done
+    for (int ch = 0; ch < nchunks(K); ++ch) {
+        const int k0 = ch * KCHUNK;
+        UnitList u;
+        add_units(u, S, bits, 0, M, 0, N, NT, std::min(KCHUNK, K - k0), 0, 0, k0);
+        if (ch == 0) ZG_TRY(run_gemm(ctx, S, u, a, a, b, b, EpiDense<false>{C, N}));
+        else ZG_TRY(run_gemm(ctx, S, u, a, a, b, b, EpiDense<true>{C, N}));
+        ZG_TRY(split_finish(ctx));  // the local work list must outlive its launch
+    }
+    return ZEST_GPU_OK;  // the local operands outlive the launches (split_finish synchronizes)
 }
 
 int split_wait_selftest(zest_gpu_context* ctx, long long limit_ns) {
