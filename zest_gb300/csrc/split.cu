@@ -197,6 +197,25 @@ __device__ __forceinline__ double u64_ldexp(unsigned long long a, bool neg, int 
 }
 
 
+// The same for a signed 64-bit T, without branches (so that the epilogue's
+// independent elements interleave): the rounding carry runs into the
+// exponent field through the bit pattern; zero, results below the normal
+// range and overflow are selected at the end.  Bit-identical to u64_ldexp.
+__device__ __forceinline__ double i64_ldexp(long long T, int E) {
+    const unsigned long long sgn = (unsigned long long)T & (1ull << 63);
+    const unsigned long long a = T < 0 ? 0ull - (unsigned long long)T : (unsigned long long)T;
+    const int lz = __clzll((long long)a);  // 64 for a == 0
+    const unsigned long long n = a << (lz & 63);
+    const unsigned long long mant = n >> 11;  // 53 bits, the leading one at bit 52
+    const unsigned long long rest = n & 0x7FFull;
+    const unsigned long long mr = mant + ((rest > 0x400ull) | ((rest == 0x400ull) & mant));
+    const int biased = (63 - lz) + E + 1023;  // exponent field of the leading one
+    const int eff = biased + int(mr >> 53);   // after a rounding carry
+    const unsigned long long bits = ((unsigned long long)(long long)(biased - 1) << 52) + mr;
+    const double v = __longlong_as_double((long long)(sgn | (eff >= 2047 ? 0x7FF0000000000000ull : bits)));
+    return (a == 0 || eff <= 0) ? 0.0 : v;
+}
+
 // fixed point: round(x 2^{nbits-e}) as int64 (|x| < 2^(e-1)), ties to even
 __device__ __forceinline__ long long to_fixed(double x, int e, int nbits) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
@@ -1140,9 +1159,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                     const int e2 = __shfl_sync(0xffffffffu, eb_b, idx & 31);
                     const int eb = idx < 32 ? e1 : e2;
                     if (rv && n < u.n) {
-                        const long long Tj = T[4 * c + j];
-                        const double v = u64_ldexp(Tj < 0 ? (unsigned long long)(-Tj) : (unsigned long long)Tj,
-                                                   Tj < 0, ea + eb + TEXP);
+                        const double v = i64_ldexp(T[4 * c + j], ea + eb + TEXP);
                         epi.store(R, u, n, v, old[j]);
                     }
                 }
