@@ -55,7 +55,7 @@ namespace zgpu {
 // ===========================================================================
 namespace {
 
-constexpr int SP_EPI_WARPS = 12;                  // epilogue warps: three per TMEM lane quarter
+constexpr int SP_EPI_WARPS = 16;                  // epilogue warps: four per TMEM lane quarter
 constexpr int SP_THREADS = 32 * (2 + SP_EPI_WARPS);  // + TMA producer + MMA issuer
 constexpr int SP_M = 128;
 constexpr int SP_KB = 16;        // K elements per pipeline stage (32 bytes of bf16)
