@@ -1,39 +1,39 @@
-// Split-precision form of the Zernike GLQ transforms on tcgen05 tensor cores.
+// Split-precision form of the GLQ contractions on tcgen05 tensor cores: every
+// Zernike contraction and the SH Legendre sums.
 //
-// Every dense contraction of the path -- the longitude DFT (as a matrix
-// product with the cos/sin table, folded over x_i +- x_{N-i}), the folded
-// Legendre sums and the radial sums -- is evaluated as
+// Every dense contraction -- the longitude DFT of the Zernike path (as a
+// matrix product with the cos/sin table, folded over x_i +- x_{N-i}), the
+// folded Legendre sums and the radial sums -- is evaluated as
 //     C[r, n] = sum_k A[r, k] B[n, k]
-// with FP64 operands represented exactly enough in BF16 fixed-point slices:
+// with FP64 operands represented in BF16 fixed-point slices:
 //   * each operand row gets an exponent e (|x| < 2^(e-1) over the row) and
-//     its values are rounded to v = round(x 2^{7S - e}), |v| <= 2^{7S-1};
-//   * v is cut into S balanced base-128 digits d_s in [-64, 63] (the leading
-//     one in [-65, 65]), each exact in BF16: x = 2^{e - 7S} sum_s d_s 128^{S-1-s};
-//   * the products d_s(A) d_t(B) with s + t = level <= S (S(S+1)/2 + S-1
-//     products) accumulate in FP32 TMEM accumulators.  Products are integers
-//     of magnitude <= 65^2 < 2^12.05, so a level with p products is exact
-//     while p K 65^2 <= 2^24: levels 0..3 get their own, exact, accumulators
-//     for K <= 992.  Levels 4..S weigh <= 2^-28 of level 0 and share one
-//     accumulator: their products read table slices pre-scaled by 2^-7 and
-//     2^-14 (exact in BF16), so its FP32 rounding stays below 2^-50 of the
-//     result.  Keeping level S makes the dropped levels > S negligible next
-//     to the 2^-7S representation error;
-//   * the epilogue recombines the five accumulators by integer Horner
-//     (T = 64 sum_a 128^{4-a} acc_a, the exact levels as integers, the shared
-//     one rounded to 2^-6 of its unit; |T| < 2^57 for K <= 992) and builds
-//     the FP64 result 2^{eA + eB - 48} T with integer operations only.
-// Only the tables (P_lm, R_nl, cos/sin) are prepared in FP64; the FFT,
-// Legendre and radial arithmetic of the forward and backward transforms runs
-// on the tensor cores.  S = 6 keeps 41 bits per operand and 26 products
-// (about 1e-12 relative error per product against FP64).
+//     its values are rounded to v = round(x 2^{8S - e}) (ties to even);
+//   * v is cut into S balanced base-256 digits d_s in [-128, 127] (the
+//     leading one in [-128, 128]), each exact in BF16;
+//   * the products d_s(A) d_t(B) with s + t = level <= S - 1 (21 products at
+//     S = 6) accumulate in FP32 TMEM accumulators.  A product is at most
+//     2^14, so a level with p products is exact while p K 2^14 <= 2^24:
+//     levels 0..3 get their own, exact, accumulators for sums of up to 256
+//     terms.  Levels 4..S-1 weigh <= 2^-32 of level 0 and share one
+//     accumulator: their products read table slices pre-scaled by 2^-8
+//     (exact in BF16).  Longer sums run as K-chunks of at most 256 terms;
+//     every chunk after the first adds its FP64 result through the
+//     accumulating form of the stage's epilogue;
+//   * the epilogue recombines the five accumulators by integer Horner into an
+//     exact int64 T and builds the FP64 result 2^{eA + eB - 8 (S + 1) - 6} T
+//     with integer operations only.
+// Only the tables (P_lm, R_nl, cos/sin) are prepared in FP64.
 //
 // Kernel: warp-specialised, persistent, one CTA per SM.  Warp 0 issues TMA
-// loads (SWIZZLE_32B, one 16-wide K block of all S data slices and the
+// loads (SWIZZLE_32B, one 16-wide K block of all S operand slices and the
 // needed table slices per pipeline stage), warp 1 issues tcgen05.mma
-// (M = 128 operand rows, N = 96 table rows per tile, five accumulators
-// resident in TMEM), warps 2..9 read the accumulators back (tcgen05.ld),
-// recombine and store through a stage-specific epilogue.  Every wait is bounded (about 2 s); on timeout the
-// kernel records an error code and winds down instead of hanging.
+// (M = 128 operand rows, N = NT = 96 (or 48) table rows per tile, five
+// accumulators resident in TMEM), warps 2..17 read the accumulators back
+// (tcgen05.ld, four warps per TMEM lane quarter), recombine and store
+// through a stage-specific epilogue.  For the SH sums the table is the
+// 128-row operand and the 2 x batch data rows are the columns.  Every wait
+// is bounded (about 2 s); on timeout the kernel records an error code and
+// winds down instead of hanging.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -1092,7 +1092,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             // NT/2 <= 64 columns per warp: lane l holds the exponents of columns col0 + l and col0 + 32 + l
             const int ca = col0 + lane, cb = col0 + 32 + lane;
             const int eb_a = (ca < col0 + CW && ca < u.n) ? ebv[u.b_row0 + ca] : 0;
-            const int eb_b = (cb < col0 + CW && cb < u.n) ? ebv[u.b_row0 + cb] : 0;
+            const int eb_b = (CW > 32 && cb < col0 + CW && cb < u.n) ? ebv[u.b_row0 + cb] : 0;
             const typename Epi::Row R = epi.row(u, row);
             const long long w0 = clock64();
             const bool got = mbar_wait(tfull, tile & 1, P.err, 4);
@@ -1155,9 +1155,14 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                 for (int j = 0; j < 4; ++j) {
                     const int n = col0 + 4 * c + j;
                     const int idx = 4 * c + j;
-                    const int e1 = __shfl_sync(0xffffffffu, eb_a, idx & 31);
-                    const int e2 = __shfl_sync(0xffffffffu, eb_b, idx & 31);
-                    const int eb = idx < 32 ? e1 : e2;
+                    int eb;
+                    if constexpr (CW <= 32) {
+                        eb = __shfl_sync(0xffffffffu, eb_a, idx);
+                    } else {
+                        const int e1 = __shfl_sync(0xffffffffu, eb_a, idx & 31);
+                        const int e2 = __shfl_sync(0xffffffffu, eb_b, idx & 31);
+                        eb = idx < 32 ? e1 : e2;
+                    }
                     if (rv && n < u.n) {
                         const double v = i64_ldexp(T[4 * c + j], ea + eb + TEXP);
                         epi.store(R, u, n, v, old[j]);
