@@ -1354,5 +1354,83 @@ private:
 };
 
 }  // namespace zt
+// ---------------------------------------------------------------------------
+// Least-squares fits to scattered data (lsq_transformer.hpp:38-190)
+// ---------------------------------------------------------------------------
+
+namespace st {
+
+class LSQTransformer {
+public:
+    LSQTransformer() : LSQTransformer(0) {}
+    explicit LSQTransformer(std::size_t order, int device = 0, void* stream = nullptr)
+        : m_ctx(device, stream), m_order(order) {}
+    [[nodiscard]] std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] GPUContext& context() noexcept { return m_ctx; }
+
+    // data at (latitude, longitude) points
+    template <SHNorm sh_norm_param, SHPhase sh_phase_param>
+    void transform(std::span<const double> data, std::span<const double> lat, std::span<const double> lon,
+                   RealSHSpan<std::array<double, 2>, sh_norm_param, sh_phase_param> expansion) {
+        if (lat.size() != data.size() || lon.size() != data.size())
+            throw GPUError(ZEST_GPU_ERR_INVALID, "LSQTransformer: data and points differ in length");
+        m_order = expansion.order();
+        zest::detail::check(zest_gpu_st_lsq(m_ctx.get(), detail::abi(sh_norm_param), detail::abi(sh_phase_param),
+                                            expansion.order(), data.size(), 1, data.data(), lat.data(), lon.data(),
+                                            reinterpret_cast<double*>(expansion.data()), ZEST_MEM_HOST));
+    }
+    template <SHNorm sh_norm_param, SHPhase sh_phase_param>
+    [[nodiscard]] auto transform(std::span<const double> data, std::span<const double> lat,
+                                 std::span<const double> lon, std::size_t order) {
+        RealSHExpansion<sh_norm_param, sh_phase_param> expansion(order);
+        transform<sh_norm_param, sh_phase_param>(data, lat, lon, expansion);
+        return expansion;
+    }
+
+private:
+    GPUContext m_ctx;
+    std::size_t m_order;
+};
+
+}  // namespace st
+
+namespace zt {
+
+class LSQTransformer {
+public:
+    LSQTransformer() : LSQTransformer(0) {}
+    explicit LSQTransformer(std::size_t order, int device = 0, void* stream = nullptr)
+        : m_ctx(device, stream), m_order(order) {}
+    [[nodiscard]] std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] GPUContext& context() noexcept { return m_ctx; }
+
+    // data at (r, longitude, colatitude) points
+    template <ZernikeNorm zernike_norm_param, st::SHNorm sh_norm_param, st::SHPhase sh_phase_param>
+    void transform(std::span<const double> data, std::span<const double> r, std::span<const double> lon,
+                   std::span<const double> colat,
+                   RealZernikeSpan<std::array<double, 2>, zernike_norm_param, sh_norm_param, sh_phase_param> expansion) {
+        if (r.size() != data.size() || lon.size() != data.size() || colat.size() != data.size())
+            throw GPUError(ZEST_GPU_ERR_INVALID, "LSQTransformer: data and points differ in length");
+        m_order = expansion.order();
+        zest::detail::check(zest_gpu_zt_lsq(m_ctx.get(), detail::abi(zernike_norm_param),
+                                            st::detail::abi(sh_norm_param), st::detail::abi(sh_phase_param),
+                                            expansion.order(), data.size(), 1, data.data(), r.data(), lon.data(),
+                                            colat.data(), reinterpret_cast<double*>(expansion.data()),
+                                            ZEST_MEM_HOST));
+    }
+    template <ZernikeNorm zernike_norm_param, st::SHNorm sh_norm_param, st::SHPhase sh_phase_param>
+    [[nodiscard]] auto transform(std::span<const double> data, std::span<const double> r,
+                                 std::span<const double> lon, std::span<const double> colat, std::size_t order) {
+        RealZernikeExpansion<zernike_norm_param, sh_norm_param, sh_phase_param> expansion(order);
+        transform<zernike_norm_param, sh_norm_param, sh_phase_param>(data, r, lon, colat, expansion);
+        return expansion;
+    }
+
+private:
+    GPUContext m_ctx;
+    std::size_t m_order;
+};
+
+}  // namespace zt
 
 }  // namespace zest

@@ -184,6 +184,25 @@ int zest_gpu_st_evaluate(zest_gpu_context* ctx, int sh_norm, int sh_phase, size_
                          const double* coeffs, size_t nlon, const double* lon, size_t nlat, const double* colat,
                          double* values, int mem);
 
+/* ---- least-squares fits to scattered data (lsq_transformer.hpp) ----
+ * `batch` data vectors of npoints values at the same points; coefficients of
+ * every order below `order` are written, item b at b * 2 * coeff_size(order).
+ * Solved by Householder QR of the design matrix (as the reference's LAPACK
+ * dgels, src/linearfit.cpp), on the device; at least as many points as
+ * unknowns (L^2 for SH, L(L+1)(L+2)/6 for Zernike).
+ * st::LSQTransformer::transform, :57-110: points (latitude, longitude); the
+ * basis P_lm(sin latitude) {cos, sin}(m longitude), as RealSHGenerator. */
+int zest_gpu_st_lsq(zest_gpu_context* ctx, int sh_norm, int sh_phase, size_t order, size_t npoints, size_t batch,
+                    const double* data, const double* lat, const double* lon, double* coeffs, int mem);
+/* zt::LSQTransformer::transform, :119-187: points (r, longitude, colatitude);
+ * the basis R_nl(r) P_lm(cos colatitude) {cos, sin}(m longitude), as
+ * ZernikeGenerator.  (The reference's version of this fit passes the points
+ * to its generator in another order and regroups the solution by l only;
+ * this is the fit its interface describes.) */
+int zest_gpu_zt_lsq(zest_gpu_context* ctx, int zernike_norm, int sh_norm, int sh_phase, size_t order, size_t npoints,
+                    size_t batch, const double* data, const double* r, const double* lon, const double* colat,
+                    double* coeffs, int mem);
+
 /* ---- power spectra (power_spectra.hpp) ----
  * norm = 1/(4 pi) for ZEST_SH_GEO, 1 for ZEST_SH_QM (sh_conventions.hpp). */
 /* st::power_spectrum, :88-104: out[b * order + l] = norm sum_m |c_lm|^2, l < order. */

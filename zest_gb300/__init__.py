@@ -109,6 +109,8 @@ _SIGNATURES = {
     "zest_gpu_st_grid_points": [_sz, _i, _vp, _vp],
     "zest_gpu_zt_evaluate": [_vp, _i, _i, _i, _sz, _sz, _vp, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _i],
     "zest_gpu_st_evaluate": [_vp, _i, _i, _sz, _sz, _vp, _sz, _vp, _sz, _vp, _vp, _i],
+    "zest_gpu_st_lsq": [_vp, _i, _i, _sz, _sz, _sz, _vp, _vp, _vp, _vp, _i],
+    "zest_gpu_zt_lsq": [_vp, _i, _i, _i, _sz, _sz, _sz, _vp, _vp, _vp, _vp, _vp, _i],
     "zest_gpu_st_power_spectrum": [_vp, _i, _sz, _sz, _vp, _vp, _i],
     "zest_gpu_st_cross_power_spectrum": [_vp, _i, _sz, _sz, _vp, _vp, _sz, _vp, _i],
     "zest_gpu_zt_power_spectrum": [_vp, _i, _sz, _sz, _vp, _vp, _i],
@@ -504,6 +506,42 @@ class Context:
         lp, _ = _ptr(lon, nlon)
         tp, _ = _ptr(colat, nlat)
         _check(self.lib.zest_gpu_st_evaluate(self._h, *conv, order, batch, cp, nlon, lp, nlat, tp, vp, cm))
+        return out
+
+    # ---- least-squares fits (LSQTransformer) ----
+    def st_lsq(self, data, order: int, lat, lon, batch: int = 1, conv=ST_GEO, out=None):
+        """SH expansions of order `order` fitted to `batch` data vectors at
+        (latitude, longitude) points (st::LSQTransformer::transform)."""
+        lat, lon = (self._points(v, data) for v in (lat, lon))
+        npts = int(lat.numel() if _is_torch(lat) else lat.size)
+        dp, dm = _ptr(data, npts * batch)
+        n = 2 * st_coeff_size(order) * batch
+        if out is None:
+            out = self._alloc_like(data, n)
+        cp, cm = _ptr(out, n)
+        if cm != dm:
+            raise ValueError("data and coefficients must both be host or both be device memory")
+        la, _ = _ptr(lat, npts)
+        lo, _ = _ptr(lon, npts)
+        _check(self.lib.zest_gpu_st_lsq(self._h, *conv, order, npts, batch, dp, la, lo, cp, dm))
+        return out
+
+    def zt_lsq(self, data, order: int, r, lon, colat, batch: int = 1, conv=ZT_GEO, out=None):
+        """Zernike expansions fitted to data at (r, longitude, colatitude)
+        points (zt::LSQTransformer::transform)."""
+        r, lon, colat = (self._points(v, data) for v in (r, lon, colat))
+        npts = int(r.numel() if _is_torch(r) else r.size)
+        dp, dm = _ptr(data, npts * batch)
+        n = 2 * zt_coeff_size(order) * batch
+        if out is None:
+            out = self._alloc_like(data, n)
+        cp, cm = _ptr(out, n)
+        if cm != dm:
+            raise ValueError("data and coefficients must both be host or both be device memory")
+        rp, _ = _ptr(r, npts)
+        lo, _ = _ptr(lon, npts)
+        co, _ = _ptr(colat, npts)
+        _check(self.lib.zest_gpu_zt_lsq(self._h, *conv, order, npts, batch, dp, rp, lo, co, cp, dm))
         return out
 
     # ---- power spectra ----

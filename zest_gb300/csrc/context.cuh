@@ -11,6 +11,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "split.cuh"
+#include "lsq.cuh"
 
 namespace zgpu {
 
@@ -176,6 +177,7 @@ struct zest_gpu_context {
     std::map<std::tuple<int, int, int>, std::unique_ptr<DevBuf>> adj_w;  // quadrature weight slabs
     std::unique_ptr<SplitState, SplitDeleter> split;
     EvalBufs eval;          // evaluation at arbitrary points
+    std::unique_ptr<LsqState, LsqDeleter> lsq;  // least-squares fits
     Profiler prof;
 };
 

@@ -1325,6 +1325,53 @@ int zest_gpu_st_evaluate(zest_gpu_context* ctx, int sn, int sp, size_t order, si
     });
 }
 
+// st::LSQTransformer::transform (lsq_transformer.hpp:57-110): data at
+// (latitude, longitude) points; zt::LSQTransformer::transform
+// (lsq_transformer.hpp:119-187): data at (r, longitude, colatitude) points.
+int zest_gpu_st_lsq(zest_gpu_context* ctx, int sn, int sp, size_t order, size_t npoints, size_t batch,
+                    const double* data, const double* lat, const double* lon, double* coeffs, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (order > 4096) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535 || npoints > 0x7fffffff) return fail(ZEST_GPU_ERR_INVALID, "too many points or items");
+    if (mem != ZEST_MEM_HOST && mem != ZEST_MEM_DEVICE)
+        return fail(ZEST_GPU_ERR_INVALID, "mem must be ZEST_MEM_HOST or ZEST_MEM_DEVICE");
+    const size_t dn = batch * npoints, cn = batch * 2 * zest_gpu_st_coeff_size(order);
+    if ((dn && !data) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    if (cn == 0) return ZEST_GPU_OK;
+    std::vector<double> la, lo, z;
+    ZG_TRY(points_to_host(mem, lat, npoints, la));
+    ZG_TRY(points_to_host(mem, lon, npoints, lo));
+    z.resize(npoints);
+    for (size_t i = 0; i < npoints; ++i) z[i] = std::sin(la[i]);
+    return with_staging(ctx, mem, data, dn, coeffs, cn, [&](const double* in, double* out) {
+        return lsq_dev(ctx, 1, 0, sn, sp, int(order), int(npoints), int(batch), in, z, lo, std::vector<double>(), out);
+    });
+}
+
+int zest_gpu_zt_lsq(zest_gpu_context* ctx, int zn, int sn, int sp, size_t order, size_t npoints, size_t batch,
+                    const double* data, const double* r, const double* lon, const double* colat, double* coeffs,
+                    int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(zn) || !valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (order > 1024) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535 || npoints > 0x7fffffff) return fail(ZEST_GPU_ERR_INVALID, "too many points or items");
+    if (mem != ZEST_MEM_HOST && mem != ZEST_MEM_DEVICE)
+        return fail(ZEST_GPU_ERR_INVALID, "mem must be ZEST_MEM_HOST or ZEST_MEM_DEVICE");
+    const size_t dn = batch * npoints, cn = batch * 2 * zest_gpu_zt_coeff_size(order);
+    if ((dn && !data) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    if (cn == 0) return ZEST_GPU_OK;
+    std::vector<double> rr, lo, co, z;
+    ZG_TRY(points_to_host(mem, r, npoints, rr));
+    ZG_TRY(points_to_host(mem, lon, npoints, lo));
+    ZG_TRY(points_to_host(mem, colat, npoints, co));
+    z.resize(npoints);
+    for (size_t i = 0; i < npoints; ++i) z[i] = std::cos(co[i]);
+    return with_staging(ctx, mem, data, dn, coeffs, cn, [&](const double* in, double* out) {
+        return lsq_dev(ctx, 0, zn, sn, sp, int(order), int(npoints), int(batch), in, z, lo, rr, out);
+    });
+}
+
 int zest_gpu_st_power_spectrum(zest_gpu_context* ctx, int sn, size_t order, size_t batch, const double* coeffs,
                                double* out, int mem) {
     ZG_TRY(check_ctx(ctx));
