@@ -641,6 +641,8 @@ def main():
         e2e = {"value": whole_job_rate(B * n_e2e, world, secs), "unit": UNIT,
                "h2d_bytes_per_step": B * (gsz + csz) * 8, "d2h_bytes_per_step": B * (csz + gsz) * 8,
                "host_buffers": "pinned", "steps": n_e2e, "step_ms": step_ms,
+               "median_step_ms": float(np.median(step_ms)),
+               "rate_at_median_step": world * B / (float(np.median(step_ms)) * 1e-3),
                "host_chunk_bytes": 512 << 20, "pipelined": "uploads, transforms and downloads overlap per chunk"}
         del gh, ch, go
 
