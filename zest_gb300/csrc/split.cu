@@ -217,19 +217,17 @@ __device__ __forceinline__ double i64_ldexp(long long T, int E) {
 }
 
 // fixed point: round(x 2^{nbits-e}) as int64 (|x| < 2^(e-1)), ties to even
+// The row exponents leave at least one bit of headroom above every element,
+// so the shift is at least 6; shifts of 63 and more round to 0.  Without
+// branches: round to nearest, ties to even (add half - 1 and the parity of
+// the kept part), zero and subnormals give 0.
 __device__ __forceinline__ long long to_fixed(double x, int e, int nbits) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
     const int E = int(bits >> 52) & 0x7FF;
     const unsigned long long M = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = 1075 + e - nbits - E;
-    unsigned long long v;
-    if (E == 0 || sh >= 63) {  // zero, subnormals, and values below half a unit
-        v = 0;
-    } else if (sh > 0) {  // round to nearest, ties to even: add half - 1 and the parity of the kept part
-        v = (M + ((1ull << (sh - 1)) - 1) + ((M >> sh) & 1ull)) >> sh;
-    } else {
-        v = M << (-sh);
-    }
+    const int sh = min(max(1075 + e - nbits - E, 1), 63);
+    unsigned long long v = (M + ((1ull << (sh - 1)) - 1) + ((M >> sh) & 1ull)) >> sh;
+    v = E == 0 ? 0ull : v;
     return (bits >> 63) ? -(long long)v : (long long)v;
 }
 
@@ -437,53 +435,40 @@ __device__ __forceinline__ uint32_t digit_f32_bits(int d, float scale) {
     return __float_as_uint(f);
 }
 
-// Balanced digits of two neighbouring elements (slice 0 most significant)
-// written as BF16 pairs: one 4-byte store per slice and copy.
-// 8-bit digits: adding 128 sum_{i<S-1} 256^i turns the lower balanced digits
-// into the plain bytes of the sum (digit = byte - 128) and leaves the leading
-// digit as the sum shifted down.
+// Balanced 8-bit digits of two neighbouring elements (slice 0 most
+// significant) written as BF16 pairs: one 4-byte store per slice and copy.
+// Adding 128 sum_{i<S-1} 256^i turns the lower balanced digits into the plain
+// bytes of the sum (digit = byte - 128) and leaves the leading digit as the
+// sum shifted down.  A lower digit's float is built by one byte permute,
+// 0x4B4000bb = 2^23 + 2^22 + byte, and one subtraction of 2^23 + 2^22 + 128.
 template <int S>
-__device__ __forceinline__ void write_digits2(long long w0, long long w1, int bits, int copies, __nv_bfloat16* out,
+__device__ __forceinline__ void write_digits2(long long w0, long long w1, int copies, __nv_bfloat16* out,
                                               long long stride, long long off) {
-    int d[2][S];
-    if (bits == 8) {
-        constexpr long long OFF = (long long)((0x8080808080808080ull) >> (8 * (9 - S)));  // 128 per lower byte
-        const long long u[2] = {w0 + OFF, w1 + OFF};
+    constexpr long long OFF = (long long)((0x8080808080808080ull) >> (8 * (9 - S)));  // 128 per lower byte
+    float f[2][S];
+    const long long u[2] = {w0 + OFF, w1 + OFF};
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < 2; ++q) {
+        const uint32_t lo = uint32_t(u[q]), hi = uint32_t((unsigned long long)u[q] >> 32);
 #pragma unroll
-            for (int s = 1; s < S; ++s) d[q][s] = int((u[q] >> (8 * (S - 1 - s))) & 255) - 128;
-            d[q][0] = int(u[q] >> (8 * (S - 1)));
+        for (int s = 1; s < S; ++s) {
+            const int b = S - 1 - s;  // byte of the sum holding digit s
+            f[q][s] = __int_as_float(int(__byte_perm(b < 4 ? lo : hi, 0x4B400000u, 0x7650u | (b & 3)))) - 12583040.0f;
         }
-    } else {
-        const long long mask = (1ll << bits) - 1;
-        const int halfv = 1 << (bits - 1), base = 1 << bits;
-        const long long w[2] = {w0, w1};
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            long long x = w[q];
-#pragma unroll
-            for (int s = S - 1; s >= 1; --s) {
-                int r = int(x & mask);
-                if (r >= halfv) r -= base;
-                d[q][s] = r;
-                x = (x - r) >> bits;
-            }
-            d[q][0] = int(x);
-        }
+        f[q][0] = __uint_as_float(digit_f32_bits(int(u[q] >> (8 * (S - 1))), 1.0f));
     }
     uint32_t* o = reinterpret_cast<uint32_t*>(out + off);
     const long long s2 = stride >> 1;  // slice stride in BF16 pairs (slice strides are even)
     if (copies == 1) {
 #pragma unroll
-        for (int s = 0; s < S; ++s)
-            o[s * s2] = __byte_perm(digit_f32_bits(d[0][s], 1.0f), digit_f32_bits(d[1][s], 1.0f), 0x7632);
+        for (int s = 0; s < S; ++s) o[s * s2] = __byte_perm(__float_as_uint(f[0][s]), __float_as_uint(f[1][s]), 0x7632);
     } else {
         for (int c = 0; c < copies; ++c) {
-            const float sc = __int_as_float((127 - bits * c) << 23);  // 2^{-bits c}, exact
+            const float sc = __int_as_float((127 - 8 * c) << 23);  // 2^{-8 c}, exact
 #pragma unroll
             for (int s = 0; s < S; ++s)
-                o[(c * S + s) * s2] = __byte_perm(digit_f32_bits(d[0][s], sc), digit_f32_bits(d[1][s], sc), 0x7632);
+                o[(c * S + s) * s2] =
+                    __byte_perm(__float_as_uint(f[0][s] * sc), __float_as_uint(f[1][s] * sc), 0x7632);
         }
     }
 }
@@ -614,7 +599,7 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
                     }
                     w[q] = x;
                 }
-                write_digits2<S>(w[0], w[1], J.bits, J.copies, J.out0, J.stride0, row * J.Kp0 + k);
+                write_digits2<S>(w[0], w[1], J.copies, J.out0, J.stride0, row * J.Kp0 + k);
             }
             if (two && k < J.Kp1) {
                 long long w[2];
@@ -629,7 +614,7 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
                     }
                     w[q] = x;
                 }
-                write_digits2<S>(w[0], w[1], J.bits, J.copies, J.out1, J.stride1, row * J.Kp1 + k);
+                write_digits2<S>(w[0], w[1], J.copies, J.out1, J.stride1, row * J.Kp1 + k);
             }
         }
     }
