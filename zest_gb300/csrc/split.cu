@@ -1106,8 +1106,10 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                 tmem_ld_wait();
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    const int u = (__float2int_rn(__uint_as_float(v[0][j])) << BITS) +
-                                  __float2int_rn(__uint_as_float(v[1][j]));
+                    // level 0 is one product per term: |acc_0| <= 256 2^14 = 2^22 per chunk,
+                    // so acc_0 + 1.5 2^23 is exact and its low bits are the integer
+                    const int i0 = __float_as_int(__uint_as_float(v[0][j]) + 12582912.0f) - 0x4B400000;
+                    const int u = (i0 << BITS) + __float2int_rn(__uint_as_float(v[1][j]));
                     const int i2 = __float2int_rn(__uint_as_float(v[2][j]));
                     const int il = __float2int_rn(64.0f * __uint_as_float(v[SC::NACC - 1][j]));
                     if constexpr (SC::NACC == 5) {
