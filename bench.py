@@ -36,8 +36,8 @@ from zest_gb300.replicas import max_over_ranks, replica_seed0, whole_job_rate  #
 
 METRIC = "Zernike fwd+bwd transforms/s, order 200x64: split-prec vs FP64 GPU at 1e-11 err"
 # DRAM read + write bytes of the split GEMMs of one forward+backward step per
-# function at order 200 (ncu capture of all eight launches at batch 4: 7.31 GB)
-GEMM_DRAM_BYTES_PER_FUNCTION_ORDER200 = 7.306e9 / 4
+# function at order 200 (ncu capture of all eight launches at batch 4: 7.30 GB)
+GEMM_DRAM_BYTES_PER_FUNCTION_ORDER200 = 7.298e9 / 4
 UNIT = "transforms/s"
 
 
@@ -586,7 +586,7 @@ def main():
         achieved = useful / (gemm_ms * 1e-3) / 1e12 if gemm_ms == gemm_ms and gemm_ms > 0 else None
         peak = peaks["bf16_tflops_sustained"] or peaks["bf16_tflops"]
         # DRAM bytes of the eight split_gemm_kernel launches of one step, from one
-        # ncu capture at order 200 x 4 (7.31 GB, proportional to the batch)
+        # ncu capture at order 200 x 4 (7.30 GB, proportional to the batch)
         launches_per_step = stage_n.get("split_gemm", 8.0) or 8.0
         traffic = GEMM_DRAM_BYTES_PER_FUNCTION_ORDER200 * B / launches_per_step if L == 200 else None
         roofline = {"bound": "tensor", "kernel": "split_gemm_kernel (per launch, averaged over a step's launches)",
