@@ -330,7 +330,7 @@ int zest_gpu_st_rotate_vjp(zest_gpu_context* ctx, size_t order, size_t batch, co
                            double* coeffs_cot, double* euler_cot, int mem);
 
 /* ---- split-precision dense product (no reference counterpart) ----
- * C = A B^T for row-major FP64 A (M x K) and B (N x K), K <= 992, evaluated
+ * C = A B^T for row-major FP64 A (M x K) and B (N x K), K <= 2048, evaluated
  * with the context's slice count on the tcgen05 path used by
  * ZEST_PRECISION_SPLIT (BF16 fixed-point slices, exact FP32 partial sums,
  * FP64 recombination).  Exposed to test and measure the emulation itself. */

@@ -121,12 +121,12 @@ def split_model(A, B, S):
     return out
 
 
-@pytest.mark.parametrize("K", [1, 16, 33, 64, 208, 256, 257, 400, 992])
+@pytest.mark.parametrize("K", [1, 16, 33, 64, 208, 256, 257, 400, 992, 2048])
 def test_split_gemm_matches_integer_model(split, K):
     # The kernel sums levels 0..3 exactly and levels 4 and up in one shared
     # FP32 accumulator, whose products weigh at most 2^-28 of level 0: the
     # kernel must agree with the all-integer model to 1e-13 of the largest
-    # entry, with one K-chunk (K <= 256) and with several (257, 400, 992).
+    # entry, with one K-chunk (K <= 256) and with several (257 up to 2048).
     rng = np.random.default_rng(100 + K)
     A = rng.normal(size=(130, K)) * np.exp(rng.normal(size=(130, 1)))
     B = rng.normal(size=(70, K))

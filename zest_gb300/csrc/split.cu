@@ -242,11 +242,10 @@ __device__ __forceinline__ int biased_exp(double x) {
 // ===========================================================================
 namespace {
 
-constexpr int SL_KMAX = 992;  // longest operand row the slicing stages (and longest sum)
-constexpr int SL_K8MAX = 256; // K bound of exact level sums with balanced 8-bit digits
-constexpr int SL_UNROLL = 8;  // independent loads per thread in the staging loops
+constexpr int SL_KMAX = 2048;  // longest operand row the slicing stages (and longest sum)
+constexpr int SL_K8MAX = 256;  // K bound of exact level sums with balanced 8-bit digits
+constexpr int SL_UNROLL = 8;   // independent loads per thread in the staging loops
 
-// digit width of a contraction of length K: 8 bits while the exact levels stay exact
 // Digits are 8 bits wide at any length: sums longer than SL_K8MAX terms run
 // as K-chunks of at most SL_K8MAX whose FP64 results are added.
 inline int digit_bits(int) { return 8; }
@@ -385,11 +384,11 @@ struct StLegBwdLoader {
     }
 };
 
-// rows (b, col); k = m: (Re F_m, Im F_m); the sin operand is Im F_k at k - 1
-// rows (b, col = (lat, rad)); k = m: the spectrum at latitude lat, formed
-// from the two parity sums E_p[b][m][j'][2 rad + {re, im}] of the Legendre
-// stage: E_0 + E_1 at the north node lat = j0u + j', E_0 - E_1 at the south
-// node lat = j0d - j' (the equator, j0u = j0d, is north).
+// rows (b, col = (lat, rad)); k = m: the spectrum (Re F_m, Im F_m) at
+// latitude lat (the sin operand takes Im F_k at k - 1), formed from the two
+// parity sums E_p[b][m][j'][2 rad + {re, im}] of the Legendre stage: E_0 + E_1
+// at the north node lat = j0u + j', E_0 - E_1 at the south node lat = j0d - j'
+// (the equator, j0u = j0d, is north).
 struct DftBwdLoader {
     static constexpr bool ROW_FAST = true, TWO = true;
     const double* E;
@@ -789,13 +788,15 @@ struct EpiStLegFwd {
     }
 };
 // Backward: table row r of group (m, p) is folded node j = r - (2m + p) kh;
-// the parity sums go to E[p][b][m][j][c].
+// the parity sums go to E[p][b][m][j][c], the imaginary parts times sgi (-1:
+// conjugated, as the inverse longitude DFT reads them).
 template <bool ACC>
 struct EpiStLegBwdE {
     static constexpr bool RMW = ACC;
     static constexpr bool CHUNK = ACC;
     double* E;
     int B, L, kh;
+    double sgi;
     struct Row { double* p; };
     __device__ Row row(const SplitUnit& u, int r) const {
         const int m = u.g, par = (u.flags >> 2) & 1;
@@ -806,7 +807,8 @@ struct EpiStLegBwdE {
         old[0] = R.p[(long long)(n >> 1) * L * kh * 2 + (n & 1)];
     }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
-        R.p[(long long)(n >> 1) * L * kh * 2 + (n & 1)] = ACC ? old[0] + v : v;
+        const double w = (n & 1) ? sgi * v : v;
+        R.p[(long long)(n >> 1) * L * kh * 2 + (n & 1)] = ACC ? old[0] + w : w;
     }
 };
 
@@ -1280,9 +1282,16 @@ struct SliceArray {
 };
 
 // Sliced tables of one Zernike plan for one slice count.
+// Sliced longitude DFT tables of one (order L, longitude count N): shared by
+// the Zernike grids and the SH LonLat grids of the same order.
+struct DftTables {
+    SliceArray cos_f, sin_f, cos_b, sin_b;
+};
+
 struct ZtSplitTables {
     int S = 0;
-    SliceArray dft_cos_f, dft_sin_f, leg_f, rad_f, rad_bT, leg_bT, dft_cos_b, dft_sin_b;
+    const DftTables* dft = nullptr;
+    SliceArray leg_f, rad_f, rad_bT, leg_bT;
 };
 
 // Sliced Legendre tables of one SH plan (the 128-row operand: no scaled copies).
@@ -1310,6 +1319,7 @@ struct SplitState {
     SliceArray op[2];           // data operands of the current stage
     std::map<std::tuple<const void*, int>, std::unique_ptr<ZtSplitTables>> zt_tables;  // per (plan, S)
     std::map<std::tuple<const void*, int>, std::unique_ptr<StSplitTables>> st_tables;  // per (plan, S)
+    std::map<std::tuple<int, int, int>, std::unique_ptr<DftTables>> dft_tables;        // per (L, N, S)
     std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<UnitList>> units;  // cached work lists
     DevBuf tmp;                 // FP64 staging of generated tables
     DevBuf cycles;              // role wait counters, kept when ZEST_GPU_SPLIT_CYCLES is set
@@ -1341,7 +1351,7 @@ namespace {
 template <class Loader>
 int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
     if (J.rows <= 0) return ZEST_GPU_OK;
-    if (J.K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: K above 992");
+    if (J.K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: K above 2048");
     if (J.bits != 7 && J.bits != 8)
         return fail(ZEST_GPU_ERR_INVALID, "split path: digit width");
     J.R = slice_rows_per_block(J.K, Loader::TWO);
@@ -1485,6 +1495,37 @@ int slice_table(zest_gpu_context* ctx, const double* src, long long rows, int K,
     return launch_slice(ctx->stream, RowMajorLoader{src, ld}, rows, K, S, bits, 0, dst);
 }
 
+// The longitude DFT tables of order L over N longitudes, sliced (cached).
+int build_dft_tables(zest_gpu_context* ctx, SplitState* st, int L, int N, int S, const DftTables** out) {
+    auto key = std::make_tuple(L, N, S);
+    auto it = st->dft_tables.find(key);
+    if (it != st->dft_tables.end()) {
+        *out = it->second.get();
+        return ZEST_GPU_OK;
+    }
+    cudaStream_t s = ctx->stream;
+    auto t = std::make_unique<DftTables>();
+    const int ld = r16(L);
+    ZG_TRY(st->tmp.ensure((size_t)L * ld * sizeof(double)));
+    double* tmp = st->tmp.as<double>();
+    auto gen = [&](int rows, int K, int row_off, int col_off, int mode, SliceArray& dst) -> int {
+        dim3 grid((ld + 127) / 128, rows);
+        dft_table_kernel<<<grid, 128, 0, s>>>(tmp, rows, K, ld, N, row_off, col_off, mode);
+        ZG_TRY(launch_check("dft_table_kernel"));
+        return slice_table(ctx, tmp, rows, K, ld, S, digit_bits(L), dst);
+    };
+    // forward: cos rows m in [0,L), cols i in [0,L); sin rows m in [1,L), cols i in [1,L)
+    ZG_TRY(gen(L, L, 0, 0, 0, t->cos_f));
+    if (L > 1) ZG_TRY(gen(L - 1, L - 1, 1, 1, 1, t->sin_f));
+    // backward: cos rows i in [0,L), cols m in [0,L); sin rows i in [1,L), cols m in [1,L)
+    ZG_TRY(gen(L, L, 0, 0, 2, t->cos_b));
+    if (L > 1) ZG_TRY(gen(L - 1, L - 1, 1, 1, 3, t->sin_b));
+    ZG_CUDA_TRY(cudaStreamSynchronize(s));
+    *out = t.get();
+    st->dft_tables.emplace(key, std::move(t));
+    return ZEST_GPU_OK;
+}
+
 int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, ZtSplitTables** out) {
     auto key = std::make_tuple((const void*)&plan, S);
     auto it = st->zt_tables.find(key);
@@ -1496,25 +1537,7 @@ int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, 
     auto t = std::make_unique<ZtSplitTables>();
     t->S = S;
     const int L = int(plan.sh.L), N = int(plan.sh.nlon), nr = int(plan.sh.nrad), kh = plan.leg.nnodes;
-    // DFT tables
-    {
-        const int ld = r16(L);
-        ZG_TRY(st->tmp.ensure((size_t)L * ld * sizeof(double)));
-        double* tmp = st->tmp.as<double>();
-        auto gen = [&](int rows, int K, int row_off, int col_off, int mode, SliceArray& dst) -> int {
-            dim3 grid((ld + 127) / 128, rows);
-            dft_table_kernel<<<grid, 128, 0, s>>>(tmp, rows, K, ld, N, row_off, col_off, mode);
-            ZG_TRY(launch_check("dft_table_kernel"));
-            return slice_table(ctx, tmp, rows, K, ld, S, digit_bits(L), dst);
-        };
-        // forward: cos rows m in [0,L), cols i in [0,L); sin rows m in [1,L), cols i in [1,L)
-        ZG_TRY(gen(L, L, 0, 0, 0, t->dft_cos_f));
-        if (L > 1) ZG_TRY(gen(L - 1, L - 1, 1, 1, 1, t->dft_sin_f));
-        // backward: cos rows i in [0,L), cols m in [0,L); sin rows i in [1,L), cols m in [1,L)
-        ZG_TRY(gen(L, L, 0, 0, 2, t->dft_cos_b));
-        if (L > 1) ZG_TRY(gen(L - 1, L - 1, 1, 1, 3, t->dft_sin_b));
-        ZG_CUDA_TRY(cudaStreamSynchronize(s));
-    }
+    ZG_TRY(build_dft_tables(ctx, st, L, N, S, &t->dft));
     // forward Legendre and radial tables (FP64 tables of the plain form)
     ZG_TRY(slice_table(ctx, plan.leg.Pf.as<double>(), plan.leg.off_h[2 * (size_t)L], kh, kh, S, digit_bits(kh),
                        t->leg_f));
@@ -1698,7 +1721,107 @@ void add_units(UnitList& ul, int S, int bits, long long a0, long long arows, int
 }
 
 // work-list keys: (stage, Lg, Lm, batch, S, pass)
-enum { WK_DFT_F = 0, WK_LEG_F, WK_RAD_F, WK_RAD_B, WK_LEG_B, WK_DFT_B, WK_DENSE, WK_ST_LEG_F, WK_ST_LEG_B };
+enum {
+    WK_DFT_F = 0, WK_LEG_F, WK_RAD_F, WK_RAD_B, WK_LEG_B, WK_DFT_B, WK_DENSE, WK_ST_LEG_F, WK_ST_LEG_B,
+    WK_ST_DFT_F, WK_ST_DFT_B
+};
+
+// Longitude DFT of `batch` grids x[b][lon][col] (C columns, item stride gsz)
+// to the spectra G[b][m][col][re, im], m < Lm (L = Lg orders per item):
+// folded cos/sin products (x_k + x_{N-k} against cos, x_k - x_{N-k} against
+// sin), K-chunked.  `wk` keys the work lists of the caller's grid family.
+int dft_forward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t, int S, int wk, const double* grids,
+                      long long gsz, int C, int N, int Lg, int Lm, int batch, double* G) {
+    const int NT = n_tile(S), bits = digit_bits(Lg);
+    const long long rows = (long long)batch * C;
+    ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
+    ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
+    {
+        StageScope sc(ctx, ST_SPLIT_SLICE);
+        ZG_TRY(launch_slice2(ctx->stream, DftFwdLoader{grids, gsz, C, N}, rows, Lg, Lg - 1, 1, S, bits, SL_FOLD,
+                             st->op[0], st->op[1]));
+    }
+    for (int ch = 0; ch < nchunks(Lg); ++ch) {
+        const int k0 = ch * KCHUNK;
+        UnitList* u;
+        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+            for (long long r = 0; r < rows; r += SP_M) {
+                const long long rr = std::min<long long>(SP_M, rows - r);
+                add_units(ul, S, bits, r, rr, 0, Lm, NT, std::min(KCHUNK, Lg - k0), 0, 0, k0);
+                if (Lm > 1) add_units(ul, S, bits, r, rr, 0, Lm - 1, NT, std::min(KCHUNK, Lg - 1 - k0), 1 | 2, 0, k0);
+            }
+        }, &u));
+        if (ch == 0)
+            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], t.cos_f, t.sin_f, EpiDftFwd<false>{G, C, Lg}));
+        else
+            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], t.cos_f, t.sin_f, EpiDftFwd<true>{G, C, Lg}));
+    }
+    return ZEST_GPU_OK;
+}
+
+// The parity sums E_p[b][m][j][kc] (kc < nr2) a Legendre stage leaves
+// unwritten, which the inverse DFT reads as 0: E_0 for m >= Lm, E_1 for
+// m >= Lm - 1 (its last group is empty).
+int zero_parity_tails(zest_gpu_context* ctx, double* E, int batch, int Lg, int Lm, int kh, int nr2) {
+    StageScope sc(ctx, ST_MEMSET);
+    const long long eblock = (long long)Lg * kh * nr2;  // one (p, b)
+    const size_t row = (size_t)kh * nr2 * sizeof(double);
+    if (Lm < Lg)
+        ZG_CUDA_TRY(cudaMemset2DAsync(E + (size_t)Lm * kh * nr2, eblock * sizeof(double), 0, (size_t)(Lg - Lm) * row,
+                                      batch, ctx->stream));
+    ZG_CUDA_TRY(cudaMemset2DAsync(E + (size_t)batch * eblock + (size_t)(Lm - 1) * kh * nr2, eblock * sizeof(double), 0,
+                                  (size_t)(Lg - Lm + 1) * row, batch, ctx->stream));
+    return ZEST_GPU_OK;
+}
+
+// Inverse longitude DFT of the spectra the loader forms (rows (b, col), C
+// columns) to the grids x[b][lon][col] (item stride gsz): a cos pass writing
+// x_0 and the cos sums C_i (to Cs, batch * Lg * C doubles), then a sin pass
+// reading them and writing x_i = C_i + S_i, x_{N-i} = C_i - S_i; both K-chunked.
+int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t, int S, int wk,
+                       const DftBwdLoader& ld, int C, int N, int Lg, int Lm, int batch, double* grids, long long gsz,
+                       double* Cs) {
+    const int NT = n_tile(S), bits = digit_bits(Lg);
+    const long long rows = (long long)batch * C;
+    ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
+    ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
+    {
+        StageScope sc(ctx, ST_SPLIT_SLICE);
+        ZG_TRY(launch_slice2(ctx->stream, ld, rows, Lg, Lg - 1, 1, S, bits, SL_PAIR, st->op[0], st->op[1]));
+    }
+    for (int ch = 0; ch < nchunks(Lg); ++ch) {
+        const int k0 = ch * KCHUNK;
+        UnitList* u;
+        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+            for (long long r = 0; r < rows; r += SP_M)
+                add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, std::min(KCHUNK, Lg - k0),
+                          0, 0, k0);
+        }, &u));
+        if (ch == 0)
+            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], t.cos_b, t.sin_b,
+                            EpiDftBwdCos<false>{grids, Cs, C, N, Lg, gsz}));
+        else
+            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], t.cos_b, t.sin_b,
+                            EpiDftBwdCos<true>{grids, Cs, C, N, Lg, gsz}));
+    }
+    // the sin pass after every cos chunk: its first chunk reads the finished C_i
+    for (int ch = 0; Lg > 1 && ch < nchunks(Lg - 1); ++ch) {
+        const int k0 = ch * KCHUNK;
+        UnitList* v;
+        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 1 + 8 * ch), [&](UnitList& ul) {
+            for (long long r = 0; r < rows; r += SP_M)
+                add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT,
+                          std::min(KCHUNK, Lg - 1 - k0), 1 | 2 | 4, 0, k0);
+        }, &v));
+        if (ch == 0)
+            ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], t.cos_b, t.sin_b,
+                            EpiDftBwdSin<false>{grids, Cs, C, N, Lg, gsz}));
+        else
+            ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], t.cos_b, t.sin_b,
+                            EpiDftBwdSin<true>{grids, Cs, C, N, Lg, gsz}));
+    }
+    return ZEST_GPU_OK;
+}
 
 // SH Legendre tables in digit slices: the forward table (weights and the
 // quadrature prefactor folded in, rows (m, p, l), K = folded nodes) and the
@@ -1769,7 +1892,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
     if (Lg < 2 || Lg > SL_KMAX || plan.sh.nrad > SL_KMAX)
-        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: orders 2..983");
+        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: orders 2..2047");
     ZtSplitTables* tb;
     ZG_TRY(build_zt_tables(ctx, st, plan, S, &tb));
     const ZtShape& sh = plan.sh;
@@ -1783,32 +1906,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
     double* flm = ctx->s1.as<double>();
 
     // ---- longitude DFT: folded cos/sin products ----
-    {
-        const int bits = digit_bits(Lg);
-        const long long rows = (long long)batch * C;
-        ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
-        ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
-        {
-            StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice2(s, DftFwdLoader{grids, sh.size(), C, N}, rows, Lg, Lg - 1, 1, S, bits, SL_FOLD,
-                                 st->op[0], st->op[1]));
-        }
-        for (int ch = 0; ch < nchunks(Lg); ++ch) {
-            const int k0 = ch * KCHUNK;
-            UnitList* u;
-            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_F), Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
-                for (long long r = 0; r < rows; r += SP_M) {
-                    const long long rr = std::min<long long>(SP_M, rows - r);
-                    add_units(ul, S, bits, r, rr, 0, Lm, NT, std::min(KCHUNK, Lg - k0), 0, 0, k0);
-                    if (Lm > 1) add_units(ul, S, bits, r, rr, 0, Lm - 1, NT, std::min(KCHUNK, Lg - 1 - k0), 1 | 2, 0, k0);
-                }
-            }, &u));
-            if (ch == 0)
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_f, tb->dft_sin_f, EpiDftFwd<false>{G, C, Lg}));
-            else
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_f, tb->dft_sin_f, EpiDftFwd<true>{G, C, Lg}));
-        }
-    }
+    ZG_TRY(dft_forward_stage(ctx, st, *tb->dft, S, WK_DFT_F, grids, sh.size(), C, N, Lg, Lm, batch, G));
     // ---- Legendre (folded over the equator) ----
     {
         const int bits = digit_bits(kh);
@@ -1872,7 +1970,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
     if (Lg < 2 || Lg > SL_KMAX || plan.sh.nrad > SL_KMAX)
-        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: orders 2..983");
+        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: orders 2..2047");
     ZtSplitTables* tb;
     ZG_TRY(build_zt_tables(ctx, st, plan, S, &tb));
     const ZtShape& sh = plan.sh;
@@ -1923,17 +2021,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             ZG_TRY(launch_slice2(s, LegBwdLoader{flm, batch, nr2, Lm}, rows, (Lm + 1) / 2, Lm / 2, 0, S, bits,
                                  SL_PAIR, st->op[0], st->op[1]));
         }
-        {
-            // orders the Legendre products do not write: E_0 for m >= Lm, E_1 for
-            // m >= Lm - 1 (its last group is empty)
-            StageScope sc(ctx, ST_MEMSET);
-            const size_t row = (size_t)kh * nr2 * sizeof(double);
-            if (Lm < Lg)
-                ZG_CUDA_TRY(cudaMemset2DAsync(E + (size_t)Lm * kh * nr2, eblock * sizeof(double), 0,
-                                              (size_t)(Lg - Lm) * row, batch, s));
-            ZG_CUDA_TRY(cudaMemset2DAsync(E + (size_t)batch * eblock + (size_t)(Lm - 1) * kh * nr2,
-                                          eblock * sizeof(double), 0, (size_t)(Lg - Lm + 1) * row, batch, s));
-        }
+        ZG_TRY(zero_parity_tails(ctx, E, batch, Lg, Lm, kh, nr2));
         for (int p = 0; p < 2; ++p)
             for (int ch = 0; ch < nchunks((Lm + 1) / 2); ++ch) {
             const int k0 = ch * KCHUNK;
@@ -1955,50 +2043,10 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
         }
     }
     // ---- longitude: inverse real DFT, cos pass then sin read-modify-write pass ----
-    {
-        const int bits = digit_bits(Lg);
-        const long long rows = (long long)batch * C;
-        ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
-        ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
-        {
-            StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice2(s, DftBwdLoader{E, Lg, C, nr, kh, plan.leg.j0u, plan.leg.j0d, batch}, rows, Lg,
-                                 Lg - 1, 1, S, bits, SL_PAIR, st->op[0], st->op[1]));
-        }
-        // the cos sums C_i go to the scratch of the (already consumed) parity sums
-        double* Cs = E;
-        for (int ch = 0; ch < nchunks(Lg); ++ch) {
-            const int k0 = ch * KCHUNK;
-            UnitList* u;
-            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
-                for (long long r = 0; r < rows; r += SP_M)
-                    add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, std::min(KCHUNK, Lg - k0),
-                              0, 0, k0);
-            }, &u));
-            if (ch == 0)
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
-                                EpiDftBwdCos<false>{grids, Cs, C, N, Lg, sh.size()}));
-            else
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
-                                EpiDftBwdCos<true>{grids, Cs, C, N, Lg, sh.size()}));
-        }
-        // the sin pass after every cos chunk: its first chunk reads the finished C_i
-        for (int ch = 0; Lg > 1 && ch < nchunks(Lg - 1); ++ch) {
-            const int k0 = ch * KCHUNK;
-            UnitList* v;
-            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_DFT_B), Lg, Lm, batch, S, 1 + 8 * ch), [&](UnitList& ul) {
-                for (long long r = 0; r < rows; r += SP_M)
-                    add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT,
-                              std::min(KCHUNK, Lg - 1 - k0), 1 | 2 | 4, 0, k0);
-            }, &v));
-            if (ch == 0)
-                ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
-                                EpiDftBwdSin<false>{grids, Cs, C, N, Lg, sh.size()}));
-            else
-                ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], tb->dft_cos_b, tb->dft_sin_b,
-                                EpiDftBwdSin<true>{grids, Cs, C, N, Lg, sh.size()}));
-        }
-    }
+    // (the cos sums C_i go to the scratch of the parity sums, consumed by the slicing)
+    ZG_TRY(dft_backward_stage(ctx, st, *tb->dft, S, WK_DFT_B,
+                              DftBwdLoader{E, Lg, C, nr, kh, plan.leg.j0u, plan.leg.j0d, batch}, C, N,
+                              Lg, Lm, batch, grids, sh.size(), E));
     return split_finish(ctx);
 }
 
@@ -2027,7 +2075,7 @@ int run_gemm_st(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A, const 
 }
 }  // namespace
 
-int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* X,
+int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* grids, double* X,
                      double* coeffs, long long csz) {
     const int S = ctx->slices;
     if (S != 6) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split SH transforms need 6 slices");
@@ -2035,9 +2083,16 @@ int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int ba
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
     const int kh = plan.leg.nnodes, nlat = int(plan.sh.nlat);
-    if (kh > SL_KMAX || (Lg + 1) / 2 > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: order too high");
+    if (Lg > SL_KMAX || kh > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split SH path: orders up to 2048");
     StSplitTables* tb;
     ZG_TRY(build_st_tables(ctx, st, plan, S, &tb));
+    if (split_st_tensor_dft(plan.sh.latlon, Lg)) {
+        // LonLat grids [lon][lat]: the longitude DFT on the tensor cores, to X[b][m][lat][re, im]
+        const DftTables* dt;
+        ZG_TRY(build_dft_tables(ctx, st, Lg, int(plan.sh.nlon), S, &dt));
+        ZG_TRY(dft_forward_stage(ctx, st, *dt, S, WK_ST_DFT_F, grids, plan.sh.size(), nlat, int(plan.sh.nlon), Lg, Lm,
+                                 batch, X));
+    }
     const int bits = 8;
     const long long per_m = 2LL * batch, rows = (long long)Lm * per_m;
     ZG_TRY(st->op[0].ensure(rows, r16(kh), S, 3));
@@ -2074,14 +2129,15 @@ int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int ba
 }
 
 int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* coeffs,
-                      long long csz, double* X) {
+                      long long csz, double* X, double* grids) {
     const int S = ctx->slices;
     if (S != 6) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split SH transforms need 6 slices");
     cudaStream_t s = ctx->stream;
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
     const int kh = plan.leg.nnodes, nlat = int(plan.sh.nlat), kl = r16((Lg + 1) / 2);
-    if (kh > SL_KMAX || kl > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: order too high");
+    if (Lg > SL_KMAX || kh > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split SH path: orders up to 2048");
+    const bool lonlat = split_st_tensor_dft(plan.sh.latlon, Lg);
     StSplitTables* tb;
     ZG_TRY(build_st_tables(ctx, st, plan, S, &tb));
     const int bits = 8;
@@ -2115,11 +2171,25 @@ int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int b
                                      }
                              },
                              &u));
+            // conjugated for the inverse DFT of a LonLat grid; the unfolding conjugates
+            const double sgi = lonlat ? -1.0 : 1.0;
             if (ch == 0)
                 return run_gemm_st<NT>(ctx, *u, tb->leg_bT, st->op[0], st->op[1],
-                                       EpiStLegBwdE<false>{E, batch, Lg, kh});
-            return run_gemm_st<NT>(ctx, *u, tb->leg_bT, st->op[0], st->op[1], EpiStLegBwdE<true>{E, batch, Lg, kh});
+                                       EpiStLegBwdE<false>{E, batch, Lg, kh, sgi});
+            return run_gemm_st<NT>(ctx, *u, tb->leg_bT, st->op[0], st->op[1],
+                                   EpiStLegBwdE<true>{E, batch, Lg, kh, sgi});
         }));
+    }
+    if (lonlat) {
+        // LonLat grids [lon][lat]: the inverse longitude DFT on the tensor cores,
+        // straight from the parity sums; X holds the cos sums
+        ZG_TRY(zero_parity_tails(ctx, E, batch, Lg, Lm, kh, 2));
+        const DftTables* dt;
+        ZG_TRY(build_dft_tables(ctx, st, Lg, int(plan.sh.nlon), S, &dt));
+        ZG_TRY(dft_backward_stage(ctx, st, *dt, S, WK_ST_DFT_B,
+                                  DftBwdLoader{E, Lg, nlat, 1, kh, plan.leg.j0u, plan.leg.j0d, batch}, nlat,
+                                  int(plan.sh.nlon), Lg, Lm, batch, grids, plan.sh.size(), X));
+        return split_finish(ctx);
     }
     {
         StageScope sc(ctx, ST_SPLIT_SLICE);
@@ -2136,7 +2206,7 @@ int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int b
 int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A, const double* B, double* C) {
     const int S = ctx->slices;
     const int NT = n_tile(S);
-    if (K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split GEMM: K above 992");
+    if (K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split GEMM: K above 2048");
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
     SliceArray a, b;

@@ -20,13 +20,18 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
                      double* coeffs);
 int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int Lm, int batch, const double* coeffs,
                       double* grids);
-// SH Legendre sums in split precision (6 slices): the folded spectra X
-// [b][m][lat][2] (after the forward FFT) -> coefficients of degrees < Lm, and
-// coefficients -> X (before the inverse FFT), as the FP64 sums do.
-int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* X,
+// True when the split SH path also runs the longitude DFT (on the tensor
+// cores, in place of the FP64 FFT): LonLat grids of order 2 and above.
+inline bool split_st_tensor_dft(bool latlon, int Lg) { return !latlon && Lg >= 2; }
+// SH transforms in split precision (6 slices).  Forward: grids -> the spectra
+// X[b][m][lat][2] (by the tensor-core DFT where split_st_tensor_dft; else X
+// already holds the forward FFT's output) -> coefficients of degrees < Lm.
+// Backward: coefficients -> grids where split_st_tensor_dft (X is scratch);
+// else -> X, for the caller's inverse FFT.
+int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* grids, double* X,
                      double* coeffs, long long csz);
 int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* coeffs,
-                      long long csz, double* X);
+                      long long csz, double* X, double* grids);
 // C = A B^T (A: M x K, B: N x K, C: M x N, row-major FP64 device buffers)
 int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A, const double* B, double* C);
 // BF16 tensor-core flops of the split GEMM launches since the last reset

@@ -454,14 +454,15 @@ int st_forward_dev(zest_gpu_context* ctx, int sn, int sp, int layout, int Lg, in
     ZG_TRY(get_fft(ctx, int(sh.nlon), &fft));
     ZG_TRY(ctx->s0.ensure((size_t)batch * Lg * sh.nlat * 2 * sizeof(double)));
     double* X = ctx->s0.as<double>();
-    {
+    const bool split = ctx->precision == ZEST_PRECISION_SPLIT;
+    if (!split || !split_st_tensor_dft(sh.latlon, Lg)) {
         StageScope sc(ctx, ST_FFT_FWD);
         if (layout == ZEST_LAYOUT_LATLON)
             ZG_TRY(launch_rfft_fwd(s, *fft, grids, sh.size(), 1, sh.nlon, int(sh.nlat), Lg, batch, 1, X));
         else
             ZG_TRY(launch_rfft_fwd(s, *fft, grids, sh.size(), sh.nlat, 1, int(sh.nlat), Lg, batch, 0, X));
     }
-    if (ctx->precision == ZEST_PRECISION_SPLIT) return split_st_forward(ctx, *plan, Lg, Lm, batch, X, coeffs, csz);
+    if (split) return split_st_forward(ctx, *plan, Lg, Lm, batch, grids, X, coeffs, csz);
     LegMeta lm;
     lm.P = plan->leg.Pf.as<double>();
     lm.off = plan->leg.off.as<long long>();
@@ -493,8 +494,11 @@ int st_backward_dev(zest_gpu_context* ctx, int sn, int sp, int layout, int Le, i
     ZG_TRY(get_fft(ctx, int(sh.nlon), &fft));
     ZG_TRY(ctx->s0.ensure((size_t)batch * Lg * sh.nlat * 2 * sizeof(double)));
     double* X = ctx->s0.as<double>();
-    if (ctx->precision == ZEST_PRECISION_SPLIT) {
-        ZG_TRY(split_st_backward(ctx, *plan, Lg, Lm, batch, coeffs, csz, X));
+    const bool split = ctx->precision == ZEST_PRECISION_SPLIT;
+    if (split && split_st_tensor_dft(sh.latlon, Lg))  // grids written by the tensor-core DFT
+        return split_st_backward(ctx, *plan, Lg, Lm, batch, coeffs, csz, X, grids);
+    if (split) {
+        ZG_TRY(split_st_backward(ctx, *plan, Lg, Lm, batch, coeffs, csz, X, grids));
         StageScope sc(ctx, ST_FFT_INV);
         if (layout == ZEST_LAYOUT_LATLON)
             return launch_rfft_inv(s, *fft, X, int(sh.nlat), Lg, batch, 1, grids, sh.size(), 1, sh.nlon);
@@ -1566,7 +1570,7 @@ int zest_gpu_st_rotate_vjp(zest_gpu_context* ctx, size_t order, size_t batch, co
 int zest_gpu_split_gemm(zest_gpu_context* ctx, size_t M, size_t N, size_t K, const double* A, const double* B,
                         double* C, int mem) {
     ZG_TRY(check_ctx(ctx));
-    if (M > (1u << 24) || N > (1u << 20) || K > 992) return fail(ZEST_GPU_ERR_INVALID, "split GEMM size out of range");
+    if (M > (1u << 24) || N > (1u << 20) || K > 2048) return fail(ZEST_GPU_ERR_INVALID, "split GEMM size out of range");
     if ((M * K && !A) || (N * K && !B) || (M * N && !C)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
     if (M == 0 || N == 0) return ZEST_GPU_OK;
     if (mem == ZEST_MEM_DEVICE) return split_dense_gemm(ctx, int(M), int(N), int(K), A, B, C);
