@@ -152,6 +152,30 @@ def test_split_zt_vs_fp64(ctx, L, batch):
     assert relmax(fs, f64) < SPLIT_TOL
 
 
+@pytest.mark.parametrize("spec", ["dft_f=48,leg_f=48,rad_f=48,rad_b=48,leg_b=96,dft_b=48",
+                                  "dft_f=96,leg_f=96,rad_f=96,rad_b=96,leg_b=96,dft_b=96"])
+def test_split_zt_column_tiles(ctx, monkeypatch, spec):
+    # ZEST_GPU_SPLIT_NT picks each stage's column tile (48: two accumulator
+    # sets in TMEM) for contexts created after it is set; every choice must
+    # give the same split-form results as the FP64 form
+    import zest_gb300
+    monkeypatch.setenv("ZEST_GPU_SPLIT_NT", spec)
+    rng = np.random.default_rng(77)
+    L, batch = 57, 3
+    c = rand_zt(rng, L, batch=batch).ravel()
+    g64 = ctx.zt_backward(c, L, batch=batch)
+    f64 = ctx.zt_forward(g64, L, batch=batch)
+    c2 = zest_gb300.Context(0)
+    try:
+        c2.set_precision(zest_gb300.PRECISION_SPLIT, 6)
+        gs = c2.zt_backward(c, L, batch=batch)
+        fs = c2.zt_forward(g64, L, batch=batch)
+    finally:
+        c2.close()
+    assert relmax(gs, g64) < SPLIT_TOL
+    assert relmax(fs, f64) < SPLIT_TOL
+
+
 def test_split_zt_config1_vs_golden(split, golden):
     g = golden("zt_config1")
     c = split.zt_forward(np.ascontiguousarray(g["grid"]).ravel(), 20)

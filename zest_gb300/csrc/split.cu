@@ -948,14 +948,17 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     // (the B tile is always loaded whole; the MMA reads its first N rows)
     static_assert(SC::NACC * NT <= 512, "accumulators must fit in TMEM");
     static_assert(NT % 48 == 0, "each epilogue warp owns whole 16-column chunks");
+    // Two accumulator sets when they fit in TMEM (NT = 48): the MMAs of the
+    // next unit then run while the epilogue drains the previous one.
+    constexpr int NBUF = 2 * SC::NACC * NT <= 512 ? 2 : 1;
 
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * STAGE);
     uint64_t* empty = full + NST;
-    uint64_t* tfull = empty + NST;
-    uint64_t* tempty = tfull + 1;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 1);
+    uint64_t* tfull = empty + NST;  // [NBUF]
+    uint64_t* tempty = tfull + 2;   // [NBUF]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long t_start = clock64();
@@ -964,8 +967,10 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(tfull, 1);
-        mbar_init(tempty, SP_EPI_WARPS);
+        for (int b = 0; b < NBUF; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], SP_EPI_WARPS);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -1023,8 +1028,11 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                 const SplitUnit u = P.units[ui];
                 const int nmma = min(NT, (u.n + 15) & ~15);
                 const uint32_t idesc = idesc_bf16_f32(SP_M, nmma);
+                // accumulator set of this unit: the k-th use of set b is unit tile = k NBUF + b
+                const int buf = NBUF == 2 ? (tile & 1) : 0;
+                const uint32_t tacc = tmem + (uint32_t)(buf * 256);
                 const long long w0 = clock64();
-                if (!mbar_wait(tempty, (tile & 1) ^ 1, P.err, 2)) { ok = false; break; }
+                if (!mbar_wait(&tempty[buf], ((tile / NBUF) & 1) ^ 1, P.err, 2)) { ok = false; break; }
                 if (P.dbg) atomicAdd(&P.dbg[1], (unsigned long long)(clock64() - w0));
                 tc_fence_after();
                 for (int kb = 0; kb < u.ksteps; ++kb, ++it) {
@@ -1047,14 +1055,14 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                         for (int s = 0; s < S; ++s) {
                             const int t = d - s;
                             if (t < 0 || t >= S) continue;
-                            umma_bf16(tmem + acc * NT, da + (uint64_t)((s * A_TILE) >> 4),
+                            umma_bf16(tacc + acc * NT, da + (uint64_t)((s * A_TILE) >> 4),
                                       db + (uint64_t)((SC::btile(d, t) * B_TILE) >> 4), idesc, first[acc] ? 0u : 1u);
                             first[acc] = false;
                         }
                     }
                     umma_commit(&empty[st]);
                 }
-                if (ok) umma_commit(tfull);
+                if (ok) umma_commit(&tfull[buf]);
             }
         }
         __syncwarp();
@@ -1081,8 +1089,10 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             const int eb_a = (ca < col0 + CW && ca < u.n) ? ebv[u.b_row0 + ca] : 0;
             const int eb_b = (CW > 32 && cb < col0 + CW && cb < u.n) ? ebv[u.b_row0 + cb] : 0;
             const typename Epi::Row R = epi.row(u, row);
+            const int buf = NBUF == 2 ? (tile & 1) : 0;
+            const uint32_t tacc = tmem + (uint32_t)(buf * 256);
             const long long w0 = clock64();
-            const bool got = mbar_wait(tfull, tile & 1, P.err, 4);
+            const bool got = mbar_wait(&tfull[buf], (tile / NBUF) & 1, P.err, 4);
             const long long w1 = clock64();
             if (!__all_sync(0xffffffffu, got)) break;
             tc_fence_after();
@@ -1104,7 +1114,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                 uint32_t v[SC::NACC][4];
 #pragma unroll
                 for (int a = 0; a < SC::NACC; ++a)
-                    tmem_ld4(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * NT + col0 + 4 * c), v[a]);
+                    tmem_ld4(tacc + ((uint32_t)(32 * q) << 16) + (uint32_t)(a * NT + col0 + 4 * c), v[a]);
                 tmem_ld_wait();
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
@@ -1127,7 +1137,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             tc_fence_before();
             __syncwarp();
             const long long w2 = clock64();
-            if (lane == 0) mbar_arrive(tempty);
+            if (lane == 0) mbar_arrive(&tempty[buf]);
             // phase 2 (overlaps the next tile's MMAs): FP64 results and stores
             if (active) {
 #pragma unroll
@@ -1282,6 +1292,12 @@ struct SliceArray {
 };
 
 // Sliced tables of one Zernike plan for one slice count.
+// work-list keys: (stage, Lg, Lm, batch, S, pass)
+enum {
+    WK_DFT_F = 0, WK_LEG_F, WK_RAD_F, WK_RAD_B, WK_LEG_B, WK_DFT_B, WK_DENSE, WK_ST_LEG_F, WK_ST_LEG_B,
+    WK_ST_DFT_F, WK_ST_DFT_B
+};
+
 // Sliced longitude DFT tables of one (order L, longitude count N): shared by
 // the Zernike grids and the SH LonLat grids of the same order.
 struct DftTables {
@@ -1324,8 +1340,21 @@ struct SplitState {
     DevBuf tmp;                 // FP64 staging of generated tables
     DevBuf cycles;              // role wait counters, kept when ZEST_GPU_SPLIT_CYCLES is set
     bool cycles_on = false;
+    int nt[16];                 // column tile (96 or 48) of each work-list stage
+    SplitState();
     double useful_flops = 0.0, issued_flops = 0.0;  // accumulated while profiling
 };
+
+// Column tiles: 96, except the backward Legendre stage of the Zernike
+// transforms.  Its sums are short (K = ceil(L/2)) and its outputs span the
+// ceil((L+1)/2) folded nodes (101 at order 200: tiles of 96 + 5); with 48 the
+// MMAs overlap the epilogue's drain (two accumulator sets).  Measured at order
+// 200 x 64: 41.7 ms of GEMMs instead of 44.0; 48 for the other stages was no
+// faster.
+SplitState::SplitState() {
+    for (int& v : nt) v = 96;
+    nt[WK_LEG_B] = 48;
+}
 
 void destroy_split(SplitState* s) { delete s; }
 
@@ -1424,6 +1453,27 @@ int get_state(zest_gpu_context* ctx, SplitState** out) {
     if (!ctx->split) {
         ctx->split.reset(new SplitState());
         ctx->split->cycles_on = std::getenv("ZEST_GPU_SPLIT_CYCLES") != nullptr;
+        // tuning override of the column tiles, "stage=nt,..." with stage one of
+        // dft_f leg_f rad_f rad_b leg_b dft_b st_dft_f st_dft_b and nt 48 or 96
+        if (const char* e = std::getenv("ZEST_GPU_SPLIT_NT")) {
+            static const char* names[] = {"dft_f", "leg_f", "rad_f", "rad_b", "leg_b", "dft_b", "dense",
+                                          "st_leg_f", "st_leg_b", "st_dft_f", "st_dft_b"};
+            std::string spec(e);
+            size_t pos = 0;
+            while (pos < spec.size()) {
+                size_t end = spec.find(',', pos);
+                if (end == std::string::npos) end = spec.size();
+                const std::string item = spec.substr(pos, end - pos);
+                const size_t eq = item.find('=');
+                if (eq != std::string::npos) {
+                    const std::string key = item.substr(0, eq);
+                    const int v = std::atoi(item.c_str() + eq + 1);
+                    for (int i = 0; i < int(sizeof(names) / sizeof(names[0])); ++i)
+                        if (key == names[i] && (v == 48 || v == 96)) ctx->split->nt[i] = v;
+                }
+                pos = end + 1;
+            }
+        }
         ZG_TRY(ctx->split->err.ensure(16));
         ZG_CUDA_TRY(cudaMemsetAsync(ctx->split->err.p, 0, 16, ctx->stream));
         ZG_CUDA_TRY(cudaHostAlloc((void**)&ctx->split->host_err, sizeof(int), cudaHostAllocMapped));
@@ -1695,6 +1745,14 @@ int run_gemm(zest_gpu_context* ctx, int S, UnitList& ul, const SliceArray& A0, c
     return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path supports 4..6 slices");
 }
 
+// run_gemm with the column tile chosen at run time (48: six slices only)
+template <class Epi>
+int run_gemm_nt(zest_gpu_context* ctx, int nt, int S, UnitList& ul, const SliceArray& A0, const SliceArray& A1,
+                const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
+    if (nt == 48) return run_gemm<48>(ctx, S, ul, A0, A1, B0, B1, epi);
+    return run_gemm<96>(ctx, S, ul, A0, A1, B0, B1, epi);
+}
+
 // tiles of a group: operand rows [a0, a0 + arows) x table rows [b0, b0 + nrows), K = kk
 void add_units(UnitList& ul, int S, int bits, long long a0, long long arows, int b0, int nrows, int NT, int kk,
                int flags, int g, int k0 = 0) {
@@ -1720,11 +1778,11 @@ void add_units(UnitList& ul, int S, int bits, long long a0, long long arows, int
         }
 }
 
-// work-list keys: (stage, Lg, Lm, batch, S, pass)
-enum {
-    WK_DFT_F = 0, WK_LEG_F, WK_RAD_F, WK_RAD_B, WK_LEG_B, WK_DFT_B, WK_DENSE, WK_ST_LEG_F, WK_ST_LEG_B,
-    WK_ST_DFT_F, WK_ST_DFT_B
-};
+
+// Column tile of a stage's launches: 96 by default; 48 (two accumulator sets
+// in TMEM) only with six slices.  Also part of the work-list key.
+inline int stage_nt(const SplitState* st, int wk, int S) { return S == 6 ? st->nt[wk] : 96; }
+inline int nt_pass(int nt) { return nt == 48 ? 1 << 16 : 0; }
 
 // Longitude DFT of `batch` grids x[b][lon][col] (C columns, item stride gsz)
 // to the spectra G[b][m][col][re, im], m < Lm (L = Lg orders per item):
@@ -1732,7 +1790,7 @@ enum {
 // sin), K-chunked.  `wk` keys the work lists of the caller's grid family.
 int dft_forward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t, int S, int wk, const double* grids,
                       long long gsz, int C, int N, int Lg, int Lm, int batch, double* G) {
-    const int NT = n_tile(S), bits = digit_bits(Lg);
+    const int NT = stage_nt(st, wk, S), bits = digit_bits(Lg);
     const long long rows = (long long)batch * C;
     ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
     ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
@@ -1744,7 +1802,7 @@ int dft_forward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t,
     for (int ch = 0; ch < nchunks(Lg); ++ch) {
         const int k0 = ch * KCHUNK;
         UnitList* u;
-        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 8 * ch + nt_pass(NT)), [&](UnitList& ul) {
             for (long long r = 0; r < rows; r += SP_M) {
                 const long long rr = std::min<long long>(SP_M, rows - r);
                 add_units(ul, S, bits, r, rr, 0, Lm, NT, std::min(KCHUNK, Lg - k0), 0, 0, k0);
@@ -1752,9 +1810,9 @@ int dft_forward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t,
             }
         }, &u));
         if (ch == 0)
-            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], t.cos_f, t.sin_f, EpiDftFwd<false>{G, C, Lg}));
+            ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], t.cos_f, t.sin_f, EpiDftFwd<false>{G, C, Lg}));
         else
-            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], t.cos_f, t.sin_f, EpiDftFwd<true>{G, C, Lg}));
+            ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], t.cos_f, t.sin_f, EpiDftFwd<true>{G, C, Lg}));
     }
     return ZEST_GPU_OK;
 }
@@ -1781,7 +1839,7 @@ int zero_parity_tails(zest_gpu_context* ctx, double* E, int batch, int Lg, int L
 int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t, int S, int wk,
                        const DftBwdLoader& ld, int C, int N, int Lg, int Lm, int batch, double* grids, long long gsz,
                        double* Cs) {
-    const int NT = n_tile(S), bits = digit_bits(Lg);
+    const int NT = stage_nt(st, wk, S), bits = digit_bits(Lg);
     const long long rows = (long long)batch * C;
     ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
     ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
@@ -1792,32 +1850,32 @@ int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t
     for (int ch = 0; ch < nchunks(Lg); ++ch) {
         const int k0 = ch * KCHUNK;
         UnitList* u;
-        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 8 * ch + nt_pass(NT)), [&](UnitList& ul) {
             for (long long r = 0; r < rows; r += SP_M)
                 add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, std::min(KCHUNK, Lg - k0),
                           0, 0, k0);
         }, &u));
         if (ch == 0)
-            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], t.cos_b, t.sin_b,
+            ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], t.cos_b, t.sin_b,
                             EpiDftBwdCos<false>{grids, Cs, C, N, Lg, gsz}));
         else
-            ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], t.cos_b, t.sin_b,
+            ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], t.cos_b, t.sin_b,
                             EpiDftBwdCos<true>{grids, Cs, C, N, Lg, gsz}));
     }
     // the sin pass after every cos chunk: its first chunk reads the finished C_i
     for (int ch = 0; Lg > 1 && ch < nchunks(Lg - 1); ++ch) {
         const int k0 = ch * KCHUNK;
         UnitList* v;
-        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 1 + 8 * ch), [&](UnitList& ul) {
+        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 1 + 8 * ch + nt_pass(NT)), [&](UnitList& ul) {
             for (long long r = 0; r < rows; r += SP_M)
                 add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg - 1, NT,
                           std::min(KCHUNK, Lg - 1 - k0), 1 | 2 | 4, 0, k0);
         }, &v));
         if (ch == 0)
-            ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], t.cos_b, t.sin_b,
+            ZG_TRY(run_gemm_nt(ctx, NT, S, *v, st->op[0], st->op[1], t.cos_b, t.sin_b,
                             EpiDftBwdSin<false>{grids, Cs, C, N, Lg, gsz}));
         else
-            ZG_TRY(run_gemm(ctx, S, *v, st->op[0], st->op[1], t.cos_b, t.sin_b,
+            ZG_TRY(run_gemm_nt(ctx, NT, S, *v, st->op[0], st->op[1], t.cos_b, t.sin_b,
                             EpiDftBwdSin<true>{grids, Cs, C, N, Lg, gsz}));
     }
     return ZEST_GPU_OK;
@@ -1887,7 +1945,6 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
                      double* coeffs) {
     (void)Le;
     const int S = ctx->slices;
-    const int NT = n_tile(S);
     cudaStream_t s = ctx->stream;
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
@@ -1909,6 +1966,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
     ZG_TRY(dft_forward_stage(ctx, st, *tb->dft, S, WK_DFT_F, grids, sh.size(), C, N, Lg, Lm, batch, G));
     // ---- Legendre (folded over the equator) ----
     {
+        const int NT = stage_nt(st, WK_LEG_F, S);
         const int bits = digit_bits(kh);
         const long long per_m = (long long)batch * nr2;
         const long long rows = (long long)Lm * per_m;
@@ -1922,7 +1980,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
         for (int ch = 0; ch < nchunks(kh); ++ch) {
             const int k0 = ch * KCHUNK;
             UnitList* u;
-            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_F), Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_F), Lg, Lm, batch, S, 8 * ch + nt_pass(NT)), [&](UnitList& ul) {
                 for (int m = 0; m < Lm; ++m)
                     for (int p = 0; p < 2; ++p) {
                         const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
@@ -1931,13 +1989,14 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
                     }
             }, &u));
             if (ch == 0)
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd<false>{flm, batch, nr2}));
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd<false>{flm, batch, nr2}));
             else
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd<true>{flm, batch, nr2}));
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd<true>{flm, batch, nr2}));
         }
     }
     // ---- radial ----
     {
+        const int NT = stage_nt(st, WK_RAD_F, S);
         const int bits = digit_bits(nr);
         const long long rows = tri_size(Lm) * batch * 2;
         ZG_TRY(st->op[0].ensure(rows, r16(nr), S));
@@ -1948,15 +2007,15 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
         for (int ch = 0; ch < nchunks(nr); ++ch) {
             const int k0 = ch * KCHUNK;
             UnitList* u;
-            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_F), Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_F), Lg, Lm, batch, S, 8 * ch + nt_pass(NT)), [&](UnitList& ul) {
                 for (int l = 0; l < Lm; ++l)
                     add_units(ul, S, bits, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2,
                               int(plan.rad.off_h[l]), (Lm - l + 1) / 2, NT, std::min(KCHUNK, nr - k0), 0, l, k0);
             }, &u));
             if (ch == 0)
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd<false>{coeffs, batch, csz}));
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd<false>{coeffs, batch, csz}));
             else
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd<true>{coeffs, batch, csz}));
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd<true>{coeffs, batch, csz}));
         }
     }
     return split_finish(ctx);
@@ -1965,7 +2024,6 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
 int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int Lm, int batch, const double* coeffs,
                       double* grids) {
     const int S = ctx->slices;
-    const int NT = n_tile(S);
     cudaStream_t s = ctx->stream;
     SplitState* st;
     ZG_TRY(get_state(ctx, &st));
@@ -1987,6 +2045,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
 
     // ---- radial: coefficients -> flm ----
     {
+        const int NT = stage_nt(st, WK_RAD_B, S);
         const int bits = digit_bits((Lg + 1) / 2);
         const long long rows = tri_size(Lm) * batch * 2;
         ZG_TRY(st->op[0].ensure(rows, kl, S));
@@ -1998,19 +2057,20 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
         for (int ch = 0; ch < nchunks((Lm + 1) / 2); ++ch) {
             const int k0 = ch * KCHUNK;
             UnitList* u;
-            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_B), Lg, Lm, batch, S, 8 * ch), [&](UnitList& ul) {
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_RAD_B), Lg, Lm, batch, S, 8 * ch + nt_pass(NT)), [&](UnitList& ul) {
                 for (int l = 0; l < Lm; ++l)
                     add_units(ul, S, bits, tri_idx(l, 0) * batch * 2, (long long)(l + 1) * batch * 2, l * nr, nr, NT,
                               std::min(KCHUNK, (Lm - l + 1) / 2 - k0), 0, l, k0);
             }, &u));
             if (ch == 0)
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<false>{flm, nr}));
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<false>{flm, nr}));
             else
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<true>{flm, nr}));
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<true>{flm, nr}));
         }
     }
     // ---- Legendre: flm -> G (north/south unfold; parity 1 read-modify-write) ----
     {
+        const int NT = stage_nt(st, WK_LEG_B, S);
         const int bits = digit_bits((Lg + 1) / 2);
         const long long per_m = (long long)batch * nr2;
         const long long rows = (long long)Lm * per_m;
@@ -2026,7 +2086,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             for (int ch = 0; ch < nchunks((Lm + 1) / 2); ++ch) {
             const int k0 = ch * KCHUNK;
             UnitList* u;
-            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_B), Lg, Lm, batch, S, p + 8 * ch), [&](UnitList& ul) {
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_B), Lg, Lm, batch, S, p + 8 * ch + nt_pass(NT)), [&](UnitList& ul) {
                 for (int m = 0; m < Lm; ++m) {
                     const int cnt = (Lm - m - p > 0) ? (Lm - m - p + 1) / 2 : 0;
                     if (cnt == 0) continue;
@@ -2035,10 +2095,10 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                 }
             }, &u));
             if (ch == 0)
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
                                 EpiLegBwdE<false>{E, batch, Lg, kh, nr2}));
             else
-                ZG_TRY(run_gemm(ctx, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
                                 EpiLegBwdE<true>{E, batch, Lg, kh, nr2}));
         }
     }
