@@ -83,7 +83,7 @@ def test_split_gemm_random(ctx, S):
 
 def split_model(A, B, S):
     """Integer model of the split product: balanced base-256 digits of the
-    row-scaled operands, levels 0..S-1 summed exactly over K-chunks of at most
+    row-scaled operands (rounded to nearest, ties away from zero), levels 0..S-1 summed exactly over K-chunks of at most
     256 terms, each chunk scaled by 2^(eA + eB - 8 (S + 1)) and the chunks
     added in FP64, first to last."""
     K = A.shape[1]
@@ -93,7 +93,8 @@ def split_model(A, B, S):
     def digits(X):
         E = np.frexp(np.abs(X).max(axis=1))[1]
         e = E + 1
-        v = np.rint(X * np.exp2(bits * S - e)[:, None]).astype(np.int64)
+        y = X * np.exp2(bits * S - e)[:, None]  # exact: a power-of-two scale
+        v = (np.sign(y) * np.floor(np.abs(y) + 0.5)).astype(np.int64)  # ties away from zero
         d = np.zeros((S,) + X.shape, dtype=np.int64)
         w = v.copy()
         for s in range(S - 1, 0, -1):

@@ -7,7 +7,7 @@
 //     C[r, n] = sum_k A[r, k] B[n, k]
 // with FP64 operands represented in BF16 fixed-point slices:
 //   * each operand row gets an exponent e (|x| < 2^(e-1) over the row) and
-//     its values are rounded to v = round(x 2^{8S - e}) (ties to even);
+//     its values are rounded to v = round(x 2^{8S - e}) (ties away from zero);
 //   * v is cut into S balanced base-256 digits d_s in [-128, 127] (the
 //     leading one in [-128, 128]), each exact in BF16;
 //   * the products d_s(A) d_t(B) with s + t = level <= S - 1 (21 products at
@@ -216,19 +216,22 @@ __device__ __forceinline__ double i64_ldexp(long long T, int E) {
     return (a == 0 || eff <= 0) ? 0.0 : v;
 }
 
-// fixed point: round(x 2^{nbits-e}) as int64 (|x| < 2^(e-1)), ties to even
-// The row exponents leave at least one bit of headroom above every element,
-// so the shift is at least 6; shifts of 63 and more round to 0.  Without
-// branches: round to nearest, ties to even (add half - 1 and the parity of
-// the kept part), zero and subnormals give 0.
+// fixed point: round(x 2^{nbits-e}) as int64 (|x| < 2^(e-1)), ties away from
+// zero.  The row exponents leave at least one bit of headroom above every
+// element, so the shift is at least 6.  Without branches: q = |x| 2^{nbits-e+1}
+// truncated (one bit more than kept), then ((q ^ s) + 1) >> 1 with s the sign
+// mask (arithmetic shift) is floor(q/2 + 1/2) for x >= 0 and its negative for
+// x < 0.  The implicit bit is set for a zero or subnormal x too: the slicing
+// keeps every row exponent at or above 64 - 1021, where their shift is at
+// least 53 and q = 0.
 __device__ __forceinline__ long long to_fixed(double x, int e, int nbits) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    const int E = int(bits >> 52) & 0x7FF;
-    const unsigned long long M = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = min(max(1075 + e - nbits - E, 1), 63);
-    unsigned long long v = (M + ((1ull << (sh - 1)) - 1) + ((M >> sh) & 1ull)) >> sh;
-    v = E == 0 ? 0ull : v;
-    return (bits >> 63) ? -(long long)v : (long long)v;
+    const long long bits = __double_as_longlong(x);
+    const int E = int((unsigned long long)bits >> 52) & 0x7FF;
+    const unsigned long long M = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh1 = min(max(1074 + e - nbits - E, 0), 62);  // the shift less one
+    const long long q = (long long)(M >> sh1);
+    const long long sg = bits >> 63;  // 0 or -1
+    return ((q ^ sg) + 1) >> 1;
 }
 
 __device__ __forceinline__ int biased_exp(double x) {
@@ -492,7 +495,9 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
     __shared__ typename Loader::Row rowh[32];
     const long long row0 = (long long)blockIdx.x * R;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    if (threadIdx.x < 32) emax[threadIdx.x] = 0;
+    // row exponents of at least 64 (2^-959): below that every value rounds to
+    // 0 (and to_fixed needs no test for zero)
+    if (threadIdx.x < 32) emax[threadIdx.x] = 64;
     if (threadIdx.x < R && row0 + threadIdx.x < J.rows) rowh[threadIdx.x] = ld.row(row0 + threadIdx.x);
     __syncthreads();
     if (Loader::ROW_FAST) {
@@ -546,7 +551,7 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
                 }
             }
             for (int o = 16; o > 0; o >>= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
-            if (lane == 0) emax[r] = tmax;
+            if (lane == 0) emax[r] = max(tmax, 64);
         }
     }
     __syncthreads();
@@ -566,24 +571,34 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
         }
         const double* ru = vu + r * K;
         const double* rd = vd + r * K;
+        // fixed-point values of this lane's pair (k, k + 1) at pair index g;
+        // those of the next iteration are computed one iteration ahead, so
+        // that lane 31's element k + 2 (a shifted second array) is lane 0's
+        // next first element, taken by a shuffle
+        auto fixed_pair = [&](int g, long long* u, long long* d) {
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int kk = 2 * g + q;
+                u[q] = kk < K ? to_fixed(ru[kk], er, nbits) : 0;
+                d[q] = (Loader::TWO && kk < K) ? to_fixed(rd[kk], er, nbits) : 0;
+            }
+        };
+        long long cu[2], cd[2];
+        fixed_pair(lane, cu, cd);
         for (int g0 = 0; g0 < np; g0 += 32) {
             const int g = g0 + lane;
             const int k = 2 * g;
-            // fixed-point values of elements k, k+1 (and k+2 for a shifted second array)
-            long long fu[3] = {0, 0, 0}, fd[3] = {0, 0, 0};
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                if (k + q < K) {
-                    fu[q] = to_fixed(ru[k + q], er, nbits);
-                    if (Loader::TWO) fd[q] = to_fixed(rd[k + q], er, nbits);
-                }
-            }
-            if (two && J.shift) {  // element k + 2: the next lane's first, or read for the last lane
-                fu[2] = __shfl_down_sync(0xffffffffu, fu[0], 1);
-                fd[2] = __shfl_down_sync(0xffffffffu, fd[0], 1);
-                if (lane == 31 && k + 2 < K) {
-                    fu[2] = to_fixed(ru[k + 2], er, nbits);
-                    if (Loader::TWO) fd[2] = to_fixed(rd[k + 2], er, nbits);
+            long long nu[2] = {0, 0}, nd[2] = {0, 0};
+            if (g0 + 32 < np) fixed_pair(g + 32, nu, nd);  // warp-uniform
+            long long fu[3] = {cu[0], cu[1], 0}, fd[3] = {cd[0], cd[1], 0};
+            if (two && J.shift) {  // element k + 2: the next lane's first; lane 31's from lane 0, one step on
+                fu[2] = __shfl_down_sync(0xffffffffu, cu[0], 1);
+                fd[2] = __shfl_down_sync(0xffffffffu, cd[0], 1);
+                const long long wu = __shfl_sync(0xffffffffu, nu[0], 0);
+                const long long wd = __shfl_sync(0xffffffffu, nd[0], 0);
+                if (lane == 31) {
+                    fu[2] = wu;
+                    fd[2] = wd;
                 }
             }
             if (k < J.Kp0) {
@@ -614,6 +629,11 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
                     w[q] = x;
                 }
                 write_digits2<S>(w[0], w[1], J.copies, J.out1, J.stride1, row * J.Kp1 + k);
+            }
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                cu[q] = nu[q];
+                cd[q] = nd[q];
             }
         }
     }
