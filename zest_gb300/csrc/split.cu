@@ -265,6 +265,8 @@ inline int slice_rows_per_block(int K, bool two) {
     return r;
 }
 
+enum { SL_ONE = 0, SL_FOLD = 1, SL_PAIR = 2 };
+
 // Loaders give the pair (up, dn) of operand element (row, k) through a per-row
 // handle computed once per block row.  ROW_FAST loaders read consecutive rows
 // at one k contiguously; the others read consecutive k of one row.  TWO
@@ -272,6 +274,7 @@ inline int slice_rows_per_block(int K, bool two) {
 // operands), the others only `up`.
 struct RowMajorLoader {  // tables and dense operands: p[r*ld + k]
     static constexpr bool ROW_FAST = false, TWO = false;
+    static constexpr int MODE = SL_ONE, SHIFT = 0;
     const double* p;
     long long ld;
     struct Row { const double* p; };
@@ -283,6 +286,7 @@ struct RowMajorLoader {  // tables and dense operands: p[r*ld + k]
 // Folded: cos operand x_k + x_{N-k} (k < L), sin operand x_k - x_{N-k} at k - 1.
 struct DftFwdLoader {
     static constexpr bool ROW_FAST = true, TWO = true;
+    static constexpr int MODE = SL_FOLD, SHIFT = 1;
     const double* grid;
     long long gsz;
     int C, N;
@@ -300,6 +304,7 @@ struct DftFwdLoader {
 // rows (m, b, kc) of the spectra; k = folded latitude node (north, south).
 struct LegFwdLoader {
     static constexpr bool ROW_FAST = true, TWO = true;
+    static constexpr int MODE = SL_FOLD, SHIFT = 0;
     const double* G;
     int B, L, Nt, nr2, j0u, j0d;
     struct Row { const double* base; };
@@ -317,6 +322,7 @@ struct LegFwdLoader {
 
 struct RadFwdLoader {  // rows ((t B + b) 2 + c); k = radial node
     static constexpr bool ROW_FAST = false, TWO = false;
+    static constexpr int MODE = SL_ONE, SHIFT = 0;
     const double* flm;
     int nr;
     struct Row { const double* p; };
@@ -326,6 +332,7 @@ struct RadFwdLoader {  // rows ((t B + b) 2 + c); k = radial node
 
 struct RadBwdLoader {  // rows ((tri(l,m) B + b) 2 + c); k = i, n = l + 2i
     static constexpr bool ROW_FAST = false, TWO = false;
+    static constexpr int MODE = SL_ONE, SHIFT = 0;
     const double* coeffs;
     long long cs;
     int B, Lm;
@@ -350,6 +357,7 @@ struct RadBwdLoader {  // rows ((tri(l,m) B + b) 2 + c); k = i, n = l + 2i
 // rows (m, b, kc) of flm; k = i: up = flm(l = m + 2i), dn = flm(l = m + 1 + 2i)
 struct LegBwdLoader {
     static constexpr bool ROW_FAST = true, TWO = true;
+    static constexpr int MODE = SL_PAIR, SHIFT = 0;
     const double* flm;
     int B, nr2, Lm;
     struct Row { const double* base; int m; };
@@ -371,6 +379,7 @@ struct LegBwdLoader {
 // (l = m + 2i, l + 1), zero from Lm on (the two parity operands).
 struct StLegBwdLoader {
     static constexpr bool ROW_FAST = true, TWO = true;
+    static constexpr int MODE = SL_PAIR, SHIFT = 0;
     const double* c;
     long long cs;
     int B, Lm;
@@ -394,6 +403,7 @@ struct StLegBwdLoader {
 // (the equator, j0u = j0d, is north).
 struct DftBwdLoader {
     static constexpr bool ROW_FAST = true, TWO = true;
+    static constexpr int MODE = SL_PAIR, SHIFT = 1;
     const double* E;
     int L, C, nrad, kh, j0u, j0d, B;
     struct Row { const double* e0; double sg; };
@@ -414,15 +424,15 @@ struct DftBwdLoader {
     }
 };
 
-// One slicing job: one operand array (mode SL_ONE, optionally folded) or two
-// from one read of the input (SL_FOLD: up + dn and up - dn; SL_PAIR: up and
-// dn), the second at index k - shift.  Both share the row exponents.
-enum { SL_ONE = 0, SL_FOLD = 1, SL_PAIR = 2 };
+// One slicing job: one operand array (SL_ONE) or two from one read of the
+// input (SL_FOLD: up + dn and up - dn; SL_PAIR: up and dn), the second at
+// index k - shift.  Both share the row exponents.  Each loader fixes its mode
+// and shift (Loader::MODE, Loader::SHIFT), so the kernel is specialised.
 struct SliceJob {
     long long rows;
     int K;       // staged k range (K0, and K1 + shift for the second array)
-    int S, bits, mode, fold, R, lr, copies;  // lr = log2(R)
-    int K0, Kp0, K1, Kp1, shift;
+    int S, bits, R, lr, copies;  // lr = log2(R)
+    int K0, Kp0, K1, Kp1;
     __nv_bfloat16* out0;
     __nv_bfloat16* out1;
     long long stride0, stride1;  // elements between slices
@@ -445,7 +455,7 @@ __device__ __forceinline__ uint32_t digit_f32_bits(int d, float scale) {
 // 0x4B4000bb = 2^23 + 2^22 + byte, and one subtraction of 2^23 + 2^22 + 128.
 template <int S>
 __device__ __forceinline__ void write_digits2(long long w0, long long w1, int copies, __nv_bfloat16* out,
-                                              long long stride, long long off) {
+                                              long long stride, long long off, bool active) {
     constexpr long long OFF = (long long)((0x8080808080808080ull) >> (8 * (9 - S)));  // 128 per lower byte
     float f[2][S];
     const long long u[2] = {w0 + OFF, w1 + OFF};
@@ -461,16 +471,21 @@ __device__ __forceinline__ void write_digits2(long long w0, long long w1, int co
     }
     uint32_t* o = reinterpret_cast<uint32_t*>(out + off);
     const long long s2 = stride >> 1;  // slice stride in BF16 pairs (slice strides are even)
+    // lanes past the row's end compute but store nothing (no divergent branch)
     if (copies == 1) {
 #pragma unroll
-        for (int s = 0; s < S; ++s) o[s * s2] = __byte_perm(__float_as_uint(f[0][s]), __float_as_uint(f[1][s]), 0x7632);
+        for (int s = 0; s < S; ++s) {
+            const uint32_t v = __byte_perm(__float_as_uint(f[0][s]), __float_as_uint(f[1][s]), 0x7632);
+            if (active) o[s * s2] = v;
+        }
     } else {
         for (int c = 0; c < copies; ++c) {
             const float sc = __int_as_float((127 - 8 * c) << 23);  // 2^{-8 c}, exact
 #pragma unroll
-            for (int s = 0; s < S; ++s)
-                o[(c * S + s) * s2] =
-                    __byte_perm(__float_as_uint(f[0][s] * sc), __float_as_uint(f[1][s] * sc), 0x7632);
+            for (int s = 0; s < S; ++s) {
+                const uint32_t v = __byte_perm(__float_as_uint(f[0][s] * sc), __float_as_uint(f[1][s] * sc), 0x7632);
+                if (active) o[(c * S + s) * s2] = v;
+            }
         }
     }
 }
@@ -555,8 +570,10 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
         }
     }
     __syncthreads();
-    const bool two = J.mode != SL_ONE;
-    const int fold_bit = (J.mode == SL_FOLD || (J.mode == SL_ONE && J.fold)) ? 1 : 0;
+    constexpr int MODE = Loader::MODE, SHIFT = Loader::SHIFT;
+    constexpr bool two = MODE != SL_ONE;
+    constexpr int fold_bit = MODE == SL_FOLD ? 1 : 0;
+    static_assert(two == Loader::TWO && (SHIFT == 0 || (two && SHIFT == 1)), "loader mode");
     const int nbits = J.bits * S;
     const int np = (two ? max(J.Kp0, J.Kp1) : J.Kp0) >> 1;  // pairs per row
     for (int r = warp; r < R; r += nw) {
@@ -591,7 +608,7 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
             long long nu[2] = {0, 0}, nd[2] = {0, 0};
             if (g0 + 32 < np) fixed_pair(g + 32, nu, nd);  // warp-uniform
             long long fu[3] = {cu[0], cu[1], 0}, fd[3] = {cd[0], cd[1], 0};
-            if (two && J.shift) {  // element k + 2: the next lane's first; lane 31's from lane 0, one step on
+            if constexpr (two && SHIFT == 1) {  // element k + 2: the next lane's first; lane 31's from lane 0, one step on
                 fu[2] = __shfl_down_sync(0xffffffffu, cu[0], 1);
                 fd[2] = __shfl_down_sync(0xffffffffu, cd[0], 1);
                 const long long wu = __shfl_sync(0xffffffffu, nu[0], 0);
@@ -601,34 +618,28 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
                     fd[2] = wd;
                 }
             }
-            if (k < J.Kp0) {
+            {
                 long long w[2];
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     long long x = 0;
                     if (k + q < J.K0) {
                         x = fu[q];
-                        if (J.mode == SL_FOLD || (J.mode == SL_ONE && J.fold == 1)) x += fd[q];
-                        else if (J.mode == SL_ONE && J.fold == 2) x -= fd[q];
+                        if constexpr (MODE == SL_FOLD) x += fd[q];
                     }
                     w[q] = x;
                 }
-                write_digits2<S>(w[0], w[1], J.copies, J.out0, J.stride0, row * J.Kp0 + k);
+                write_digits2<S>(w[0], w[1], J.copies, J.out0, J.stride0, row * J.Kp0 + k, k < J.Kp0);
             }
-            if (two && k < J.Kp1) {
+            if constexpr (two) {
                 long long w[2];
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     long long x = 0;
-                    if (k + q < J.K1) {
-                        const int src = q + J.shift;  // shift is 0 or 1
-                        const long long a = src == 0 ? fu[0] : (src == 1 ? fu[1] : fu[2]);
-                        const long long b = src == 0 ? fd[0] : (src == 1 ? fd[1] : fd[2]);
-                        x = J.mode == SL_FOLD ? a - b : b;
-                    }
+                    if (k + q < J.K1) x = MODE == SL_FOLD ? fu[q + SHIFT] - fd[q + SHIFT] : fd[q + SHIFT];
                     w[q] = x;
                 }
-                write_digits2<S>(w[0], w[1], J.copies, J.out1, J.stride1, row * J.Kp1 + k);
+                write_digits2<S>(w[0], w[1], J.copies, J.out1, J.stride1, row * J.Kp1 + k, k < J.Kp1);
             }
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
@@ -1406,7 +1417,6 @@ int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
     J.R = slice_rows_per_block(J.K, Loader::TWO);
     J.lr = 0;
     while ((1 << J.lr) < J.R) ++J.lr;
-    if (J.shift < 0 || J.shift > 1) return fail(ZEST_GPU_ERR_INVALID, "split path: slice shift");
     const size_t smem = (size_t)(Loader::TWO ? 2 : 1) * J.R * J.K * sizeof(double);
     const long long blocks = (J.rows + J.R - 1) / J.R;
     auto go = [&](auto kern) -> int {
@@ -1422,9 +1432,10 @@ int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
     return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path supports 4..6 slices");
 }
 
-// One operand array from `up` (fold 0) or up +- dn (fold 1 / 2).
+// One operand array from `up`.
 template <class Loader>
-int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S, int bits, int fold, SliceArray& out) {
+int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S, int bits, SliceArray& out) {
+    static_assert(Loader::MODE == SL_ONE, "one-array loader");
     out.bits = bits;
     SliceJob J{};
     J.rows = rows;
@@ -1432,8 +1443,6 @@ int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S,
     J.Kp0 = out.Kp;
     J.S = S;
     J.bits = bits;
-    J.mode = SL_ONE;
-    J.fold = fold;
     J.copies = out.copies;
     J.out0 = out.ptr();
     J.stride0 = out.rows * out.Kp;
@@ -1449,15 +1458,15 @@ int launch_slice2(cudaStream_t s, const Loader& ld, long long rows, int K0, int 
     out0.bits = out1.bits = bits;
     SliceJob J{};
     J.rows = rows;
+    if (mode != Loader::MODE || shift != Loader::SHIFT)
+        return fail(ZEST_GPU_ERR_INVALID, "split path: slicing mode of the loader");
     J.K0 = K0;
     J.K1 = K1;
-    J.shift = shift;
     J.K = std::max(K0, K1 + shift);
     J.Kp0 = out0.Kp;
     J.Kp1 = out1.Kp;
     J.S = S;
     J.bits = bits;
-    J.mode = mode;
     J.copies = out0.copies;
     if (out1.copies != out0.copies) return fail(ZEST_GPU_ERR_INVALID, "split path: slice copies differ");
     J.out0 = out0.ptr();
@@ -1562,7 +1571,7 @@ __global__ void transpose_blocks_kernel(const double* __restrict__ in, const lon
 int slice_table(zest_gpu_context* ctx, const double* src, long long rows, int K, int ld, int S, int bits,
                 SliceArray& dst, int copies = 3) {
     ZG_TRY(dst.ensure(rows, r16(K), S, copies));
-    return launch_slice(ctx->stream, RowMajorLoader{src, ld}, rows, K, S, bits, 0, dst);
+    return launch_slice(ctx->stream, RowMajorLoader{src, ld}, rows, K, S, bits, dst);
 }
 
 // The longitude DFT tables of order L over N longitudes, sliced (cached).
@@ -2022,7 +2031,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
         ZG_TRY(st->op[0].ensure(rows, r16(nr), S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, RadFwdLoader{flm, nr}, rows, nr, S, bits, 0, st->op[0]));
+            ZG_TRY(launch_slice(s, RadFwdLoader{flm, nr}, rows, nr, S, bits, st->op[0]));
         }
         for (int ch = 0; ch < nchunks(nr); ++ch) {
             const int k0 = ch * KCHUNK;
@@ -2071,7 +2080,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
         ZG_TRY(st->op[0].ensure(rows, kl, S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, RadBwdLoader{coeffs, csz, batch, Lm}, rows, (Lm + 1) / 2, S, bits, 0,
+            ZG_TRY(launch_slice(s, RadBwdLoader{coeffs, csz, batch, Lm}, rows, (Lm + 1) / 2, S, bits,
                                 st->op[0]));
         }
         for (int ch = 0; ch < nchunks((Lm + 1) / 2); ++ch) {
@@ -2293,8 +2302,8 @@ int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A
     ZG_TRY(a.ensure(M, r16(K), S));
     ZG_TRY(b.ensure(N, r16(K), S, 3));
     const int bits = digit_bits(K);
-    ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{A, K}, M, K, S, bits, 0, a));
-    ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{B, K}, N, K, S, bits, 0, b));
+    ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{A, K}, M, K, S, bits, a));
+    ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{B, K}, N, K, S, bits, b));
     for (int ch = 0; ch < nchunks(K); ++ch) {
         const int k0 = ch * KCHUNK;
         UnitList u;
