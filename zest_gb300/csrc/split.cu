@@ -38,6 +38,8 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <mutex>
+#include <set>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -254,6 +256,22 @@ constexpr int SL_UNROLL = 8;   // independent loads per thread in the staging lo
 inline int digit_bits(int) { return 8; }
 constexpr int KCHUNK = SL_K8MAX;
 inline int nchunks(int K) { return (K + KCHUNK - 1) / KCHUNK; }
+
+// Sets a kernel's launch attributes once per (kernel, device), not at every
+// launch (setting them is a driver call).
+template <class Kern, class Set>
+int set_attributes_once(Kern kern, Set&& set) {
+    static std::mutex mu;
+    static std::set<std::pair<const void*, int>> done;
+    int dev = 0;
+    ZG_CUDA_TRY(cudaGetDevice(&dev));
+    const auto key = std::make_pair(reinterpret_cast<const void*>(kern), dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count(key)) return ZEST_GPU_OK;
+    ZG_TRY(set(kern));
+    done.insert(key);
+    return ZEST_GPU_OK;
+}
 
 // Rows per slicing block: a power of two (so that in row-fast loops every
 // thread stays on one row), up to 32 rows (longer contiguous runs in the
@@ -1420,7 +1438,12 @@ int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
     const size_t smem = (size_t)(Loader::TWO ? 2 : 1) * J.R * J.K * sizeof(double);
     const long long blocks = (J.rows + J.R - 1) / J.R;
     auto go = [&](auto kern) -> int {
-        ZG_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+        ZG_TRY(set_attributes_once(kern, [](auto k) -> int {
+            ZG_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+            ZG_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                             cudaSharedmemCarveoutMaxShared));
+            return ZEST_GPU_OK;
+        }));
         kern<<<(unsigned)blocks, 256, smem, s>>>(ld, J);
         return launch_check("slice_kernel");
     };
@@ -1703,8 +1726,10 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
         P.dbg = st->cycles.as<unsigned long long>();
     }
     const size_t smem = split_smem_bytes<S, BITS, NT>();
-    ZG_CUDA_TRY(cudaFuncSetAttribute(split_gemm_kernel<S, BITS, NT, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
+    ZG_TRY(set_attributes_once(split_gemm_kernel<S, BITS, NT, Epi>, [smem](auto k) -> int {
+        ZG_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        return ZEST_GPU_OK;
+    }));
     int nsm = 0;
     ZG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
     const int grid = std::min<int>(int(units.size()), nsm);
