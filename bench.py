@@ -624,7 +624,8 @@ def main():
             ctx.zt_forward(gh, L, batch=B, out=ch)
             ctx.zt_backward(ch, L, batch=B, out=go)
 
-        e2e_step()
+        for _ in range(2):  # first touches of the pinned buffers by the copy engines
+            e2e_step()
         torch.cuda.synchronize()
         barrier()
         n_e2e = max(1, min(args.steps, 5))
