@@ -91,6 +91,44 @@ def test_ragged_batch_matches_per_item(ctx, precision, tol):
         ctx.set_precision(0)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_ragged_graph_recorded_anew_after_buffers_are_freed(ctx, precision):
+    # A repeated call replays a CUDA graph that holds the context's scratch,
+    # table and work-list pointers.  A transform that regrows the scratch, and
+    # trim(), free buffers the graph used: the next call must record a new
+    # graph (and give the same results), not replay the old one.
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(40 + precision)
+    orders = np.sort(rng.integers(8, 25, size=12))
+    gsz = sum(int(np.prod(zt_grid_shape(int(L)))) for L in orders)
+    cs, e = make_batch(rng, orders)
+    c0 = torch.from_numpy(np.concatenate(cs)).cuda()
+    coeffs = torch.empty_like(c0)
+    euler = torch.from_numpy(e.ravel()).cuda()
+    grids = torch.zeros(gsz, dtype=torch.float64, device="cuda")
+
+    def call():
+        coeffs.copy_(c0)
+        ctx.zt_rotate_backward_ragged(orders, coeffs, euler, grids)
+        ctx.synchronize()
+        return coeffs.cpu().numpy(), grids.cpu().numpy()
+
+    ctx.set_precision(precision)
+    try:
+        ref = call()  # eager run, then the graph is recorded
+        runs = [call()]  # replay
+        big = np.concatenate([rand_zt(rng, 48) for _ in range(6)])
+        ctx.zt_backward(big, 48, batch=6)  # regrows the shared scratch
+        runs.append(call())
+        ctx.trim()  # frees every buffer
+        runs.append(call())
+        for i, (c, g) in enumerate(runs):
+            assert relmax(c, ref[0]) < 1e-14, i
+            assert relmax(g, ref[1]) < 1e-14, i
+    finally:
+        ctx.set_precision(0)
+
+
 def test_ragged_rejects_unsorted_orders(ctx):
     torch = pytest.importorskip("torch")
     import zest_gb300 as zg

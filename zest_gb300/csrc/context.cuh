@@ -2,6 +2,8 @@
 // driver (zest_gpu.cu) and the split-precision driver (split.cu).
 #pragma once
 
+#include <atomic>
+
 #include <map>
 #include <memory>
 #include <string>
@@ -16,6 +18,15 @@
 namespace zgpu {
 
 // ---------------------------------------------------------------------------
+// Number of device buffers freed so far (process-wide).  A captured CUDA
+// graph holds raw device pointers: it may be replayed only while this count is
+// what it was at capture, i.e. while no buffer it might use has been freed or
+// moved by a reallocation.
+inline std::atomic<unsigned long long>& alloc_epoch() {
+    static std::atomic<unsigned long long> epoch{0};
+    return epoch;
+}
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -24,7 +35,10 @@ struct DevBuf {
     DevBuf& operator=(const DevBuf&) = delete;
     ~DevBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            cudaFree(p);
+            alloc_epoch().fetch_add(1, std::memory_order_relaxed);
+        }
         p = nullptr;
         bytes = 0;
     }
@@ -110,6 +124,7 @@ struct RaggedPlan {
     std::vector<std::tuple<int, int, int>> buckets;            // {order, first item, count}
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    unsigned long long epoch = 0;  // alloc_epoch() when the graph was recorded
     ~RaggedPlan() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);

@@ -785,7 +785,9 @@ static int ragged_on_graph_stream(zest_gpu_context* ctx, int zn, int sn, int sp,
     const bool same = P && P->orders == orders && P->coeffs == coeffs && P->euler == euler && P->grids == grids &&
                       P->zn == zn && P->sn == sn && P->sp == sp && P->type == type &&
                       P->precision == ctx->precision && P->slices == ctx->slices;
-    if (same && P->exec) {
+    // the graph's kernels hold pointers to scratch, tables and work lists: a
+    // buffer freed or reallocated since it was recorded means recording anew
+    if (same && P->exec && P->epoch == alloc_epoch().load(std::memory_order_relaxed)) {
         ZG_CUDA_TRY(cudaGraphLaunch(P->exec, ctx->stream));
         if (P->precision == ZEST_PRECISION_SPLIT) ZG_TRY(split_check_flag(ctx));
         return ZEST_GPU_OK;
@@ -845,6 +847,7 @@ static int ragged_on_graph_stream(zest_gpu_context* ctx, int zn, int sn, int sp,
     if (ec != cudaSuccess) return fail(ZEST_GPU_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
     P->graph = g;
     ZG_CUDA_TRY(cudaGraphInstantiate(&P->exec, g, 0));
+    P->epoch = alloc_epoch().load(std::memory_order_relaxed);
     return ZEST_GPU_OK;
 }
 
