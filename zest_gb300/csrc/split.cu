@@ -1394,15 +1394,10 @@ struct SplitState {
     double useful_flops = 0.0, issued_flops = 0.0;  // accumulated while profiling
 };
 
-// Column tiles: 96, except the backward Legendre stage of the Zernike
-// transforms.  Its sums are short (K = ceil(L/2)) and its outputs span the
-// ceil((L+1)/2) folded nodes (101 at order 200: tiles of 96 + 5); with 48 the
-// MMAs overlap the epilogue's drain (two accumulator sets).  Measured at order
-// 200 x 64: 41.7 ms of GEMMs instead of 44.0; 48 for the other stages was no
-// faster.
+// Column tiles are chosen per launch (stage_nt) unless pinned by the tuning
+// override: 0 = automatic.
 SplitState::SplitState() {
-    for (int& v : nt) v = 96;
-    nt[WK_LEG_B] = 48;
+    for (int& v : nt) v = 0;
 }
 
 void destroy_split(SplitState* s) { delete s; }
@@ -1833,9 +1828,21 @@ void add_units(UnitList& ul, int S, int bits, long long a0, long long arows, int
 }
 
 
-// Column tile of a stage's launches: 96 by default; 48 (two accumulator sets
-// in TMEM) only with six slices.  Also part of the work-list key.
-inline int stage_nt(const SplitState* st, int wk, int S) { return S == 6 ? st->nt[wk] : 96; }
+// Column tile of a stage's launches (48 only with six slices), also part of
+// the work-list key; ncols = the most table rows a group of the stage has.
+//   * 48 where no group has more than 48 columns: a 96-wide tile would be at
+//     least half empty (the small orders of a ragged batch);
+//   * 48 for the backward Legendre stage of the Zernike transforms: its sums
+//     are short (K = ceil(L/2)) and its outputs span ceil((L+1)/2) folded
+//     nodes (101 at order 200: tiles of 96 + 5); with 48 the MMAs overlap the
+//     epilogue's drain (two accumulator sets).  Measured at order 200 x 64:
+//     41.7 ms of GEMMs instead of 44.0; 48 for the other stages was no faster;
+//   * 96 otherwise.
+inline int stage_nt(const SplitState* st, int wk, int S, int ncols) {
+    if (S != 6) return 96;
+    if (st->nt[wk]) return st->nt[wk];
+    return (ncols <= 48 || wk == WK_LEG_B) ? 48 : 96;
+}
 inline int nt_pass(int nt) { return nt == 48 ? 1 << 16 : 0; }
 
 // Longitude DFT of `batch` grids x[b][lon][col] (C columns, item stride gsz)
@@ -1844,7 +1851,7 @@ inline int nt_pass(int nt) { return nt == 48 ? 1 << 16 : 0; }
 // sin), K-chunked.  `wk` keys the work lists of the caller's grid family.
 int dft_forward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t, int S, int wk, const double* grids,
                       long long gsz, int C, int N, int Lg, int Lm, int batch, double* G) {
-    const int NT = stage_nt(st, wk, S), bits = digit_bits(Lg);
+    const int NT = stage_nt(st, wk, S, Lm), bits = digit_bits(Lg);
     const long long rows = (long long)batch * C;
     ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
     ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
@@ -1893,7 +1900,7 @@ int zero_parity_tails(zest_gpu_context* ctx, double* E, int batch, int Lg, int L
 int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t, int S, int wk,
                        const DftBwdLoader& ld, int C, int N, int Lg, int Lm, int batch, double* grids, long long gsz,
                        double* Cs) {
-    const int NT = stage_nt(st, wk, S), bits = digit_bits(Lg);
+    const int NT = stage_nt(st, wk, S, Lg), bits = digit_bits(Lg);
     const long long rows = (long long)batch * C;
     ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
     ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
@@ -2020,7 +2027,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
     ZG_TRY(dft_forward_stage(ctx, st, *tb->dft, S, WK_DFT_F, grids, sh.size(), C, N, Lg, Lm, batch, G));
     // ---- Legendre (folded over the equator) ----
     {
-        const int NT = stage_nt(st, WK_LEG_F, S);
+        const int NT = stage_nt(st, WK_LEG_F, S, (Lm + 1) / 2);
         const int bits = digit_bits(kh);
         const long long per_m = (long long)batch * nr2;
         const long long rows = (long long)Lm * per_m;
@@ -2050,7 +2057,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
     }
     // ---- radial ----
     {
-        const int NT = stage_nt(st, WK_RAD_F, S);
+        const int NT = stage_nt(st, WK_RAD_F, S, (Lm + 1) / 2);
         const int bits = digit_bits(nr);
         const long long rows = tri_size(Lm) * batch * 2;
         ZG_TRY(st->op[0].ensure(rows, r16(nr), S));
@@ -2099,7 +2106,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
 
     // ---- radial: coefficients -> flm ----
     {
-        const int NT = stage_nt(st, WK_RAD_B, S);
+        const int NT = stage_nt(st, WK_RAD_B, S, nr);
         const int bits = digit_bits((Lg + 1) / 2);
         const long long rows = tri_size(Lm) * batch * 2;
         ZG_TRY(st->op[0].ensure(rows, kl, S));
@@ -2124,7 +2131,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
     }
     // ---- Legendre: flm -> G (north/south unfold; parity 1 read-modify-write) ----
     {
-        const int NT = stage_nt(st, WK_LEG_B, S);
+        const int NT = stage_nt(st, WK_LEG_B, S, kh);
         const int bits = digit_bits((Lg + 1) / 2);
         const long long per_m = (long long)batch * nr2;
         const long long rows = (long long)Lm * per_m;
