@@ -1,5 +1,5 @@
 // Context and per-order plan structures of the GLQ path, shared by the FP64
-// driver (zest_gpu.cu) and the split-precision driver (split.cu).
+// host code (zest_gpu.cu) and the split-precision host code (split.cu).
 #pragma once
 
 #include <atomic>

@@ -258,7 +258,7 @@ constexpr int KCHUNK = SL_K8MAX;
 inline int nchunks(int K) { return (K + KCHUNK - 1) / KCHUNK; }
 
 // Sets a kernel's launch attributes once per (kernel, device), not at every
-// launch (setting them is a driver call).
+// launch (setting them is a CUDA runtime call).
 template <class Kern, class Set>
 int set_attributes_once(Kern kern, Set&& set) {
     static std::mutex mu;
