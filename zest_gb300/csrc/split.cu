@@ -996,7 +996,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     // the MMA's N follows the unit's valid table rows, rounded up to 16
     // (the B tile is always loaded whole; the MMA reads its first N rows)
     static_assert(SC::NACC * NT <= 512, "accumulators must fit in TMEM");
-    static_assert(NT % 48 == 0, "each epilogue warp owns whole 16-column chunks");
+    static_assert(NT % 16 == 0 && NT >= 16, "the MMA's N and the epilogue's 4-column loads");
     // Two accumulator sets when they fit in TMEM (NT = 48): the MMAs of the
     // next unit then run while the epilogue drains the previous one.
     constexpr int NBUF = 2 * SC::NACC * NT <= 512 ? 2 : 1;
@@ -2175,12 +2175,13 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
 // Split-precision SH Legendre sums.  The table is the 128-row operand: with
 // 2 x batch data rows per order m the data could not fill a row tile.  The
 // data (the folded spectra, or the coefficients) is the scaled-copy operand,
-// sliced per call; its 2 x batch rows are the columns, in tiles of 48 (or 96
-// for batches above 24).
+// sliced per call; its 2 x batch rows are the columns, in tiles of 16 (batches
+// up to 8: a tile loads no unused data rows), 48 (up to 24) or 96.
 // ===========================================================================
 namespace {
 template <class F>
 int st_with_nt(int batch, F&& f) {
+    if (2 * batch <= 16) return f(std::integral_constant<int, 16>{});
     return 2 * batch <= 48 ? f(std::integral_constant<int, 48>{}) : f(std::integral_constant<int, 96>{});
 }
 // SH sums always use 8-bit digits and 6 slices; sums longer than 256 run as
