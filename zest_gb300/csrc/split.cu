@@ -27,8 +27,9 @@
 // Kernel: warp-specialised, persistent, one CTA per SM.  Warp 0 issues TMA
 // loads (SWIZZLE_32B, one 16-wide K block of all S operand slices and the
 // needed table slices per pipeline stage), warp 1 issues tcgen05.mma
-// (M = 128 operand rows, N = NT = 96 (or 48) table rows per tile, five
-// accumulators resident in TMEM), warps 2..17 read the accumulators back
+// (M = 128 operand rows, N = NT = 96, 48 or 16 table rows per tile, five
+// accumulators resident in TMEM, two sets of them where they fit, so that
+// the next tile's MMAs overlap the drain), warps 2..17 read the accumulators back
 // (tcgen05.ld, four warps per TMEM lane quarter), recombine and store
 // through a stage-specific epilogue.  For the SH sums the table is the
 // 128-row operand and the 2 x batch data rows are the columns.  Every wait
