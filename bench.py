@@ -349,6 +349,130 @@ def run_evaluate(args, rank: int, world: int, barrier) -> None:
             "stages_ms": stages, "cpu_baseline": cpu, "clocks": clocks}), flush=True)
 
 
+def _timed_loop(step, args, barrier):
+    """Warm-up, then args.steps steps between CUDA events on the current stream
+    (the context's stream is the legacy default stream): ms per step, clocks."""
+    import torch
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    return max_over_ranks(e0.elapsed_time(e1), None) / args.steps, clocks
+
+
+def run_spectra(args, rank: int, world: int, barrier) -> None:
+    """Power spectra (power_spectra.hpp): the SH spectra of 8 expansions at
+    lmax 1023 (the C2 coefficients) per step, and beside them the Zernike
+    spectra of 64 expansions at order 200.  One thread per output sums over m
+    in FP64; the bound is reading the coefficients once.  The CPU baseline is
+    the C restatement of the same sums on one item."""
+    import torch
+    import zest_gb300 as zg
+    ctx = zg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    L, B = 1024, 8
+    rng = np.random.default_rng(1024 + rank)
+    ncoef = zg.st_coeff_size(L)
+    c = rng.normal(size=(B, ncoef, 2))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    cd = torch.from_numpy(c.ravel()).to(dev)
+    sd = torch.empty(B * L, dtype=torch.float64, device=dev)
+    ms, clocks = _timed_loop(lambda: ctx.st_power_spectrum(cd, L, batch=B, out=sd), args, barrier)
+    Lz, Bz = 200, 64
+    zc = torch.from_numpy(zt_coeffs(Lz, Bz, seed0=replica_seed0(rank, Bz)).ravel()).to(dev)
+    zs = torch.empty(Bz * (((Lz + 1) * (Lz + 1)) >> 2), dtype=torch.float64, device=dev)
+    ms_z, _ = _timed_loop(lambda: ctx.zt_power_spectrum(zc, Lz, batch=Bz, out=zs), args, barrier)
+    nbytes = B * ncoef * 16 + B * L * 8
+    achieved = nbytes / (ms * 1e-3) / 1e9
+    peaks = measured_peaks()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import Oracle
+        orc = Oracle()
+        t0 = time.perf_counter()
+        want = orc.st_power_spectrum(c[0].ravel(), L)
+        secs = time.perf_counter() - t0
+        got = sd[:L].cpu().numpy()
+        cpu = {"value": 1.0 / secs, "unit": "spectra/s", "cores": 1, "kind": "port",
+               "sample": "one lmax-1023 SH spectrum, C restatement",
+               "max_rel_err_vs_port": float(np.max(np.abs(got - want)) / np.max(np.abs(want)))}
+    if rank == 0:
+        print(json.dumps({
+            "metric": "SH power spectra per second, lmax 1023 x 8", "value": world * B / (ms * 1e-3),
+            "unit": "spectra/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "sh_power_spectrum", "order": L, "batch": B},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                         "algorithmic": "coefficients read once + spectra written"},
+            "zernike_order200_x64": {"ms": ms_z, "spectra_per_s": world * Bz / (ms_z * 1e-3)},
+            "cpu_baseline": cpu, "clocks": clocks}), flush=True)
+
+
+def run_lsq(args, rank: int, world: int, barrier) -> None:
+    """Least-squares fits to scattered data (st::LSQTransformer): 16 data
+    vectors at 20,000 seeded points fitted with SH expansions of order 32
+    (1,024 real unknowns) per step; the design matrix is built on the device
+    and solved by QR (cuSOLVER).  Beside it, the Zernike fit of order 12.  The
+    CPU baseline is numpy's least-squares solve of the same design matrix,
+    built from the oracle's tables outside the timed region."""
+    import torch
+    import zest_gb300 as zg
+    ctx = zg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    L, B, npts = 32, 16, 20000
+    rng = np.random.default_rng(3232 + rank)
+    lat = np.arcsin(rng.uniform(-1, 1, npts))
+    lon = rng.uniform(0, 2 * np.pi, npts)
+    data = rng.normal(size=(B, npts))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    dd = torch.from_numpy(data.ravel()).to(dev)
+    lat_d, lon_d = (torch.from_numpy(v).to(dev) for v in (lat, lon))
+    cd = torch.empty(B * 2 * zg.st_coeff_size(L), dtype=torch.float64, device=dev)
+    ms, clocks = _timed_loop(lambda: ctx.st_lsq(dd, L, lat_d, lon_d, batch=B, out=cd), args, barrier)
+    Lz = 12
+    r = rng.uniform(0, 1, npts) ** (1 / 3)
+    colat = np.arccos(rng.uniform(-1, 1, npts))
+    r_d, colat_d = (torch.from_numpy(v).to(dev) for v in (r, colat))
+    czd = torch.empty(B * 2 * zg.zt_coeff_size(Lz), dtype=torch.float64, device=dev)
+    ms_z, _ = _timed_loop(lambda: ctx.zt_lsq(dd, Lz, r_d, lon_d, colat_d, batch=B, out=czd), args, barrier)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import Oracle, tri_idx
+        orc = Oracle()
+        P = orc.plm_real(L, 0, 0, np.sin(lat))
+        cols = []
+        for l in range(L):
+            for m in range(l + 1):
+                p_ = P[tri_idx(l, m)]
+                cols.append(p_ * np.cos(m * lon))
+                if m:
+                    cols.append(p_ * np.sin(m * lon))
+        A = np.stack(cols, axis=1)
+        t0 = time.perf_counter()
+        np.linalg.lstsq(A, data.T, rcond=None)
+        secs = time.perf_counter() - t0
+        cpu = {"value": B / secs, "unit": "fits/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": "numpy lstsq of the same 20000 x 1024 design matrix, 16 right-hand sides"}
+    if rank == 0:
+        print(json.dumps({
+            "metric": "SH least-squares fits per second, order 32, 20000 points, 16 data vectors",
+            "value": world * B / (ms * 1e-3), "unit": "fits/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "sh_lsq", "order": L, "points": npts, "batch": B},
+            "roofline": None, "zernike_order12": {"ms": ms_z, "fits_per_s": world * B / (ms_z * 1e-3)},
+            "cpu_baseline": cpu, "clocks": clocks}), flush=True)
+
+
 def run_batching(args, rank: int, world: int, barrier) -> None:
     """4096 expansions, orders drawn uniformly from [8, 128] (sorted), c_nlm ~
     N(0, (n+1)^-2) with Im(m=0) = 0, Haar-uniform Euler angles; one step =
@@ -446,7 +570,8 @@ def main():
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["transforms", "batching", "sh", "evaluate"], default="transforms",
+    ap.add_argument("--workload", choices=["transforms", "batching", "sh", "evaluate", "spectra", "lsq"],
+                    default="transforms",
                     help="transforms: the headline (order 200 x 64 forward+backward); batching: 4096 "
                          "expansions of orders U{8..128}, rotate + backward in one graph")
     ap.add_argument("--items", type=int, default=4096)
@@ -484,6 +609,12 @@ def main():
         return
     if args.workload == "evaluate":
         run_evaluate(args, rank, world, barrier)
+        return
+    if args.workload == "spectra":
+        run_spectra(args, rank, world, barrier)
+        return
+    if args.workload == "lsq":
+        run_lsq(args, rank, world, barrier)
         return
 
     L, B = args.order, args.batch
