@@ -36,8 +36,8 @@ from zest_gb300.replicas import max_over_ranks, replica_seed0, whole_job_rate  #
 
 METRIC = "Zernike fwd+bwd transforms/s, order 200x64: split-prec vs FP64 GPU at 1e-11 err"
 # DRAM read + write bytes of the split GEMMs of one forward+backward step per
-# function at order 200 (ncu capture of all eight launches at batch 4: 7.30 GB)
-GEMM_DRAM_BYTES_PER_FUNCTION_ORDER200 = 7.298e9 / 4
+# function at order 200 (ncu capture of all eight launches at batch 4: 6.70 GB)
+GEMM_DRAM_BYTES_PER_FUNCTION_ORDER200 = 6.701e9 / 4
 UNIT = "transforms/s"
 
 
