@@ -1,7 +1,8 @@
 """Batches of expansions of different orders: zest_gpu_zt_rotate_backward_ragged
-(rotate every expansion, then backward-transform each to its own grid, one
-rotation launch for all, replayed from a CUDA graph on repeated calls), and
-the autotuner of the FP64 tile shapes.
+(rotate every expansion, then backward-transform each to its own grid; in
+FP64 one rotation launch for all, in split precision the X(+-pi/2) products
+of all vectors of one l as split GEMMs; replayed from a CUDA graph on
+repeated calls), and the autotuner of the FP64 tile shapes.
 
 The batch must give what per-item zest_gpu_zt_rotate + zest_gpu_zt_backward
 give (1e-13 relative max-norm in FP64; 1e-11 in split precision), on the
@@ -83,7 +84,8 @@ def test_ragged_batch_matches_per_item(ctx, precision, tol):
             co = go = 0
             for i, L in enumerate(orders):
                 n = 2 * zt_coeff_size(int(L))
-                assert relmax(got_c[co:co + n], rot[i]) < 1e-13, (call, i)
+                # split precision rotates on the tensor cores too (its bound, 1e-11)
+                assert relmax(got_c[co:co + n], rot[i]) < (1e-13 if precision == 0 else 1e-11), (call, i)
                 assert relmax(got_g[go:go + gsz[i]], want[i]) < tol, (call, i)
                 co += n
                 go += gsz[i]

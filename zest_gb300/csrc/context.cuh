@@ -120,6 +120,8 @@ struct RaggedPlan {
     int Lmax = 0;
     long long nwork = 0;
     DevBuf coff, work;                                         // per-item coefficient offsets, {item, n, l}
+    DevBuf vecl;                                               // the {item, n, l} vectors sorted by l
+    std::vector<long long> voff;                               // vecl rows of order l: [voff[l], voff[l+1])
     std::vector<long long> coff_h, goff_h;
     std::vector<std::tuple<int, int, int>> buckets;            // {order, first item, count}
     cudaGraph_t graph = nullptr;

@@ -93,6 +93,9 @@ int launch_rotate_euler_grad(cudaStream_t s, int kind, int L, int batch, const d
 int launch_rotate_ragged(cudaStream_t s, int kind, int Lmax, int items, double* coeffs, const long long* coff,
                          const int4* work, long long nwork, const double* wigner, const double* euler, int type,
                          double* phase_scratch);
+// The phase tables e^{-i m angle} [item][alpha', beta', gamma'][m < Lmax] of a
+// ragged rotation (double2 entries in phase_scratch).
+int launch_phases(cudaStream_t s, int Lmax, int items, const double* euler, int type, double* phase_scratch);
 // Euler angles (3 per item) of the inverse rotations.
 int launch_invert_euler(cudaStream_t s, int batch, const double* euler, double* out);
 

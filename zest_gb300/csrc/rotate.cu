@@ -370,6 +370,13 @@ int launch_rotate_ragged(cudaStream_t s, int kind, int Lmax, int items, double* 
     return launch_check("rotate_ragged_kernel");
 }
 
+int launch_phases(cudaStream_t s, int Lmax, int items, const double* euler, int type, double* phase_scratch) {
+    if (items <= 0 || Lmax <= 0) return ZEST_GPU_OK;
+    phase_kernel<<<dim3((Lmax + 127) / 128, items), 128, 0, s>>>(Lmax, items, euler, type,
+                                                                reinterpret_cast<double2*>(phase_scratch));
+    return launch_check("phase_kernel");
+}
+
 int launch_invert_euler(cudaStream_t s, int batch, const double* euler, double* out) {
     if (batch <= 0) return ZEST_GPU_OK;
     invert_euler_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, euler, out);

@@ -1345,13 +1345,19 @@ struct SliceArray {
 // work-list keys: (stage, Lg, Lm, batch, S, pass)
 enum {
     WK_DFT_F = 0, WK_LEG_F, WK_RAD_F, WK_RAD_B, WK_LEG_B, WK_DFT_B, WK_DENSE, WK_ST_LEG_F, WK_ST_LEG_B,
-    WK_ST_DFT_F, WK_ST_DFT_B
+    WK_ST_DFT_F, WK_ST_DFT_B, WK_ROT
 };
 
 // Sliced longitude DFT tables of one (order L, longitude count N): shared by
 // the Zernike grids and the SH LonLat grids of the same order.
 struct DftTables {
     SliceArray cos_f, sin_f, cos_b, sin_b;
+};
+
+// Sliced tables of the two X(+-pi/2) products of a rotation, all l < Lmax:
+// rows tri(l) + m, K = m' (see rot_table_kernel).
+struct RotTables {
+    SliceArray re1, im1, re2, im2;
 };
 
 struct ZtSplitTables {
@@ -1386,6 +1392,7 @@ struct SplitState {
     std::map<std::tuple<const void*, int>, std::unique_ptr<ZtSplitTables>> zt_tables;  // per (plan, S)
     std::map<std::tuple<const void*, int>, std::unique_ptr<StSplitTables>> st_tables;  // per (plan, S)
     std::map<std::tuple<int, int, int>, std::unique_ptr<DftTables>> dft_tables;        // per (L, N, S)
+    std::map<std::tuple<int, int>, std::unique_ptr<RotTables>> rot_tables;             // per (Lmax, S)
     std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<UnitList>> units;  // cached work lists
     DevBuf tmp;                 // FP64 staging of generated tables
     DevBuf cycles;              // role wait counters, kept when ZEST_GPU_SPLIT_CYCLES is set
@@ -2322,6 +2329,219 @@ int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int b
         ZG_TRY(launch_check("st_unfold_kernel"));
     }
     return split_finish(ctx);
+}
+
+// ===========================================================================
+// Split-precision rotation of ragged Zernike batches (Rotor::rotate,
+// rotor.hpp:210-243; rotate_l, wignerd_collection.hpp:122-296).  Every rotated
+// (n, l) vector of every item is one operand row, the rows sorted by l.  The
+// two X(+-pi/2) products of rotate_l are, per l, real matrices applied to the
+// real and the imaginary parts apart (the parity structure of d^l(pi/2) and
+// of a real function's complex coefficients):
+//   Re t_m = sum_m' Re1[m][m'] Re v_m',   Im t_m = sum_m' Im1[m][m'] Im v_m'
+// with Re1[m][0] = D(m, 0), Re1[m][m'] = 2 D(m, m') for m' >= 1 of the
+// parity of l + m, Im1[m][m'] = 2 D(m, m') for m' >= 1 of the other parity;
+// D(m, m') = (-1)^{m+m'} d(m', m) for X(pi/2) and d(m', m) for X(-pi/2)
+// (d(m', m) at wig[wig_off(l) + (l+1) m' + m]).  So each product is a split
+// GEMM per l-group with the table as the scaled-copy operand.  The phases and
+// the real/complex conversions are applied where the operands are sliced
+// (gamma', beta') and by a last elementwise pass (alpha').
+// ===========================================================================
+namespace {
+
+__global__ void rot_table_kernel(const double* __restrict__ wig, int Kp, int which, double* __restrict__ out) {
+    const long long t = blockIdx.y;  // tri(l) + m
+    int l = int((sqrtf(8.0f * float(t) + 1.0f) - 1.0f) * 0.5f);
+    while ((long long)(l + 1) * (l + 2) / 2 <= t) ++l;
+    while ((long long)l * (l + 1) / 2 > t) --l;
+    const int m = int(t - (long long)l * (l + 1) / 2);
+    const int mp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (mp >= Kp) return;
+    double v = 0.0;
+    if (mp <= l) {
+        const double x = wig[wig_off(l) + (long long)(l + 1) * mp + m];
+        const double D = (which < 2 && ((m + mp) & 1)) ? -x : x;
+        const int q = (l + m) & 1;
+        if ((which & 1) == 0) v = mp == 0 ? D : (((mp & 1) == q) ? 2.0 * D : 0.0);
+        else v = (mp >= 1 && (mp & 1) != q) ? 2.0 * D : 0.0;
+    }
+    out[t * Kp + mp] = v;
+}
+
+int build_rot_tables(zest_gpu_context* ctx, SplitState* st, const double* wig, int Lmax, int S, const RotTables** out) {
+    auto key = std::make_tuple(Lmax, S);
+    auto it = st->rot_tables.find(key);
+    if (it != st->rot_tables.end()) {
+        *out = it->second.get();
+        return ZEST_GPU_OK;
+    }
+    auto t = std::make_unique<RotTables>();
+    const int Kp = r16(Lmax);
+    const long long rows = tri_size(Lmax);
+    ZG_TRY(st->tmp.ensure((size_t)rows * Kp * sizeof(double)));
+    SliceArray* dst[4] = {&t->re1, &t->im1, &t->re2, &t->im2};
+    for (int w = 0; w < 4; ++w) {
+        rot_table_kernel<<<dim3((Kp + 127) / 128, (unsigned)rows), 128, 0, ctx->stream>>>(wig, Kp, w,
+                                                                                          st->tmp.as<double>());
+        ZG_TRY(launch_check("rot_table_kernel"));
+        ZG_TRY(slice_table(ctx, st->tmp.as<double>(), rows, Lmax, Kp, S, 8, *dst[w]));
+    }
+    ZG_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    *out = t.get();
+    st->rot_tables.emplace(key, std::move(t));
+    return ZEST_GPU_OK;
+}
+
+// row v = vecs[v] = {item, n, l}: k = m: r2c(c_m) e^{-i m gamma'} (Re, Im)
+struct RotInLoader {
+    static constexpr bool ROW_FAST = false, TWO = true;
+    static constexpr int MODE = SL_PAIR, SHIFT = 0;
+    const int4* vecs;
+    const long long* coff;
+    const double* coeffs;
+    const double2* ph;
+    int Lmax;
+    struct Row { const double* c; const double2* pg; int l; };
+    __device__ Row row(long long r) const {
+        const int4 w = vecs[r];
+        return Row{coeffs + coff[w.x] + 2 * zidx(w.y, w.z, 0), ph + ((long long)w.x * 3 + 2) * Lmax, w.z};
+    }
+    __device__ void get(const Row& R, int k, double& up, double& dn) const {
+        if (k > R.l) {
+            up = dn = 0.0;
+            return;
+        }
+        const double isq2 = 1.0 / 1.41421356237309504880168872420969808;
+        double xr = R.c[2 * k], xi = R.c[2 * k + 1];
+        if (k > 0) {
+            xr *= isq2;
+            xi *= -isq2;
+        }
+        const double2 p = R.pg[k];
+        up = xr * p.x - xi * p.y;
+        dn = xr * p.y + xi * p.x;
+    }
+};
+
+// row v: k = m: t_m e^{-i m beta'} (Re, Im), t = T[v][m][re, im]
+struct RotMidLoader {
+    static constexpr bool ROW_FAST = false, TWO = true;
+    static constexpr int MODE = SL_PAIR, SHIFT = 0;
+    const int4* vecs;
+    const double* T;
+    const double2* ph;
+    int Lmax;
+    struct Row { const double* t; const double2* pb; int l; };
+    __device__ Row row(long long r) const {
+        const int4 w = vecs[r];
+        return Row{T + r * 2LL * Lmax, ph + ((long long)w.x * 3 + 1) * Lmax, w.z};
+    }
+    __device__ void get(const Row& R, int k, double& up, double& dn) const {
+        if (k > R.l) {
+            up = dn = 0.0;
+            return;
+        }
+        const double tr = R.t[2 * k], ti = R.t[2 * k + 1];
+        const double2 p = R.pb[k];
+        up = tr * p.x - ti * p.y;
+        dn = tr * p.y + ti * p.x;
+    }
+};
+
+// rows v, columns m = aux + n: T[v][m][part], part = 0 (real) for the units
+// of the first operand pair, 1 (imaginary) for the second
+struct EpiRot {
+    static constexpr bool RMW = false;
+    static constexpr bool CHUNK = false;
+    double* T;
+    int Lmax;
+    struct Row { double* p; };
+    __device__ Row row(const SplitUnit& u, int r) const {
+        return Row{T + ((long long)r * Lmax + u.aux) * 2 + (u.flags & 1)};
+    }
+    __device__ void load(const Row&, int, double*) const {}
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double*) const { R.p[2 * n] = v; }
+};
+
+// coefficients of vector v, m <= l: c2r(u_m e^{-i m alpha'}), u = U[v][m]
+__global__ void rot_out_kernel(long long nvec, const int4* __restrict__ vecs, const long long* __restrict__ coff,
+                               double* __restrict__ coeffs, const double* __restrict__ U, int Lmax,
+                               const double2* __restrict__ ph) {
+    const long long v = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (v >= nvec) return;
+    const int lane = threadIdx.x & 31;
+    const int4 w = vecs[v];
+    double* c = coeffs + coff[w.x] + 2 * zidx(w.y, w.z, 0);
+    const double2* pa = ph + ((long long)w.x * 3 + 0) * Lmax;
+    const double* u = U + v * 2LL * Lmax;
+    const double sq2 = 1.41421356237309504880168872420969808;
+    for (int m = lane; m <= w.z; m += 32) {
+        const double2 p = pa[m];
+        double xr = u[2 * m] * p.x - u[2 * m + 1] * p.y;
+        double xi = u[2 * m] * p.y + u[2 * m + 1] * p.x;
+        if (m > 0) {
+            xr *= sq2;
+            xi *= -sq2;
+        }
+        c[2 * m] = xr;
+        c[2 * m + 1] = xi;
+    }
+}
+
+}  // namespace
+
+int split_rotate_ragged(zest_gpu_context* ctx, int Lmax, int items, long long nvec, const int4* vecs,
+                        const std::vector<long long>& voff, const long long* coff, double* coeffs, const double* wig,
+                        const double* euler, int type, double* phase) {
+    if (nvec <= 0) return ZEST_GPU_OK;
+    if (Lmax > SL_K8MAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split rotation: orders up to 256");
+    const int S = ctx->slices;
+    cudaStream_t s = ctx->stream;
+    SplitState* st;
+    ZG_TRY(get_state(ctx, &st));
+    const RotTables* tb;
+    ZG_TRY(build_rot_tables(ctx, st, wig, Lmax, S, &tb));
+    ZG_TRY(launch_phases(s, Lmax, items, euler, type, phase));
+    const double2* ph = reinterpret_cast<const double2*>(phase);
+    const int Kp = r16(Lmax);
+    ZG_TRY(ctx->s0.ensure((size_t)nvec * 2 * Lmax * sizeof(double)));
+    double* T = ctx->s0.as<double>();
+    ZG_TRY(st->op[0].ensure(nvec, Kp, S));
+    ZG_TRY(st->op[1].ensure(nvec, Kp, S));
+    // one work list for both products: per l, the rows of its vectors against
+    // its l + 1 table rows, real parts (operands 0) and imaginary parts (1)
+    unsigned h = 2166136261u;  // FNV-1a of the row offsets: the list's key
+    for (long long o : voff) h = (h ^ unsigned(o)) * 16777619u;
+    const int NT = stage_nt(st, WK_ROT, S, Lmax);
+    UnitList* u;
+    ZG_TRY(get_units(ctx, std::make_tuple(int(WK_ROT), Lmax, int(nvec), int(h & 0x7fffffff), S, nt_pass(NT)),
+                     [&](UnitList& ul) {
+                         for (int l = 0; l < Lmax; ++l) {
+                             const long long cnt = voff[l + 1] - voff[l];
+                             add_units(ul, S, 8, voff[l], cnt, int(tri_size(l)), l + 1, NT, l + 1, 0, l);
+                             add_units(ul, S, 8, voff[l], cnt, int(tri_size(l)), l + 1, NT, l + 1, 1 | 2, l);
+                         }
+                     },
+                     &u));
+    {
+        StageScope sc(ctx, ST_SPLIT_SLICE);
+        ZG_TRY(launch_slice2(s, RotInLoader{vecs, coff, coeffs, ph, Lmax}, nvec, Lmax, Lmax, 0, S, 8, SL_PAIR,
+                             st->op[0], st->op[1]));
+    }
+    ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], tb->re1, tb->im1, EpiRot{T, Lmax}));
+    {
+        StageScope sc(ctx, ST_SPLIT_SLICE);
+        ZG_TRY(launch_slice2(s, RotMidLoader{vecs, T, ph, Lmax}, nvec, Lmax, Lmax, 0, S, 8, SL_PAIR, st->op[0],
+                             st->op[1]));
+    }
+    ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], tb->re2, tb->im2, EpiRot{T, Lmax}));
+    {
+        StageScope sc(ctx, ST_ROTATE);
+        const int W = 8;
+        rot_out_kernel<<<(unsigned)((nvec + W - 1) / W), W * 32, 0, s>>>(nvec, vecs, coff, coeffs, T, Lmax, ph);
+        ZG_TRY(launch_check("rot_out_kernel"));
+    }
+    return ZEST_GPU_OK;
 }
 
 // Dense FP64 product C = A B^T through the split path (A: M x K, B: N x K,

@@ -2,6 +2,8 @@
 // contractions and of the SH Legendre sums; see split.cu.
 #pragma once
 
+#include <vector>
+
 struct zest_gpu_context;
 
 namespace zgpu {
@@ -32,6 +34,14 @@ int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int ba
                      double* coeffs, long long csz);
 int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* coeffs,
                       long long csz, double* X, double* grids);
+// Rotor::rotate of a ragged batch of real Zernike expansions with the two
+// X(+-pi/2) products of every rotated vector as split GEMMs (orders up to
+// 256): vecs = the {item, n, l} vectors sorted by l, vector rows
+// [voff[l], voff[l+1]) of order l; coff = each item's coefficient offset;
+// phase = scratch for the [item][3][Lmax] phase tables.
+int split_rotate_ragged(zest_gpu_context* ctx, int Lmax, int items, long long nvec, const int4* vecs,
+                        const std::vector<long long>& voff, const long long* coff, double* coeffs, const double* wig,
+                        const double* euler, int type, double* phase);
 // C = A B^T (A: M x K, B: N x K, C: M x N, row-major FP64 device buffers)
 int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A, const double* B, double* C);
 // BF16 tensor-core flops of the split GEMM launches since the last reset

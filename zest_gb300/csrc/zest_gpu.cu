@@ -738,7 +738,11 @@ static int ragged_sequence(zest_gpu_context* ctx, RaggedPlan& P, double* coeffs,
                            double* grids) {
     const double* wig;
     ZG_TRY(get_wigner(ctx, P.Lmax, &wig));
-    {
+    if (P.precision == ZEST_PRECISION_SPLIT && P.Lmax <= 256) {
+        // the X(+-pi/2) products of all vectors of one l as split GEMMs
+        ZG_TRY(split_rotate_ragged(ctx, P.Lmax, int(P.orders.size()), P.nwork, P.vecl.as<int4>(), P.voff, P.coff.as<long long>(),
+                                   coeffs, wig, euler, P.type, ctx->phase.as<double>()));
+    } else {
         StageScope sc(ctx, ST_ROTATE);
         ZG_TRY(launch_rotate_ragged(ctx->stream, 0, P.Lmax, int(P.orders.size()), coeffs, P.coff.as<long long>(),
                                     P.work.as<int4>(), P.nwork, wig, euler, P.type, ctx->phase.as<double>()));
@@ -826,6 +830,16 @@ static int ragged_on_graph_stream(zest_gpu_context* ctx, int zn, int sn, int sp,
     np->nwork = (long long)work.size();
     ZG_TRY(upload(np->coff, np->coff_h, ctx->stream));
     ZG_TRY(upload(np->work, work, ctx->stream));
+    {
+        // the same vectors grouped by l (stable: item, then n, within a group)
+        std::vector<int4> byl(work.size());
+        np->voff.assign((size_t)np->Lmax + 1, 0);
+        for (const int4& w : work) ++np->voff[(size_t)w.z + 1];
+        for (int l = 0; l < np->Lmax; ++l) np->voff[(size_t)l + 1] += np->voff[(size_t)l];
+        std::vector<long long> fill(np->voff.begin(), np->voff.end() - 1);
+        for (const int4& w : work) byl[(size_t)fill[(size_t)w.z]++] = w;
+        ZG_TRY(upload(np->vecl, byl, ctx->stream));
+    }
     ZG_TRY(ctx->phase.ensure((size_t)n * 6 * std::max(np->Lmax, 1) * sizeof(double)));
     ctx->ragged = std::move(np);
     P = ctx->ragged.get();
