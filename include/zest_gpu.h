@@ -268,8 +268,11 @@ int zest_gpu_zt_rotate_noalloc(void* stream, size_t order, size_t batch, double*
  * and grids packed back to back in item order.  The first call for a given
  * (orders, buffers, conventions, precision) runs the work eagerly and records
  * it into a CUDA graph on the context; a later identical call replays the
- * graph.  Results are those of zest_gpu_zt_rotate + zest_gpu_zt_backward per
- * item. */
+ * graph (recorded anew if any of the context's device buffers was freed or
+ * reallocated since, e.g. by zest_gpu_trim).  Results are those of
+ * zest_gpu_zt_rotate + zest_gpu_zt_backward per item; in
+ * ZEST_PRECISION_SPLIT (orders up to 256) the rotation's d(pi/2) products
+ * also run in split precision on the tensor cores, within 1e-11 of FP64. */
 int zest_gpu_zt_rotate_backward_ragged(zest_gpu_context* ctx, int zernike_norm, int sh_norm, int sh_phase,
                                        size_t n_items, const int* orders, double* coeffs, const double* euler,
                                        int rotation_type, double* grids);
