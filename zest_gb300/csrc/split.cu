@@ -1397,7 +1397,7 @@ struct SplitState {
     DevBuf tmp;                 // FP64 staging of generated tables
     DevBuf cycles;              // role wait counters, kept when ZEST_GPU_SPLIT_CYCLES is set
     bool cycles_on = false;
-    int nt[16];                 // column tile (96 or 48) of each work-list stage
+    int nt[16];                 // column tile of each work-list stage: 0 = chosen per launch, or 48 / 96
     SplitState();
     double useful_flops = 0.0, issued_flops = 0.0;  // accumulated while profiling
 };
