@@ -2510,11 +2510,18 @@ int split_rotate_ragged(zest_gpu_context* ctx, int Lmax, int items, long long nv
     ZG_TRY(st->op[1].ensure(nvec, Kp, S));
     // one work list for both products: per l, the rows of its vectors against
     // its l + 1 table rows, real parts (operands 0) and imaginary parts (1)
-    unsigned h = 2166136261u;  // FNV-1a of the row offsets: the list's key
-    for (long long o : voff) h = (h ^ unsigned(o)) * 16777619u;
+    // the list's key: two independent hashes of the row offsets (FNV-1a and
+    // a weighted sum), with the order, the vector count and the tile
+    unsigned h1 = 2166136261u;
+    unsigned long long h2 = 0;
+    for (size_t l = 0; l < voff.size(); ++l) {
+        h1 = (h1 ^ unsigned(voff[l])) * 16777619u;
+        h2 = h2 * 1000003ull + (unsigned long long)voff[l] * (2 * l + 1);
+    }
     const int NT = stage_nt(st, WK_ROT, S, Lmax);
     UnitList* u;
-    ZG_TRY(get_units(ctx, std::make_tuple(int(WK_ROT), Lmax, int(nvec), int(h & 0x7fffffff), S, nt_pass(NT)),
+    ZG_TRY(get_units(ctx, std::make_tuple(int(WK_ROT), Lmax + nt_pass(NT), int(nvec), int(h1 & 0x7fffffff), S,
+                                          int((h2 ^ (h2 >> 31)) & 0x7fffffff)),
                      [&](UnitList& ul) {
                          for (int l = 0; l < Lmax; ++l) {
                              const long long cnt = voff[l + 1] - voff[l];
