@@ -219,6 +219,36 @@ def test_st_kats(oracle, kat, latlon):
         assert np.max(np.abs(np.ravel(back) - grid.ravel())) < 1e-10, (sn, sp)
 
 
+@pytest.mark.parametrize("conv", [(1, 0, 0), (0, 1, 1)])
+def test_zt_converges_order100(oracle, conv):
+    # tests/test_zernike_glq_transformer.cpp:938-980: a Gaussian on the ball,
+    # forward then backward at order 100, comes back to 1e-13 (absolute)
+    L = 100
+    lon, z, r = ball_points(oracle, L)
+    LON, Z, R = np.meshgrid(lon, z, r, indexing="ij")
+    S = np.sqrt(1.0 - Z * Z)
+    g = np.exp(-((R * S * np.cos(LON) - 0.3) ** 2 + (R * S * np.sin(LON) + 0.1) ** 2 + (R * Z - 0.043) ** 2))
+    back = oracle.zt_backward(oracle.zt_forward(g, L, L, *conv), L, L, *conv)
+    assert np.max(np.abs(np.ravel(back) - g.ravel())) < 1e-13
+
+
+@pytest.mark.parametrize("latlon", [0, 1])
+@pytest.mark.parametrize("conv", CONVS_ST)
+def test_st_converges_order100(oracle, latlon, conv):
+    # tests/test_sh_glq_transformer.cpp:779-818: exp(-(x - x0) . (1/2, 1/2, 1/2))
+    # on the sphere, forward then backward at order 100, to 1e-10 (absolute)
+    L = 100
+    lon, z = sphere_points(oracle, L, latlon)
+    if latlon:
+        Z, LON = np.meshgrid(z, lon, indexing="ij")
+    else:
+        LON, Z = np.meshgrid(lon, z, indexing="ij")
+    S = np.sqrt(1.0 - Z * Z)
+    f = np.exp(-(0.5 * (S * np.cos(LON) - 0.3) + 0.5 * (S * np.sin(LON) + 0.1) + 0.5 * (Z - 0.043)))
+    back = oracle.st_backward(oracle.st_forward(f, L, L, *conv, bool(latlon)), L, L, *conv, bool(latlon))
+    assert np.max(np.abs(np.ravel(back) - f.ravel())) < 1e-10
+
+
 @pytest.mark.parametrize("L", [1, 2, 5, 8, 16, 24])
 @pytest.mark.parametrize("latlon", [0, 1])
 @pytest.mark.parametrize("conv", CONVS_ST)
