@@ -8,6 +8,7 @@ max|x - x_ref| / max|x_ref| (the bar the reference parity is quoted at)."""
 import numpy as np
 import pytest
 
+from kats import ST_KATS, ZT_KATS, ball_points, sphere_points
 from oracle import tri_idx, tri_size, zidx, zt_coeff_size
 
 pytestmark = pytest.mark.gpu
@@ -171,7 +172,68 @@ def test_zt_kat_z000(ctx):
         assert np.max(np.abs(c - ref)) < 1e-10
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("kat", range(len(ZT_KATS)))
+def test_zt_kats(ctx, oracle, kat, precision):
+    # tests/test_zernike_glq_transformer.cpp:136-870 (the cases in tests/kats.py):
+    # single Zernike functions expand to their one coefficient and evaluate
+    # back, in all conventions, in the FP64 and the split-precision form
+    import zest_gb300
+    (n, l, m), f, normed, want = ZT_KATS[kat]
+    L = 6
+    lon, z, r = ball_points(oracle, L)
+    LON, Z, R = np.meshgrid(lon, z, r, indexing="ij")
+    if precision:
+        ctx.set_precision(zest_gb300.PRECISION_SPLIT, 6)
+    try:
+        for zn, sn, sp in CONVS_ZT:
+            znorm = normed if zn == 0 else 1.0
+            shnorm = 0.5 / np.sqrt(np.pi) if sn == 1 else 1.0
+            phase = -1.0 if sp == 0 else 1.0
+            grid = np.ascontiguousarray(znorm * shnorm * f(LON, Z, R, phase))
+            c = np.asarray(ctx.zt_forward(grid.ravel(), L, conv=(zn, sn, sp))).reshape(-1, 2)
+            ref = np.zeros_like(c)
+            ref[zidx(n, l, m)] = want
+            assert np.max(np.abs(c - ref)) < 1e-10, (zn, sn, sp)
+            back = ctx.zt_backward(np.ascontiguousarray(c).ravel(), L, conv=(zn, sn, sp))
+            assert np.max(np.abs(np.ravel(back) - grid.ravel())) < 1e-10, (zn, sn, sp)
+    finally:
+        ctx.set_precision(zest_gb300.PRECISION_FP64)
+
+
 # ---- SH ----
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("latlon", [0, 1])
+@pytest.mark.parametrize("kat", range(len(ST_KATS)))
+def test_st_kats(ctx, oracle, kat, latlon, precision):
+    # tests/test_sh_glq_transformer.cpp:53-777 (the cases in tests/kats.py),
+    # both layouts, all conventions, the FP64 and the split-precision form
+    import zest_gb300
+    f, want = ST_KATS[kat]
+    L = 6
+    lon, z = sphere_points(oracle, L, latlon)
+    if latlon:
+        Z, LON = np.meshgrid(z, lon, indexing="ij")
+    else:
+        LON, Z = np.meshgrid(lon, z, indexing="ij")
+    if precision:
+        ctx.set_precision(zest_gb300.PRECISION_SPLIT, 6)
+    try:
+        for sn, sp in CONVS_ST:
+            shnorm = 0.5 / np.sqrt(np.pi) if sn == 1 else 1.0
+            phase = -1.0 if sp == 0 else 1.0
+            grid = np.ascontiguousarray(shnorm * f(LON, Z, phase))
+            c = np.asarray(ctx.st_forward(grid.ravel(), L, conv=(sn, sp), layout=latlon)).reshape(-1, 2)
+            ref = np.zeros_like(c)
+            for (l, m), v in want.items():
+                ref[tri_idx(l, m)] = v
+            assert np.max(np.abs(c - ref)) < 1e-10, (sn, sp)
+            back = ctx.st_backward(np.ascontiguousarray(c).ravel(), L, conv=(sn, sp), layout=latlon)
+            assert np.max(np.abs(np.ravel(back) - grid.ravel())) < 1e-10, (sn, sp)
+    finally:
+        ctx.set_precision(zest_gb300.PRECISION_FP64)
+
+
 @pytest.mark.parametrize("L", [1, 2, 5, 8, 16, 24])
 @pytest.mark.parametrize("latlon", [0, 1])
 @pytest.mark.parametrize("conv", CONVS_ST)
