@@ -70,6 +70,22 @@ def test_radial_closed_forms(oracle):
     assert np.max(np.abs(z[:, -1] - 1.0)) < 1e-12
 
 
+def test_radial_normed_orthonormal(oracle):
+    # tests/test_radial_zernike_recursion.cpp:244-333: the normed R_nl of one l
+    # are orthonormal under the weight r^2 on [0, 1] (GL quadrature of order
+    # + 2 nodes, r = (1 + x)/2, weight w r^2 / 2), to 1e-13
+    from oracle import rad_idx
+    L = 6
+    x, w = oracle.gl_nodes_weights(L + 2)
+    r = 0.5 * (1.0 + x)
+    R = oracle.radial_zernike(L, 0, r)
+    wt = 0.5 * r * r * w
+    for l in range(L):
+        ns = list(range(l, L, 2))
+        gram = np.array([[np.sum(wt * R[rad_idx(a, l)] * R[rad_idx(b, l)]) for b in ns] for a in ns])
+        assert np.max(np.abs(gram - np.eye(len(ns)))) < 1e-13, l
+
+
 def test_wignerd_table(oracle, golden):
     assert relmax(oracle.wignerd(16), golden("tables")["wignerd_16"]) == 0.0
 
