@@ -241,13 +241,17 @@ int zest_gpu_zt_power_spectrum(zest_gpu_context* ctx, int sh_norm, size_t order,
  * per device; nothing in it has to start at zero, since each call writes
  * every byte it reads.  A call needs 8 nvec(order) bytes (rounded up to 256)
  * plus 48 order batch bytes, nvec(order) ~ order^2 / 4; larger requests
- * return ZEST_GPU_ERR_UNSUPPORTED and do nothing.  Orders above 1447 never
- * fit; order 200 fits up to batch 428, order 64 up to batch 1362.
+ * return ZEST_GPU_ERR_UNSUPPORTED and do nothing.  The largest order that
+ * fits is 1435 at batch 1; order 200 fits up to batch 428, order 64 up to
+ * batch 1362.
  *
  * The first call on each device sets up: it looks up the array's address
  * with cudaGetSymbolAddress, which also loads the library's kernels onto the
  * device.  Make that first call with the device current and before any
- * stream capture on it.  Later calls on that device only launch kernels.
+ * stream capture on it.  The address is kept with the id of the CUDA context
+ * it belongs to; after the device's context is replaced (cudaDeviceReset, or
+ * the primary context released and retained again) the next call sets up
+ * again in the new context.  Other calls only launch kernels.
  *
  * The array is shared by every caller in the process: two calls that can
  * run at the same time on one device (on streams without ordering between

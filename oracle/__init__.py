@@ -377,14 +377,37 @@ class Reference(_Lib):
     def _zt_ps(self, sn, L, c, out):
         self._f("zt_power_spectrum", [_c_int, _c_sz, _p_dbl, _p_dbl])(sn, L, _ptr(c), _ptr(out))
 
-    def zt_fwd_bwd_batch(self, grids, L, nthreads, zn=1, sn=0, sp=0):
+    def zt_fwd_bwd_steps(self, grids, L, nthreads, nsteps=1, zn=1, sn=0, sp=0):
+        """`nsteps` timed steps of forward + backward of every grid on
+        `nthreads` threads; each thread builds its transformer once, before
+        the timing.  Returns (seconds per step, coefficients, grids)."""
         grids = np.ascontiguousarray(grids, dtype=np.float64)
         batch = grids.shape[0]
         coeffs = np.zeros((batch, zt_coeff_size(L), 2))
         out = np.zeros_like(grids)
-        fn = self._f("zt_fwd_bwd_batch", [_c_int, _c_int, _c_int, _c_sz, _c_sz, _p_dbl, _p_dbl, _p_dbl, _c_int], _c_dbl)
-        secs = fn(zn, sn, sp, L, batch, _ptr(grids), _ptr(coeffs), _ptr(out), nthreads)
+        secs = np.zeros(nsteps)
+        fn = self._f("zt_fwd_bwd_steps", [_c_int, _c_int, _c_int, _c_sz, _c_sz, _p_dbl, _p_dbl, _p_dbl, _c_int,
+                                          _c_int, _p_dbl])
+        fn(zn, sn, sp, L, batch, _ptr(grids), _ptr(coeffs), _ptr(out), nthreads, nsteps, _ptr(secs))
         return secs, coeffs, out
+
+    def zt_rotate_backward_ragged(self, orders, coeffs, euler, nthreads, rtype=0, zn=1, sn=0, sp=0,
+                                  want_grids=False):
+        """Rotor::rotate then backward_transform of items of sorted, uneven
+        orders on `nthreads` threads (set-up untimed).  `coeffs` (the items'
+        coefficients back to back) is rotated in place.  Returns (seconds,
+        grids back to back or None)."""
+        orders = np.ascontiguousarray(orders, dtype=np.int32)
+        e = np.ascontiguousarray(euler, dtype=np.float64).ravel()
+        assert coeffs.dtype == np.float64 and coeffs.flags["C_CONTIGUOUS"]
+        grids = None
+        if want_grids:
+            grids = np.zeros(sum(int(np.prod(zt_grid_shape(int(L)))) for L in orders))
+        fn = self._f("zt_rotate_backward_ragged", [_c_int, _c_int, _c_int, _c_sz, ctypes.POINTER(_c_int), _p_dbl,
+                                                   _p_dbl, _c_int, _p_dbl, _c_int], _c_dbl)
+        secs = fn(zn, sn, sp, orders.size, orders.ctypes.data_as(ctypes.POINTER(_c_int)), _ptr(coeffs), _ptr(e),
+                  rtype, _ptr(grids) if grids is not None else None, nthreads)
+        return secs, grids
 
 
 def zt_sample_config1(lon: np.ndarray, colat: np.ndarray, r: np.ndarray) -> np.ndarray:

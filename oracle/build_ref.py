@@ -3,10 +3,12 @@ compiled from its own sources, wrapped by oracle/ref_shim.cpp.
 
 Test infrastructure only (golden fixtures, CPU baseline arm of bench.py).
 
-Where the reference checkout is present (the development container), its
+The reference checkout is named by `--reference DIR` or the environment
+variable ZEST_REFERENCE_DIR; there is no default.  Where one is given, its
 headers and the few translation units the transform/rotation path needs are
 staged into oracle/_ref/src/ and compiled with g++ directly -- the reference's
-own CMake build is not used.  oracle/_ref/ is git-ignored (it never enters the
+own CMake build is not used.  Without one, the sources staged earlier are
+compiled.  oracle/_ref/ is git-ignored (it never enters the
 repository history) but it is shipped with the working tree to the GPU host;
 there, where the checkout is absent and the x86 objects have been removed,
 the staged sources are compiled again for the host CPU.
@@ -25,7 +27,12 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_OUT = os.path.join(HERE, "_ref")
 STAGE = os.path.join(REF_OUT, "src")
-REFERENCE_CHECKOUT = "/root/reference"
+
+
+def reference_checkout(path: str | None = None) -> str | None:
+    """The reference checkout: `path`, else ZEST_REFERENCE_DIR, else None."""
+    return path or os.environ.get("ZEST_REFERENCE_DIR") or None
+
 
 # Translation units of the reference needed by ref_shim.cpp.
 REF_SOURCES = [
@@ -39,10 +46,12 @@ REF_SOURCES = [
 LIB = os.path.join(REF_OUT, "libzest_ref.so")
 
 
-def _stage() -> str | None:
+def _stage(checkout: str | None) -> str | None:
     """Copy reference headers + needed sources into oracle/_ref/src."""
-    inc = os.path.join(REFERENCE_CHECKOUT, "include")
-    src = os.path.join(REFERENCE_CHECKOUT, "src")
+    if not checkout:
+        return None
+    inc = os.path.join(checkout, "include")
+    src = os.path.join(checkout, "src")
     if not os.path.isdir(inc):
         return None
     os.makedirs(os.path.join(STAGE, "include"), exist_ok=True)
@@ -67,9 +76,9 @@ def _is_elf_for_this_machine(path: str) -> bool:
     return machine == want
 
 
-def build(force: bool = False, verbose: bool = False) -> str | None:
+def build(force: bool = False, verbose: bool = False, reference: str | None = None) -> str | None:
     """Build libzest_ref.so; returns its path or None when no sources exist."""
-    staged = _stage()
+    staged = _stage(reference_checkout(reference))
     if staged is None and not os.path.isdir(STAGE):
         return None
     shim = os.path.join(HERE, "ref_shim.cpp")
@@ -89,5 +98,10 @@ def build(force: bool = False, verbose: bool = False) -> str | None:
 
 
 if __name__ == "__main__":
-    path = build(force="--force" in sys.argv, verbose=True)
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--reference", help="reference checkout to stage the sources from")
+    ap.add_argument("--force", action="store_true")
+    a = ap.parse_args()
+    path = build(force=a.force, verbose=True, reference=a.reference)
     print(path if path else "reference sources unavailable")

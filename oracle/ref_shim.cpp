@@ -14,8 +14,12 @@
 //   zest::gl::gl_nodes_and_weights  include/gauss_legendre.hpp:1549-1565
 //   zest::{zt,st}::GridEvaluator    include/grid_evaluator.hpp:52-325
 //   zest::zt::power_spectrum        include/power_spectra.hpp:124-146
+#include <algorithm>
 #include <array>
+#include <barrier>
 #include <chrono>
+#include <memory>
+#include <utility>
 #include <cstddef>
 #include <cstring>
 #include <thread>
@@ -287,31 +291,113 @@ int ref_zt_power_spectrum(int sn, std::size_t order, const double* coeffs, doubl
     });
 }
 
-// CPU baseline: forward then backward transform of `batch` Zernike functions
-// of one order, one reference transformer per std::thread.  Returns seconds.
-double ref_zt_fwd_bwd_batch(int zn, int sn, int sp, std::size_t order, std::size_t batch,
-                            const double* grids, double* coeffs, double* grids_out, int nthreads) {
+// CPU baseline: `nsteps` steps of forward then backward transform of `batch`
+// Zernike functions of one order on `nthreads` std::threads, items
+// b = t, t + nthreads, ... on thread t.  Each thread builds its reference
+// transformer (the O(L^3) tables) once, before the first step; only the
+// steps are timed.  Writes each step's seconds to step_secs[0..nsteps).
+int ref_zt_fwd_bwd_steps(int zn, int sn, int sp, std::size_t order, std::size_t batch, const double* grids,
+                         double* coeffs, double* grids_out, int nthreads, int nsteps, double* step_secs) {
     const std::size_t gsz = ZtLayout::size(order);
     const std::size_t csz = zest::zt::RealZernikeExpansionGeo::size(order);
-    double secs = 0.0;
-    dispatch_zt(zn, sn, sp, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
-        auto t0 = std::chrono::steady_clock::now();
+    return dispatch_zt(zn, sn, sp, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
+        std::barrier sync(nthreads + 1);
         std::vector<std::thread> pool;
         for (int t = 0; t < nthreads; ++t) {
             pool.emplace_back([&, t]() {
                 zest::zt::GLQTransformer<Z, N, P, ZtLayout> tr(order);
-                for (std::size_t b = t; b < batch; b += nthreads) {
-                    zest::zt::BallGLQGridSpan<const double, ZtLayout> g(grids + b * gsz, order);
-                    zest::zt::RealZernikeSpan<std::array<double, 2>, Z, N, P> e(
-                        reinterpret_cast<std::array<double, 2>*>(coeffs + 2 * b * csz), order);
-                    tr.forward_transform(g, e);
-                    zest::zt::BallGLQGridSpan<double, ZtLayout> go(grids_out + b * gsz, order);
-                    tr.backward_transform(e, go);
+                sync.arrive_and_wait();  // tables built
+                for (int step = 0; step < nsteps; ++step) {
+                    sync.arrive_and_wait();  // step starts
+                    for (std::size_t b = t; b < batch; b += nthreads) {
+                        zest::zt::BallGLQGridSpan<const double, ZtLayout> g(grids + b * gsz, order);
+                        zest::zt::RealZernikeSpan<std::array<double, 2>, Z, N, P> e(
+                            reinterpret_cast<std::array<double, 2>*>(coeffs + 2 * b * csz), order);
+                        tr.forward_transform(g, e);
+                        zest::zt::BallGLQGridSpan<double, ZtLayout> go(grids_out + b * gsz, order);
+                        tr.backward_transform(e, go);
+                    }
+                    sync.arrive_and_wait();  // step ends
                 }
             });
         }
+        sync.arrive_and_wait();
+        for (int step = 0; step < nsteps; ++step) {
+            const auto t0 = std::chrono::steady_clock::now();
+            sync.arrive_and_wait();
+            sync.arrive_and_wait();
+            step_secs[step] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        }
         for (auto& th : pool) th.join();
+    });
+}
+
+// CPU baseline of batches of uneven order: Rotor::rotate (in place) then
+// backward_transform of item i to a grid of its own order, for n_items items
+// sorted by order.  Thread t takes a contiguous run of items of about equal
+// cost (order^4).  Before timing, each thread builds its Rotor and
+// WignerdPiHalfCollection for the largest order of its run and one
+// transformer per order in its run, as a reference user with a ragged batch
+// would keep them.  With grids_out null each thread overwrites one grid of
+// its own (the results are discarded).  Returns the seconds of the timed run.
+double ref_zt_rotate_backward_ragged(int zn, int sn, int sp, std::size_t n_items, const int* orders,
+                                     double* coeffs, const double* euler, int rtype, double* grids_out,
+                                     int nthreads) {
+    std::vector<std::size_t> coff(n_items + 1, 0), goff(n_items + 1, 0);
+    std::vector<double> cost(n_items + 1, 0.0);
+    for (std::size_t i = 0; i < n_items; ++i) {
+        const std::size_t L = std::size_t(orders[i]);
+        coff[i + 1] = coff[i] + 2 * zest::zt::RealZernikeExpansionGeo::size(L);
+        goff[i + 1] = goff[i] + ZtLayout::size(L);
+        cost[i + 1] = cost[i] + double(L) * double(L) * double(L) * double(L);
+    }
+    std::vector<std::size_t> first(nthreads + 1, n_items);
+    first[0] = 0;
+    for (int t = 1; t < nthreads; ++t) {
+        const double target = cost[n_items] * t / nthreads;
+        first[t] = std::size_t(std::lower_bound(cost.begin(), cost.end(), target) - cost.begin());
+        first[t] = std::min(std::max(first[t], first[t - 1]), n_items);
+    }
+    double secs = 0.0;
+    dispatch_zt(zn, sn, sp, [&]<ZernikeNorm Z, SHNorm N, SHPhase P>() {
+        using Tr = zest::zt::GLQTransformer<Z, N, P, ZtLayout>;
+        std::barrier sync(nthreads + 1);
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthreads; ++t) {
+            pool.emplace_back([&, t]() {
+                const std::size_t i0 = first[t], i1 = first[t + 1];
+                std::size_t lmax = 1;
+                for (std::size_t i = i0; i < i1; ++i) lmax = std::max(lmax, std::size_t(orders[i]));
+                zest::Rotor rotor(lmax);
+                zest::WignerdPiHalfCollection wig(lmax);
+                std::vector<std::pair<int, std::unique_ptr<Tr>>> trs;
+                for (std::size_t i = i0; i < i1; ++i)
+                    if (trs.empty() || trs.back().first != orders[i])
+                        trs.emplace_back(orders[i], std::make_unique<Tr>(std::size_t(orders[i])));
+                std::vector<double> own(grids_out ? 0 : ZtLayout::size(lmax));
+                sync.arrive_and_wait();  // set-up done
+                sync.arrive_and_wait();  // timed run starts
+                std::size_t k = 0;
+                for (std::size_t i = i0; i < i1; ++i) {
+                    const std::size_t L = std::size_t(orders[i]);
+                    while (trs[k].first != orders[i]) ++k;
+                    zest::zt::RealZernikeSpan<std::array<double, 2>, Z, N, P> e(
+                        reinterpret_cast<std::array<double, 2>*>(coeffs + coff[i]), L);
+                    rotor.rotate(e, wig, std::array<double, 3>{euler[3 * i], euler[3 * i + 1], euler[3 * i + 2]},
+                                 rot_type(rtype));
+                    zest::zt::BallGLQGridSpan<double, ZtLayout> g(grids_out ? grids_out + goff[i] : own.data(), L);
+                    trs[k].second->backward_transform(
+                        zest::zt::RealZernikeSpan<const std::array<double, 2>, Z, N, P>(e), g);
+                }
+                sync.arrive_and_wait();  // timed run ends
+            });
+        }
+        sync.arrive_and_wait();
+        const auto t0 = std::chrono::steady_clock::now();
+        sync.arrive_and_wait();
+        sync.arrive_and_wait();
         secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        for (auto& th : pool) th.join();
     });
     return secs;
 }

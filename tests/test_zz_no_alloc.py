@@ -50,6 +50,32 @@ def _noalloc(zg, stream, L, batch, coeffs, euler, rtype, wig, wig_order):
                                           ctypes.c_void_p(euler), rtype, ctypes.c_void_p(wig), wig_order)
 
 
+# One module load (the library's kernels and its fixed scratch array) is the
+# only device memory the set-up call may bring in; later calls bring in none.
+MODULE_LOAD_TOLERANCE = 64 << 20
+
+
+def _torch_counters(torch):
+    st = torch.cuda.memory_stats(0)
+    return {k: st.get(k, 0) for k in ("allocation.all.allocated", "segment.all.allocated",
+                                      "allocated_bytes.all.allocated", "reserved_bytes.all.allocated")}
+
+
+def _free_bytes_after(torch, fn):
+    """Device free bytes before and after fn(), measured on a synchronized
+    device.  The free figure covers the whole device, which other processes
+    may share, so a mismatch is measured once more before it counts."""
+    for attempt in range(2):
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info(0)[0]
+        out = fn()
+        torch.cuda.synchronize()
+        free1 = torch.cuda.mem_get_info(0)[0]
+        if attempt == 1 or free1 == free0:
+            return free0, free1, out
+    raise AssertionError("unreachable")
+
+
 def test_zt_rotate_noalloc_matches_context_path(env):
     torch, zg, ctx = env
     L, batch = 40, 5
@@ -63,14 +89,21 @@ def test_zt_rotate_noalloc_matches_context_path(env):
         ref = ctx.zt_rotate(c.copy(), L, euler.copy(), batch=batch, rotation_type=rtype)
         dc = torch.from_numpy(c).cuda()
         de = torch.from_numpy(euler).cuda()
-        torch.cuda.synchronize()
-        free0 = torch.cuda.mem_get_info(0)[0]
-        rc = _noalloc(zg, stream, L, batch, dc.data_ptr(), de.data_ptr(), rtype, wig.data_ptr(), L + 3)
-        torch.cuda.synchronize()
-        free1 = torch.cuda.mem_get_info(0)[0]
+        dc_start = dc.clone()
+        counters0 = _torch_counters(torch)
+
+        def run():
+            dc.copy_(dc_start)
+            return _noalloc(zg, stream, L, batch, dc.data_ptr(), de.data_ptr(), rtype, wig.data_ptr(), L + 3)
+
+        free0, free1, rc = _free_bytes_after(torch, run)
         assert rc == 0, zg.library().zest_gpu_last_error()
         assert relmax(dc.cpu().numpy(), ref) < TOL
-        if call > 0:  # past the set-up call, device memory use does not move
+        # no allocation through torch's allocator
+        assert _torch_counters(torch) == counters0
+        if call == 0:  # the set-up call: at most one module load
+            assert free0 - free1 <= MODULE_LOAD_TOLERANCE
+        else:  # past the set-up call, device memory use does not move
             assert free1 == free0
 
 
@@ -78,16 +111,23 @@ def test_zt_rotate_noalloc_rejects_oversize_and_short_table(env):
     torch, zg, ctx = env
     lib = zg.library()
     wig = torch.from_numpy(ctx.wignerd_table(8)).cuda()
-    c = torch.zeros(2 * zt_coeff_size(1448), dtype=torch.float64, device="cuda")
+    # every call below returns before any launch, so a small buffer stands in
+    c = torch.zeros(64, dtype=torch.float64, device="cuda")
     e = torch.zeros(3, dtype=torch.float64, device="cuda")
     before = c.clone()
-    # order 1448: the vector list alone is above the fixed scratch size
-    rc = _noalloc(zg, 0, 1448, 1, c.data_ptr(), e.data_ptr(), 0, wig.data_ptr(), 8)
+    # order 1436 at batch 1: the vector list and one item's phases exceed the fixed scratch
+    rc = _noalloc(zg, 0, 1436, 1, c.data_ptr(), e.data_ptr(), 0, wig.data_ptr(), 8)
     assert rc == zg.ERR_UNSUPPORTED
     assert b"scratch" in lib.zest_gpu_last_error()
+    # order 1435 at batch 1 fits: the size check passes and the short Wigner table is what fails
+    rc = _noalloc(zg, 0, 1435, 1, c.data_ptr(), e.data_ptr(), 0, wig.data_ptr(), 8)
+    assert rc == zg.ERR_INVALID
+    assert b"Wigner" in lib.zest_gpu_last_error()
     # order 200 fits up to batch 428
     rc = _noalloc(zg, 0, 200, 429, c.data_ptr(), e.data_ptr(), 0, wig.data_ptr(), 8)
     assert rc == zg.ERR_UNSUPPORTED
+    rc = _noalloc(zg, 0, 200, 428, c.data_ptr(), e.data_ptr(), 0, wig.data_ptr(), 8)
+    assert rc == zg.ERR_INVALID
     # a Wigner table smaller than the expansion order
     rc = _noalloc(zg, 0, 12, 1, c.data_ptr(), e.data_ptr(), 0, wig.data_ptr(), 8)
     assert rc == zg.ERR_INVALID

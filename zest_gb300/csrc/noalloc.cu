@@ -15,6 +15,8 @@
 //   [vec_bytes, + 48 L B)     phases, 3 tables of L double2 per batch item
 // Every byte a call reads is written earlier in the same call, so nothing in
 // the array has to start at zero.
+#include <cuda.h>
+
 #include <mutex>
 #include <string>
 
@@ -27,8 +29,43 @@ namespace {
 
 static __device__ __align__(256) unsigned char zt_rotate_scratch[ZEST_GPU_NOALLOC_SCRATCH_BYTES];
 
+// The array's device address, cached per device together with the id of the
+// CUDA context it was looked up in.  A context that is destroyed and created
+// anew (cudaDeviceReset, or the primary context released and retained again)
+// gets a new id, and the address is looked up again in it: an address from an
+// earlier context is never passed to a kernel.
+struct ScratchSlot {
+    unsigned long long ctx_id = 0;
+    void* addr = nullptr;
+};
 std::mutex g_scratch_mu;
-void* g_scratch_addr[ZEST_GPU_NOALLOC_MAX_DEVICES] = {};
+ScratchSlot g_scratch[ZEST_GPU_NOALLOC_MAX_DEVICES];
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// cuCtxGetCurrent and cuCtxGetId through the runtime's driver entry points
+// (the library links only the CUDA runtime); resolved once per process.
+bool context_fns(CtxGetCurrentFn* get_current, CtxGetIdFn* get_id) {
+    static CtxGetCurrentFn cur = nullptr;
+    static CtxGetIdFn id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            cur = reinterpret_cast<CtxGetCurrentFn>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            id = reinterpret_cast<CtxGetIdFn>(p);
+        cudaGetLastError();
+    });
+    *get_current = cur;
+    *get_id = id;
+    return cur && id;
+}
 
 // rotated vectors of order L with the given l: n = n0, n0 + 2, .. < L
 __host__ __device__ inline long long vec_count(int L, int l) {
@@ -53,23 +90,44 @@ __global__ void zt_vector_list_kernel(int L, int2* __restrict__ out) {
     for (long long i = 0; i < c; ++i) out[off + i] = make_int2(n0 + 2 * int(i), l);
 }
 
-// Address of the array on the current device; the first call per device looks
-// it up with that device current.
+// Address of the array in the current device's current context.  The first
+// call per device (and the first after that device's context was replaced)
+// looks it up with cudaGetSymbolAddress, which also loads the library's
+// kernels into the context; later calls only compare the context id.
 int scratch_of_current_device(unsigned char** out) {
     int dev = -1;
     ZG_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= ZEST_GPU_NOALLOC_MAX_DEVICES)
         return zgpu::fail(ZEST_GPU_ERR_UNSUPPORTED, "zt_rotate_noalloc: device index above 63");
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, zt_rotate_scratch);
-        if (e != cudaSuccess || !p)
+    CtxGetCurrentFn get_current = nullptr;
+    CtxGetIdFn get_id = nullptr;
+    if (!context_fns(&get_current, &get_id))
+        return zgpu::fail(ZEST_GPU_ERR_CUDA, "zt_rotate_noalloc: cuCtxGetCurrent/cuCtxGetId are unavailable");
+    auto lookup = [](void** p) -> int {
+        const cudaError_t e = cudaGetSymbolAddress(p, zt_rotate_scratch);
+        if (e != cudaSuccess || !*p)
             return zgpu::fail(ZEST_GPU_ERR_CUDA, std::string("zt_rotate_noalloc: cudaGetSymbolAddress of the scratch "
                                                              "array failed: ") + cudaGetErrorString(e));
-        g_scratch_addr[dev] = p;
+        return ZEST_GPU_OK;
+    };
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    CUcontext cu_ctx = nullptr;
+    void* fresh = nullptr;
+    if (get_current(&cu_ctx) != CUDA_SUCCESS) cu_ctx = nullptr;
+    if (!cu_ctx) {  // no context yet on this thread: the lookup creates the device's primary context
+        ZG_TRY(lookup(&fresh));
+        if (get_current(&cu_ctx) != CUDA_SUCCESS) cu_ctx = nullptr;
     }
-    *out = static_cast<unsigned char*>(g_scratch_addr[dev]);
+    unsigned long long ctx_id = 0;
+    if (!cu_ctx || get_id(cu_ctx, &ctx_id) != CUDA_SUCCESS)
+        return zgpu::fail(ZEST_GPU_ERR_CUDA, "zt_rotate_noalloc: no current CUDA context on the device");
+    ScratchSlot& slot = g_scratch[dev];
+    if (!slot.addr || slot.ctx_id != ctx_id) {
+        if (!fresh) ZG_TRY(lookup(&fresh));
+        slot.addr = fresh;
+        slot.ctx_id = ctx_id;
+    }
+    *out = static_cast<unsigned char*>(slot.addr);
     return ZEST_GPU_OK;
 }
 

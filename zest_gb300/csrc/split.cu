@@ -1379,6 +1379,7 @@ struct UnitList {
     double useful = 0.0;  // 2 * rows * table rows * K * products, valid tiles only
     double issued = 0.0;  // the same for full 128 x NT x 16k tiles
     DevBuf dev;
+    std::vector<long long> rows;  // exact row offsets a hashed key stands for (ragged rotation)
 };
 
 struct SplitState {
@@ -2519,17 +2520,28 @@ int split_rotate_ragged(zest_gpu_context* ctx, int Lmax, int items, long long nv
         h2 = h2 * 1000003ull + (unsigned long long)voff[l] * (2 * l + 1);
     }
     const int NT = stage_nt(st, WK_ROT, S, Lmax);
+    auto fill = [&](UnitList& ul) {
+        for (int l = 0; l < Lmax; ++l) {
+            const long long cnt = voff[l + 1] - voff[l];
+            add_units(ul, S, 8, voff[l], cnt, int(tri_size(l)), l + 1, NT, l + 1, 0, l);
+            add_units(ul, S, 8, voff[l], cnt, int(tri_size(l)), l + 1, NT, l + 1, 1 | 2, l);
+        }
+        ul.rows = voff;
+    };
     UnitList* u;
     ZG_TRY(get_units(ctx, std::make_tuple(int(WK_ROT), Lmax + nt_pass(NT), int(nvec), int(h1 & 0x7fffffff), S,
                                           int((h2 ^ (h2 >> 31)) & 0x7fffffff)),
-                     [&](UnitList& ul) {
-                         for (int l = 0; l < Lmax; ++l) {
-                             const long long cnt = voff[l + 1] - voff[l];
-                             add_units(ul, S, 8, voff[l], cnt, int(tri_size(l)), l + 1, NT, l + 1, 0, l);
-                             add_units(ul, S, 8, voff[l], cnt, int(tri_size(l)), l + 1, NT, l + 1, 1 | 2, l);
-                         }
-                     },
-                     &u));
+                     fill, &u));
+    if (u->rows != voff) {
+        // two batches whose row offsets share both hashes: the cached list
+        // belongs to the other one, so it is rebuilt for this batch
+        ZG_CUDA_TRY(cudaStreamSynchronize(s));  // the old list may still be read by a queued launch
+        u->v.clear();
+        u->max_ksteps = 0;
+        u->useful = u->issued = 0.0;
+        u->dev.release();
+        fill(*u);
+    }
     {
         StageScope sc(ctx, ST_SPLIT_SLICE);
         ZG_TRY(launch_slice2(s, RotInLoader{vecs, coff, coeffs, ph, Lmax}, nvec, Lmax, Lmax, 0, S, 8, SL_PAIR,
