@@ -1,0 +1,5 @@
+// Drop-in header with the reference's name (gauss_legendre.hpp): the GPU
+// implementation of the whole transform and rotation interface lives in
+// zest_gpu.hpp.
+#pragma once
+#include "zest_gpu.hpp"

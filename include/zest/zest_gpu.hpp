@@ -39,11 +39,15 @@
 
 #include <algorithm>
 #include <array>
+#include <cassert>
 #include <cmath>
+#include <complex>
 #include <concepts>
 #include <cstddef>
 #include <cstdint>
+#include <cstdio>
 #include <new>
+#include <numbers>
 #include <span>
 #include <stdexcept>
 #include <type_traits>
@@ -106,6 +110,72 @@ private:
     zest_gpu_context* m_ctx = nullptr;
 };
 
+namespace detail {
+// The reference's free functions (spectra, expansion conversions) run on a
+// context per thread.
+inline GPUContext& thread_context() {
+    thread_local GPUContext ctx(0);
+    return ctx;
+}
+}  // namespace detail
+
+// ---------------------------------------------------------------------------
+// Coefficient layouts, include/layout.hpp:36-420
+// ---------------------------------------------------------------------------
+enum class IndexingMode { negative, nonnegative };
+enum class Parity { even = 0, odd = 1 };
+
+// (l, m), 0 <= m <= l (or -l <= m <= l) at l(l+1)/2 + m (l(l+1) + m)
+template <IndexingMode indexing_mode_param>
+struct TriangleLayout {
+    using index_type = std::conditional_t<indexing_mode_param == IndexingMode::negative, int, std::size_t>;
+    using size_type = std::size_t;
+    static constexpr IndexingMode indexing_mode = indexing_mode_param;
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept {
+        if constexpr (indexing_mode == IndexingMode::nonnegative) return (order * (order + 1)) >> 1;
+        else return order * order;
+    }
+    [[nodiscard]] static constexpr std::size_t idx(index_type l, index_type m) noexcept {
+        if constexpr (indexing_mode == IndexingMode::nonnegative) return ((l * (l + 1)) >> 1) + m;
+        else return std::size_t(l * (l + 1) + m);
+    }
+};
+
+// Rows of one parity of l only, (l, m) at floor(l^2/4) + m (l(l+1)/2 + m):
+// the (l, m) coefficients of one radial index n of a Zernike expansion
+template <IndexingMode indexing_mode_param>
+struct RowSkippingTriangleLayout {
+    using index_type = std::conditional_t<indexing_mode_param == IndexingMode::negative, int, std::size_t>;
+    using size_type = std::size_t;
+    static constexpr IndexingMode indexing_mode = indexing_mode_param;
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept {
+        if constexpr (indexing_mode == IndexingMode::nonnegative) return ((order + 1) * (order + 1)) >> 2;
+        else return (order * (order + 1)) >> 1;
+    }
+    [[nodiscard]] static constexpr std::size_t idx(index_type l, index_type m) noexcept {
+        if constexpr (indexing_mode == IndexingMode::nonnegative) return ((l * l) >> 2) + m;
+        else return std::size_t(((l * (l + 1)) >> 1) + m);
+    }
+};
+
+// (n, l, m), l = n mod 2, .., n: (n+1)(n+3)(2n+1)/24 + floor(l^2/4) + m
+template <IndexingMode indexing_mode_param>
+struct ZernikeTetrahedralLayout {
+    using index_type = std::conditional_t<indexing_mode_param == IndexingMode::negative, int, std::size_t>;
+    using size_type = std::size_t;
+    static constexpr IndexingMode indexing_mode = indexing_mode_param;
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept {
+        if constexpr (indexing_mode == IndexingMode::nonnegative) return (order + 1) * (order + 3) * (2 * order + 1) / 24;
+        else return order * (order + 1) * (order + 2) / 6;
+    }
+    [[nodiscard]] static constexpr std::size_t idx(index_type n, index_type l, index_type m) noexcept {
+        if constexpr (indexing_mode == IndexingMode::nonnegative)
+            return (n + 1) * (n + 3) * (2 * n + 1) / 24 + ((l * l) >> 2) + m;
+        else
+            return std::size_t(n * (n + 1) * (n + 2) / 6 + ((l * (l + 1)) >> 1) + m);
+    }
+};
+
 // Containers are cache-line (64-byte) aligned, as the reference's.
 template <typename T>
 struct CacheLineAllocator {
@@ -137,7 +207,41 @@ enum class SHNorm { geo, qm };
 namespace detail {
 constexpr int abi(SHNorm n) noexcept { return n == SHNorm::geo ? ZEST_SH_GEO : ZEST_SH_QM; }
 constexpr int abi(SHPhase p) noexcept { return p == SHPhase::none ? ZEST_SH_PHASE_NONE : ZEST_SH_PHASE_CS; }
+inline constexpr double inv_sqrtpi = 0.564189583547756286948079451560772586;
 }  // namespace detail
+
+// Normalisation constant of the SH coefficients, sh_conventions.hpp:56-63:
+// 1 (qm) or 1/(4 pi) (geo).
+template <SHNorm sh_norm_param>
+[[nodiscard]] constexpr double normalization() noexcept {
+    if constexpr (sh_norm_param == SHNorm::qm) return 1.0;
+    else return 1.0 / (4.0 * 3.141592653589793238462643383279502884);
+}
+
+// Factor converting coefficients between SH normalisations,
+// sh_conventions.hpp:73-96 (the same operations, so the same double).
+template <SHNorm from, SHNorm to>
+[[nodiscard]] constexpr double conversion_const() noexcept {
+    if constexpr (from == to) {
+        return 1.0;
+    } else {
+        constexpr double inv_sqrt_4pi = 0.5 * detail::inv_sqrtpi;
+        constexpr double sqrt_4pi = 1.0 / inv_sqrt_4pi;
+        double norm = from == SHNorm::qm ? 1.0 : sqrt_4pi;
+        norm *= to == SHNorm::qm ? 1.0 : inv_sqrt_4pi;
+        return norm;
+    }
+}
+
+// An expansion holding the rows of one parity of l in the row-skipping layout
+// (a zt::ZernikeSHSpan), real_sh_expansion.hpp:309-316.
+template <typename T>
+concept row_skipping_real_sh_expansion =
+    std::same_as<typename std::remove_cvref_t<T>::Layout, RowSkippingTriangleLayout<IndexingMode::nonnegative>> &&
+    requires {
+        { std::remove_cvref_t<T>::norm } -> std::convertible_to<SHNorm>;
+        { std::remove_cvref_t<T>::phase } -> std::convertible_to<SHPhase>;
+    };
 
 // [lon][lat]: (2L - 1, pad8(L))
 template <typename AlignmentType = CacheLineAlignment>
@@ -252,10 +356,19 @@ private:
     std::size_t m_order = 0;
 };
 
+// Either grid type of the sphere, sh_glq_transformer.hpp:367-377.
+template <typename T>
+concept sphere_glq_grid =
+    std::same_as<std::remove_cvref_t<T>, SphereGLQGridSpan<typename std::remove_cvref_t<T>::element_type,
+                                                           typename std::remove_cvref_t<T>::Layout>> ||
+    std::same_as<std::remove_cvref_t<T>, SphereGLQGrid<typename std::remove_cvref_t<T>::element_type,
+                                                       typename std::remove_cvref_t<T>::Layout>>;
+
 // Real SH coefficients {cos, sin} of degree l and order m at l(l+1)/2 + m.
 template <typename ElementType, SHNorm sh_norm_param, SHPhase sh_phase_param>
 class RealSHSpan {
 public:
+    using Layout = TriangleLayout<IndexingMode::nonnegative>;
     using element_type = ElementType;
     using value_type = std::remove_cv_t<ElementType>;
     using ConstView = RealSHSpan<const value_type, sh_norm_param, sh_phase_param>;
@@ -293,6 +406,7 @@ private:
 template <SHNorm sh_norm_param, SHPhase sh_phase_param, typename ElementType = std::array<double, 2>>
 class RealSHExpansion {
 public:
+    using Layout = TriangleLayout<IndexingMode::nonnegative>;
     using element_type = ElementType;
     using value_type = std::remove_cv_t<ElementType>;
     using View = RealSHSpan<element_type, sh_norm_param, sh_phase_param>;
@@ -348,6 +462,39 @@ concept real_sh_expansion = requires {
 } && std::convertible_to<T, RealSHSpan<typename std::remove_cvref_t<T>::element_type,
                                        std::remove_cvref_t<T>::norm, std::remove_cvref_t<T>::phase>>;
 
+namespace detail {
+// In-place conversion of host (or device) coefficients on the device.
+inline void convert(int kind, std::size_t order, void* data, int src_zn, int src_sn, int src_sp, int dst_zn,
+                    int dst_sn, int dst_sp, bool to_complex, MemoryKind mem = MemoryKind::host) {
+    zest::detail::check(zest_gpu_convert_expansion(zest::detail::thread_context().get(), kind, order, 1,
+                                                   static_cast<double*>(data), src_zn, src_sn, src_sp, dst_zn,
+                                                   dst_sn, dst_sp, int(to_complex), int(mem)));
+}
+}  // namespace detail
+
+// Real SH expansion -> complex expansion of the destination conventions, in
+// place (the input is modified; the result views the same data),
+// real_sh_expansion.hpp:345-387.
+template <SHNorm dest_sh_norm, SHPhase dest_sh_phase, real_sh_expansion ExpansionType>
+RealSHSpan<std::complex<double>, dest_sh_norm, dest_sh_phase> to_complex_expansion(ExpansionType&& expansion) {
+    using E = std::remove_cvref_t<ExpansionType>;
+    detail::convert(ZEST_EXPANSION_SH, expansion.order(), expansion.data(), 0, detail::abi(E::norm),
+                    detail::abi(E::phase), 0, detail::abi(dest_sh_norm), detail::abi(dest_sh_phase), true);
+    return RealSHSpan<std::complex<double>, dest_sh_norm, dest_sh_phase>(
+        reinterpret_cast<std::complex<double>*>(expansion.data()), expansion.order());
+}
+
+// Complex SH expansion -> real expansion of the destination conventions, in
+// place, real_sh_expansion.hpp:399-436.
+template <SHNorm dest_sh_norm, SHPhase dest_sh_phase, real_sh_expansion ExpansionType>
+RealSHSpan<std::array<double, 2>, dest_sh_norm, dest_sh_phase> to_real_expansion(ExpansionType&& expansion) {
+    using E = std::remove_cvref_t<ExpansionType>;
+    detail::convert(ZEST_EXPANSION_SH, expansion.order(), expansion.data(), 0, detail::abi(E::norm),
+                    detail::abi(E::phase), 0, detail::abi(dest_sh_norm), detail::abi(dest_sh_phase), false);
+    return RealSHSpan<std::array<double, 2>, dest_sh_norm, dest_sh_phase>(
+        reinterpret_cast<std::array<double, 2>*>(expansion.data()), expansion.order());
+}
+
 // Spherical-harmonic transforms on the GLQ grid, sh_glq_transformer.hpp:520-754.
 template <SHNorm sh_norm_param, SHPhase sh_phase_param, typename GridLayoutType = DefaultLayout>
 class GLQTransformer {
@@ -386,6 +533,28 @@ public:
         RealSHSpan<const std::array<double, 2>, sh_norm_param, sh_phase_param> expansion, std::size_t order) {
         SphereGLQGrid<double, GridLayout> grid(order);
         backward_transform(expansion, grid);
+        return grid;
+    }
+
+    // Backward transform of an expansion of one parity of l (a zt::ZernikeSHSpan),
+    // sh_glq_transformer.hpp:680-700 and :743-754.
+    template <row_skipping_real_sh_expansion Expansion>
+        requires(std::remove_cvref_t<Expansion>::norm == sh_norm_param) &&
+                (std::remove_cvref_t<Expansion>::phase == sh_phase_param) &&
+                std::same_as<typename std::remove_cvref_t<Expansion>::value_type, std::array<double, 2>>
+    void backward_transform(Expansion&& expansion, SphereGLQGridSpan<double, GridLayout> values) {
+        resize(values.order());
+        zest::detail::check(zest_gpu_st_backward_rows(
+            m_ctx.get(), detail::abi(sh_norm_param), detail::abi(sh_phase_param), GridLayout::abi, expansion.order(),
+            values.order(), 1, reinterpret_cast<const double*>(expansion.data()), values.data(), ZEST_MEM_HOST));
+    }
+    template <row_skipping_real_sh_expansion Expansion>
+        requires(std::remove_cvref_t<Expansion>::norm == sh_norm_param) &&
+                (std::remove_cvref_t<Expansion>::phase == sh_phase_param) &&
+                std::same_as<typename std::remove_cvref_t<Expansion>::value_type, std::array<double, 2>>
+    [[nodiscard]] SphereGLQGrid<double, GridLayout> backward_transform(Expansion&& expansion, std::size_t order) {
+        SphereGLQGrid<double, GridLayout> grid(order);
+        backward_transform(std::forward<Expansion>(expansion), grid);
         return grid;
     }
 
@@ -447,6 +616,70 @@ constexpr int abi(ZernikeNorm n) noexcept {
     return n == ZernikeNorm::normed ? ZEST_ZERNIKE_NORMED : ZEST_ZERNIKE_UNNORMED;
 }
 }  // namespace detail
+
+// Normalisation of the radial Zernike functions, zernike_conventions.hpp:44-51.
+template <ZernikeNorm zernike_norm_param>
+[[nodiscard]] inline double normalization(std::size_t n) noexcept {
+    if constexpr (zernike_norm_param == ZernikeNorm::normed) return 1.0;
+    else return double(2 * n + 3);
+}
+
+// Factor converting coefficients between Zernike normalisations,
+// zernike_conventions.hpp:61-76.
+template <ZernikeNorm from, ZernikeNorm to>
+[[nodiscard]] inline double conversion_factor(std::size_t n) noexcept {
+    if constexpr (from == to) return 1.0;
+    else if constexpr (to == ZernikeNorm::normed) return 1.0 / std::sqrt(double(2 * n + 3));
+    else return std::sqrt(double(2 * n + 3));
+}
+
+// The (l, m) coefficients of one radial index n of a Zernike expansion: a
+// span of `order` = n + 1 in the row-skipping layout (rows l = n mod 2, .., n),
+// zernike_expansion.hpp:103-140.
+template <typename ElementType, typename LayoutType, ZernikeNorm zernike_norm_param, st::SHNorm sh_norm_param,
+          st::SHPhase sh_phase_param>
+    requires std::same_as<LayoutType, RowSkippingTriangleLayout<LayoutType::indexing_mode>>
+class ZernikeSHSpan {
+public:
+    using Layout = LayoutType;
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    using index_type = typename Layout::index_type;
+    using ConstView = ZernikeSHSpan<const value_type, LayoutType, zernike_norm_param, sh_norm_param, sh_phase_param>;
+    static constexpr ZernikeNorm zernike_norm = zernike_norm_param;
+    static constexpr st::SHNorm norm = sh_norm_param;
+    static constexpr st::SHPhase phase = sh_phase_param;
+
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept { return Layout::size(order); }
+
+    constexpr ZernikeSHSpan() noexcept = default;
+    constexpr ZernikeSHSpan(element_type* data, std::size_t order) noexcept
+        : m_data(data), m_size(Layout::size(order)), m_order(order) {}
+    constexpr ZernikeSHSpan(std::span<element_type> buffer, std::size_t order) noexcept
+        : m_data(buffer.data()), m_size(Layout::size(order)), m_order(order) {}
+    constexpr ZernikeSHSpan(element_type* data, std::size_t size, std::size_t order) noexcept
+        : m_data(data), m_size(size), m_order(order) {}
+
+    [[nodiscard]] constexpr std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] constexpr std::size_t size() const noexcept { return m_size; }
+    [[nodiscard]] constexpr element_type* data() const noexcept { return m_data; }
+    [[nodiscard]] constexpr std::span<element_type> flatten() const noexcept { return {m_data, m_size}; }
+    // rows of the parity of order - 1
+    [[nodiscard]] constexpr Parity parity() const noexcept { return Parity((m_order & 1) ^ 1); }
+    [[nodiscard]] constexpr element_type& operator()(index_type l, index_type m) const noexcept {
+        return m_data[Layout::idx(l, m)];
+    }
+    [[nodiscard]] constexpr operator ConstView() const noexcept
+        requires(!std::is_const_v<ElementType>)
+    {
+        return ConstView(m_data, m_size, m_order);
+    }
+
+private:
+    element_type* m_data = nullptr;
+    std::size_t m_size = 0;
+    std::size_t m_order = 0;
+};
 
 // [lon][lat][rad]: (2L - 1, L + 1, pad8(L + 1))
 template <typename AlignmentType = CacheLineAlignment>
@@ -542,15 +775,26 @@ private:
     std::size_t m_order = 0;
 };
 
+// Either grid type of the ball, zernike_glq_transformer.hpp:318-328.
+template <typename T>
+concept ball_glq_grid =
+    std::same_as<std::remove_cvref_t<T>, BallGLQGridSpan<typename std::remove_cvref_t<T>::element_type,
+                                                         typename std::remove_cvref_t<T>::Layout>> ||
+    std::same_as<std::remove_cvref_t<T>, BallGLQGrid<typename std::remove_cvref_t<T>::element_type,
+                                                     typename std::remove_cvref_t<T>::Layout>>;
+
 // Real Zernike coefficients {cos, sin} of (n, l, m), n - l even, at
 // (n+1)(n+3)(2n+1)/24 + floor(l^2/4) + m.
 template <typename ElementType, ZernikeNorm zernike_norm_param, st::SHNorm sh_norm_param,
           st::SHPhase sh_phase_param>
 class RealZernikeSpan {
 public:
+    using Layout = ZernikeTetrahedralLayout<IndexingMode::nonnegative>;
     using element_type = ElementType;
     using value_type = std::remove_cv_t<ElementType>;
     using ConstView = RealZernikeSpan<const value_type, zernike_norm_param, sh_norm_param, sh_phase_param>;
+    using SubSpan = ZernikeSHSpan<ElementType, RowSkippingTriangleLayout<IndexingMode::nonnegative>,
+                                  zernike_norm_param, sh_norm_param, sh_phase_param>;
     static constexpr ZernikeNorm zernike_norm = zernike_norm_param;
     static constexpr st::SHNorm sh_norm = sh_norm_param;
     static constexpr st::SHPhase sh_phase = sh_phase_param;
@@ -574,6 +818,10 @@ public:
     [[nodiscard]] constexpr element_type& operator()(std::size_t n, std::size_t l, std::size_t m) const noexcept {
         return m_data[idx(n, l, m)];
     }
+    // the (l, m) coefficients of radial index n, zernike_expansion.hpp:186-190
+    [[nodiscard]] constexpr SubSpan operator[](std::size_t n) const noexcept {
+        return SubSpan(m_data + idx(n, 0, 0), n + 1);
+    }
     [[nodiscard]] constexpr operator ConstView() const noexcept
         requires(!std::is_const_v<ElementType>)
     {
@@ -589,6 +837,7 @@ template <ZernikeNorm zernike_norm_param, st::SHNorm sh_norm_param, st::SHPhase 
           typename ElementType = std::array<double, 2>>
 class RealZernikeExpansion {
 public:
+    using Layout = ZernikeTetrahedralLayout<IndexingMode::nonnegative>;
     using element_type = ElementType;
     using value_type = std::remove_cv_t<ElementType>;
     using View = RealZernikeSpan<element_type, zernike_norm_param, sh_norm_param, sh_phase_param>;
@@ -656,6 +905,59 @@ concept real_zernike_expansion = requires {
 } && std::convertible_to<T, RealZernikeSpan<typename std::remove_cvref_t<T>::element_type,
                                             std::remove_cvref_t<T>::zernike_norm, std::remove_cvref_t<T>::sh_norm,
                                             std::remove_cvref_t<T>::sh_phase>>;
+
+// Real Zernike expansion -> complex expansion of the destination conventions,
+// in place (the input is modified; the result views the same data),
+// zernike_expansion.hpp:484-557.
+template <ZernikeNorm dest_zernike_norm, st::SHNorm dest_sh_norm, st::SHPhase dest_sh_phase,
+          real_zernike_expansion ExpansionType>
+RealZernikeSpan<std::complex<double>, dest_zernike_norm, dest_sh_norm, dest_sh_phase> to_complex_expansion(
+    ExpansionType&& expansion) {
+    using E = std::remove_cvref_t<ExpansionType>;
+    st::detail::convert(ZEST_EXPANSION_ZERNIKE, expansion.order(), expansion.data(), detail::abi(E::zernike_norm),
+                        st::detail::abi(E::sh_norm), st::detail::abi(E::sh_phase), detail::abi(dest_zernike_norm),
+                        st::detail::abi(dest_sh_norm), st::detail::abi(dest_sh_phase), true);
+    return RealZernikeSpan<std::complex<double>, dest_zernike_norm, dest_sh_norm, dest_sh_phase>(
+        reinterpret_cast<std::complex<double>*>(expansion.data()), expansion.order());
+}
+
+// Complex Zernike expansion -> real expansion, in place, zernike_expansion.hpp:568-634.
+template <ZernikeNorm dest_zernike_norm, st::SHNorm dest_sh_norm, st::SHPhase dest_sh_phase,
+          real_zernike_expansion ExpansionType>
+RealZernikeSpan<std::array<double, 2>, dest_zernike_norm, dest_sh_norm, dest_sh_phase> to_real_expansion(
+    ExpansionType&& expansion) {
+    using E = std::remove_cvref_t<ExpansionType>;
+    st::detail::convert(ZEST_EXPANSION_ZERNIKE, expansion.order(), expansion.data(), detail::abi(E::zernike_norm),
+                        st::detail::abi(E::sh_norm), st::detail::abi(E::sh_phase), detail::abi(dest_zernike_norm),
+                        st::detail::abi(dest_sh_norm), st::detail::abi(dest_sh_phase), false);
+    return RealZernikeSpan<std::array<double, 2>, dest_zernike_norm, dest_sh_norm, dest_sh_phase>(
+        reinterpret_cast<std::array<double, 2>*>(expansion.data()), expansion.order());
+}
+
+// The same for the coefficients of one radial index (a ZernikeSHSpan): only
+// the SH conventions change, zernike_expansion.hpp:644-775.
+template <st::SHNorm dest_sh_norm, st::SHPhase dest_sh_phase, typename ExpansionType>
+    requires st::row_skipping_real_sh_expansion<ExpansionType> &&
+             std::same_as<typename std::remove_cvref_t<ExpansionType>::value_type, std::array<double, 2>>
+auto to_complex_expansion(ExpansionType&& expansion) {
+    using E = std::remove_cvref_t<ExpansionType>;
+    st::detail::convert(ZEST_EXPANSION_ZERNIKE_ROW, expansion.order(), expansion.data(), detail::abi(E::zernike_norm),
+                        st::detail::abi(E::norm), st::detail::abi(E::phase), detail::abi(E::zernike_norm),
+                        st::detail::abi(dest_sh_norm), st::detail::abi(dest_sh_phase), true);
+    return ZernikeSHSpan<std::complex<double>, typename E::Layout, E::zernike_norm, dest_sh_norm, dest_sh_phase>(
+        reinterpret_cast<std::complex<double>*>(expansion.data()), expansion.order());
+}
+template <st::SHNorm dest_sh_norm, st::SHPhase dest_sh_phase, typename ExpansionType>
+    requires st::row_skipping_real_sh_expansion<ExpansionType> &&
+             std::same_as<typename std::remove_cvref_t<ExpansionType>::value_type, std::complex<double>>
+auto to_real_expansion(ExpansionType&& expansion) {
+    using E = std::remove_cvref_t<ExpansionType>;
+    st::detail::convert(ZEST_EXPANSION_ZERNIKE_ROW, expansion.order(), expansion.data(), detail::abi(E::zernike_norm),
+                        st::detail::abi(E::norm), st::detail::abi(E::phase), detail::abi(E::zernike_norm),
+                        st::detail::abi(dest_sh_norm), st::detail::abi(dest_sh_phase), false);
+    return ZernikeSHSpan<std::array<double, 2>, typename E::Layout, E::zernike_norm, dest_sh_norm, dest_sh_phase>(
+        reinterpret_cast<std::array<double, 2>*>(expansion.data()), expansion.order());
+}
 
 // Zernike transforms on the GLQ grid of the ball, zernike_glq_transformer.hpp:510-707.
 template <ZernikeNorm zernike_norm_param, st::SHNorm sh_norm_param, st::SHPhase sh_phase_param,
@@ -843,6 +1145,18 @@ public:
         zest::detail::check(zest_gpu_st_rotate(m_ctx.get(), span.order(), 1, reinterpret_cast<double*>(span.data()),
                                                euler_angles.data(), abi(type), ZEST_MEM_HOST));
     }
+    // An expansion of one parity of l in the row-skipping layout (the
+    // coefficients of one radial index of a Zernike expansion), rotor.hpp:165-193.
+    template <st::row_skipping_real_sh_expansion ExpansionType>
+        requires std::same_as<typename std::remove_cvref_t<ExpansionType>::value_type, std::array<double, 2>>
+    void rotate(ExpansionType&& expansion, const WignerdPiHalfCollection& wigner_d_pi2,
+                const std::array<double, 3>& euler_angles, RotationType type) {
+        check_wigner(wigner_d_pi2, expansion.order());
+        expand(expansion.order());
+        zest::detail::check(zest_gpu_rows_rotate(m_ctx.get(), expansion.order(), 1,
+                                                 reinterpret_cast<double*>(expansion.data()), euler_angles.data(),
+                                                 abi(type), ZEST_MEM_HOST));
+    }
     template <typename ExpansionType>
         requires zt::real_zernike_expansion<ExpansionType> || st::real_sh_expansion<ExpansionType>
     void rotate(ExpansionType&& expansion, const WignerdPiHalfCollection& wigner_d_pi2,
@@ -921,14 +1235,6 @@ private:
 // ---------------------------------------------------------------------------
 // Evaluation at arbitrary points and power spectra
 // ---------------------------------------------------------------------------
-
-namespace detail {
-// The reference's spectra are free functions; they run on a context per thread.
-inline GPUContext& thread_context() {
-    thread_local GPUContext ctx(0);
-    return ctx;
-}
-}  // namespace detail
 
 namespace st {
 
@@ -1429,6 +1735,230 @@ public:
 private:
     GPUContext m_ctx;
     std::size_t m_order;
+};
+
+}  // namespace zt
+
+
+// ---------------------------------------------------------------------------
+// Tables: Gauss-Legendre nodes and weights, the P_lm and R_nl recursions
+// ---------------------------------------------------------------------------
+namespace gl {
+
+// Nodes of both halves (UnpackedLayout) or of the non-negative half only
+// (PackedLayout), gauss_legendre.hpp:43-86.
+struct PackedLayout {
+    [[nodiscard]] static constexpr std::size_t size(std::size_t num_total_nodes) noexcept {
+        return (num_total_nodes + 1) >> 1;
+    }
+    [[nodiscard]] static constexpr std::size_t total_nodes(std::size_t size, std::size_t parity) noexcept {
+        return 2 * size - parity;
+    }
+};
+struct UnpackedLayout {
+    [[nodiscard]] static constexpr std::size_t size(std::size_t num_total_nodes) noexcept { return num_total_nodes; }
+    [[nodiscard]] static constexpr std::size_t total_nodes(std::size_t size, std::size_t) noexcept { return size; }
+};
+
+// Nodes as cosines x in [-1, 1] (ascending) or as angles arccos(x).
+enum class GLNodeStyle { angle, cos };
+
+// Gauss-Legendre nodes and weights, gauss_legendre.hpp:1549-1565: as many as
+// `nodes` holds, of a rule of Layout::total_nodes(nodes.size(), parity) nodes.
+// The nodes come from a double-double Newton solve (within 2 ulp of the
+// reference's tables and Bogaert formulas); angle-style nodes are the
+// colatitudes of the quadrature grids.
+template <typename Layout, GLNodeStyle node_style_param, typename R>
+void gl_nodes_and_weights(R&& nodes, R&& weights, std::size_t parity) {
+    const std::size_t size = std::size(nodes);
+    if (size == 0) return;
+    const std::size_t n = Layout::total_nodes(size, parity);
+    constexpr bool packed = std::same_as<Layout, PackedLayout>;
+    zest::detail::check(zest_gpu_gl_nodes_weights(n, packed, std::data(nodes), std::data(weights)));
+    if constexpr (node_style_param == GLNodeStyle::angle) {
+        // the LatLon SH grid of order n has the n angle-style nodes as its colatitudes
+        std::vector<double> lon(zest_gpu_st_grid_size(n, ZEST_LAYOUT_LATLON) / n), colat(n);
+        zest::detail::check(zest_gpu_st_grid_points(n, ZEST_LAYOUT_LATLON, lon.data(), colat.data()));
+        std::copy(colat.end() - std::ptrdiff_t(size), colat.end(), std::data(nodes));
+    }
+}
+
+}  // namespace gl
+
+namespace st {
+
+using PlmLayout = TriangleLayout<IndexingMode::nonnegative>;
+
+// P_lm of one point at PlmLayout::idx(l, m), plm_recursion.hpp:46-48.
+template <typename ElementType, SHNorm sh_norm_param, SHPhase sh_phase_param>
+class PlmSpan {
+public:
+    using Layout = PlmLayout;
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    static constexpr SHNorm norm = sh_norm_param;
+    static constexpr SHPhase phase = sh_phase_param;
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept { return Layout::size(order); }
+    constexpr PlmSpan() noexcept = default;
+    constexpr PlmSpan(element_type* data, std::size_t order) noexcept : m_data(data), m_order(order) {}
+    constexpr PlmSpan(std::span<element_type> buffer, std::size_t order) noexcept
+        : m_data(buffer.data()), m_order(order) {}
+    [[nodiscard]] constexpr std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] constexpr std::size_t size() const noexcept { return size(m_order); }
+    [[nodiscard]] constexpr element_type* data() const noexcept { return m_data; }
+    [[nodiscard]] constexpr std::span<element_type> flatten() const noexcept { return {m_data, size()}; }
+    [[nodiscard]] constexpr element_type& operator()(std::size_t l, std::size_t m) const noexcept {
+        return m_data[Layout::idx(l, m)];
+    }
+
+private:
+    element_type* m_data = nullptr;
+    std::size_t m_order = 0;
+};
+
+// P_lm of vec_size points: the values of (l, m) contiguous at
+// PlmLayout::idx(l, m) * vec_size, plm_recursion.hpp:53-55.
+template <typename ElementType, SHNorm sh_norm_param, SHPhase sh_phase_param>
+class PlmVecSpan {
+public:
+    using Layout = PlmLayout;
+    using element_type = ElementType;
+    using value_type = std::remove_cv_t<ElementType>;
+    static constexpr SHNorm norm = sh_norm_param;
+    static constexpr SHPhase phase = sh_phase_param;
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order, std::size_t vec_size) noexcept {
+        return Layout::size(order) * vec_size;
+    }
+    constexpr PlmVecSpan() noexcept = default;
+    constexpr PlmVecSpan(element_type* data, std::size_t order, std::size_t vec_size) noexcept
+        : m_data(data), m_order(order), m_vec_size(vec_size) {}
+    constexpr PlmVecSpan(std::span<element_type> buffer, std::size_t order, std::size_t vec_size) noexcept
+        : m_data(buffer.data()), m_order(order), m_vec_size(vec_size) {}
+    [[nodiscard]] constexpr std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] constexpr std::size_t vec_size() const noexcept { return m_vec_size; }
+    [[nodiscard]] constexpr std::size_t size() const noexcept { return size(m_order, m_vec_size); }
+    [[nodiscard]] constexpr element_type* data() const noexcept { return m_data; }
+    [[nodiscard]] constexpr std::span<element_type> flatten() const noexcept { return {m_data, size()}; }
+    [[nodiscard]] constexpr std::span<element_type> operator()(std::size_t l, std::size_t m) const noexcept {
+        return {m_data + Layout::idx(l, m) * m_vec_size, m_vec_size};
+    }
+
+private:
+    element_type* m_data = nullptr;
+    std::size_t m_order = 0;
+    std::size_t m_vec_size = 0;
+};
+
+// The associated Legendre recursion, plm_recursion.hpp:62-362, evaluated on
+// the device in FP64 with the reference's operations in its order (the
+// tables are bit-identical to the reference's).
+class PlmRecursion {
+public:
+    PlmRecursion() = default;
+    explicit PlmRecursion(std::size_t max_order) : m_max_order(max_order) {}
+    [[nodiscard]] std::size_t max_order() const noexcept { return m_max_order; }
+    void expand(std::size_t max_order) { m_max_order = std::max(m_max_order, max_order); }
+    void expand_vec(std::size_t) {}
+
+    template <SHNorm sh_norm_param, SHPhase sh_phase_param>
+    void plm_real(double z, PlmSpan<double, sh_norm_param, sh_phase_param> plm) {
+        run(false, sh_norm_param, sh_phase_param, plm.order(), 1, &z, plm.data());
+    }
+    template <SHNorm sh_norm_param, SHPhase sh_phase_param>
+    void plm_real(std::span<const double> z, PlmVecSpan<double, sh_norm_param, sh_phase_param> plm) {
+        run(false, sh_norm_param, sh_phase_param, plm.order(), z.size(), z.data(), plm.data());
+    }
+    template <SHNorm sh_norm_param, SHPhase sh_phase_param>
+    void plm_complex(double z, PlmSpan<double, sh_norm_param, sh_phase_param> plm) {
+        run(true, sh_norm_param, sh_phase_param, plm.order(), 1, &z, plm.data());
+    }
+    template <SHNorm sh_norm_param, SHPhase sh_phase_param>
+    void plm_complex(std::span<const double> z, PlmVecSpan<double, sh_norm_param, sh_phase_param> plm) {
+        run(true, sh_norm_param, sh_phase_param, plm.order(), z.size(), z.data(), plm.data());
+    }
+
+private:
+    void run(bool complex_basis, SHNorm norm, SHPhase phase, std::size_t order, std::size_t nz, const double* z,
+             double* out) {
+        expand(order);
+        auto* ctx = zest::detail::thread_context().get();
+        zest::detail::check(complex_basis
+                                ? zest_gpu_plm_complex_table(ctx, order, detail::abi(norm), detail::abi(phase), nz,
+                                                             z, out, ZEST_MEM_HOST)
+                                : zest_gpu_plm_table(ctx, order, detail::abi(norm), detail::abi(phase), nz, z, out,
+                                                     ZEST_MEM_HOST));
+    }
+    std::size_t m_max_order = 0;
+};
+
+}  // namespace st
+
+namespace zt {
+
+// R_nl at index floor((n+1)^2/4) + floor(l/2), zernike_expansion.hpp:43-75.
+struct RadialZernikeLayout {
+    using index_type = std::size_t;
+    using size_type = std::size_t;
+    [[nodiscard]] static constexpr std::size_t size(std::size_t order) noexcept {
+        return ((order + 1) * (order + 1)) >> 2;
+    }
+    [[nodiscard]] static constexpr std::size_t idx(std::size_t n, std::size_t l) noexcept {
+        return (((n + 1) * (n + 1)) >> 2) + (l >> 1);
+    }
+};
+
+// R_nl of vec_size radii: the values of (n, l) contiguous.
+template <typename ElementType, ZernikeNorm zernike_norm_param>
+class RadialZernikeVecSpan {
+public:
+    using Layout = RadialZernikeLayout;
+    using element_type = ElementType;
+    static constexpr ZernikeNorm zernike_norm = zernike_norm_param;
+    constexpr RadialZernikeVecSpan() noexcept = default;
+    constexpr RadialZernikeVecSpan(element_type* data, std::size_t order, std::size_t vec_size) noexcept
+        : m_data(data), m_order(order), m_vec_size(vec_size) {}
+    constexpr RadialZernikeVecSpan(std::span<element_type> buffer, std::size_t order, std::size_t vec_size) noexcept
+        : m_data(buffer.data()), m_order(order), m_vec_size(vec_size) {}
+    [[nodiscard]] constexpr std::size_t order() const noexcept { return m_order; }
+    [[nodiscard]] constexpr std::size_t vec_size() const noexcept { return m_vec_size; }
+    [[nodiscard]] constexpr std::size_t size() const noexcept { return Layout::size(m_order) * m_vec_size; }
+    [[nodiscard]] constexpr element_type* data() const noexcept { return m_data; }
+    [[nodiscard]] constexpr std::span<element_type> flatten() const noexcept { return {m_data, size()}; }
+    [[nodiscard]] constexpr std::span<element_type> operator()(std::size_t n, std::size_t l) const noexcept {
+        return {m_data + Layout::idx(n, l) * m_vec_size, m_vec_size};
+    }
+
+private:
+    element_type* m_data = nullptr;
+    std::size_t m_order = 0;
+    std::size_t m_vec_size = 0;
+};
+
+// The radial Zernike recursion, radial_zernike_recursion.hpp:38-297, on the
+// device in FP64 (bit-identical to the reference's values).
+class RadialZernikeRecursion {
+public:
+    RadialZernikeRecursion() = default;
+    explicit RadialZernikeRecursion(std::size_t max_order) : m_max_order(max_order) {}
+    [[nodiscard]] std::size_t max_order() const noexcept { return m_max_order; }
+    void expand(std::size_t max_order) { m_max_order = std::max(m_max_order, max_order); }
+
+    template <ZernikeNorm zernike_norm_param>
+    void zernike(double r, RadialZernikeSpan<double, zernike_norm_param> out) {
+        run(zernike_norm_param, out.order(), 1, &r, out.data());
+    }
+    template <ZernikeNorm zernike_norm_param>
+    void zernike(std::span<const double> r, RadialZernikeVecSpan<double, zernike_norm_param> out) {
+        run(zernike_norm_param, out.order(), r.size(), r.data(), out.data());
+    }
+
+private:
+    void run(ZernikeNorm norm, std::size_t order, std::size_t nr, const double* r, double* out) {
+        expand(order);
+        zest::detail::check(zest_gpu_radial_table(zest::detail::thread_context().get(), order, detail::abi(norm), nr,
+                                                  r, out, ZEST_MEM_HOST));
+    }
+    std::size_t m_max_order = 0;
 };
 
 }  // namespace zt

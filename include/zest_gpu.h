@@ -63,6 +63,10 @@ extern "C" {
 /* SH grid layouts: LonLatLayout (the default) / LatLonLayout */
 #define ZEST_LAYOUT_LONLAT 0
 #define ZEST_LAYOUT_LATLON 1
+/* expansion layouts of zest_gpu_convert_expansion */
+#define ZEST_EXPANSION_ZERNIKE 0     /* RealZernikeSpan: ZernikeTetrahedralLayout, layout.hpp:385-420 */
+#define ZEST_EXPANSION_SH 1          /* RealSHSpan: TriangleLayout, layout.hpp:203-240 */
+#define ZEST_EXPANSION_ZERNIKE_ROW 2 /* zt::ZernikeSHSpan: RowSkippingTriangleLayout, layout.hpp:334-371 */
 /* arithmetic of the contractions */
 #define ZEST_PRECISION_FP64 0  /* FP64 everywhere (plain form) */
 #define ZEST_PRECISION_SPLIT 1 /* BF16 fixed-point slices on tcgen05, exact FP32 partial sums, FP64 recombination */
@@ -75,14 +79,16 @@ typedef struct zest_gpu_context zest_gpu_context;
 /* ---- context ---- */
 /* Creates a context on `device` bound to `stream` (a cudaStream_t; NULL = the
  * legacy default stream).  Replaces the scratch/caches a reference
- * transformer holds (zernike_glq_transformer.hpp:951-964). */
+ * transformer holds (zernike_glq_transformer.hpp:951-964).  A new context
+ * computes in FP64, or in the split-precision form (six slices) when the
+ * environment variable ZEST_GPU_PRECISION is "split". */
 int zest_gpu_ctx_create(zest_gpu_context** ctx, int device, void* stream);
 int zest_gpu_ctx_destroy(zest_gpu_context* ctx);
 /* Message of the last failing call on this thread ("" if none). */
 const char* zest_gpu_last_error(void);
 /* Precision of the dense contractions; `slices` = number of BF16 digit
- * slices per operand for ZEST_PRECISION_SPLIT (4..6, 0 = default 6): 8-bit
- * digits for contraction lengths up to 256, 7-bit digits above. */
+ * slices per operand for ZEST_PRECISION_SPLIT (4..6, 0 = default 6), 8-bit
+ * digits, sums longer than 256 terms in chunks of at most 256. */
 int zest_gpu_set_precision(zest_gpu_context* ctx, int precision, int slices);
 int zest_gpu_synchronize(zest_gpu_context* ctx);
 /* Releases cached tables and scratch (they are rebuilt on demand). */
@@ -136,6 +142,34 @@ int zest_gpu_st_backward(zest_gpu_context* ctx, int sh_norm, int sh_phase, int l
                          size_t exp_order, size_t grid_order, size_t batch,
                          const double* coeffs, double* grids, int mem);
 
+/* st::GLQTransformer<...>::backward_transform of a row-skipping SH expansion
+ * (one parity of l), sh_glq_transformer.hpp:680-700 (:743-754): coefficients
+ * in the row-skipping layout of exp_order ((exp_order + 1)^2 / 4 pairs per
+ * item).  As the reference, the expansion is read as the row-skipping span of
+ * order min(exp_order, grid_order), whose rows have the parity of that order;
+ * the rows of the other parity contribute nothing. */
+int zest_gpu_st_backward_rows(zest_gpu_context* ctx, int sh_norm, int sh_phase, int layout,
+                              size_t exp_order, size_t grid_order, size_t batch,
+                              const double* coeffs, double* grids, int mem);
+
+/* ---- real <-> complex expansions (in place) ----
+ * to_complex_expansion (to_complex = 1) / to_real_expansion (0) of
+ *   SH expansions, real_sh_expansion.hpp:345-436 (kind ZEST_EXPANSION_SH);
+ *   Zernike expansions, zernike_expansion.hpp:484-634 (ZEST_EXPANSION_ZERNIKE);
+ *   per-n Zernike SH spans, zernike_expansion.hpp:636-775
+ *   (ZEST_EXPANSION_ZERNIKE_ROW; no Zernike normalisation change).
+ * The coefficients of `batch` expansions of `order` are rescaled from the
+ * source conventions (src_*) to the destination ones (dst_*): m = 0 pairs by
+ * st::conversion_const (times zt::conversion_factor(n) when the Zernike
+ * normalisation changes), m > 0 pairs (a, b) to (f a, -f b) with
+ * f = conversion_const / sqrt(2) (to complex) or conversion_const sqrt(2) (to
+ * real), negated for odd m when the phase convention changes.  Each factor is
+ * computed as the reference computes it, so the results are bit-identical. */
+int zest_gpu_convert_expansion(zest_gpu_context* ctx, int kind, size_t order, size_t batch, double* coeffs,
+                               int src_zernike_norm, int src_sh_norm, int src_sh_phase,
+                               int dst_zernike_norm, int dst_sh_norm, int dst_sh_phase,
+                               int to_complex, int mem);
+
 /* ---- rotations (in place) ----
  * Rotor::rotate(real Zernike expansion, WignerdPiHalfCollection, euler, type)
  *   rotor.hpp:214-243; (real SH expansion) rotor.hpp:125-141.
@@ -146,6 +180,12 @@ int zest_gpu_zt_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
                        double* coeffs, const double* euler, int rotation_type, int mem);
 int zest_gpu_st_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
                        double* coeffs, const double* euler, int rotation_type, int mem);
+/* Rotor::rotate of a row-skipping (single-parity) SH expansion, rotor.hpp:165-193:
+ * a zt::ZernikeSHSpan of `order` (the n = order - 1 row of a Zernike
+ * expansion: rows l = (order - 1) mod 2, + 2, .., < order, pair
+ * floor(l^2/4) + m, (order + 1)^2 / 4 pairs per item), l = 0 included. */
+int zest_gpu_rows_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
+                         double* coeffs, const double* euler, int rotation_type, int mem);
 /* Rotor::polar_rotate, rotor.hpp:316-378 (one angle per batch item). */
 int zest_gpu_zt_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch,
                              double* coeffs, const double* angles, int rotation_type, int mem);
@@ -352,6 +392,10 @@ int zest_gpu_gl_nodes_weights(size_t n, int packed, double* nodes, double* weigh
  * out[idx(l,m) * nz + i]. */
 int zest_gpu_plm_table(zest_gpu_context* ctx, size_t order, int sh_norm, int sh_phase,
                        size_t nz, const double* z, double* out, int mem);
+/* st::PlmRecursion::plm_complex(span z, PlmVecSpan), plm_recursion.hpp:133-139:
+ * the same table without the sqrt(2) of the real basis for m > 0. */
+int zest_gpu_plm_complex_table(zest_gpu_context* ctx, size_t order, int sh_norm, int sh_phase,
+                               size_t nz, const double* z, double* out, int mem);
 /* zt::RadialZernikeRecursion::zernike(span r, RadialZernikeVecSpan),
  * radial_zernike_recursion.hpp:152-288; out[(floor((n+1)^2/4) + l/2) * nr + k]. */
 int zest_gpu_radial_table(zest_gpu_context* ctx, size_t order, int zernike_norm,

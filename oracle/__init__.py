@@ -344,6 +344,25 @@ class Reference(_Lib):
     def _st_polar(self, sn, sp, L, c, angle, rtype):
         self._f("st_polar_rotate", [_c_int, _c_int, _c_sz, _p_dbl, _c_dbl, _c_int])(sn, sp, L, _ptr(c), angle, rtype)
 
+    def rows_rotate(self, coeffs, L, euler, rtype=0, sn=0, sp=0):
+        c = np.array(coeffs, dtype=np.float64, copy=True, order="C")
+        e = np.ascontiguousarray(euler, dtype=np.float64)
+        self._f("rows_rotate", [_c_int, _c_int, _c_sz, _p_dbl, _p_dbl, _c_int])(sn, sp, L, _ptr(c), _ptr(e), rtype)
+        return c
+
+    def st_backward_rows(self, coeffs, Le, Lg=None, sn=0, sp=0, latlon=False):
+        Lg = Le if Lg is None else Lg
+        c = np.ascontiguousarray(coeffs, dtype=np.float64)
+        out = np.zeros(st_grid_shape(Lg, latlon))
+        self._f("st_backward_rows", [_c_int, _c_int, _c_int, _c_sz, _c_sz, _p_dbl, _p_dbl])(
+            sn, sp, int(latlon), Le, Lg, _ptr(c), _ptr(out))
+        return out
+
+    def convert(self, coeffs, kind, L, src, dst, to_complex):
+        c = np.array(coeffs, dtype=np.float64, copy=True, order="C")
+        self._f("convert", [_c_int, _c_sz, _p_dbl] + [_c_int] * 7)(kind, L, _ptr(c), *src, *dst, int(to_complex))
+        return c
+
     def zt_grid_points(self, L: int):
         lon = np.zeros(zt_grid_shape(L)[0])
         colat = np.zeros(zt_grid_shape(L)[1])

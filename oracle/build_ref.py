@@ -43,6 +43,19 @@ REF_SOURCES = [
     "grid_evaluator.cpp",
 ]
 
+# The reference's own test programs for the transform and rotation path.
+# They are staged beside the sources (never committed) and compiled, unchanged,
+# against this project's drop-in headers by tests/test_reference_tests.py.
+REF_TESTS = [
+    "test_zernike_glq_transformer.cpp",
+    "test_sh_glq_transformer.cpp",
+    "test_rotor.cpp",
+    "test_plm_recursion.cpp",
+    "test_radial_zernike_recursion.cpp",
+    "test_gauss_legendre.cpp",
+]
+TEST_STAGE = os.path.join(REF_OUT, "tests")
+
 LIB = os.path.join(REF_OUT, "libzest_ref.so")
 
 
@@ -60,6 +73,11 @@ def _stage(checkout: str | None) -> str | None:
             shutil.copy2(os.path.join(inc, name), os.path.join(STAGE, "include", name))
     for name in REF_SOURCES:
         shutil.copy2(os.path.join(src, name), os.path.join(STAGE, name))
+    tests = os.path.join(checkout, "tests")
+    os.makedirs(TEST_STAGE, exist_ok=True)
+    for name in REF_TESTS:
+        if os.path.exists(os.path.join(tests, name)):
+            shutil.copy2(os.path.join(tests, name), os.path.join(TEST_STAGE, name))
     return STAGE
 
 

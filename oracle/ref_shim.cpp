@@ -18,6 +18,7 @@
 #include <array>
 #include <barrier>
 #include <chrono>
+#include <complex>
 #include <memory>
 #include <utility>
 #include <cstddef>
@@ -210,6 +211,71 @@ int ref_zt_rotate(int zn, int sn, int sp, std::size_t order, double* coeffs, con
         zest::zt::RealZernikeSpan<std::array<double, 2>, Z, N, P> e(
             reinterpret_cast<std::array<double, 2>*>(coeffs), order);
         rot.rotate(e, w, std::array<double, 3>{euler[0], euler[1], euler[2]}, rot_type(type));
+    });
+}
+
+// Rotor::rotate of a per-n Zernike SH span (row-skipping layout, rotor.hpp:165-193).
+int ref_rows_rotate(int sn, int sp, std::size_t order, double* coeffs, const double* euler, int type) {
+    return dispatch_st(sn, sp, [&]<SHNorm N, SHPhase P>() {
+        using Span = zest::zt::ZernikeSHSpan<std::array<double, 2>,
+                                             zest::RowSkippingTriangleLayout<zest::IndexingMode::nonnegative>,
+                                             ZernikeNorm::normed, N, P>;
+        zest::WignerdPiHalfCollection w(order);
+        zest::Rotor rot(order);
+        Span e(reinterpret_cast<std::array<double, 2>*>(coeffs), order);
+        rot.rotate(e, w, std::array<double, 3>{euler[0], euler[1], euler[2]}, rot_type(type));
+    });
+}
+
+// st::GLQTransformer::backward_transform of a per-n Zernike SH span
+// (sh_glq_transformer.hpp:680-700).
+int ref_st_backward_rows(int sn, int sp, int latlon, std::size_t exp_order, std::size_t grid_order,
+                         const double* coeffs, double* grid) {
+    return dispatch_st(sn, sp, [&]<SHNorm N, SHPhase P>() {
+        using Span = zest::zt::ZernikeSHSpan<const std::array<double, 2>,
+                                             zest::RowSkippingTriangleLayout<zest::IndexingMode::nonnegative>,
+                                             ZernikeNorm::normed, N, P>;
+        Span e(reinterpret_cast<const std::array<double, 2>*>(coeffs), exp_order);
+        auto run = [&]<typename Layout>() {
+            zest::st::GLQTransformer<N, P, Layout> tr(grid_order);
+            zest::st::SphereGLQGridSpan<double, Layout> g(grid, grid_order);
+            tr.backward_transform(e, g);
+        };
+        if (latlon) run.template operator()<StLatLon>();
+        else run.template operator()<StLonLat>();
+    });
+}
+
+// to_complex_expansion (to_complex = 1) / to_real_expansion (0) of a Zernike
+// (kind 0), SH (kind 1) or per-n Zernike SH span (kind 2) from the source to
+// the destination conventions, in place (zernike_expansion.hpp:484-775,
+// real_sh_expansion.hpp:345-436).
+int ref_convert(int kind, std::size_t order, double* coeffs, int szn, int ssn, int ssp, int dzn, int dsn, int dsp,
+                int to_complex) {
+    using Row = zest::RowSkippingTriangleLayout<zest::IndexingMode::nonnegative>;
+    return dispatch_zt(szn, ssn, ssp, [&]<ZernikeNorm SZ, SHNorm SN, SHPhase SP>() {
+        dispatch_zt(dzn, dsn, dsp, [&]<ZernikeNorm DZ, SHNorm DN, SHPhase DP>() {
+            auto* a = reinterpret_cast<std::array<double, 2>*>(coeffs);
+            auto* c = reinterpret_cast<std::complex<double>*>(coeffs);
+            if (kind == 0) {
+                if (to_complex)
+                    zest::zt::to_complex_expansion<DZ, DN, DP>(zest::zt::RealZernikeSpan<std::array<double, 2>, SZ, SN, SP>(a, order));
+                else
+                    zest::zt::to_real_expansion<DZ, DN, DP>(zest::zt::RealZernikeSpan<std::complex<double>, SZ, SN, SP>(c, order));
+            } else if (kind == 1) {
+                if (to_complex)
+                    zest::st::to_complex_expansion<DN, DP>(zest::st::RealSHSpan<std::array<double, 2>, SN, SP>(a, order));
+                else
+                    zest::st::to_real_expansion<DN, DP>(zest::st::RealSHSpan<std::complex<double>, SN, SP>(c, order));
+            } else {
+                if (to_complex)
+                    zest::zt::to_complex_expansion<DN, DP>(
+                        zest::zt::ZernikeSHSpan<std::array<double, 2>, Row, SZ, SN, SP>(a, order));
+                else
+                    zest::zt::to_real_expansion<DN, DP>(
+                        zest::zt::ZernikeSHSpan<std::complex<double>, Row, SZ, SN, SP>(c, order));
+            }
+        });
     });
 }
 

@@ -1,0 +1,69 @@
+"""The reference's own test programs for the transform and rotation path
+(tests/test_zernike_glq_transformer.cpp, tests/test_sh_glq_transformer.cpp,
+tests/test_rotor.cpp, and for the tables tests/test_plm_recursion.cpp,
+tests/test_radial_zernike_recursion.cpp, tests/test_gauss_legendre.cpp),
+compiled unchanged against this project's drop-in
+headers (include/zest) and linked to libzest_gb300.so, so that every
+transform and rotation they check runs through the C-ABI on the GPU.
+
+oracle/build_ref.py stages the reference's test sources beside its library
+sources under oracle/_ref/tests (git-ignored); where they are absent, these
+tests skip.  The programs are built with their asserts live (-UNDEBUG).  On
+the CPU this file only builds them (the drop-in API must compile and link);
+on the GPU it runs each one in the FP64 form and, with ZEST_GPU_PRECISION=split
+(every context then starts in the split-precision form), on the tensor cores."""
+import concurrent.futures as cf
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+STAGE = os.path.join(ROOT, "oracle", "_ref", "tests")
+OUT = os.path.join(STAGE, "_build")
+NAMES = ["test_zernike_glq_transformer", "test_sh_glq_transformer", "test_rotor", "test_plm_recursion",
+         "test_radial_zernike_recursion", "test_gauss_legendre"]
+
+
+def _sources():
+    if not all(os.path.exists(os.path.join(STAGE, n + ".cpp")) for n in NAMES):
+        pytest.skip("the reference's test sources are not staged (oracle/build_ref.py --reference DIR)")
+    return [os.path.join(STAGE, n + ".cpp") for n in NAMES]
+
+
+def _compile(src: str, lib: str) -> str:
+    exe = os.path.join(OUT, os.path.basename(src)[:-4])
+    libdir = os.path.dirname(lib)
+    cmd = ["g++", "-std=c++20", "-O2", "-UNDEBUG", "-w", "-I", os.path.join(ROOT, "include", "zest"),
+           "-I", os.path.join(ROOT, "include"), src, "-o", exe, "-L", libdir, "-lzest_gb300",
+           f"-Wl,-rpath,{libdir}"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise AssertionError(f"{os.path.basename(src)} does not build against include/zest:\n{res.stderr[-4000:]}")
+    return exe
+
+
+@pytest.fixture(scope="module")
+def programs():
+    srcs = _sources()
+    from zest_gb300 import build
+    lib = build.build()
+    os.makedirs(OUT, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
+        exes = list(ex.map(lambda s: _compile(s, lib), srcs))
+    return dict(zip(NAMES, exes))
+
+
+def test_reference_tests_build_against_drop_in(programs):
+    for name, exe in programs.items():
+        assert os.access(exe, os.X_OK), name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+@pytest.mark.parametrize("name", NAMES)
+def test_reference_test_program_passes(programs, name, precision):
+    env = dict(os.environ, ZEST_GPU_PRECISION=precision)
+    res = subprocess.run([programs[name]], capture_output=True, text=True, env=env, timeout=600)
+    assert res.returncode == 0, (f"{name} ({precision}) exited {res.returncode}\n"
+                                 f"stdout:\n{res.stdout[-3000:]}\nstderr:\n{res.stderr[-3000:]}")

@@ -26,6 +26,7 @@ ZERNIKE_NORMED, ZERNIKE_UNNORMED = 0, 1
 SH_GEO, SH_QM = 0, 1
 SH_PHASE_NONE, SH_PHASE_CS = 0, 1
 ROTATION_OBJECT, ROTATION_COORDINATE = 0, 1
+EXPANSION_ZERNIKE, EXPANSION_SH, EXPANSION_ZERNIKE_ROW = 0, 1, 2
 LAYOUT_LONLAT, LAYOUT_LATLON = 0, 1
 PRECISION_FP64, PRECISION_SPLIT = 0, 1
 MEM_DEVICE, MEM_HOST = 0, 1
@@ -114,6 +115,10 @@ _SIGNATURES = {
     "zest_gpu_st_power_spectrum": [_vp, _i, _sz, _sz, _vp, _vp, _i],
     "zest_gpu_st_cross_power_spectrum": [_vp, _i, _sz, _sz, _vp, _vp, _sz, _vp, _i],
     "zest_gpu_zt_power_spectrum": [_vp, _i, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_rows_rotate": [_vp, _sz, _sz, _vp, _vp, _i, _i],
+    "zest_gpu_st_backward_rows": [_vp, _i, _i, _i, _sz, _sz, _sz, _vp, _vp, _i],
+    "zest_gpu_convert_expansion": [_vp, _i, _sz, _sz, _vp, _i, _i, _i, _i, _i, _i, _i, _i],
+    "zest_gpu_plm_complex_table": [_vp, _sz, _i, _i, _sz, _vp, _vp, _i],
 }
 _SIZE_FUNCS = {
     "zest_gpu_zt_grid_size": [_sz],
@@ -173,6 +178,11 @@ def st_grid_shape(order: int, layout: int = LAYOUT_LONLAT):
     if layout == LAYOUT_LATLON:
         return (order, pad8(2 * order - 1 if order else 0))
     return (2 * order - 1 if order else 0, pad8(order))
+
+
+def rows_coeff_size(order: int) -> int:
+    """Pairs of a row-skipping SH expansion of `order` (zt::ZernikeSHSpan)."""
+    return ((order + 1) * (order + 1)) // 4
 
 
 def st_coeff_size(order: int) -> int:
@@ -330,6 +340,36 @@ class Context:
         _check(self.lib.zest_gpu_st_polar_rotate(self._h, order, batch, cp, ap, rotation_type, cm))
         return coeffs
 
+    def rows_rotate(self, coeffs, order: int, euler, batch: int = 1, rotation_type: int = ROTATION_OBJECT):
+        """Rotor::rotate of row-skipping (single-parity) SH expansions of
+        `order`: the coefficients of radial index n = order - 1 of a Zernike
+        expansion (zt::ZernikeSHSpan)."""
+        cp, cm = _ptr(coeffs, 2 * rows_coeff_size(order) * batch)
+        ep, em = _ptr(euler, 3 * batch)
+        _check(self.lib.zest_gpu_rows_rotate(self._h, order, batch, cp, ep, rotation_type, cm))
+        return coeffs
+
+    def st_backward_rows(self, coeffs, exp_order: int, grid_order: Optional[int] = None, batch: int = 1,
+                         conv=ST_GEO, layout: int = LAYOUT_LONLAT, out=None):
+        """SH backward transform of row-skipping (single-parity) expansions."""
+        grid_order = exp_order if grid_order is None else grid_order
+        gsz = int(np.prod(st_grid_shape(grid_order, layout))) * batch
+        cp, cm = _ptr(coeffs, 2 * rows_coeff_size(exp_order) * batch)
+        if out is None:
+            out = self._alloc_like(coeffs, gsz)
+        gp, gm = _ptr(out, gsz)
+        _check(self.lib.zest_gpu_st_backward_rows(self._h, *conv, layout, exp_order, grid_order, batch, cp, gp, cm))
+        return out
+
+    def convert_expansion(self, coeffs, kind: int, order: int, src, dst, to_complex: bool, batch: int = 1):
+        """to_complex_expansion / to_real_expansion in place: `src` and `dst`
+        are (zernike_norm, sh_norm, sh_phase) triples."""
+        n = {EXPANSION_ZERNIKE: zt_coeff_size, EXPANSION_SH: st_coeff_size,
+             EXPANSION_ZERNIKE_ROW: rows_coeff_size}[kind](order)
+        cp, cm = _ptr(coeffs, 2 * n * batch)
+        _check(self.lib.zest_gpu_convert_expansion(self._h, kind, order, batch, cp, *src, *dst, int(to_complex), cm))
+        return coeffs
+
     def set_autotune(self, enable: bool = True):
         _check(self.lib.zest_gpu_set_autotune(self._h, int(enable)))
 
@@ -442,11 +482,12 @@ class Context:
         return C
 
     # ---- tables ----
-    def plm_table(self, order: int, sh_norm: int, sh_phase: int, z: np.ndarray) -> np.ndarray:
+    def plm_table(self, order: int, sh_norm: int, sh_phase: int, z: np.ndarray, complex_basis: bool = False
+                  ) -> np.ndarray:
         z = np.ascontiguousarray(z, dtype=np.float64)
         out = np.zeros((order * (order + 1) // 2, z.size))
-        _check(self.lib.zest_gpu_plm_table(self._h, order, sh_norm, sh_phase, z.size,
-                                           _vp(z.ctypes.data), _vp(out.ctypes.data), MEM_HOST))
+        fn = self.lib.zest_gpu_plm_complex_table if complex_basis else self.lib.zest_gpu_plm_table
+        _check(fn(self._h, order, sh_norm, sh_phase, z.size, _vp(z.ctypes.data), _vp(out.ctypes.data), MEM_HOST))
         return out
 
     def radial_table(self, order: int, zernike_norm: int, r: np.ndarray) -> np.ndarray:

@@ -75,7 +75,9 @@ void st_tile_shape(int& bm, int& bn);
 
 // ---- rotations ------------------------------------------------------------------
 // Rotor::rotate on a batch of real expansions (in place).  kind 0 = Zernike,
-// 1 = SH; vec_list holds the nvec rotated (n, l) vectors of one expansion.
+// 1 = SH, 2 = SH rows of one parity in the row-skipping layout (a per-n
+// Zernike SH span); vec_list holds the nvec rotated (n, l) vectors of one
+// expansion.
 // phase_scratch: 6 * L * batch doubles.
 int launch_rotate_vectors(cudaStream_t s, int kind, int L, int batch, double* coeffs, long long cstride,
                           const int2* vec_list, int nvec, const double* wigner, const double* euler, int type,
@@ -109,5 +111,26 @@ int launch_st_gram(cudaStream_t s, const double* in, double* out, int L, int bat
 // out[i] = in[i] * w[i % slab] (divide = 0) or in[i] / w[i % slab] (divide = 1) over n values.
 int launch_grid_weights(cudaStream_t s, const double* in, double* out, long long n, const double* w, long long slab,
                         int divide);
+
+// ---- coefficient layouts (layouts.cu) ------------------------------------------------
+enum { CONVERT_ZERNIKE = 0, CONVERT_SH = 1, CONVERT_ROWS = 2 };
+// In-place real <-> complex conversion of `pairs` coefficient pairs per item:
+// m = 0 pairs times shnorm, m > 0 pairs (x, y) -> (f x, -f y) with f = norm,
+// negated for odd m when phase_change; zconv = +1 / -1 multiplies both by
+// sqrt(2n + 3) / 1 / sqrt(2n + 3) (Zernike normalisation change), 0 not.
+// parity: the row parity of a row-skipping (CONVERT_ROWS) expansion.
+struct ConvertParams {
+    int kind = 0;
+    int parity = 0;
+    int zconv = 0;
+    int phase_change = 0;
+    long long pairs = 0;
+    double shnorm = 1.0;
+    double norm = 1.0;
+};
+int launch_convert(cudaStream_t s, const ConvertParams& P, int batch, double* coeffs);
+// Row-skipping SH expansions of order Lm (src_pairs pairs apart) -> triangle
+// expansions of order Lm, the rows of the other parity zero.
+int launch_rows_to_triangle(cudaStream_t s, int Lm, long long src_pairs, int batch, const double* src, double* dst);
 
 }  // namespace zgpu

@@ -77,6 +77,12 @@ __device__ __forceinline__ double2 xrot(const double2* v, const double* __restri
     return make_double2(2.0 * re, 2.0 * im);
 }
 
+// First coefficient of vector (n, l): Zernike tetrahedral layout (kind 0),
+// SH triangle (kind 1) or row-skipping triangle, floor(l^2 / 4) (kind 2).
+__device__ __forceinline__ long long vec_base(int kind, int n, int l) {
+    return kind == 0 ? zidx(n, l, 0) : kind == 1 ? tri_idx(l, 0) : ((long long)l * l) >> 2;
+}
+
 // vec_list[v] = {n, l} (Zernike) or {l, l} (SH); vectors of item b are v + b*nvec
 __global__ void rotate_kernel(int L, int nvec, int batch, double* __restrict__ coeffs, long long cstride, int kind,
                               const int2* __restrict__ vec_list, const double* __restrict__ wig,
@@ -89,7 +95,7 @@ __global__ void rotate_kernel(int L, int nvec, int batch, double* __restrict__ c
     const int b = int(vid / nvec);
     const int2 nl = vec_list[vid - (long long)b * nvec];
     const int n = nl.x, l = nl.y;
-    double* c = coeffs + b * cstride + 2 * (kind == 0 ? zidx(n, l, 0) : tri_idx(l, 0));
+    double* c = coeffs + b * cstride + 2 * vec_base(kind, n, l);
     const double2* pa = ph + ((long long)b * 3 + 0) * L;
     const double2* pb = ph + ((long long)b * 3 + 1) * L;
     const double2* pg = ph + ((long long)b * 3 + 2) * L;
@@ -132,7 +138,7 @@ __global__ void rotate_ragged_kernel(int Lmax, long long nwork, double* __restri
     if (wid >= nwork) return;
     const int4 w = work[wid];
     const int b = w.x, n = w.y, l = w.z;
-    double* c = coeffs + coff[b] + 2 * (kind == 0 ? zidx(n, l, 0) : tri_idx(l, 0));
+    double* c = coeffs + coff[b] + 2 * vec_base(kind, n, l);
     const double2* pa = ph + ((long long)b * 3 + 0) * Lmax;
     const double2* pb = ph + ((long long)b * 3 + 1) * Lmax;
     const double2* pg = ph + ((long long)b * 3 + 2) * Lmax;
@@ -179,7 +185,7 @@ __global__ void rotate_grad_kernel(int L, int nvec, int batch, const double* __r
     const int b = int(vid / nvec);
     const int2 nl = vec_list[vid - (long long)b * nvec];
     const int n = nl.x, l = nl.y;
-    const long long off = b * cstride + 2 * (kind == 0 ? zidx(n, l, 0) : tri_idx(l, 0));
+    const long long off = b * cstride + 2 * vec_base(kind, n, l);
     const double* c = x + off;
     const double* yb = ybar + off;
     const double2* pa = ph + ((long long)b * 3 + 0) * L;
@@ -294,7 +300,7 @@ __global__ void polar_kernel(int L, int nvec, int batch, double* __restrict__ co
     const int b = int(vid / nvec);
     const int2 nl = vec_list[vid - (long long)b * nvec];
     const int n = nl.x, l = nl.y;
-    double* c = coeffs + b * cstride + 2 * (kind == 0 ? zidx(n, l, 0) : tri_idx(l, 0));
+    double* c = coeffs + b * cstride + 2 * vec_base(kind, n, l);
     const double ang = type == 0 ? angles[b] : -angles[b];
     const double isq2 = 1.0 / 1.41421356237309504880168872420969808;
     const double sq2 = 1.41421356237309504880168872420969808;

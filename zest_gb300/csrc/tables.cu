@@ -169,13 +169,16 @@ __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, 
 __device__ __forceinline__ double dv(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ double sq(int l) { return __dsqrt_rn(double(l)); }
 
+// cnorm: sqrt(2) for the real basis (plm_real), 1 for plm_complex
+// (plm_recursion.hpp:96-139); it enters the recursion where the reference's
+// complex_norm does (the m > 0 start value).
 template <class Writer>
-__global__ void plm_kernel(int L, int sh_norm, int sh_phase, int nz, const double* __restrict__ z, Writer w) {
+__global__ void plm_kernel(int L, int sh_norm, int sh_phase, int nz, const double* __restrict__ z, Writer w,
+                           double cnorm = 1.41421356237309504880168872420969808) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int m = blockIdx.y;
     if (i >= nz || m >= L) return;
     const double inv_sqrt_4pi = 0.28209479177387814347403972578038629;
-    const double sqrt2 = 1.41421356237309504880168872420969808;
     const double uc = 1.0e-280;
     const double phase = sh_phase ? 1.0 : -1.0;
     const double zi = z[i];
@@ -198,7 +201,7 @@ __global__ void plm_kernel(int L, int sh_norm, int sh_phase, int nz, const doubl
         return;
     }
     const double u = __dsqrt_rn(mul(sub(1.0, zi), 1.0 + zi));
-    double pmm = sh_norm ? mul(mul(uc, sqrt2), inv_sqrt_4pi) : mul(uc, sqrt2);
+    double pmm = sh_norm ? mul(mul(uc, cnorm), inv_sqrt_4pi) : mul(uc, cnorm);
     double us = dv(1.0, uc);
     const int mlast = (m < L - 1) ? m : L - 2;
     for (int k = 1; k <= mlast; ++k) {
@@ -394,10 +397,12 @@ __global__ void wignerd_kernel(int L, double* __restrict__ d) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-int launch_plm_ref(cudaStream_t s, int L, int sh_norm, int sh_phase, int nz, const double* z, double* out) {
+int launch_plm_ref(cudaStream_t s, int L, int sh_norm, int sh_phase, int nz, const double* z, double* out,
+                   bool complex_basis) {
     if (L <= 0 || nz <= 0) return ZEST_GPU_OK;
     dim3 grid((nz + 127) / 128, L);
-    plm_kernel<<<grid, 128, 0, s>>>(L, sh_norm, sh_phase, nz, z, PlmRefWriter{out, nz});
+    const double cnorm = complex_basis ? 1.0 : 1.41421356237309504880168872420969808;
+    plm_kernel<<<grid, 128, 0, s>>>(L, sh_norm, sh_phase, nz, z, PlmRefWriter{out, nz}, cnorm);
     return launch_check("plm_kernel");
 }
 

@@ -14,7 +14,9 @@ void gl_nodes_weights(long n, bool packed, double* nodes, double* weights);
 void gl_colatitudes(long n, double* theta);
 
 // P_lm(z_i) in the reference vector layout out[idx(l,m) * nz + i].
-int launch_plm_ref(cudaStream_t s, int L, int sh_norm, int sh_phase, int nz, const double* z, double* out);
+// complex_basis: P_lm of PlmRecursion::plm_complex (no sqrt(2) for m > 0)
+int launch_plm_ref(cudaStream_t s, int L, int sh_norm, int sh_phase, int nz, const double* z, double* out,
+                   bool complex_basis = false);
 // P_lm(z_i) * scale[i] * (m > 0 ? mscale : 1) in the folded GEMM layout:
 // row off[2m + ((l-m)&1)] + ((l-m)>>1), column i (ld columns); rows l >= Lrows skipped.
 int launch_plm_gemm(cudaStream_t s, int L, int Lrows, int sh_norm, int sh_phase, int nz, const double* z,

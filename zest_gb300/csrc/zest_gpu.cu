@@ -7,6 +7,7 @@
 // once per (order, conventions) and cached, like the reference's resize().
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -536,6 +537,12 @@ static int get_wigner(zest_gpu_context* ctx, int L, const double** out) {
     return ZEST_GPU_OK;
 }
 
+// coefficient pairs of one expansion of order L: Zernike, SH triangle, or the
+// row-skipping triangle of one parity ((L + 1)^2 / 4, include/layout.hpp:356-362)
+static long long coeff_pairs(int kind, long long L) {
+    return kind == 0 ? zsize(L) : kind == 1 ? tri_size(L) : ((L + 1) * (L + 1)) >> 2;
+}
+
 // rotated (n, l) vectors of one expansion, grouped by l
 static int get_vectors(zest_gpu_context* ctx, int kind, int L, const int2** out, int* nvec) {
     auto key = std::make_tuple(kind, L);
@@ -545,6 +552,8 @@ static int get_vectors(zest_gpu_context* ctx, int kind, int L, const int2** out,
         for (int l = 0; l < L; ++l) {
             if (kind == 0) {
                 for (int n = (l == 0 ? 2 : l); n < L; n += 2) v.push_back(make_int2(n, l));
+            } else if (kind == 2) {  // rows l = (L - 1) mod 2, + 2, .. < L; l = 0 too, as the Zernike n-rows
+                if ((l & 1) == ((L - 1) & 1)) v.push_back(make_int2(L - 1, l));
             } else if (l >= 1) {
                 v.push_back(make_int2(l, l));
             }
@@ -566,7 +575,7 @@ int rotate_dev(zest_gpu_context* ctx, int kind, int L, int batch, double* coeffs
     int nvec;
     ZG_TRY(get_vectors(ctx, kind, L, &vl, &nvec));
     ZG_TRY(ctx->phase.ensure((size_t)batch * 6 * L * sizeof(double)));
-    const long long cstride = kind == 0 ? 2 * zsize(L) : 2 * tri_size(L);
+    const long long cstride = 2 * coeff_pairs(kind, L);
     StageScope sc(ctx, ST_ROTATE);
     return launch_rotate_vectors(ctx->stream, kind, L, batch, coeffs, cstride, vl, nvec, wig, euler, type,
                                  ctx->phase.as<double>());
@@ -577,7 +586,7 @@ int polar_dev(zest_gpu_context* ctx, int kind, int L, int batch, double* coeffs,
     const int2* vl;
     int nvec;
     ZG_TRY(get_vectors(ctx, kind, L, &vl, &nvec));
-    const long long cstride = kind == 0 ? 2 * zsize(L) : 2 * tri_size(L);
+    const long long cstride = 2 * coeff_pairs(kind, L);
     StageScope sc(ctx, ST_ROTATE);
     return launch_polar_vectors(ctx->stream, kind, L, batch, coeffs, cstride, vl, nvec, angles, type);
 }
@@ -1006,6 +1015,20 @@ int zest_gpu_ctx_create(zest_gpu_context** out, int device, void* stream) {
     auto* ctx = new zest_gpu_context();
     ctx->device = device;
     ctx->stream = static_cast<cudaStream_t>(stream);
+    // ZEST_GPU_PRECISION=split starts every new context in the split-precision
+    // form (six slices), so code written against the reference's classes,
+    // which have no precision setting, runs on the tensor cores unchanged.
+    const char* want = std::getenv("ZEST_GPU_PRECISION");
+    if (want && std::string(want) == "split") {
+        const int st = zest_gpu_set_precision(ctx, ZEST_PRECISION_SPLIT, 6);
+        if (st != ZEST_GPU_OK) {
+            delete ctx;
+            return st;
+        }
+    } else if (want && *want && std::string(want) != "fp64") {
+        delete ctx;
+        return fail(ZEST_GPU_ERR_INVALID, std::string("ZEST_GPU_PRECISION must be split or fp64, not ") + want);
+    }
     *out = ctx;
     return ZEST_GPU_OK;
 }
@@ -1183,13 +1206,78 @@ int zest_gpu_st_backward(zest_gpu_context* ctx, int sn, int sp, int layout, size
     });
 }
 
+// Row-skipping (single-parity) SH expansions of order exp_order, truncated to
+// min(exp_order, grid_order) as the reference truncates its span (the rows
+// then take the parity of the truncated order), expanded to the triangle
+// layout and backward-transformed.
+int zest_gpu_st_backward_rows(zest_gpu_context* ctx, int sn, int sp, int layout, size_t exp_order,
+                              size_t grid_order, size_t batch, const double* coeffs, double* grids, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn) || !valid01(sp) || !valid01(layout)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention/layout");
+    if (grid_order > kMaxOrder || exp_order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    const long long rpairs = coeff_pairs(2, (long long)exp_order);
+    const size_t gn = batch * zest_gpu_st_grid_size(grid_order, layout), cn = batch * 2 * size_t(rpairs);
+    if ((gn && !grids) || (cn && !coeffs)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    const int Lm = int(std::min(exp_order, grid_order));
+    return with_staging(ctx, mem, coeffs, cn, grids, gn, [&](const double* in, double* out) {
+        ZG_TRY(ctx->adj0.ensure((size_t)batch * 2 * tri_size(Lm) * sizeof(double) + 16));
+        ZG_TRY(launch_rows_to_triangle(ctx->stream, Lm, rpairs, int(batch), in, ctx->adj0.as<double>()));
+        return st_backward_dev(ctx, sn, sp, layout, Lm, int(grid_order), int(batch), ctx->adj0.as<double>(), out);
+    });
+}
+
+// The constants of the reference's conversions, computed as it computes
+// them: st::conversion_const (include/sh_conventions.hpp:70-96) and the
+// complex factor 1/sqrt(2) or sqrt(2) (include/real_sh_expansion.hpp:349, 400).
+static double sh_conversion_const(int from, int to) {
+    if (from == to) return 1.0;
+    const double inv_sqrt_4pi = 0.5 * 0.564189583547756286948079451560772586;  // 0.5 / sqrt(pi)
+    const double sqrt_4pi = 1.0 / inv_sqrt_4pi;
+    double norm = from == ZEST_SH_QM ? 1.0 : sqrt_4pi;
+    norm *= to == ZEST_SH_QM ? 1.0 : inv_sqrt_4pi;
+    return norm;
+}
+
+int zest_gpu_convert_expansion(zest_gpu_context* ctx, int kind, size_t order, size_t batch, double* coeffs,
+                               int src_zn, int src_sn, int src_sp, int dst_zn, int dst_sn, int dst_sp,
+                               int to_complex, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (kind != ZEST_EXPANSION_ZERNIKE && kind != ZEST_EXPANSION_SH && kind != ZEST_EXPANSION_ZERNIKE_ROW)
+        return fail(ZEST_GPU_ERR_INVALID, "invalid expansion kind");
+    if (!valid01(src_zn) || !valid01(src_sn) || !valid01(src_sp) || !valid01(dst_zn) || !valid01(dst_sn) ||
+        !valid01(dst_sp) || !valid01(to_complex))
+        return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (kind != ZEST_EXPANSION_ZERNIKE && src_zn != dst_zn)
+        return fail(ZEST_GPU_ERR_INVALID, "a Zernike normalisation change needs a whole Zernike expansion");
+    if (order > kMaxOrder) return fail(ZEST_GPU_ERR_INVALID, "order too large");
+    if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
+    ConvertParams P;
+    P.kind = kind == ZEST_EXPANSION_ZERNIKE ? CONVERT_ZERNIKE : kind == ZEST_EXPANSION_SH ? CONVERT_SH : CONVERT_ROWS;
+    P.pairs = coeff_pairs(P.kind, (long long)order);
+    P.parity = order ? int((order - 1) & 1) : 0;
+    P.zconv = src_zn == dst_zn ? 0 : (dst_zn == ZEST_ZERNIKE_NORMED ? -1 : 1);
+    P.phase_change = src_sp != dst_sp;
+    P.shnorm = sh_conversion_const(src_sn, dst_sn);
+    const double sqrt2 = 1.41421356237309504880168872420969808;
+    const double cnorm = to_complex ? 1.0 / sqrt2 : sqrt2;
+    P.norm = P.shnorm * cnorm;
+    const size_t cn = batch * 2 * size_t(P.pairs);
+    if (cn && !coeffs) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, coeffs, cn, coeffs, cn, [&](const double* in, double* out) {
+        if (in != out && cn)
+            ZG_CUDA_TRY(cudaMemcpyAsync(out, in, cn * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        return launch_convert(ctx->stream, P, int(batch), out);
+    });
+}
+
 static int rotate_common(zest_gpu_context* ctx, int kind, size_t order, size_t batch, double* coeffs,
                          const double* angles, int nang, int type, int mem, bool polar) {
     ZG_TRY(check_ctx(ctx));
     if (!valid01(type)) return fail(ZEST_GPU_ERR_INVALID, "invalid rotation type");
     if (order > 2048) return fail(ZEST_GPU_ERR_INVALID, "rotation order too large");
     if (batch > 65535) return fail(ZEST_GPU_ERR_INVALID, "batch too large (max 65535)");
-    const size_t cn = batch * 2 * (kind == 0 ? zest_gpu_zt_coeff_size(order) : zest_gpu_st_coeff_size(order));
+    const size_t cn = batch * 2 * size_t(coeff_pairs(kind, (long long)order));
     const size_t an = batch * nang;
     if ((cn && !coeffs) || (an && !angles)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
     auto run = [&](double* c, const double* a) {
@@ -1216,6 +1304,10 @@ int zest_gpu_zt_rotate(zest_gpu_context* ctx, size_t order, size_t batch, double
 int zest_gpu_st_rotate(zest_gpu_context* ctx, size_t order, size_t batch, double* coeffs, const double* euler,
                        int rotation_type, int mem) {
     return rotate_common(ctx, 1, order, batch, coeffs, euler, 3, rotation_type, mem, false);
+}
+int zest_gpu_rows_rotate(zest_gpu_context* ctx, size_t order, size_t batch, double* coeffs, const double* euler,
+                         int rotation_type, int mem) {
+    return rotate_common(ctx, 2, order, batch, coeffs, euler, 3, rotation_type, mem, false);
 }
 int zest_gpu_zt_polar_rotate(zest_gpu_context* ctx, size_t order, size_t batch, double* coeffs, const double* angles,
                              int rotation_type, int mem) {
@@ -1632,6 +1724,18 @@ int zest_gpu_plm_table(zest_gpu_context* ctx, size_t order, int sn, int sp, size
     if ((nz && !z) || (on && !out)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
     return with_staging(ctx, mem, z, nz, out, on, [&](const double* zi, double* o) {
         return launch_plm_ref(ctx->stream, int(order), sn, sp, int(nz), zi, o);
+    });
+}
+
+int zest_gpu_plm_complex_table(zest_gpu_context* ctx, size_t order, int sn, int sp, size_t nz, const double* z,
+                               double* out, int mem) {
+    ZG_TRY(check_ctx(ctx));
+    if (!valid01(sn) || !valid01(sp)) return fail(ZEST_GPU_ERR_INVALID, "invalid convention");
+    if (order > kMaxOrder || nz > (1u << 20)) return fail(ZEST_GPU_ERR_INVALID, "size too large");
+    const size_t on = (size_t)tri_size((long long)order) * nz;
+    if ((nz && !z) || (on && !out)) return fail(ZEST_GPU_ERR_INVALID, "null data pointer");
+    return with_staging(ctx, mem, z, nz, out, on, [&](const double* zi, double* o) {
+        return launch_plm_ref(ctx->stream, int(order), sn, sp, int(nz), zi, o, true);
     });
 }
 
