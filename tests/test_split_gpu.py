@@ -51,7 +51,8 @@ def rand_zt(rng, L, power=1.5, batch=1):
     return c
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 80, 16), (1, 1, 1), (129, 81, 17), (300, 200, 208), (1000, 37, 256)])
+@pytest.mark.parametrize("M,N,K", [(128, 80, 16), (1, 1, 1), (129, 81, 17), (300, 200, 208), (1000, 37, 256),
+                                   (256, 33, 48), (200, 161, 64)])
 def test_split_gemm_exact_on_integers(split, M, N, K):
     # integers with |x| < 2^20 are represented exactly by 6 slices of 8 bits
     # (the dropped products involve only zero digits), and the level sums are
@@ -124,10 +125,11 @@ def split_model(A, B, S):
 
 @pytest.mark.parametrize("K", [1, 16, 33, 64, 208, 256, 257, 400, 992, 2048])
 def test_split_gemm_matches_integer_model(split, K):
-    # The kernel sums levels 0..3 exactly and levels 4 and up in one shared
-    # FP32 accumulator, whose products weigh at most 2^-28 of level 0: the
-    # kernel must agree with the all-integer model to 1e-13 of the largest
-    # entry, with one K-chunk (K <= 256) and with several (257 up to 2048).
+    # The kernel sums every level in its own FP32 accumulator: levels 0..3
+    # exactly, levels 4 and 5 (2^-32 and 2^-40 of level 0) rounded to
+    # integers once they pass 2^24.  It must agree with the all-integer model
+    # to 1e-13 of the largest entry, with one K-chunk (K <= 256) and with
+    # several (257 up to 2048).
     rng = np.random.default_rng(100 + K)
     A = rng.normal(size=(130, K)) * np.exp(rng.normal(size=(130, 1)))
     B = rng.normal(size=(70, K))
@@ -153,12 +155,13 @@ def test_split_zt_vs_fp64(ctx, L, batch):
     assert relmax(fs, f64) < SPLIT_TOL
 
 
-@pytest.mark.parametrize("spec", ["dft_f=48,leg_f=48,rad_f=48,rad_b=48,leg_b=96,dft_b=48",
-                                  "dft_f=96,leg_f=96,rad_f=96,rad_b=96,leg_b=96,dft_b=96"])
+@pytest.mark.parametrize("spec", ["dft_f=32,leg_f=32,rad_f=32,rad_b=32,leg_b=80,dft_b=32",
+                                  "dft_f=80,leg_f=80,rad_f=80,rad_b=80,leg_b=32,dft_b=80"])
 def test_split_zt_column_tiles(ctx, monkeypatch, spec):
-    # ZEST_GPU_SPLIT_NT picks each stage's column tile (48: two accumulator
-    # sets in TMEM) for contexts created after it is set; every choice must
-    # give the same split-form results as the FP64 form
+    # ZEST_GPU_SPLIT_NT picks each stage's column tile (32: two accumulator
+    # sets in TMEM, one MMA per slice of A; 80: one set, MMAs of up to three
+    # products) for contexts created after it is set; every choice must give
+    # the same split-form results as the FP64 form
     import zest_gb300
     monkeypatch.setenv("ZEST_GPU_SPLIT_NT", spec)
     rng = np.random.default_rng(77)

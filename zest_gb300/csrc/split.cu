@@ -11,30 +11,31 @@
 //   * v is cut into S balanced base-256 digits d_s in [-128, 127] (the
 //     leading one in [-128, 128]), each exact in BF16;
 //   * the products d_s(A) d_t(B) with s + t = level <= S - 1 (21 products at
-//     S = 6) accumulate in FP32 TMEM accumulators.  A product is at most
-//     2^14, so a level with p products is exact while p K 2^14 <= 2^24:
-//     levels 0..3 get their own, exact, accumulators for sums of up to 256
-//     terms.  Levels 4..S-1 weigh <= 2^-32 of level 0 and share one
-//     accumulator: their products read table slices pre-scaled by 2^-8
-//     (exact in BF16).  Longer sums run as K-chunks of at most 256 terms;
-//     every chunk after the first adds its FP64 result through the
-//     accumulating form of the stage's epilogue;
-//   * the epilogue recombines the five accumulators by integer Horner into an
-//     exact int64 T and builds the FP64 result 2^{eA + eB - 8 (S + 1) - 6} T
-//     with integer operations only.
+//     S = 6) accumulate in FP32 TMEM accumulators, one per level.  A product
+//     is at most 2^14, so a level with p products is exact while
+//     p K 2^14 <= 2^24: levels 0..3 are exact for sums of up to 256 terms;
+//     levels 4 and 5 (2^-32 and 2^-40 of level 0) hold integers rounded to
+//     their FP32 spacing once they pass 2^24.  Longer sums run as K-chunks of
+//     at most 256 terms; every chunk after the first adds its FP64 result
+//     through the accumulating form of the stage's epilogue;
+//   * the epilogue recombines the S accumulators by integer Horner into an
+//     int64 T and builds the FP64 result 2^{eA + eB - 8 (S + 1)} T with
+//     integer operations only.
 // Only the tables (P_lm, R_nl, cos/sin) are prepared in FP64.
 //
 // Kernel: warp-specialised, persistent, one CTA per SM.  Warp 0 issues TMA
-// loads (SWIZZLE_32B, one 16-wide K block of all S operand slices and the
-// needed table slices per pipeline stage), warp 1 issues tcgen05.mma
-// (M = 128 operand rows, N = NT = 96, 48 or 16 table rows per tile, five
-// accumulators resident in TMEM, two sets of them where they fit, so that
-// the next tile's MMAs overlap the drain), warps 2..17 read the accumulators back
-// (tcgen05.ld, four warps per TMEM lane quarter), recombine and store
-// through a stage-specific epilogue.  For the SH sums the table is the
-// 128-row operand and the 2 x batch data rows are the columns.  Every wait
-// is bounded (about 2 s); on timeout the kernel records an error code and
-// winds down instead of hanging.
+// loads (SWIZZLE_32B, one 16-wide K block of the S slices of both operands
+// per pipeline stage, the B slices back to back), warp 1 issues tcgen05.mma
+// (M = 128 operand rows; the products of one A slice with consecutive B
+// slices go to consecutive accumulators, so up to 256 / NT of them form one
+// MMA of N = g NT: 9 MMAs per K block at NT = 80), warps 2..17 read the
+// accumulators back (tcgen05.ld, four warps per TMEM lane quarter),
+// recombine and store through a stage-specific epilogue.  Six accumulators
+// of NT = 80 columns fill the 512 TMEM columns; with NT = 32 (or 16) two sets
+// fit, so that the next tile's MMAs overlap the drain.  For the SH sums the
+// table is the 128-row operand and the 2 x batch data rows are the columns.
+// Every wait is bounded (about 2 s); on timeout the kernel records an error
+// code and winds down instead of hanging.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -116,11 +117,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* e
         }
     }
 }
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+// One box of a [slice][row][k] slice array: all S slices of a tile, planes
+// of `rows` rows one after the other in shared memory.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
+                                            int c2) {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
         : "memory");
 }
 __device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
@@ -918,8 +922,6 @@ struct EpiDftBwdSin {
 struct SplitParams {
     const SplitUnit* units;
     int nunits;
-    int a_rows_total[2];  // rows per slice of the two A slice arrays
-    int b_rows_total[2];  // rows per slice of the two B (table) slice arrays
     const int* ea[2];
     const int* eb[2];
     int* err;
@@ -927,58 +929,32 @@ struct SplitParams {
     unsigned long long* dbg;  // optional cycle counters (null in normal use)
 };
 
-// Product schedule of S slices of BITS-bit digits.  Levels d = s + t up to
-// DMAX are kept (DMAX = S with 7-bit digits, S - 1 with 8-bit digits).
-// Levels below MB = 4 have their own exact accumulators; levels MB..DMAX
-// share the last one: a level-(MB + c) product reads table slices pre-scaled
-// by 2^{-BITS c} (exact in BF16), so the shared accumulator holds
-// sum_c acc_{MB+c} 2^{-BITS c} in level-MB units.  (The tensor cores'
-// FP32 accumulation does not round these fractional sums to nearest, so the
-// shared accumulator must weigh little: from level 3 on, 2^-24 of level 0,
-// its error reaches 1e-12 of the result at K = 208; from level 4 on it stays
-// near 1e-15.)  Table slice arrays
-// hold the S unscaled slices followed by the scaled copies (copy c at slice
-// c S).  Stage tiles: copy 0 for t < U, then copy c >= 1 for t in
-// [t0(c), t0(c) + cnt(c)).
-template <int S, int BITS>
+// Product schedule of S slices of 8-bit digits.  The products
+// d_s(A) d_t(B) of level d = s + t <= S - 1 are kept (21 at S = 6) and each
+// level has its own FP32 accumulator in TMEM, so every accumulator holds an
+// integer: a product is at most 2^14, levels 0..3 stay exact (below 2^24)
+// for sums of up to 256 terms, and levels 4 and 5, which may pass 2^24, are
+// rounded to integers of their own weight (2^-32 and 2^-40 of level 0).  No
+// operand needs pre-scaled copies of its slices.
+//
+// The products of one A slice s with the B slices t, t + 1, .. go to the
+// accumulators s + t, s + t + 1, ..: with the B slices of a stage stored one
+// after the other (NT rows each) and the accumulators NT columns apart, up to
+// 256 / NT of them are one MMA of N = g NT (9 MMAs per K block at S = 6,
+// NT = 80, instead of 21 of N = NT).  Each MMA reads its A tile once for g
+// products, which is what keeps the shared-memory reads per MAC low enough
+// for the tensor pipe.
+template <int S>
 struct Sched {
-    static constexpr int DMAX = BITS == 8 ? S - 1 : S;
-    static constexpr int MB = 4;
-    static constexpr int NACC = (DMAX < MB ? DMAX : MB) + 1;
-    static constexpr int NCOPY = DMAX < MB ? 1 : DMAX - MB + 1;
-    static constexpr int U = (DMAX < MB ? DMAX : MB) + 1 < S ? (DMAX < MB ? DMAX : MB) + 1 : S;
-    __host__ __device__ static constexpr int t0(int c) { return MB + c - (S - 1) > 0 ? MB + c - (S - 1) : 0; }
-    __host__ __device__ static constexpr int cnt(int c) { return (MB + c < S - 1 ? MB + c : S - 1) - t0(c) + 1; }
-    __host__ __device__ static constexpr int first(int c) {
-        int j = U;
-        for (int q = 1; q < c; ++q) j += cnt(q);
-        return j;
-    }
-    static constexpr int NB = first(NCOPY);  // B tiles per stage
-    static constexpr int PRODUCTS = (DMAX + 1) * (DMAX + 2) / 2 - (DMAX >= S ? (DMAX - S + 1) * (DMAX - S + 2) : 0);
-    // table slice index of stage tile j
-    __host__ __device__ static constexpr int bslice(int j) {
-        if (j < U) return j;
-        int c = 1, r = j - U;
-        while (r >= cnt(c)) r -= cnt(c++);
-        return c * S + t0(c) + r;
-    }
-    // accumulator and stage tile of the B operand of product (s, t) at level d
-    __host__ __device__ static constexpr int acc(int d) { return d < MB ? d : MB; }
-    __host__ __device__ static constexpr int btile(int d, int t) { return d <= MB ? t : first(d - MB) + t - t0(d - MB); }
+    static constexpr int NACC = S;                      // accumulators: levels 0..S-1
+    static constexpr int NB = S;                        // B tiles per stage: the S slices
+    static constexpr int PRODUCTS = S * (S + 1) / 2;    // slice products per K block
 };
-static_assert(Sched<6, 7>::NB == 16 && Sched<6, 7>::PRODUCTS == 26 && Sched<6, 7>::NACC == 5, "7-bit, 6 slices");
-static_assert(Sched<6, 8>::NB == 11 && Sched<6, 8>::PRODUCTS == 21 && Sched<6, 8>::NACC == 5, "8-bit, 6 slices");
-static_assert(Sched<5, 7>::NB == 9 && Sched<4, 8>::NB == 4 && Sched<4, 8>::NACC == 4 && Sched<5, 8>::NB == 5 &&
-                  Sched<4, 7>::NB == 4,
-              "schedules");
-static_assert(Sched<6, 7>::bslice(15) == 17 && Sched<6, 7>::btile(6, 5) == 15 && Sched<6, 8>::bslice(10) == 11 &&
-                  Sched<6, 8>::btile(5, 5) == 10 && Sched<6, 8>::btile(4, 4) == 4,
-              "tile maps");
+static_assert(Sched<6>::PRODUCTS == 21 && Sched<4>::PRODUCTS == 10, "schedules");
 
 template <int S, int BITS, int NT>
 __host__ __device__ constexpr int stage_count() {
-    constexpr int st = S * 128 * 32 + Sched<S, BITS>::NB * (((NT * 32 + 1023) / 1024) * 1024);
+    constexpr int st = S * 128 * 32 + Sched<S>::NB * NT * 32;
     constexpr int n = (220 * 1024) / st;
     return n > 6 ? 6 : n;
 }
@@ -988,16 +964,20 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
     split_gemm_kernel(const __grid_constant__ CUtensorMap mapA0, const __grid_constant__ CUtensorMap mapA1,
                       const __grid_constant__ CUtensorMap mapB0, const __grid_constant__ CUtensorMap mapB1,
                       const SplitParams P, const Epi epi) {
-    using SC = Sched<S, BITS>;
+    using SC = Sched<S>;
+    static_assert(BITS == 8, "8-bit digits");
     constexpr int NST = stage_count<S, BITS, NT>();
-    constexpr int A_TILE = SP_M * 32;                            // one slice, 16 K elements
-    constexpr int B_TILE = ((NT * 32 + 1023) / 1024) * 1024;
+    constexpr int A_TILE = SP_M * 32;  // one slice, 16 K elements
+    constexpr int B_TILE = NT * 32;    // one slice of NT table rows: the B slices are contiguous
     constexpr int STAGE = S * A_TILE + SC::NB * B_TILE;
     constexpr uint32_t TX = S * (SP_M * 32) + SC::NB * (NT * 32);
-    // the MMA's N follows the unit's valid table rows, rounded up to 16
-    // (the B tile is always loaded whole; the MMA reads its first N rows)
+    constexpr int GMAX = 256 / NT;     // products of one A slice per MMA (N = g NT <= 256)
+    // every B tile is loaded whole; a unit of at most 32 valid table rows runs
+    // its 21 products as MMAs of N = its rows rounded up to 16, the others as
+    // grouped MMAs of full tiles
     static_assert(SC::NACC * NT <= 512, "accumulators must fit in TMEM");
-    static_assert(NT % 16 == 0 && NT >= 16, "the MMA's N and the epilogue's 4-column loads");
+    static_assert(NT % 16 == 0 && NT >= 16 && NT <= 128, "the MMA's N and the epilogue's 4-column loads");
+    static_assert(STAGE % 1024 == 0 && B_TILE % 256 == 0, "stage and tile alignment of the 32-byte swizzle");
     // Two accumulator sets when they fit in TMEM (NT = 48): the MMAs of the
     // next unit then run while the epilogue drains the previous one.
     constexpr int NBUF = 2 * SC::NACC * NT <= 512 ? 2 : 1;
@@ -1041,8 +1021,6 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                 const SplitUnit u = P.units[ui];
                 const CUtensorMap* ma = (u.flags & 1) ? &mapA1 : &mapA0;
                 const CUtensorMap* mb = (u.flags & 2) ? &mapB1 : &mapB0;
-                const int arows = (u.flags & 1) ? P.a_rows_total[1] : P.a_rows_total[0];
-                const int brows = (u.flags & 2) ? P.b_rows_total[1] : P.b_rows_total[0];
                 for (int kb = 0; kb < u.ksteps; ++kb, ++it) {
                     const int st = it % NST;
                     const uint32_t ph = (it / NST) & 1;
@@ -1052,13 +1030,9 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                     mbar_expect_tx(&full[st], TX);
                     unsigned char* sa = smem + st * STAGE;
                     unsigned char* sb = sa + S * A_TILE;
-#pragma unroll
-                    for (int s = 0; s < S; ++s)
-                        tma_load_2d(sa + s * A_TILE, ma, &full[st], (u.k0 + kb) * SP_KB, s * arows + u.a_row0);
-#pragma unroll
-                    for (int j = 0; j < SC::NB; ++j)
-                        tma_load_2d(sb + j * B_TILE, mb, &full[st], (u.k0 + kb) * SP_KB,
-                                    SC::bslice(j) * brows + u.b_row0);
+                    // one box per operand: the S slices of 128 rows (A) and of NT rows (B)
+                    tma_load_3d(sa, ma, &full[st], (u.k0 + kb) * SP_KB, u.a_row0, 0);
+                    tma_load_3d(sb, mb, &full[st], (u.k0 + kb) * SP_KB, u.b_row0, 0);
                 }
             }
             // drain: wait (bounded) for the copies this thread issued
@@ -1076,8 +1050,9 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             bool ok = true;
             for (int ui = blockIdx.x; ui < P.nunits && ok; ui += gridDim.x, ++tile) {
                 const SplitUnit u = P.units[ui];
-                const int nmma = min(NT, (u.n + 15) & ~15);
-                const uint32_t idesc = idesc_bf16_f32(SP_M, nmma);
+                // narrow units: one MMA per product, N = valid rows rounded up to 16
+                const bool narrow = u.n <= 32 && NT > 32;
+                const uint32_t idesc1 = idesc_bf16_f32(SP_M, narrow ? ((u.n + 15) & ~15) : NT);
                 // accumulator set of this unit: the k-th use of set b is unit tile = k NBUF + b
                 const int buf = NBUF == 2 ? (tile & 1) : 0;
                 const uint32_t tacc = tmem + (uint32_t)(buf * 256);
@@ -1095,19 +1070,24 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                     // descriptors differ only in the start-address field (address >> 4)
                     const uint64_t da = desc_sw32(smem_u32(smem + st * STAGE));
                     const uint64_t db = da + (uint64_t)((S * A_TILE) >> 4);
-                    bool first[SC::NACC];
+                    // A slice 0 comes first: its products start every accumulator
+                    // (levels 0..S-1) in the first K block, all later ones add
 #pragma unroll
-                    for (int a = 0; a < SC::NACC; ++a) first[a] = (kb == 0);
+                    for (int s = 0; s < S; ++s) {
+                        const uint32_t acc = (kb > 0 || s > 0) ? 1u : 0u;
+                        const uint64_t as = da + (uint64_t)((s * A_TILE) >> 4);
+                        if (narrow) {
 #pragma unroll
-                    for (int d = 0; d <= SC::DMAX; ++d) {
-                        const int acc = SC::acc(d);
+                            for (int t = 0; t < S - s; ++t)
+                                umma_bf16(tacc + (uint32_t)((s + t) * NT), as, db + (uint64_t)((t * B_TILE) >> 4),
+                                          idesc1, acc);
+                        } else {
 #pragma unroll
-                        for (int s = 0; s < S; ++s) {
-                            const int t = d - s;
-                            if (t < 0 || t >= S) continue;
-                            umma_bf16(tacc + acc * NT, da + (uint64_t)((s * A_TILE) >> 4),
-                                      db + (uint64_t)((SC::btile(d, t) * B_TILE) >> 4), idesc, first[acc] ? 0u : 1u);
-                            first[acc] = false;
+                            for (int t = 0; t < S - s; t += GMAX) {
+                                const int g = (S - s - t) < GMAX ? (S - s - t) : GMAX;
+                                umma_bf16(tacc + (uint32_t)((s + t) * NT), as, db + (uint64_t)((t * B_TILE) >> 4),
+                                          idesc_bf16_f32(SP_M, g * NT), acc);
+                            }
                         }
                     }
                     umma_commit(&empty[st]);
@@ -1147,14 +1127,14 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             if (!__all_sync(0xffffffffu, got)) break;
             tc_fence_after();
             // phase 1: drain the accumulators of this warp's columns into exact
-            // integers, then hand TMEM back to the MMA issuer
-            // 32-bit conversions only: exact levels are integers of at most 2^24 and
-            // the last accumulator times 2^6 stays below 2^31 within the K bounds;
-            // the top two levels combine in 32 bits (|acc_0| 2^BITS + |acc_1| < 2^31).
-            // T = sum_{a < NACC-1} acc_a 2^{BITS (NACC-1-a) + 6} + round(2^6 acc_last),
-            // in units of 2^-6 of a level-(NACC-1) product: 2^{eA + eB - BITS (NACC + 1) - 6}.
-            constexpr int TEXP = -BITS * (SC::NACC + 1) - 6;
-            static_assert(SC::NACC == 4 || SC::NACC == 5, "four or five accumulators");
+            // integers, then hand TMEM back to the MMA issuer.  Every
+            // accumulator holds an integer: acc_0 (|acc_0| <= 256 2^14 = 2^22)
+            // by an exact FP32 offset, the others by conversion; levels 0 and 1
+            // combine in 32 bits (|acc_0| 2^8 + |acc_1| < 2^31), the rest by
+            // Horner in 64 bits:  T = sum_d acc_d 2^{8 (S-1-d)}  (|T| < 2^63),
+            // and the product is T 2^{eA + eB - 8 (S + 1)}.
+            constexpr int TEXP = -8 * (S + 1);
+            static_assert(SC::NACC == S && S >= 2, "one accumulator per level");
             long long T[CW];
             // warps whose columns are all past the unit's valid rows skip the work
             const bool active = col0 < u.n;
@@ -1168,19 +1148,11 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                 tmem_ld_wait();
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    // level 0 is one product per term: |acc_0| <= 256 2^14 = 2^22 per chunk,
-                    // so acc_0 + 1.5 2^23 is exact and its low bits are the integer
                     const int i0 = __float_as_int(__uint_as_float(v[0][j]) + 12582912.0f) - 0x4B400000;
-                    const int u = (i0 << BITS) + __float2int_rn(__uint_as_float(v[1][j]));
-                    const int i2 = __float2int_rn(__uint_as_float(v[2][j]));
-                    const int il = __float2int_rn(64.0f * __uint_as_float(v[SC::NACC - 1][j]));
-                    if constexpr (SC::NACC == 5) {
-                        const int i3 = __float2int_rn(__uint_as_float(v[3][j]));
-                        T[4 * c + j] = ((long long)u << (3 * BITS + 6)) + ((long long)i2 << (2 * BITS + 6)) +
-                                       ((long long)i3 << (BITS + 6)) + (long long)il;
-                    } else {
-                        T[4 * c + j] = ((long long)u << (2 * BITS + 6)) + ((long long)i2 << (BITS + 6)) + (long long)il;
-                    }
+                    long long t = (long long)((i0 << 8) + __float2int_rn(__uint_as_float(v[1][j])));
+#pragma unroll
+                    for (int a = 2; a < SC::NACC; ++a) t = t * 256 + __float2int_rn(__uint_as_float(v[a][j]));
+                    T[4 * c + j] = t;
                 }
             }
             }
@@ -1265,7 +1237,7 @@ __global__ void wait_expiry_kernel(int* err, int* host_err, long long limit_ns) 
 template <int S, int BITS, int NT>
 constexpr size_t split_smem_bytes() {
     constexpr int NST = stage_count<S, BITS, NT>();
-    return (size_t)NST * (S * SP_M * 32 + Sched<S, BITS>::NB * (((NT * 32 + 1023) / 1024) * 1024)) + 1024 + 256;
+    return (size_t)NST * (S * SP_M * 32 + Sched<S>::NB * NT * 32) + 1024 + 256;
 }
 
 }  // namespace
@@ -1296,16 +1268,18 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// [S][rows][Kp] bf16 slice array -> 2D map (Kp, S*rows), box (16, box_rows), 32B swizzle
+// [S][rows][Kp] bf16 slice array -> 3D map (Kp, rows, S), box (16, box_rows,
+// S), 32B swizzle: one copy brings a tile of every slice, the slices one
+// after the other in shared memory (rows past the array's end read as 0)
 int make_map(CUtensorMap* map, const void* base, long long rows, int Kp, int S, int box_rows) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return fail(ZEST_GPU_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
-    if ((long long)S * rows >= (1ll << 31)) return fail(ZEST_GPU_ERR_UNSUPPORTED, "slice array too tall for TMA");
-    cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)(S * rows)};
-    cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
-    cuuint32_t box[2] = {16, (cuuint32_t)box_rows};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+    if (rows >= (1ll << 31)) return fail(ZEST_GPU_ERR_UNSUPPORTED, "slice array too tall for TMA");
+    cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)S};
+    cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)rows * Kp * 2};
+    cuuint32_t box[3] = {16, (cuuint32_t)box_rows, (cuuint32_t)S};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(ZEST_GPU_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
@@ -1314,14 +1288,14 @@ int make_map(CUtensorMap* map, const void* base, long long rows, int Kp, int S, 
 
 inline int r16(int k) { return (k + 15) & ~15; }
 
-// table rows per tile: five accumulators of NT columns within the 512 TMEM columns
-int n_tile(int) { return 96; }
+// table rows per tile: S accumulators of NT columns within the 512 TMEM columns
+// (6 x 80, 5 x 96, 4 x 64 with two accumulator sets)
+int n_tile(int S) { return S == 6 ? 80 : S == 5 ? 96 : 64; }
 
 }  // namespace
 
-// Slice arrays of one operand: [S][rows][Kp] bf16 + per-row exponents.
-// Slice arrays of one operand: [copies * S][rows][Kp] bf16 + per-row exponents.
-// Tables carry three copies (digits, digits x 2^-7, digits x 2^-14).
+// Slice arrays of one operand: [copies * S][rows][Kp] bf16 + per-row exponents
+// (the GEMMs read one copy: every level has its own accumulator).
 struct SliceArray {
     DevBuf data, ex;
     long long rows = 0;
@@ -1398,7 +1372,7 @@ struct SplitState {
     DevBuf tmp;                 // FP64 staging of generated tables
     DevBuf cycles;              // role wait counters, kept when ZEST_GPU_SPLIT_CYCLES is set
     bool cycles_on = false;
-    int nt[16];                 // column tile of each work-list stage: 0 = chosen per launch, or 48 / 96
+    int nt[16];                 // column tile of each work-list stage: 0 = chosen per launch, or 32 / 80
     SplitState();
     double useful_flops = 0.0, issued_flops = 0.0;  // accumulated while profiling
 };
@@ -1510,7 +1484,7 @@ int get_state(zest_gpu_context* ctx, SplitState** out) {
         ctx->split.reset(new SplitState());
         ctx->split->cycles_on = std::getenv("ZEST_GPU_SPLIT_CYCLES") != nullptr;
         // tuning override of the column tiles, "stage=nt,..." with stage one of
-        // dft_f leg_f rad_f rad_b leg_b dft_b st_dft_f st_dft_b and nt 48 or 96
+        // dft_f leg_f rad_f rad_b leg_b dft_b st_dft_f st_dft_b and nt 32 or 80
         if (const char* e = std::getenv("ZEST_GPU_SPLIT_NT")) {
             static const char* names[] = {"dft_f", "leg_f", "rad_f", "rad_b", "leg_b", "dft_b", "dense",
                                           "st_leg_f", "st_leg_b", "st_dft_f", "st_dft_b"};
@@ -1525,7 +1499,7 @@ int get_state(zest_gpu_context* ctx, SplitState** out) {
                     const std::string key = item.substr(0, eq);
                     const int v = std::atoi(item.c_str() + eq + 1);
                     for (int i = 0; i < int(sizeof(names) / sizeof(names[0])); ++i)
-                        if (key == names[i] && (v == 48 || v == 96)) ctx->split->nt[i] = v;
+                        if (key == names[i] && (v == 32 || v == 80)) ctx->split->nt[i] = v;
                 }
                 pos = end + 1;
             }
@@ -1596,7 +1570,7 @@ __global__ void transpose_blocks_kernel(const double* __restrict__ in, const lon
 }
 
 int slice_table(zest_gpu_context* ctx, const double* src, long long rows, int K, int ld, int S, int bits,
-                SliceArray& dst, int copies = 3) {
+                SliceArray& dst, int copies = 1) {
     ZG_TRY(dst.ensure(rows, r16(K), S, copies));
     return launch_slice(ctx->stream, RowMajorLoader{src, ld}, rows, K, S, bits, dst);
 }
@@ -1693,14 +1667,17 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
     ZG_TRY(get_state(ctx, &st));
     cudaStream_t s = ctx->stream;
     CUtensorMap ma0, ma1, mb0, mb1;
-    if (B0.copies != 3 || B1.copies != 3) return fail(ZEST_GPU_ERR_INVALID, "split GEMM: table slices lack scaled copies");
+    if (A0.copies != 1 || A1.copies != 1 || B0.copies != 1 || B1.copies != 1)
+        return fail(ZEST_GPU_ERR_INVALID, "split GEMM: operands must hold one copy of their slices");
     // the FP32 level sums stay exact only up to these lengths
     if (ul.max_ksteps * SP_KB > (BITS == 8 ? SL_K8MAX : SL_KMAX))
         return fail(ZEST_GPU_ERR_INVALID, "split GEMM: sum too long for exact level sums");
-    ZG_TRY(make_map(&ma0, A0.ptr(), A0.rows, A0.Kp, S * A0.copies, SP_M));
-    ZG_TRY(make_map(&ma1, A1.ptr(), A1.rows, A1.Kp, S * A1.copies, SP_M));
-    ZG_TRY(make_map(&mb0, B0.ptr(), B0.rows, B0.Kp, S * 3, NT));
-    ZG_TRY(make_map(&mb1, B1.ptr(), B1.rows, B1.Kp, S * 3, NT));
+    if (A0.S != S || A1.S != S || B0.S != S || B1.S != S)
+        return fail(ZEST_GPU_ERR_INVALID, "split GEMM: operands sliced with another slice count");
+    ZG_TRY(make_map(&ma0, A0.ptr(), A0.rows, A0.Kp, S, SP_M));
+    ZG_TRY(make_map(&ma1, A1.ptr(), A1.rows, A1.Kp, S, SP_M));
+    ZG_TRY(make_map(&mb0, B0.ptr(), B0.rows, B0.Kp, S, NT));
+    ZG_TRY(make_map(&mb1, B1.ptr(), B1.rows, B1.Kp, S, NT));
     if (!ul.dev.p) {  // work lists are uploaded once and cached with their key
         ZG_TRY(ul.dev.ensure(units.size() * sizeof(SplitUnit)));
         ZG_CUDA_TRY(cudaMemcpyAsync(ul.dev.p, units.data(), units.size() * sizeof(SplitUnit),
@@ -1713,10 +1690,6 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
     SplitParams P;
     P.units = ul.dev.as<SplitUnit>();
     P.nunits = int(units.size());
-    P.a_rows_total[0] = int(A0.rows);
-    P.a_rows_total[1] = int(A1.rows);
-    P.b_rows_total[0] = int(B0.rows);
-    P.b_rows_total[1] = int(B1.rows);
     P.ea[0] = A0.ex.as<int>();
     P.ea[1] = A1.ex.as<int>();
     P.eb[0] = B0.ex.as<int>();
@@ -1782,33 +1755,26 @@ int get_units(zest_gpu_context* ctx, std::tuple<int, int, int, int, int, int> ke
     return ZEST_GPU_OK;
 }
 
-template <int NT = 96, class Epi>
-int run_gemm(zest_gpu_context* ctx, int S, UnitList& ul, const SliceArray& A0, const SliceArray& A1,
-             const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
+// The split GEMM of a work list, its column tile NT chosen at run time: with
+// six slices 80 (one accumulator set) or 32 (two sets, so that the next
+// unit's MMAs overlap the epilogue's drain); five slices use 96 and four 64.
+// Later K-chunks of long sums need six slices.
+template <class Epi>
+int run_gemm_nt(zest_gpu_context* ctx, int nt, int S, UnitList& ul, const SliceArray& A0, const SliceArray& A1,
+                const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
     const int bits = A0.bits;
     if (A1.bits != bits || B0.bits != bits || B1.bits != bits)
         return fail(ZEST_GPU_ERR_INVALID, "split GEMM: operands sliced with different digit widths");
     if (bits != 8) return fail(ZEST_GPU_ERR_INVALID, "split GEMM: operands need 8-bit digits");
-    if constexpr (NT != 96 || Epi::CHUNK) {
-        // narrow tiles (SH sums) and the later K-chunks of long sums come with 6 slices only
-        if (S != 6) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: sums longer than 256 terms need 6 slices");
-        return run_gemm_t<6, 8, NT>(ctx, ul, A0, A1, B0, B1, epi);
-    } else {
-        switch (S) {
-        case 4: return run_gemm_t<4, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
-        case 5: return run_gemm_t<5, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
-        case 6: return run_gemm_t<6, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
-        }
+    if (Epi::CHUNK && S != 6)
+        return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: sums longer than 256 terms need 6 slices");
+    switch (S) {
+    case 6: return nt == 32 ? run_gemm_t<6, 8, 32>(ctx, ul, A0, A1, B0, B1, epi)
+                            : run_gemm_t<6, 8, 80>(ctx, ul, A0, A1, B0, B1, epi);
+    case 5: return run_gemm_t<5, 8, 96>(ctx, ul, A0, A1, B0, B1, epi);
+    case 4: return run_gemm_t<4, 8, 64>(ctx, ul, A0, A1, B0, B1, epi);
     }
     return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path supports 4..6 slices");
-}
-
-// run_gemm with the column tile chosen at run time (48: six slices only)
-template <class Epi>
-int run_gemm_nt(zest_gpu_context* ctx, int nt, int S, UnitList& ul, const SliceArray& A0, const SliceArray& A1,
-                const SliceArray& B0, const SliceArray& B1, const Epi& epi) {
-    if (nt == 48) return run_gemm<48>(ctx, S, ul, A0, A1, B0, B1, epi);
-    return run_gemm<96>(ctx, S, ul, A0, A1, B0, B1, epi);
 }
 
 // tiles of a group: operand rows [a0, a0 + arows) x table rows [b0, b0 + nrows), K = kk
@@ -1826,33 +1792,33 @@ void add_units(UnitList& ul, int S, int bits, long long a0, long long arows, int
             u.b_row0 = b0 + c;
             u.n = std::min(NT, nrows - c);
             u.ksteps = ksteps;
+            // a unit of at most 32 valid rows runs N = its rows rounded up to 16
+            const int ncols = (u.n <= 32 && NT > 32) ? r16(u.n) : NT;
             u.flags = flags;
             u.g = g;
             u.aux = c;
             u.k0 = k0 / 16;
             ul.v.push_back(u);
             ul.useful += 2.0 * u.a_rows * u.n * kk * P;
-            ul.issued += 2.0 * SP_M * NT * 16.0 * ksteps * P;
+            ul.issued += 2.0 * SP_M * ncols * 16.0 * ksteps * P;
         }
 }
 
 
-// Column tile of a stage's launches (48 only with six slices), also part of
-// the work-list key; ncols = the most table rows a group of the stage has.
-//   * 48 where no group has more than 48 columns: a 96-wide tile would be at
-//     least half empty (the small orders of a ragged batch);
-//   * 48 for the backward Legendre stage of the Zernike transforms: its sums
-//     are short (K = ceil(L/2)) and its outputs span ceil((L+1)/2) folded
-//     nodes (101 at order 200: tiles of 96 + 5); with 48 the MMAs overlap the
-//     epilogue's drain (two accumulator sets).  Measured at order 200 x 64:
-//     41.7 ms of GEMMs instead of 44.0; 48 for the other stages was no faster;
-//   * 96 otherwise.
+// Column tile of a stage's launches with six slices, also part of the
+// work-list key; ncols = the most table rows a group of the stage has.
+//   * 32 where no group has more than 32 columns (the small orders of a
+//     ragged batch): two accumulator sets, and an 80-wide tile would be at
+//     least 60% empty;
+//   * 80 otherwise: one set of six 80-column accumulators, MMAs of up to
+//     three products (N = 240).
+// A tuning override (ZEST_GPU_SPLIT_NT) can pin a stage to 32 or 80.
 inline int stage_nt(const SplitState* st, int wk, int S, int ncols) {
-    if (S != 6) return 96;
+    if (S != 6) return n_tile(S);
     if (st->nt[wk]) return st->nt[wk];
-    return (ncols <= 48 || wk == WK_LEG_B) ? 48 : 96;
+    return ncols <= 32 ? 32 : 80;
 }
-inline int nt_pass(int nt) { return nt == 48 ? 1 << 16 : 0; }
+inline int nt_pass(int nt) { return nt == 32 ? 1 << 16 : 0; }
 
 // Longitude DFT of `batch` grids x[b][lon][col] (C columns, item stride gsz)
 // to the spectra G[b][m][col][re, im], m < Lm (L = Lg orders per item):
@@ -2185,13 +2151,13 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
 // 2 x batch data rows per order m the data could not fill a row tile.  The
 // data (the folded spectra, or the coefficients) is the scaled-copy operand,
 // sliced per call; its 2 x batch rows are the columns, in tiles of 16 (batches
-// up to 8: a tile loads no unused data rows), 48 (up to 24) or 96.
+// up to 8: a tile loads no unused data rows), 32 (up to 16) or 80.
 // ===========================================================================
 namespace {
 template <class F>
 int st_with_nt(int batch, F&& f) {
     if (2 * batch <= 16) return f(std::integral_constant<int, 16>{});
-    return 2 * batch <= 48 ? f(std::integral_constant<int, 48>{}) : f(std::integral_constant<int, 96>{});
+    return 2 * batch <= 32 ? f(std::integral_constant<int, 32>{}) : f(std::integral_constant<int, 80>{});
 }
 // SH sums always use 8-bit digits and 6 slices; sums longer than 256 run as
 // K-chunks of at most 256 whose FP64 results are added (the later chunks
@@ -2226,8 +2192,8 @@ int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int ba
     }
     const int bits = 8;
     const long long per_m = 2LL * batch, rows = (long long)Lm * per_m;
-    ZG_TRY(st->op[0].ensure(rows, r16(kh), S, 3));
-    ZG_TRY(st->op[1].ensure(rows, r16(kh), S, 3));
+    ZG_TRY(st->op[0].ensure(rows, r16(kh), S));
+    ZG_TRY(st->op[1].ensure(rows, r16(kh), S));
     {
         StageScope sc(ctx, ST_SPLIT_SLICE);
         LegFwdLoader ld{X, batch, Lg, nlat, 2, plan.leg.j0u, plan.leg.j0d};
@@ -2273,8 +2239,8 @@ int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int b
     ZG_TRY(build_st_tables(ctx, st, plan, S, &tb));
     const int bits = 8;
     const long long per_m = 2LL * batch, rows = (long long)Lm * per_m;
-    ZG_TRY(st->op[0].ensure(rows, kl, S, 3));
-    ZG_TRY(st->op[1].ensure(rows, kl, S, 3));
+    ZG_TRY(st->op[0].ensure(rows, kl, S));
+    ZG_TRY(st->op[1].ensure(rows, kl, S));
     {
         StageScope sc(ctx, ST_SPLIT_SLICE);
         ZG_TRY(launch_slice2(s, StLegBwdLoader{coeffs, csz, batch, Lm}, rows, (Lm + 1) / 2, Lm / 2, 0, S, bits,
@@ -2573,7 +2539,7 @@ int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A
     ZG_TRY(get_state(ctx, &st));
     SliceArray a, b;
     ZG_TRY(a.ensure(M, r16(K), S));
-    ZG_TRY(b.ensure(N, r16(K), S, 3));
+    ZG_TRY(b.ensure(N, r16(K), S));
     const int bits = digit_bits(K);
     ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{A, K}, M, K, S, bits, a));
     ZG_TRY(launch_slice(ctx->stream, RowMajorLoader{B, K}, N, K, S, bits, b));
@@ -2581,8 +2547,8 @@ int split_dense_gemm(zest_gpu_context* ctx, int M, int N, int K, const double* A
         const int k0 = ch * KCHUNK;
         UnitList u;
         add_units(u, S, bits, 0, M, 0, N, NT, std::min(KCHUNK, K - k0), 0, 0, k0);
-        if (ch == 0) ZG_TRY(run_gemm(ctx, S, u, a, a, b, b, EpiDense<false>{C, N}));
-        else ZG_TRY(run_gemm(ctx, S, u, a, a, b, b, EpiDense<true>{C, N}));
+        if (ch == 0) ZG_TRY(run_gemm_nt(ctx, NT, S, u, a, a, b, b, EpiDense<false>{C, N}));
+        else ZG_TRY(run_gemm_nt(ctx, NT, S, u, a, a, b, b, EpiDense<true>{C, N}));
         ZG_TRY(split_finish(ctx));  // the local work list must outlive its launch
     }
     return ZEST_GPU_OK;  // the local operands outlive the launches (split_finish synchronizes)

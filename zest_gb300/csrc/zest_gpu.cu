@@ -568,7 +568,9 @@ static int get_vectors(zest_gpu_context* ctx, int kind, int L, const int2** out,
 }
 
 int rotate_dev(zest_gpu_context* ctx, int kind, int L, int batch, double* coeffs, const double* euler, int type) {
-    if (batch == 0 || L <= 1) return ZEST_GPU_OK;
+    // a whole expansion of order 1 has nothing to rotate; the row span of
+    // order 1 (n = 0) still rotates its l = 0 vector, as the reference does
+    if (batch == 0 || L < 1 || (L == 1 && kind != 2)) return ZEST_GPU_OK;
     const double* wig;
     ZG_TRY(get_wigner(ctx, L, &wig));
     const int2* vl;
