@@ -283,7 +283,14 @@ int set_attributes_once(Kern kern, Set&& set) {
 // row-fast loads), with the staged FP64 rows within 96 KB.
 inline int slice_rows_per_block(int K, bool two) {
     const int per_row = K * (two ? 16 : 8);
-    int r = 32;
+    // ZEST_GPU_SLICE_ROWS (a power of two up to 32) caps the rows per block,
+    // to measure the trade between longer row-fast reads and blocks per SM
+    static const int cap = [] {
+        const char* e = std::getenv("ZEST_GPU_SLICE_ROWS");
+        const int v = e ? std::atoi(e) : 32;
+        return (v >= 1 && v <= 32 && (v & (v - 1)) == 0) ? v : 32;
+    }();
+    int r = cap;
     while (r > 1 && r * per_row > 96 * 1024) r >>= 1;
     return r;
 }
@@ -924,6 +931,7 @@ struct SplitParams {
     int nunits;
     const int* ea[2];
     const int* eb[2];
+    int narrow;               // units of at most this many valid table rows run one MMA per product
     int* err;
     int* host_err;            // mapped host word: each CTA copies a set flag there as it exits
     unsigned long long* dbg;  // optional cycle counters (null in normal use)
@@ -1051,7 +1059,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             for (int ui = blockIdx.x; ui < P.nunits && ok; ui += gridDim.x, ++tile) {
                 const SplitUnit u = P.units[ui];
                 // narrow units: one MMA per product, N = valid rows rounded up to 16
-                const bool narrow = u.n <= 32 && NT > 32;
+                const bool narrow = u.n <= P.narrow && NT > 32;
                 const uint32_t idesc1 = idesc_bf16_f32(SP_M, narrow ? ((u.n + 15) & ~15) : NT);
                 // accumulator set of this unit: the k-th use of set b is unit tile = k NBUF + b
                 const int buf = NBUF == 2 ? (tile & 1) : 0;
@@ -1372,6 +1380,7 @@ struct SplitState {
     DevBuf tmp;                 // FP64 staging of generated tables
     DevBuf cycles;              // role wait counters, kept when ZEST_GPU_SPLIT_CYCLES is set
     bool cycles_on = false;
+    int narrow = 32;            // widest unit (valid table rows) run as one MMA per product
     int nt[16];                 // column tile of each work-list stage: 0 = chosen per launch, or 32 / 80
     SplitState();
     double useful_flops = 0.0, issued_flops = 0.0;  // accumulated while profiling
@@ -1483,6 +1492,12 @@ int get_state(zest_gpu_context* ctx, SplitState** out) {
     if (!ctx->split) {
         ctx->split.reset(new SplitState());
         ctx->split->cycles_on = std::getenv("ZEST_GPU_SPLIT_CYCLES") != nullptr;
+        // tuning override: units of at most this many valid table rows (16..64)
+        // issue one MMA per product instead of grouped full-width MMAs
+        if (const char* e = std::getenv("ZEST_GPU_SPLIT_NARROW")) {
+            const int v = std::atoi(e);
+            if (v >= 16 && v <= 64) ctx->split->narrow = v;
+        }
         // tuning override of the column tiles, "stage=nt,..." with stage one of
         // dft_f leg_f rad_f rad_b leg_b dft_b st_dft_f st_dft_b and nt 32 or 80
         if (const char* e = std::getenv("ZEST_GPU_SPLIT_NT")) {
@@ -1696,6 +1711,7 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
     P.eb[1] = B1.ex.as<int>();
     P.err = st->err.as<int>();
     P.host_err = st->host_err_dev;
+    P.narrow = st->narrow;
     P.dbg = nullptr;
     if (st->cycles_on) {
         ZG_TRY(st->cycles.ensure(8 * sizeof(unsigned long long)));
