@@ -488,6 +488,48 @@ def run_lsq(args, rank: int, world: int, barrier) -> None:
             "cpu_baseline": cpu, "clocks": clocks}), flush=True)
 
 
+def run_rotate(args, rank: int, world: int, barrier) -> None:
+    """Rotor::rotate of 256 Zernike expansions of order 64 (the alignment
+    configuration's batch), Haar-uniform Euler angles, coefficients
+    N(0, (n+1)^-2): the FP64 rotation (one warp per (n, l) vector) and, in
+    split precision, the two X(+-pi/2) products of all vectors of one l as
+    split GEMMs on the tensor cores.  One step = one rotation call on device
+    memory (in place)."""
+    import torch
+    import zest_gb300 as zg
+    ctx = zg.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    L, B = 64, 256
+    rng = np.random.default_rng(6400 + rank)
+    c = zt_coeffs(L, B, seed0=replica_seed0(rank, B)) * 1.0
+    e = np.stack([rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)), rng.uniform(0, 2 * np.pi, B)], 1)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    c0 = torch.from_numpy(c.ravel()).to(dev)
+    ed = torch.from_numpy(np.ascontiguousarray(e).ravel()).to(dev)
+    cd = c0.clone()
+    out = {}
+    for name, prec in (("fp64", zg.PRECISION_FP64), ("split", zg.PRECISION_SPLIT)):
+        ctx.set_precision(prec, 6 if prec else 0)
+        ms, clocks = _timed_loop(lambda: ctx.zt_rotate(cd, L, ed, batch=B), args, barrier)
+        cd.copy_(c0)
+        ctx.zt_rotate(cd, L, ed, batch=B)
+        torch.cuda.synchronize()
+        out[name] = {"ms": ms, "result": cd.clone(), "clocks": clocks}
+        cd.copy_(c0)
+    ctx.set_precision(zg.PRECISION_FP64)
+    a, b = out["split"]["result"].reshape(B, -1), out["fp64"]["result"].reshape(B, -1)
+    err = float(((a - b).abs().amax(1) / b.abs().amax(1)).max())
+    if rank == 0:
+        print(json.dumps({
+            "metric": "Zernike rotations per second, order 64 x 256 (Rotor::rotate)",
+            "value": world * B / (out["split"]["ms"] * 1e-3), "unit": "rotations/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out["split"]["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 digit slices, fp64 recombination",
+            "data": "synthetic", "config": {"workload": "zernike_rotate", "order": L, "batch": B},
+            "fp64_gpu": {"value": world * B / (out["fp64"]["ms"] * 1e-3), "ms_per_step": out["fp64"]["ms"]},
+            "split_vs_fp64": out["fp64"]["ms"] / out["split"]["ms"],
+            "max_rel_err_vs_fp64": err, "clocks": out["split"]["clocks"]}), flush=True)
+
+
 def run_batching(args, rank: int, world: int, barrier) -> None:
     """4096 expansions, orders drawn uniformly from [8, 128] (sorted), c_nlm ~
     N(0, (n+1)^-2) with Im(m=0) = 0, Haar-uniform Euler angles; one step =
@@ -649,7 +691,7 @@ def main():
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["transforms", "batching", "sh", "evaluate", "spectra", "lsq"],
+    ap.add_argument("--workload", choices=["transforms", "batching", "sh", "evaluate", "spectra", "lsq", "rotate"],
                     default="transforms",
                     help="transforms: the headline (order 200 x 64 forward+backward); batching: 4096 "
                          "expansions of orders U{8..128}, rotate + backward in one graph")
@@ -694,6 +736,9 @@ def main():
         return
     if args.workload == "lsq":
         run_lsq(args, rank, world, barrier)
+        return
+    if args.workload == "rotate":
+        run_rotate(args, rank, world, barrier)
         return
 
     L, B = args.order, args.batch

@@ -251,3 +251,26 @@ def test_split_zt_long_sums_in_chunks(ctx, L):
         ctx.set_precision(zest_gb300.PRECISION_FP64)
     assert relmax(gs, g64) < SPLIT_TOL
     assert relmax(fs, f64) < SPLIT_TOL
+
+
+@pytest.mark.parametrize("kind,L,batch", [(0, 64, 256), (0, 7, 3), (0, 130, 2), (1, 100, 8), (1, 2, 1), (2, 33, 5),
+                                          (2, 34, 4)])
+@pytest.mark.parametrize("rtype", [0, 1])
+def test_split_single_order_rotation(ctx, kind, L, batch, rtype):
+    # Rotor::rotate of a batch of one order in split precision: the two
+    # X(+-pi/2) products of every vector as split GEMMs, against the FP64
+    # rotation of the same expansions (Zernike, SH and row-skipping spans)
+    import zest_gb300 as zg
+    rng = np.random.default_rng(1000 * kind + L + 7 * rtype)
+    size = {0: zg.zt_coeff_size, 1: zg.st_coeff_size, 2: zg.rows_coeff_size}[kind](L)
+    c = rng.normal(size=(batch, size, 2)).ravel()
+    e = rng.uniform(-np.pi, np.pi, size=3 * batch)
+    fn = {0: ctx.zt_rotate, 1: ctx.st_rotate, 2: ctx.rows_rotate}[kind]
+    want = fn(c.copy(), L, e.copy(), batch=batch, rotation_type=rtype)
+    ctx.set_precision(zg.PRECISION_SPLIT, 6)
+    try:
+        got = fn(c.copy(), L, e.copy(), batch=batch, rotation_type=rtype)
+    finally:
+        ctx.set_precision(zg.PRECISION_FP64)
+    for g, w in zip(got.reshape(batch, -1), want.reshape(batch, -1)):
+        assert relmax(g, w) < SPLIT_TOL

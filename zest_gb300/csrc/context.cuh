@@ -133,6 +133,14 @@ struct RaggedPlan {
     }
 };
 
+// The rotated vectors of a batch of expansions of one order, sorted by l
+// ({item, n, l, first coefficient}), and each item's coefficient offset.
+struct UniformRotation {
+    DevBuf vecs, coff;
+    std::vector<long long> voff;
+    long long nvec = 0;
+};
+
 struct TileEntry {
     DevBuf buf;
     int count = 0;
@@ -178,6 +186,7 @@ struct zest_gpu_context {
     std::map<int, std::unique_ptr<FftEntry>> ffts;
     std::map<int, std::unique_ptr<DevBuf>> wigner;
     std::map<std::tuple<int, int>, std::pair<std::unique_ptr<DevBuf>, int>> vec_lists;
+    std::map<std::tuple<int, int, int>, std::unique_ptr<UniformRotation>> uniform_rot;  // split rotations
     std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<TileEntry>> tiles;
     bool autotune = true;                                     // time the tile shapes on first use
     size_t host_chunk_bytes = size_t(1) << 29;                // pipelined host calls: input bytes per chunk

@@ -42,6 +42,7 @@
 #include <algorithm>
 #include <mutex>
 #include <set>
+#include <type_traits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -310,6 +311,21 @@ struct RowMajorLoader {  // tables and dense operands: p[r*ld + k]
     struct Row { const double* p; };
     __device__ Row row(long long r) const { return Row{p + r * ld}; }
     __device__ void get(const Row& R, int k, double& up, double&) const { up = R.p[k]; }
+};
+
+// row i of two row-major tables of one shape: (P[i][k], Q[i][k])
+struct TablePairLoader {
+    static constexpr bool ROW_FAST = false, TWO = true;
+    static constexpr int MODE = SL_PAIR, SHIFT = 1;
+    const double* P;
+    const double* Q;
+    long long ld;
+    struct Row { const double* p; const double* q; };
+    __device__ Row row(long long r) const { return Row{P + r * ld, Q + r * ld}; }
+    __device__ void get(const Row& R, int k, double& up, double& dn) const {
+        up = R.p[k];
+        dn = R.q[k];
+    }
 };
 
 // rows (b, col) of the ball grids; k = longitude: (x_k, x_{N-k}), x_0 alone.
@@ -810,16 +826,19 @@ struct EpiLegBwdE {
     static constexpr bool CHUNK = ACC;
     double* E;
     int B, L, kh, nr2;
-    struct Row { double* p; double sg; };
+    struct Row { double* p; unsigned long long sgn; };  // sgn: the sign bit flipped for imaginary parts
     __device__ Row row(const SplitUnit& u, int r) const {
         const int m = u.g, par = (u.flags >> 2) & 1;
         const long long local = r - (long long)m * B * nr2;
         const int b = int(local / nr2), kc = int(local - (long long)b * nr2);
-        return Row{E + ((((long long)par * B + b) * L + m) * kh + u.aux) * nr2 + kc, (kc & 1) ? -1.0 : 1.0};
+        return Row{E + ((((long long)par * B + b) * L + m) * kh + u.aux) * nr2 + kc,
+                   (kc & 1) ? (1ull << 63) : 0ull};
     }
     __device__ void load(const Row& R, int n, double* old) const { old[0] = R.p[(long long)n * nr2]; }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
-        R.p[(long long)n * nr2] = ACC ? old[0] + R.sg * v : R.sg * v;
+        // the conjugate by a sign-bit flip (an integer operation, not an FP64 multiply)
+        const double w = __longlong_as_double(__double_as_longlong(v) ^ (long long)R.sgn);
+        R.p[(long long)n * nr2] = ACC ? old[0] + w : w;
     }
 };
 
@@ -849,15 +868,15 @@ struct EpiStLegFwd {
     }
 };
 // Backward: table row r of group (m, p) is folded node j = r - (2m + p) kh;
-// the parity sums go to E[p][b][m][j][c], the imaginary parts times sgi (-1:
-// conjugated, as the inverse longitude DFT reads them).
+// the parity sums go to E[p][b][m][j][c], the imaginary parts with the sign bit
+// flipped (flip_im: conjugated, as the inverse longitude DFT reads them).
 template <bool ACC>
 struct EpiStLegBwdE {
     static constexpr bool RMW = ACC;
     static constexpr bool CHUNK = ACC;
     double* E;
     int B, L, kh;
-    double sgi;
+    unsigned long long flip_im;  // 1 << 63: the imaginary parts conjugated (a sign-bit flip), else 0
     struct Row { double* p; };
     __device__ Row row(const SplitUnit& u, int r) const {
         const int m = u.g, par = (u.flags >> 2) & 1;
@@ -868,7 +887,7 @@ struct EpiStLegBwdE {
         old[0] = R.p[(long long)(n >> 1) * L * kh * 2 + (n & 1)];
     }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
-        const double w = (n & 1) ? sgi * v : v;
+        const double w = __longlong_as_double(__double_as_longlong(v) ^ (long long)((n & 1) ? flip_im : 0ull));
         R.p[(long long)(n >> 1) * L * kh * 2 + (n & 1)] = ACC ? old[0] + w : w;
     }
 };
@@ -923,6 +942,60 @@ struct EpiDftBwdSin {
         const int i = R.i0 + n;
         R.x[(long long)i * C] = old[0] + v;
         R.x[(long long)(N - i) * C] = old[1] - v;
+    }
+};
+
+// The same inverse DFT for sums of at most 256 terms, combined in integers:
+// the cos and sin tables are sliced together, so that row i of both shares
+// one exponent, and the data operands share theirs (one slicing job), so
+// C_i and S_i are exact integers T_c, T_s on the same scale 2^e.  The cos
+// pass writes x_0 = C_0 and the raw T_c (int64) of i >= 1 to the scratch; the
+// sin pass forms x_i = 2^e (T_c + T_s) and x_{N-i} = 2^e (T_c - T_s) exactly
+// before one rounding each, with integer operations only (no FP64 adds).
+// The table digits are at most 64 in magnitude (|2 cos|, |2 sin| <= 2), so
+// |T| < 2^61 and the sums cannot overflow.
+template <class E, class = void>
+struct raw_epi : std::false_type {};
+template <class E>
+struct raw_epi<E, std::void_t<decltype(E::RAW)>> : std::integral_constant<bool, E::RAW> {};
+
+struct EpiDftBwdCosRaw {
+    static constexpr bool RMW = false;
+    static constexpr bool CHUNK = false;
+    static constexpr bool RAW = true;
+    double* grid;
+    long long* Ts;
+    int C, N, L;
+    long long gsz;
+    struct Row { double* x; long long* t; int aux; };
+    __device__ Row row(const SplitUnit& u, int r) const {
+        const long long b = r / C, col = r - b * C;
+        return Row{grid + b * gsz + col, Ts + (b * L + u.aux) * C + col, u.aux};
+    }
+    __device__ void load_raw(const Row&, int, long long*) const {}
+    __device__ void store_raw(const Row& R, const SplitUnit&, int n, long long T, int e, long long) const {
+        if (R.aux + n == 0) *R.x = i64_ldexp(T, e);
+        else R.t[(long long)n * C] = T;
+    }
+};
+struct EpiDftBwdSinRaw {
+    static constexpr bool RMW = true;
+    static constexpr bool CHUNK = false;
+    static constexpr bool RAW = true;
+    double* grid;
+    const long long* Ts;
+    int C, N, L;
+    long long gsz;
+    struct Row { double* x; const long long* t; int i0; };
+    __device__ Row row(const SplitUnit& u, int r) const {
+        const long long b = r / C, col = r - b * C;
+        return Row{grid + b * gsz + col, Ts + (b * L + u.aux + 1) * C + col, u.aux + 1};
+    }
+    __device__ void load_raw(const Row& R, int n, long long* old) const { *old = R.t[(long long)n * C]; }
+    __device__ void store_raw(const Row& R, const SplitUnit&, int n, long long T, int e, long long old) const {
+        const int i = R.i0 + n;
+        R.x[(long long)i * C] = i64_ldexp(old + T, e);
+        R.x[(long long)(N - i) * C] = i64_ldexp(old - T, e);
     }
 };
 
@@ -1169,6 +1242,35 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             const long long w2 = clock64();
             if (lane == 0) mbar_arrive(&tempty[buf]);
             // phase 2 (overlaps the next tile's MMAs): FP64 results and stores
+            if constexpr (raw_epi<Epi>::value) {
+            if (active) {
+#pragma unroll
+            for (int c = 0; c < CW / 4; ++c) {
+                long long oldr[4] = {0, 0, 0, 0};
+                if constexpr (Epi::RMW) {
+                    if (rv) {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            if (col0 + 4 * c + j < u.n) epi.load_raw(R, col0 + 4 * c + j, &oldr[j]);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int n = col0 + 4 * c + j;
+                    const int idx = 4 * c + j;
+                    int eb;
+                    if constexpr (CW <= 32) {
+                        eb = __shfl_sync(0xffffffffu, eb_a, idx);
+                    } else {
+                        const int e1 = __shfl_sync(0xffffffffu, eb_a, idx & 31);
+                        const int e2 = __shfl_sync(0xffffffffu, eb_b, idx & 31);
+                        eb = idx < 32 ? e1 : e2;
+                    }
+                    if (rv && n < u.n) epi.store_raw(R, u, n, T[4 * c + j], ea + eb + TEXP, oldr[j]);
+                }
+            }
+            }
+            } else {
             if (active) {
 #pragma unroll
             for (int c = 0; c < CW / 4; ++c) {
@@ -1197,6 +1299,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                         epi.store(R, u, n, v, old[j]);
                     }
                 }
+            }
             }
             }
             if (P.dbg && warp == 2 && lane == 0) {
@@ -1334,6 +1437,9 @@ enum {
 // the Zernike grids and the SH LonLat grids of the same order.
 struct DftTables {
     SliceArray cos_f, sin_f, cos_b, sin_b;
+    // the inverse tables sliced together (orders up to 256): row i of both
+    // (sin row 0 = 0) shares one exponent; the sin slices hold m >= 1 at m - 1
+    SliceArray cos_bj, sin_bj;
 };
 
 // Sliced tables of the two X(+-pi/2) products of a rotation, all l < Lmax:
@@ -1601,7 +1707,9 @@ int build_dft_tables(zest_gpu_context* ctx, SplitState* st, int L, int N, int S,
     cudaStream_t s = ctx->stream;
     auto t = std::make_unique<DftTables>();
     const int ld = r16(L);
-    ZG_TRY(st->tmp.ensure((size_t)L * ld * sizeof(double)));
+    // room for the two inverse tables sliced together (below), so that no
+    // queued slicing job reads a buffer that was reallocated
+    ZG_TRY(st->tmp.ensure((size_t)2 * L * ld * sizeof(double)));
     double* tmp = st->tmp.as<double>();
     auto gen = [&](int rows, int K, int row_off, int col_off, int mode, SliceArray& dst) -> int {
         dim3 grid((ld + 127) / 128, rows);
@@ -1613,8 +1721,24 @@ int build_dft_tables(zest_gpu_context* ctx, SplitState* st, int L, int N, int S,
     ZG_TRY(gen(L, L, 0, 0, 0, t->cos_f));
     if (L > 1) ZG_TRY(gen(L - 1, L - 1, 1, 1, 1, t->sin_f));
     // backward: cos rows i in [0,L), cols m in [0,L); sin rows i in [1,L), cols m in [1,L)
-    ZG_TRY(gen(L, L, 0, 0, 2, t->cos_b));
-    if (L > 1) ZG_TRY(gen(L - 1, L - 1, 1, 1, 3, t->sin_b));
+    // (K-chunked sums, orders above 256; single sums use the joint tables below)
+    if (L > KCHUNK || L == 1) ZG_TRY(gen(L, L, 0, 0, 2, t->cos_b));
+    if (L > KCHUNK) ZG_TRY(gen(L - 1, L - 1, 1, 1, 3, t->sin_b));
+    if (L > 1 && L <= KCHUNK) {
+        // both inverse tables over all rows i and m, sliced in one job with shared row
+        // exponents (the earlier tables' slicing jobs are queued before these writes)
+        ZG_CUDA_TRY(cudaStreamSynchronize(s));
+        double* P = tmp;
+        double* Q = P + (size_t)L * ld;
+        dim3 grid((ld + 127) / 128, L);
+        dft_table_kernel<<<grid, 128, 0, s>>>(P, L, L, ld, N, 0, 0, 2);
+        ZG_TRY(launch_check("dft_table_kernel"));
+        dft_table_kernel<<<grid, 128, 0, s>>>(Q, L, L, ld, N, 0, 0, 3);
+        ZG_TRY(launch_check("dft_table_kernel"));
+        ZG_TRY(t->cos_bj.ensure(L, r16(L), S));
+        ZG_TRY(t->sin_bj.ensure(L, r16(L), S));
+        ZG_TRY(launch_slice2(s, TablePairLoader{P, Q, ld}, L, L, L - 1, 1, S, 8, SL_PAIR, t->cos_bj, t->sin_bj));
+    }
     ZG_CUDA_TRY(cudaStreamSynchronize(s));
     *out = t.get();
     st->dft_tables.emplace(key, std::move(t));
@@ -1898,6 +2022,25 @@ int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t
     {
         StageScope sc(ctx, ST_SPLIT_SLICE);
         ZG_TRY(launch_slice2(ctx->stream, ld, rows, Lg, Lg - 1, 1, S, bits, SL_PAIR, st->op[0], st->op[1]));
+    }
+    if (Lg > 1 && Lg <= KCHUNK && t.cos_bj.rows) {
+        // single sums: the cos and sin results combined in integers
+        long long* Ts = reinterpret_cast<long long*>(Cs);
+        UnitList* u;
+        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 4 + nt_pass(NT)), [&](UnitList& ul) {
+            for (long long r = 0; r < rows; r += SP_M)
+                add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 0, Lg, NT, Lg, 0, 0, 0);
+        }, &u));
+        ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], t.cos_bj, t.sin_bj,
+                           EpiDftBwdCosRaw{grids, Ts, C, N, Lg, gsz}));
+        UnitList* v;
+        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 5 + nt_pass(NT)), [&](UnitList& ul) {
+            for (long long r = 0; r < rows; r += SP_M)  // sin rows i = 1 + (0 .. Lg - 2) of the joint table
+                add_units(ul, S, bits, r, std::min<long long>(SP_M, rows - r), 1, Lg - 1, NT, Lg - 1, 1 | 2 | 4, 0,
+                          0);
+        }, &v));
+        return run_gemm_nt(ctx, NT, S, *v, st->op[0], st->op[1], t.cos_bj, t.sin_bj,
+                           EpiDftBwdSinRaw{grids, Ts, C, N, Lg, gsz});
     }
     for (int ch = 0; ch < nchunks(Lg); ++ch) {
         const int k0 = ch * KCHUNK;
@@ -2285,7 +2428,7 @@ int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int b
                              },
                              &u));
             // conjugated for the inverse DFT of a LonLat grid; the unfolding conjugates
-            const double sgi = lonlat ? -1.0 : 1.0;
+            const unsigned long long sgi = lonlat ? (1ull << 63) : 0ull;
             if (ch == 0)
                 return run_gemm_st<NT>(ctx, *u, tb->leg_bT, st->op[0], st->op[1],
                                        EpiStLegBwdE<false>{E, batch, Lg, kh, sgi});
@@ -2375,7 +2518,7 @@ int build_rot_tables(zest_gpu_context* ctx, SplitState* st, const double* wig, i
     return ZEST_GPU_OK;
 }
 
-// row v = vecs[v] = {item, n, l}: k = m: r2c(c_m) e^{-i m gamma'} (Re, Im)
+// row v = vecs[v] = {item, n, l, base}: k = m: r2c(c_m) e^{-i m gamma'} (Re, Im)
 struct RotInLoader {
     static constexpr bool ROW_FAST = false, TWO = true;
     static constexpr int MODE = SL_PAIR, SHIFT = 0;
@@ -2387,7 +2530,7 @@ struct RotInLoader {
     struct Row { const double* c; const double2* pg; int l; };
     __device__ Row row(long long r) const {
         const int4 w = vecs[r];
-        return Row{coeffs + coff[w.x] + 2 * zidx(w.y, w.z, 0), ph + ((long long)w.x * 3 + 2) * Lmax, w.z};
+        return Row{coeffs + coff[w.x] + 2 * (long long)w.w, ph + ((long long)w.x * 3 + 2) * Lmax, w.z};
     }
     __device__ void get(const Row& R, int k, double& up, double& dn) const {
         if (k > R.l) {
@@ -2454,7 +2597,7 @@ __global__ void rot_out_kernel(long long nvec, const int4* __restrict__ vecs, co
     if (v >= nvec) return;
     const int lane = threadIdx.x & 31;
     const int4 w = vecs[v];
-    double* c = coeffs + coff[w.x] + 2 * zidx(w.y, w.z, 0);
+    double* c = coeffs + coff[w.x] + 2 * (long long)w.w;
     const double2* pa = ph + ((long long)w.x * 3 + 0) * Lmax;
     const double* u = U + v * 2LL * Lmax;
     const double sq2 = 1.41421356237309504880168872420969808;

@@ -34,11 +34,13 @@ int split_st_forward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int ba
                      double* coeffs, long long csz);
 int split_st_backward(zest_gpu_context* ctx, StPlan& plan, int Lg, int Lm, int batch, const double* coeffs,
                       long long csz, double* X, double* grids);
-// Rotor::rotate of a ragged batch of real Zernike expansions with the two
-// X(+-pi/2) products of every rotated vector as split GEMMs (orders up to
-// 256): vecs = the {item, n, l} vectors sorted by l, vector rows
-// [voff[l], voff[l+1]) of order l; coff = each item's coefficient offset;
-// phase = scratch for the [item][3][Lmax] phase tables.
+// Rotor::rotate of a batch of real expansions (Zernike, SH or row-skipping,
+// of equal or different orders) with the two X(+-pi/2) products of every
+// rotated vector as split GEMMs (orders up to 256): vecs = the
+// {item, n, l, first coefficient of the vector within its item} vectors
+// sorted by l, vector rows [voff[l], voff[l+1]) of order l; coff = each
+// item's coefficient offset; phase = scratch for the [item][3][Lmax] phase
+// tables.
 int split_rotate_ragged(zest_gpu_context* ctx, int Lmax, int items, long long nvec, const int4* vecs,
                         const std::vector<long long>& voff, const long long* coff, double* coeffs, const double* wig,
                         const double* euler, int type, double* phase);
@@ -51,6 +53,9 @@ void split_flops(zest_gpu_context* ctx, bool reset, double* useful, double* issu
 // Synchronizes the context stream and reports (and clears) a bounded-wait
 // timeout recorded by the split GEMMs launched since the last check.
 int split_check_flag(zest_gpu_context* ctx);
+// End of a split-path call: split_check_flag, except while the stream is
+// being captured into a graph (whose replays are checked by the caller).
+int split_finish(zest_gpu_context* ctx);
 // Makes one bounded mbarrier wait run out after limit_ns (nothing arrives on
 // it) and reports it as the GEMMs' timeouts are reported: ZEST_GPU_ERR_TIMEOUT.
 int split_wait_selftest(zest_gpu_context* ctx, long long limit_ns);

@@ -567,12 +567,53 @@ static int get_vectors(zest_gpu_context* ctx, int kind, int L, const int2** out,
     return ZEST_GPU_OK;
 }
 
+// The rotated vectors of `batch` expansions of one order, sorted by l, for
+// the split-precision rotation (cached per kind, order and batch).
+static int get_uniform_rotation(zest_gpu_context* ctx, int kind, int L, int batch, UniformRotation** out) {
+    auto key = std::make_tuple(kind, L, batch);
+    auto it = ctx->uniform_rot.find(key);
+    if (it == ctx->uniform_rot.end()) {
+        auto u = std::make_unique<UniformRotation>();
+        std::vector<int4> v;
+        u->voff.assign((size_t)L + 1, 0);
+        for (int l = 0; l < L; ++l) {
+            for (int b = 0; b < batch; ++b) {
+                if (kind == 0) {
+                    for (int n = (l == 0 ? 2 : l); n < L; n += 2) v.push_back(make_int4(b, n, l, int(zidx(n, l, 0))));
+                } else if (kind == 2) {
+                    if ((l & 1) == ((L - 1) & 1)) v.push_back(make_int4(b, L - 1, l, int(((long long)l * l) >> 2)));
+                } else if (l >= 1) {
+                    v.push_back(make_int4(b, l, l, int(tri_idx(l, 0))));
+                }
+            }
+            u->voff[(size_t)l + 1] = (long long)v.size();
+        }
+        std::vector<long long> coff((size_t)batch);
+        for (int b = 0; b < batch; ++b) coff[(size_t)b] = (long long)b * 2 * coeff_pairs(kind, L);
+        u->nvec = (long long)v.size();
+        ZG_TRY(upload(u->vecs, v, ctx->stream));
+        ZG_TRY(upload(u->coff, coff, ctx->stream));
+        it = ctx->uniform_rot.emplace(key, std::move(u)).first;
+    }
+    *out = it->second.get();
+    return ZEST_GPU_OK;
+}
+
 int rotate_dev(zest_gpu_context* ctx, int kind, int L, int batch, double* coeffs, const double* euler, int type) {
     // a whole expansion of order 1 has nothing to rotate; the row span of
     // order 1 (n = 0) still rotates its l = 0 vector, as the reference does
     if (batch == 0 || L < 1 || (L == 1 && kind != 2)) return ZEST_GPU_OK;
     const double* wig;
     ZG_TRY(get_wigner(ctx, L, &wig));
+    if (ctx->precision == ZEST_PRECISION_SPLIT && L <= 256 && L >= 2) {
+        // the X(+-pi/2) products of all vectors of one l as split GEMMs
+        UniformRotation* u;
+        ZG_TRY(get_uniform_rotation(ctx, kind, L, batch, &u));
+        ZG_TRY(ctx->phase.ensure((size_t)batch * 6 * L * sizeof(double)));
+        ZG_TRY(split_rotate_ragged(ctx, L, batch, u->nvec, u->vecs.as<int4>(), u->voff, u->coff.as<long long>(),
+                                   coeffs, wig, euler, type, ctx->phase.as<double>()));
+        return split_finish(ctx);
+    }
     const int2* vl;
     int nvec;
     ZG_TRY(get_vectors(ctx, kind, L, &vl, &nvec));
@@ -833,8 +874,8 @@ static int ragged_on_graph_stream(zest_gpu_context* ctx, int zn, int sn, int sp,
         np->Lmax = std::max(np->Lmax, L);
         if (np->buckets.empty() || std::get<0>(np->buckets.back()) != L) np->buckets.emplace_back(L, i, 0);
         ++std::get<2>(np->buckets.back());
-        for (int l = 0; l < L; ++l)  // the rotated (n, l) vectors, as get_vectors
-            for (int nn = (l == 0 ? 2 : l); nn < L; nn += 2) work.push_back(make_int4(i, nn, l, 0));
+        for (int l = 0; l < L; ++l)  // the rotated (n, l) vectors, as get_vectors, with their first coefficient
+            for (int nn = (l == 0 ? 2 : l); nn < L; nn += 2) work.push_back(make_int4(i, nn, l, int(zidx(nn, l, 0))));
     }
     np->coff_h[n] = co;
     np->goff_h[n] = go;
