@@ -320,10 +320,12 @@ int zest_gpu_zt_rotate_noalloc(void* stream, size_t order, size_t batch, double*
 int zest_gpu_zt_rotate_backward_ragged(zest_gpu_context* ctx, int zernike_norm, int sh_norm, int sh_phase,
                                        size_t n_items, const int* orders, double* coeffs, const double* euler,
                                        int rotation_type, double* grids);
-/* Autotuning of the FP64 contraction tile shapes: when enabled (the default),
- * the first run of each Zernike stage at a new size times the candidate shapes
- * on the context stream and keeps the fastest; disabled, a size rule picks
- * them.  The shapes change only how the output is tiled, not any result. */
+/* Autotuning of the contraction tile shapes: when enabled (the default), the
+ * first run of each Zernike stage at a new size times the candidate shapes on
+ * the context stream and keeps the fastest (the FP64 tile shapes; in
+ * ZEST_PRECISION_SPLIT the column tile, 80 or 32, of each single-sum tensor
+ * core stage); disabled, a size rule picks them.  The shapes change only how
+ * the output is tiled, not any result. */
 int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable);
 /* Pipelining of host-memory Zernike transforms (mem = ZEST_MEM_HOST): a
  * batch whose per-item input or output exceeds `bytes` in total is cut into

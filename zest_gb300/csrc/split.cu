@@ -1487,6 +1487,7 @@ struct SplitState {
     DevBuf cycles;              // role wait counters, kept when ZEST_GPU_SPLIT_CYCLES is set
     bool cycles_on = false;
     int narrow = 32;            // widest unit (valid table rows) run as one MMA per product
+    std::map<std::tuple<int, int, int, int>, int> tuned;  // timed column tile per (stage, Lg, Lm, batch)
     int nt[16];                 // column tile of each work-list stage: 0 = chosen per launch, or 32 / 80
     SplitState();
     double useful_flops = 0.0, issued_flops = 0.0;  // accumulated while profiling
@@ -1960,13 +1961,61 @@ inline int stage_nt(const SplitState* st, int wk, int S, int ncols) {
 }
 inline int nt_pass(int nt) { return nt == 32 ? 1 << 16 : 0; }
 
+// Runs one split GEMM stage, `launch(nt)`, with its column tile: a tuning
+// override (ZEST_GPU_SPLIT_NT) if set; else, with the context's autotuner on,
+// outside graph capture and for a stage whose launches overwrite their
+// outputs (single sums), the faster of 80 and 32, timed with CUDA events on
+// the context stream at the stage's first run at this size (each candidate
+// once untimed, then once timed; the tile changes no result); else the rule
+// of stage_nt.
+template <class Launch>
+int tuned_stage(zest_gpu_context* ctx, SplitState* st, int wk, int S, int Lg, int Lm, int batch, int ncols,
+                bool idempotent, Launch&& launch) {
+    int nt = stage_nt(st, wk, S, ncols);
+    if (S != 6 || st->nt[wk] || !ctx->autotune || !idempotent) return launch(nt);
+    const auto key = std::make_tuple(wk, Lg, Lm, batch);
+    auto it = st->tuned.find(key);
+    if (it != st->tuned.end()) return launch(it->second);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    ZG_CUDA_TRY(cudaStreamIsCapturing(ctx->stream, &cap));
+    if (cap != cudaStreamCaptureStatusNone) return launch(nt);
+    cudaEvent_t e0, e1;
+    ZG_CUDA_TRY(cudaEventCreate(&e0));
+    ZG_CUDA_TRY(cudaEventCreate(&e1));
+    const bool prof = ctx->prof.on;  // the timing runs stay out of the stage profile
+    ctx->prof.on = false;
+    const int cand[2] = {80, 32};
+    float best = 0.0f;
+    int rc = ZEST_GPU_OK;
+    for (int i = 0; i < 2 && rc == ZEST_GPU_OK; ++i) {
+        rc = launch(cand[i]);
+        if (rc == ZEST_GPU_OK && cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = fail(ZEST_GPU_ERR_CUDA, "event");
+        if (rc == ZEST_GPU_OK) rc = launch(cand[i]);
+        if (rc == ZEST_GPU_OK && cudaEventRecord(e1, ctx->stream) != cudaSuccess) rc = fail(ZEST_GPU_ERR_CUDA, "event");
+        float ms = 0.0f;
+        if (rc == ZEST_GPU_OK &&
+            (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+            rc = fail(ZEST_GPU_ERR_CUDA, "split tile autotuner: timing failed");
+        if (rc == ZEST_GPU_OK && (i == 0 || ms < best)) {
+            best = ms;
+            nt = cand[i];
+        }
+    }
+    ctx->prof.on = prof;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != ZEST_GPU_OK) return rc;
+    st->tuned.emplace(key, nt);
+    return launch(nt);
+}
+
 // Longitude DFT of `batch` grids x[b][lon][col] (C columns, item stride gsz)
 // to the spectra G[b][m][col][re, im], m < Lm (L = Lg orders per item):
 // folded cos/sin products (x_k + x_{N-k} against cos, x_k - x_{N-k} against
 // sin), K-chunked.  `wk` keys the work lists of the caller's grid family.
 int dft_forward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t, int S, int wk, const double* grids,
                       long long gsz, int C, int N, int Lg, int Lm, int batch, double* G) {
-    const int NT = stage_nt(st, wk, S, Lm), bits = digit_bits(Lg);
+    const int bits = digit_bits(Lg);
     const long long rows = (long long)batch * C;
     ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
     ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
@@ -1975,22 +2024,27 @@ int dft_forward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t,
         ZG_TRY(launch_slice2(ctx->stream, DftFwdLoader{grids, gsz, C, N}, rows, Lg, Lg - 1, 1, S, bits, SL_FOLD,
                              st->op[0], st->op[1]));
     }
-    for (int ch = 0; ch < nchunks(Lg); ++ch) {
-        const int k0 = ch * KCHUNK;
-        UnitList* u;
-        ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 8 * ch + nt_pass(NT)), [&](UnitList& ul) {
-            for (long long r = 0; r < rows; r += SP_M) {
-                const long long rr = std::min<long long>(SP_M, rows - r);
-                add_units(ul, S, bits, r, rr, 0, Lm, NT, std::min(KCHUNK, Lg - k0), 0, 0, k0);
-                if (Lm > 1) add_units(ul, S, bits, r, rr, 0, Lm - 1, NT, std::min(KCHUNK, Lg - 1 - k0), 1 | 2, 0, k0);
-            }
-        }, &u));
-        if (ch == 0)
-            ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], t.cos_f, t.sin_f, EpiDftFwd<false>{G, C, Lg}));
-        else
-            ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], t.cos_f, t.sin_f, EpiDftFwd<true>{G, C, Lg}));
-    }
-    return ZEST_GPU_OK;
+    return tuned_stage(ctx, st, wk, S, Lg, Lm, batch, Lm, nchunks(Lg) == 1, [&](int NT) -> int {
+        for (int ch = 0; ch < nchunks(Lg); ++ch) {
+            const int k0 = ch * KCHUNK;
+            UnitList* u;
+            ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 8 * ch + nt_pass(NT)), [&](UnitList& ul) {
+                for (long long r = 0; r < rows; r += SP_M) {
+                    const long long rr = std::min<long long>(SP_M, rows - r);
+                    add_units(ul, S, bits, r, rr, 0, Lm, NT, std::min(KCHUNK, Lg - k0), 0, 0, k0);
+                    if (Lm > 1)
+                        add_units(ul, S, bits, r, rr, 0, Lm - 1, NT, std::min(KCHUNK, Lg - 1 - k0), 1 | 2, 0, k0);
+                }
+            }, &u));
+            if (ch == 0)
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], t.cos_f, t.sin_f,
+                                   EpiDftFwd<false>{G, C, Lg}));
+            else
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], t.cos_f, t.sin_f,
+                                   EpiDftFwd<true>{G, C, Lg}));
+        }
+        return ZEST_GPU_OK;
+    });
 }
 
 // The parity sums E_p[b][m][j][kc] (kc < nr2) a Legendre stage leaves
@@ -2015,7 +2069,7 @@ int zero_parity_tails(zest_gpu_context* ctx, double* E, int batch, int Lg, int L
 int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t, int S, int wk,
                        const DftBwdLoader& ld, int C, int N, int Lg, int Lm, int batch, double* grids, long long gsz,
                        double* Cs) {
-    const int NT = stage_nt(st, wk, S, Lg), bits = digit_bits(Lg);
+    const int bits = digit_bits(Lg);
     const long long rows = (long long)batch * C;
     ZG_TRY(st->op[0].ensure(rows, r16(Lg), S));
     ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
@@ -2024,7 +2078,9 @@ int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t
         ZG_TRY(launch_slice2(ctx->stream, ld, rows, Lg, Lg - 1, 1, S, bits, SL_PAIR, st->op[0], st->op[1]));
     }
     if (Lg > 1 && Lg <= KCHUNK && t.cos_bj.rows) {
-        // single sums: the cos and sin results combined in integers
+      // single sums: the cos and sin results combined in integers (the pair of
+      // launches overwrites its outputs: tuned)
+      return tuned_stage(ctx, st, wk, S, Lg, Lm, batch, Lg, true, [&](int NT) -> int {
         long long* Ts = reinterpret_cast<long long*>(Cs);
         UnitList* u;
         ZG_TRY(get_units(ctx, std::make_tuple(wk, Lg, Lm, batch, S, 4 + nt_pass(NT)), [&](UnitList& ul) {
@@ -2041,7 +2097,9 @@ int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t
         }, &v));
         return run_gemm_nt(ctx, NT, S, *v, st->op[0], st->op[1], t.cos_bj, t.sin_bj,
                            EpiDftBwdSinRaw{grids, Ts, C, N, Lg, gsz});
+      });
     }
+    const int NT = stage_nt(st, wk, S, Lg);
     for (int ch = 0; ch < nchunks(Lg); ++ch) {
         const int k0 = ch * KCHUNK;
         UnitList* u;
@@ -2161,7 +2219,6 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
     ZG_TRY(dft_forward_stage(ctx, st, *tb->dft, S, WK_DFT_F, grids, sh.size(), C, N, Lg, Lm, batch, G));
     // ---- Legendre (folded over the equator) ----
     {
-        const int NT = stage_nt(st, WK_LEG_F, S, (Lm + 1) / 2);
         const int bits = digit_bits(kh);
         const long long per_m = (long long)batch * nr2;
         const long long rows = (long long)Lm * per_m;
@@ -2172,6 +2229,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
             LegFwdLoader ld{G, batch, Lg, nt, nr2, plan.leg.j0u, plan.leg.j0d};
             ZG_TRY(launch_slice2(s, ld, rows, kh, kh, 0, S, bits, SL_FOLD, st->op[0], st->op[1]));
         }
+        ZG_TRY(tuned_stage(ctx, st, WK_LEG_F, S, Lg, Lm, batch, (Lm + 1) / 2, nchunks(kh) == 1, [&](int NT) -> int {
         for (int ch = 0; ch < nchunks(kh); ++ch) {
             const int k0 = ch * KCHUNK;
             UnitList* u;
@@ -2188,10 +2246,11 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
             else
                 ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], tb->leg_f, tb->leg_f, EpiLegFwd<true>{flm, batch, nr2}));
         }
+        return ZEST_GPU_OK;
+        }));
     }
     // ---- radial ----
     {
-        const int NT = stage_nt(st, WK_RAD_F, S, (Lm + 1) / 2);
         const int bits = digit_bits(nr);
         const long long rows = tri_size(Lm) * batch * 2;
         ZG_TRY(st->op[0].ensure(rows, r16(nr), S));
@@ -2199,6 +2258,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
             StageScope sc(ctx, ST_SPLIT_SLICE);
             ZG_TRY(launch_slice(s, RadFwdLoader{flm, nr}, rows, nr, S, bits, st->op[0]));
         }
+        ZG_TRY(tuned_stage(ctx, st, WK_RAD_F, S, Lg, Lm, batch, (Lm + 1) / 2, nchunks(nr) == 1, [&](int NT) -> int {
         for (int ch = 0; ch < nchunks(nr); ++ch) {
             const int k0 = ch * KCHUNK;
             UnitList* u;
@@ -2212,6 +2272,8 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
             else
                 ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->rad_f, tb->rad_f, EpiRadFwd<true>{coeffs, batch, csz}));
         }
+        return ZEST_GPU_OK;
+        }));
     }
     return split_finish(ctx);
 }
@@ -2240,7 +2302,6 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
 
     // ---- radial: coefficients -> flm ----
     {
-        const int NT = stage_nt(st, WK_RAD_B, S, nr);
         const int bits = digit_bits((Lg + 1) / 2);
         const long long rows = tri_size(Lm) * batch * 2;
         ZG_TRY(st->op[0].ensure(rows, kl, S));
@@ -2249,6 +2310,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             ZG_TRY(launch_slice(s, RadBwdLoader{coeffs, csz, batch, Lm}, rows, (Lm + 1) / 2, S, bits,
                                 st->op[0]));
         }
+        ZG_TRY(tuned_stage(ctx, st, WK_RAD_B, S, Lg, Lm, batch, nr, nchunks((Lm + 1) / 2) == 1, [&](int NT) -> int {
         for (int ch = 0; ch < nchunks((Lm + 1) / 2); ++ch) {
             const int k0 = ch * KCHUNK;
             UnitList* u;
@@ -2262,10 +2324,11 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
             else
                 ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<true>{flm, nr}));
         }
+        return ZEST_GPU_OK;
+        }));
     }
     // ---- Legendre: flm -> G (north/south unfold; parity 1 read-modify-write) ----
     {
-        const int NT = stage_nt(st, WK_LEG_B, S, kh);
         const int bits = digit_bits((Lg + 1) / 2);
         const long long per_m = (long long)batch * nr2;
         const long long rows = (long long)Lm * per_m;
@@ -2277,6 +2340,7 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                                  SL_PAIR, st->op[0], st->op[1]));
         }
         ZG_TRY(zero_parity_tails(ctx, E, batch, Lg, Lm, kh, nr2));
+        ZG_TRY(tuned_stage(ctx, st, WK_LEG_B, S, Lg, Lm, batch, kh, nchunks((Lm + 1) / 2) == 1, [&](int NT) -> int {
         for (int p = 0; p < 2; ++p)
             for (int ch = 0; ch < nchunks((Lm + 1) / 2); ++ch) {
             const int k0 = ch * KCHUNK;
@@ -2296,6 +2360,8 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                 ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[1], tb->leg_bT, tb->leg_bT,
                                 EpiLegBwdE<true>{E, batch, Lg, kh, nr2}));
         }
+        return ZEST_GPU_OK;
+        }));
     }
     // ---- longitude: inverse real DFT, cos pass then sin read-modify-write pass ----
     // (the cos sums C_i go to the scratch of the parity sums, consumed by the slicing)
