@@ -163,6 +163,12 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t (&r)[4]) {
                  : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// a * b + c with a 32 x 32 -> 64-bit signed product
+__device__ __forceinline__ long long mad_wide_s32(int a, int b, long long c) {
+    long long r;
+    asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(r) : "r"(a), "r"(b), "l"(c));
+    return r;
+}
 
 // K-major operand tile, SWIZZLE_32B: rows of 32 bytes, 8-row groups 256 bytes apart.
 __device__ __forceinline__ uint64_t desc_sw32(uint32_t saddr) {
@@ -224,28 +230,6 @@ __device__ __forceinline__ double i64_ldexp(long long T, int E) {
     return (a == 0 || eff <= 0) ? 0.0 : v;
 }
 
-// fixed point: round(x 2^{nbits-e}) as int64 (|x| < 2^(e-1)), ties away from
-// zero.  The row exponents leave at least one bit of headroom above every
-// element, so the shift is at least 6.  Without branches: q = |x| 2^{nbits-e+1}
-// truncated (one bit more than kept), then ((q ^ s) + 1) >> 1 with s the sign
-// mask (arithmetic shift) is floor(q/2 + 1/2) for x >= 0 and its negative for
-// x < 0.  The implicit bit is set for a zero or subnormal x too: the slicing
-// keeps every row exponent at or above 64 - 1021, where their shift is at
-// least 53 and q = 0.
-__device__ __forceinline__ long long to_fixed(double x, int e, int nbits) {
-    const long long bits = __double_as_longlong(x);
-    const int E = int((unsigned long long)bits >> 52) & 0x7FF;
-    const unsigned long long M = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh1 = min(max(1074 + e - nbits - E, 0), 62);  // the shift less one
-    const long long q = (long long)(M >> sh1);
-    const long long sg = bits >> 63;  // 0 or -1
-    return ((q ^ sg) + 1) >> 1;
-}
-
-__device__ __forceinline__ int biased_exp(double x) {
-    return int(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FF);
-}
-
 }  // namespace
 
 // ===========================================================================
@@ -255,7 +239,7 @@ namespace {
 
 constexpr int SL_KMAX = 2048;  // longest operand row the slicing stages (and longest sum)
 constexpr int SL_K8MAX = 256;  // K bound of exact level sums with balanced 8-bit digits
-constexpr int SL_UNROLL = 8;   // independent loads per thread in the staging loops
+constexpr int SL_UNROLL = 8;   // independent loads per thread in the staging loops (halved for 4 inputs)
 
 // Digits are 8 bits wide at any length: sums longer than SL_K8MAX terms run
 // as K-chunks of at most SL_K8MAX whose FP64 results are added.
@@ -281,9 +265,8 @@ int set_attributes_once(Kern kern, Set&& set) {
 
 // Rows per slicing block: a power of two (so that in row-fast loops every
 // thread stays on one row), up to 32 rows (longer contiguous runs in the
-// row-fast loads), with the staged FP64 rows within 96 KB.
-inline int slice_rows_per_block(int K, bool two) {
-    const int per_row = K * (two ? 16 : 8);
+// row-fast loads), with the staged FP64 rows (row_bytes each) within 96 KB.
+inline int slice_rows_per_block(int row_bytes) {
     // ZEST_GPU_SLICE_ROWS (a power of two up to 32) caps the rows per block,
     // to measure the trade between longer row-fast reads and blocks per SM
     static const int cap = [] {
@@ -292,11 +275,11 @@ inline int slice_rows_per_block(int K, bool two) {
         return (v >= 1 && v <= 32 && (v & (v - 1)) == 0) ? v : 32;
     }();
     int r = cap;
-    while (r > 1 && r * per_row > 96 * 1024) r >>= 1;
+    while (r > 1 && r * row_bytes > 96 * 1024) r >>= 1;
     return r;
 }
 
-enum { SL_ONE = 0, SL_FOLD = 1, SL_PAIR = 2 };
+enum { SL_ONE = 0, SL_FOLD = 1, SL_PAIR = 2, SL_PFOLD = 3 };
 
 // Loaders give the pair (up, dn) of operand element (row, k) through a per-row
 // handle computed once per block row.  ROW_FAST loaders read consecutive rows
@@ -446,38 +429,46 @@ struct StLegBwdLoader {
 // latitude lat (the sin operand takes Im F_k at k - 1), formed from the two
 // parity sums E_p[b][m][j'][2 rad + {re, im}] of the Legendre stage: E_0 + E_1
 // at the north node lat = j0u + j', E_0 - E_1 at the south node lat = j0d - j'
-// (the equator, j0u = j0d, is north).
+// (the equator, j0u = j0d, is north).  The sums are formed exactly in
+// integers by the slicing (SL_PFOLD): the loader gives (Re E_0, Im E_0,
+// Re E_1, Im E_1), E_1 negated for a south row by a sign-bit flip.
 struct DftBwdLoader {
     static constexpr bool ROW_FAST = true, TWO = true;
-    static constexpr int MODE = SL_PAIR, SHIFT = 1;
+    static constexpr int MODE = SL_PFOLD, SHIFT = 1;
     const double* E;
     int L, C, nrad, kh, j0u, j0d, B;
-    struct Row { const double* e0; double sg; };
+    struct Row { const double* e0; int neg; };  // neg: the sign bit of E_1's high word
     __device__ Row row(long long r) const {
         const long long b = r / C;
         const int col = int(r - b * C);
         const int lat = col / nrad, rad = col - lat * nrad;
         const bool north = lat >= j0u;
         const int jf = north ? lat - j0u : j0d - lat;
-        return Row{E + ((b * L) * kh + jf) * (2LL * nrad) + 2 * rad, north ? 1.0 : -1.0};
+        return Row{E + ((b * L) * kh + jf) * (2LL * nrad) + 2 * rad, north ? 0 : int(0x80000000u)};
     }
-    __device__ void get(const Row& R, int k, double& up, double& dn) const {
+    __device__ void get4(const Row& R, int k, double* v) const {
         const long long mo = (long long)k * kh * 2 * nrad;
         const double2 a = *reinterpret_cast<const double2*>(R.e0 + mo);
         const double2 c = *reinterpret_cast<const double2*>(R.e0 + mo + (long long)B * L * kh * 2 * nrad);
-        up = a.x + R.sg * c.x;
-        dn = a.y + R.sg * c.y;
+        v[0] = a.x;
+        v[1] = a.y;
+        v[2] = __hiloint2double(__double2hiint(c.x) ^ R.neg, __double2loint(c.x));
+        v[3] = __hiloint2double(__double2hiint(c.y) ^ R.neg, __double2loint(c.y));
     }
 };
 
 // One slicing job: one operand array (SL_ONE) or two from one read of the
-// input (SL_FOLD: up + dn and up - dn; SL_PAIR: up and dn), the second at
-// index k - shift.  Both share the row exponents.  Each loader fixes its mode
-// and shift (Loader::MODE, Loader::SHIFT), so the kernel is specialised.
+// input (SL_FOLD: up + dn and up - dn; SL_PAIR: up and dn; SL_PFOLD: the
+// sums of two pairs), the second at index k - shift.  Both share the row
+// exponents.  Each loader fixes its mode and shift (Loader::MODE,
+// Loader::SHIFT), so the kernel is specialised.
 struct SliceJob {
     long long rows;
-    int K;       // staged k range (K0, and K1 + shift for the second array)
-    int S, bits, R, lr, copies;  // lr = log2(R)
+    int K;            // longest valid k of any staged input (loads stop there)
+    int Ku, Kd;       // inputs of the first array are zero from Ku on, of the second from Kd on
+    int KS;           // staged k range: max(Kp0, Kp1) + shift, the rest zero
+    int Ks;           // shared-memory row stride in doubles (padded layout, below)
+    int S, bits, R, lr;  // lr = log2(R)
     int K0, Kp0, K1, Kp1;
     __nv_bfloat16* out0;
     __nv_bfloat16* out1;
@@ -486,212 +477,255 @@ struct SliceJob {
     int* ex1;
 };
 
-// BF16 bits of the small integer d (|d| <= 2^8) times 2^{-sh}: the float is
-// exact and has at most 8 significant bits, so its upper half is the BF16.
-__device__ __forceinline__ uint32_t digit_f32_bits(int d, float scale) {
-    const float f = (__int_as_float(0x4B400000 + d) - 12582912.0f) * scale;
-    return __float_as_uint(f);
+// Staged inputs per operand row: 1 (SL_ONE), 2 (SL_FOLD, SL_PAIR) or 4 (SL_PFOLD).
+template <class Loader>
+__host__ __device__ constexpr int staged_arrays() {
+    return Loader::MODE == SL_ONE ? 1 : (Loader::MODE == SL_PFOLD ? 4 : 2);
 }
 
-// Balanced 8-bit digits of two neighbouring elements (slice 0 most
-// significant) written as BF16 pairs: one 4-byte store per slice and copy.
-// Adding 128 sum_{i<S-1} 256^i turns the lower balanced digits into the plain
-// bytes of the sum (digit = byte - 128) and leaves the leading digit as the
-// sum shifted down.  A lower digit's float is built by one byte permute,
-// 0x4B4000bb = 2^23 + 2^22 + byte, and one subtraction of 2^23 + 2^22 + 128.
+// Shared-memory position of element k of a staged row: one double of padding
+// after every 8, so that the lanes of a warp reading 8 consecutive elements
+// each at neighbouring chunks (stride 9 doubles) hit distinct banks.
+__device__ __forceinline__ int sl_pos(int k) { return k + (k >> 3); }
+
+// Row stride of the staged rows: room for KS padded elements, and 2 mod 4
+// doubles, so that the row-fast staging (16 rows x 2 k per warp) stores
+// conflict-free.
+inline int sl_row_stride(int KS) {
+    const int p = KS + (KS >> 3) + 1;
+    return p + ((6 - p % 4) % 4);
+}
+
+// fixed point: round(x 2^{nbits-e}) as int64 (|x| < 2^(e-1)), ties away from
+// zero, with Cr = 1074 + e - nbits.  q = |x| 2^{nbits-e+1} truncated (one bit
+// more than kept), then ((q ^ s) + 1) >> 1 with s the sign mask is
+// floor(q/2 + 1/2) for x >= 0 and its negative for x < 0.  The shift
+// Cr - E(x) is at least 5 for every element of a row (the row exponent keeps
+// a bit of headroom); PTX shifts of 64 or more give 0, so a zero or an element
+// far below the row's largest rounds to 0 without a branch.
+__device__ __forceinline__ long long to_fixed_c(double x, int Cr) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const unsigned E = unsigned(bits >> 52) & 0x7FFu;
+    const unsigned long long M = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    unsigned long long q;
+    asm("shr.b64 %0, %1, %2;" : "=l"(q) : "l"(M), "r"(unsigned(Cr) - E));
+    const long long sg = (long long)bits >> 63;  // 0 or -1
+    return (((long long)q ^ sg) + 1) >> 1;
+}
+
+// Balanced 8-bit digits of 8 neighbouring elements (slice 0 most
+// significant), written as 8 BF16 per slice with one 16-byte store.  Adding
+// 128 sum_{i<S-1} 256^i turns the lower balanced digits into the plain bytes
+// of the sum (digit = byte - 128) and leaves the leading digit as the sum
+// shifted down.  A lower digit's float is built by one byte permute,
+// 0x4B4000bb = 2^23 + 2^22 + byte, and one subtraction of 2^23 + 2^22 + 128;
+// the float is exact with at most 8 significant bits, so its upper half is the
+// BF16.
 template <int S>
-__device__ __forceinline__ void write_digits2(long long w0, long long w1, int copies, __nv_bfloat16* out,
-                                              long long stride, long long off, bool active) {
+__device__ __forceinline__ void store_digits8(const long long (&w)[8], __nv_bfloat16* out, long long stride) {
     constexpr long long OFF = (long long)((0x8080808080808080ull) >> (8 * (9 - S)));  // 128 per lower byte
-    float f[2][S];
-    const long long u[2] = {w0 + OFF, w1 + OFF};
+    uint32_t lo[8], hi[8];
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-        const uint32_t lo = uint32_t(u[q]), hi = uint32_t((unsigned long long)u[q] >> 32);
-#pragma unroll
-        for (int s = 1; s < S; ++s) {
-            const int b = S - 1 - s;  // byte of the sum holding digit s
-            f[q][s] = __int_as_float(int(__byte_perm(b < 4 ? lo : hi, 0x4B400000u, 0x7650u | (b & 3)))) - 12583040.0f;
-        }
-        f[q][0] = __uint_as_float(digit_f32_bits(int(u[q] >> (8 * (S - 1))), 1.0f));
+    for (int q = 0; q < 8; ++q) {
+        const unsigned long long u = (unsigned long long)(w[q] + OFF);
+        lo[q] = uint32_t(u);
+        hi[q] = uint32_t(u >> 32);
     }
-    uint32_t* o = reinterpret_cast<uint32_t*>(out + off);
-    const long long s2 = stride >> 1;  // slice stride in BF16 pairs (slice strides are even)
-    // lanes past the row's end compute but store nothing (no divergent branch)
-    if (copies == 1) {
 #pragma unroll
-        for (int s = 0; s < S; ++s) {
-            const uint32_t v = __byte_perm(__float_as_uint(f[0][s]), __float_as_uint(f[1][s]), 0x7632);
-            if (active) o[s * s2] = v;
-        }
-    } else {
-        for (int c = 0; c < copies; ++c) {
-            const float sc = __int_as_float((127 - 8 * c) << 23);  // 2^{-8 c}, exact
+    for (int s = 0; s < S; ++s) {
+        uint32_t o[4];
 #pragma unroll
-            for (int s = 0; s < S; ++s) {
-                const uint32_t v = __byte_perm(__float_as_uint(f[0][s] * sc), __float_as_uint(f[1][s] * sc), 0x7632);
-                if (active) o[(c * S + s) * s2] = v;
+        for (int p = 0; p < 4; ++p) {
+            float f[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int q = 2 * p + h;
+                if (s == 0) {
+                    const long long u = (long long)(((unsigned long long)hi[q] << 32) | lo[q]);
+                    f[h] = __int_as_float(0x4B400000 + int(u >> (8 * (S - 1)))) - 12582912.0f;
+                } else {
+                    const int b = S - 1 - s;  // byte of the sum holding digit s
+                    f[h] = __int_as_float(int(__byte_perm(b < 4 ? lo[q] : hi[q], 0x4B400000u, 0x7650u | (b & 3)))) -
+                           12583040.0f;
+                }
             }
+            o[p] = __byte_perm(__float_as_uint(f[0]), __float_as_uint(f[1]), 0x7632);
         }
+        *reinterpret_cast<uint4*>(out + s * stride) = make_uint4(o[0], o[1], o[2], o[3]);
     }
 }
 
-// One CTA converts R rows (R a power of two, <= 32) of K values.  Phase 1
-// stages the FP64 values in shared memory and finds each row's largest
-// exponent: for row-fast operands lane l of a warp reads row l mod R (so a
-// warp reads R consecutive rows at 32/R neighbouring k), otherwise one warp
-// walks one row along k; the maxima are reduced with warp shuffles.
-// Phase 2 gives each row to one warp and each lane a pair of neighbouring k:
-// the pair (and, for a shifted second array, the next element, taken from the
-// neighbouring lane) is rounded to the row's fixed-point grid once, folded
-// exactly in integers where requested, split into balanced base-2^bits digits
-// and written as S BF16 slices per copy (copies scaled by 2^-bits, 2^-2bits).
+template <class Loader>
+__device__ __forceinline__ void load_staged(const Loader& ld, const typename Loader::Row& R, int k, double* v) {
+    if constexpr (Loader::MODE == SL_PFOLD) {
+        ld.get4(R, k, v);
+    } else {
+        double dn = 0.0;
+        ld.get(R, k, v[0], dn);
+        if constexpr (Loader::TWO) v[1] = dn;
+    }
+}
+
+// One CTA converts R rows (R a power of two, <= 32) of staged values.
+// Phase 1 stages the FP64 inputs in shared memory (zero beyond each input's
+// valid range, up to KS) and finds each row's largest exponent: for row-fast
+// operands lane l of a warp reads row l mod R (so a warp reads R consecutive
+// rows at 32/R neighbouring k), otherwise one warp walks one row along k.
+// Phase 2 cuts the rows into chunks of 8 neighbouring k and gives each thread
+// one chunk of one row at a time: the chunk's values (and, for a shifted
+// second array, the next one) are rounded to the row's fixed-point grid once,
+// folded exactly in integers where requested, split into balanced 8-bit
+// digits and written as S BF16 slices, 16 bytes per slice and array.
 template <class Loader, int S>
 __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
+    constexpr int MODE = Loader::MODE, SHIFT = Loader::SHIFT, NA = staged_arrays<Loader>();
+    constexpr int fold_bit = (MODE == SL_FOLD || MODE == SL_PFOLD) ? 1 : 0;
+    constexpr int UNR = NA == 4 ? SL_UNROLL / 2 : SL_UNROLL;  // loads in flight per thread and input
+    static_assert((NA > 1) == Loader::TWO && (SHIFT == 0 || (NA > 1 && SHIFT == 1)), "loader mode");
     extern __shared__ double sl_smem[];
-    const int R = J.R, K = J.K, lr = J.lr;
-    double* vu = sl_smem;
-    double* vd = sl_smem + (size_t)R * K;
-    __shared__ int emax[32];
+    const int R = J.R, lr = J.lr, Ks = J.Ks, KS = J.KS;
+    const int astride = R * Ks;  // between the staged arrays
+    __shared__ unsigned emax[32];  // largest |x| high word per row (sign cleared)
     __shared__ typename Loader::Row rowh[32];
     const long long row0 = (long long)blockIdx.x * R;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    // row exponents of at least 64 (2^-959): below that every value rounds to
-    // 0 (and to_fixed needs no test for zero)
-    if (threadIdx.x < 32) emax[threadIdx.x] = 64;
+    if (threadIdx.x < 32) emax[threadIdx.x] = 0;
     if (threadIdx.x < R && row0 + threadIdx.x < J.rows) rowh[threadIdx.x] = ld.row(row0 + threadIdx.x);
     __syncthreads();
+    // input a feeds the first array (a even) or the second (a odd): zero from Ku / Kd
+    auto lim = [&](int a) { return (NA == 1 || (a & 1) == 0 || MODE == SL_FOLD) ? J.Ku : J.Kd; };
     if (Loader::ROW_FAST) {
         const int r = lane & (R - 1), kl = lane >> lr, kstep = 32 >> lr;
         const bool rv = row0 + r < J.rows;
-        int tmax = 0;
-        // SL_UNROLL independent loads in flight per thread before any store
+        unsigned tmax = 0;
         const int kst = nw * kstep;
-        for (int k0 = warp * kstep + kl; k0 < K; k0 += SL_UNROLL * kst) {
-            double up[SL_UNROLL], dn[SL_UNROLL];
+        double* srow = sl_smem + r * Ks;
+        for (int k0 = warp * kstep + kl; k0 < KS; k0 += UNR * kst) {
+            double v[UNR][NA];
 #pragma unroll
-            for (int u = 0; u < SL_UNROLL; ++u) {
-                up[u] = 0.0;
-                dn[u] = 0.0;
+            for (int u = 0; u < UNR; ++u) {
+#pragma unroll
+                for (int a = 0; a < NA; ++a) v[u][a] = 0.0;
                 const int k = k0 + u * kst;
-                if (rv && k < K) ld.get(rowh[r], k, up[u], dn[u]);
+                if (rv && k < J.K) load_staged(ld, rowh[r], k, v[u]);
             }
 #pragma unroll
-            for (int u = 0; u < SL_UNROLL; ++u) {
+            for (int u = 0; u < UNR; ++u) {
                 const int k = k0 + u * kst;
-                if (k < K) {
-                    vu[r * K + k] = up[u];
-                    if (Loader::TWO) vd[r * K + k] = dn[u];
+                if (k < KS) {
+#pragma unroll
+                    for (int a = 0; a < NA; ++a) {
+                        const double x = k < lim(a) ? v[u][a] : 0.0;
+                        srow[a * astride + sl_pos(k)] = x;
+                        tmax = max(tmax, unsigned(__double2hiint(x)) & 0x7FFFFFFFu);
+                    }
                 }
-                tmax = max(tmax, Loader::TWO ? max(biased_exp(up[u]), biased_exp(dn[u])) : biased_exp(up[u]));
             }
         }
         for (int o = R; o < 32; o <<= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
         if (lane < R && tmax) atomicMax(&emax[lane], tmax);
     } else {
         for (int r = warp; r < R; r += nw) {
-            int tmax = 0;
-            if (row0 + r < J.rows) {
-                for (int k0 = lane; k0 < K; k0 += 32 * SL_UNROLL) {
-                    double up[SL_UNROLL], dn[SL_UNROLL];
+            unsigned tmax = 0;
+            const bool rv = row0 + r < J.rows;
+            double* srow = sl_smem + r * Ks;
+            for (int k0 = lane; k0 < KS; k0 += 32 * UNR) {
+                double v[UNR][NA];
 #pragma unroll
-                    for (int u = 0; u < SL_UNROLL; ++u) {
-                        up[u] = 0.0;
-                        dn[u] = 0.0;
-                        if (k0 + 32 * u < K) ld.get(rowh[r], k0 + 32 * u, up[u], dn[u]);
-                    }
+                for (int u = 0; u < UNR; ++u) {
 #pragma unroll
-                    for (int u = 0; u < SL_UNROLL; ++u) {
-                        const int k = k0 + 32 * u;
-                        if (k < K) {
-                            vu[r * K + k] = up[u];
-                            if (Loader::TWO) vd[r * K + k] = dn[u];
+                    for (int a = 0; a < NA; ++a) v[u][a] = 0.0;
+                    const int k = k0 + 32 * u;
+                    if (rv && k < J.K) load_staged(ld, rowh[r], k, v[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < UNR; ++u) {
+                    const int k = k0 + 32 * u;
+                    if (k < KS) {
+#pragma unroll
+                        for (int a = 0; a < NA; ++a) {
+                            const double x = k < lim(a) ? v[u][a] : 0.0;
+                            srow[a * astride + sl_pos(k)] = x;
+                            tmax = max(tmax, unsigned(__double2hiint(x)) & 0x7FFFFFFFu);
                         }
-                        tmax = max(tmax, Loader::TWO ? max(biased_exp(up[u]), biased_exp(dn[u])) : biased_exp(up[u]));
                     }
                 }
             }
             for (int o = 16; o > 0; o >>= 1) tmax = max(tmax, __shfl_xor_sync(0xffffffffu, tmax, o));
-            if (lane == 0) emax[r] = max(tmax, 64);
+            if (lane == 0) emax[r] = tmax;
         }
     }
     __syncthreads();
-    constexpr int MODE = Loader::MODE, SHIFT = Loader::SHIFT;
-    constexpr bool two = MODE != SL_ONE;
-    constexpr int fold_bit = MODE == SL_FOLD ? 1 : 0;
-    static_assert(two == Loader::TWO && (SHIFT == 0 || (two && SHIFT == 1)), "loader mode");
-    const int nbits = J.bits * S;
-    const int np = (two ? max(J.Kp0, J.Kp1) : J.Kp0) >> 1;  // pairs per row
-    for (int r = warp; r < R; r += nw) {
+    const int nbits = 8 * S;
+    // row exponents: |x| < 2^(E_max - 1022), at least 64 - 1022 (below that
+    // every value rounds to 0); one more bit of headroom for the balanced
+    // leading digit, and one for a folded sum
+    if (threadIdx.x < R && row0 + threadIdx.x < J.rows) {
+        const int er = max(int(emax[threadIdx.x] >> 20), 64) - 1022 + 1 + fold_bit;
+        J.ex0[row0 + threadIdx.x] = er;
+        if (NA > 1) J.ex1[row0 + threadIdx.x] = er;
+    }
+    const int nch0 = J.Kp0 >> 3, nch1 = NA > 1 ? J.Kp1 >> 3 : 0;
+    const int nch = max(nch0, nch1);
+    const int items = R * nch;
+    int r = threadIdx.x / nch, c = threadIdx.x - r * nch;
+    const int dr = blockDim.x / nch, dc = blockDim.x - dr * nch;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
         const long long row = row0 + r;
-        if (row >= J.rows) continue;  // warp-uniform
-        // |x| < 2^(E_max - 1022); one more bit of headroom for the balanced
-        // leading digit, and one for a folded sum
-        const int er = emax[r] - 1022 + 1 + fold_bit;
-        if (lane == 0) {
-            J.ex0[row] = er;
-            if (two) J.ex1[row] = er;
-        }
-        const double* ru = vu + r * K;
-        const double* rd = vd + r * K;
-        // fixed-point values of this lane's pair (k, k + 1) at pair index g;
-        // those of the next iteration are computed one iteration ahead, so
-        // that lane 31's element k + 2 (a shifted second array) is lane 0's
-        // next first element, taken by a shuffle
-        auto fixed_pair = [&](int g, long long* u, long long* d) {
+        if (row < J.rows) {
+            const int Cr = 1074 + (max(int(emax[r] >> 20), 64) - 1022 + 1 + fold_bit) - nbits;
+            const double* base = sl_smem + r * Ks + 9 * c;  // element 8c
+            constexpr int NJ = 8 + SHIFT;
+            auto at = [&](int a, int j) { return base[a * astride + j + (j >> 3)]; };
+            if constexpr (MODE == SL_ONE) {
+                long long w[8];
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                const int kk = 2 * g + q;
-                u[q] = kk < K ? to_fixed(ru[kk], er, nbits) : 0;
-                d[q] = (Loader::TWO && kk < K) ? to_fixed(rd[kk], er, nbits) : 0;
-            }
-        };
-        long long cu[2], cd[2];
-        fixed_pair(lane, cu, cd);
-        for (int g0 = 0; g0 < np; g0 += 32) {
-            const int g = g0 + lane;
-            const int k = 2 * g;
-            long long nu[2] = {0, 0}, nd[2] = {0, 0};
-            if (g0 + 32 < np) fixed_pair(g + 32, nu, nd);  // warp-uniform
-            long long fu[3] = {cu[0], cu[1], 0}, fd[3] = {cd[0], cd[1], 0};
-            if constexpr (two && SHIFT == 1) {  // element k + 2: the next lane's first; lane 31's from lane 0, one step on
-                fu[2] = __shfl_down_sync(0xffffffffu, cu[0], 1);
-                fd[2] = __shfl_down_sync(0xffffffffu, cd[0], 1);
-                const long long wu = __shfl_sync(0xffffffffu, nu[0], 0);
-                const long long wd = __shfl_sync(0xffffffffu, nd[0], 0);
-                if (lane == 31) {
-                    fu[2] = wu;
-                    fd[2] = wd;
+                for (int q = 0; q < 8; ++q) w[q] = to_fixed_c(at(0, q), Cr);
+                store_digits8<S>(w, J.out0 + row * J.Kp0 + 8 * c, J.stride0);
+            } else if constexpr (MODE == SL_FOLD) {
+                long long fu[NJ], fd[NJ];
+#pragma unroll
+                for (int j = 0; j < NJ; ++j) {
+                    fu[j] = to_fixed_c(at(0, j), Cr);
+                    fd[j] = to_fixed_c(at(1, j), Cr);
                 }
-            }
-            {
-                long long w[2];
+                long long w[8];
+                if (c < nch0) {
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    long long x = 0;
-                    if (k + q < J.K0) {
-                        x = fu[q];
-                        if constexpr (MODE == SL_FOLD) x += fd[q];
+                    for (int q = 0; q < 8; ++q) w[q] = fu[q] + fd[q];
+                    store_digits8<S>(w, J.out0 + row * J.Kp0 + 8 * c, J.stride0);
+                }
+                if (c < nch1) {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) w[q] = fu[q + SHIFT] - fd[q + SHIFT];
+                    store_digits8<S>(w, J.out1 + row * J.Kp1 + 8 * c, J.stride1);
+                }
+            } else {
+                // SL_PAIR: up | dn; SL_PFOLD: up + up2 | dn + dn2 (inputs 0, 2 | 1, 3)
+                long long w[8];
+                if (c < nch0) {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        w[q] = to_fixed_c(at(0, q), Cr);
+                        if constexpr (MODE == SL_PFOLD) w[q] += to_fixed_c(at(2, q), Cr);
                     }
-                    w[q] = x;
+                    store_digits8<S>(w, J.out0 + row * J.Kp0 + 8 * c, J.stride0);
                 }
-                write_digits2<S>(w[0], w[1], J.copies, J.out0, J.stride0, row * J.Kp0 + k, k < J.Kp0);
-            }
-            if constexpr (two) {
-                long long w[2];
+                if (c < nch1) {
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    long long x = 0;
-                    if (k + q < J.K1) x = MODE == SL_FOLD ? fu[q + SHIFT] - fd[q + SHIFT] : fd[q + SHIFT];
-                    w[q] = x;
+                    for (int q = 0; q < 8; ++q) {
+                        w[q] = to_fixed_c(at(1, q + SHIFT), Cr);
+                        if constexpr (MODE == SL_PFOLD) w[q] += to_fixed_c(at(3, q + SHIFT), Cr);
+                    }
+                    store_digits8<S>(w, J.out1 + row * J.Kp1 + 8 * c, J.stride1);
                 }
-                write_digits2<S>(w[0], w[1], J.copies, J.out1, J.stride1, row * J.Kp1 + k, k < J.Kp1);
             }
-#pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                cu[q] = nu[q];
-                cd[q] = nd[q];
-            }
+        }
+        c += dc;
+        r += dr;
+        if (c >= nch) {
+            c -= nch;
+            ++r;
         }
     }
 }
@@ -1212,8 +1246,9 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
             // accumulator holds an integer: acc_0 (|acc_0| <= 256 2^14 = 2^22)
             // by an exact FP32 offset, the others by conversion; levels 0 and 1
             // combine in 32 bits (|acc_0| 2^8 + |acc_1| < 2^31), the rest by
-            // Horner in 64 bits:  T = sum_d acc_d 2^{8 (S-1-d)}  (|T| < 2^63),
-            // and the product is T 2^{eA + eB - 8 (S + 1)}.
+            // 32 x 32 -> 64-bit multiply-adds (six slices) or Horner in 64 bits:
+            // T = sum_d acc_d 2^{8 (S-1-d)}  (|T| < 2^63), and the product is
+            // T 2^{eA + eB - 8 (S + 1)}.
             constexpr int TEXP = -8 * (S + 1);
             static_assert(SC::NACC == S && S >= 2, "one accumulator per level");
             long long T[CW];
@@ -1230,9 +1265,24 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int i0 = __float_as_int(__uint_as_float(v[0][j]) + 12582912.0f) - 0x4B400000;
-                    long long t = (long long)((i0 << 8) + __float2int_rn(__uint_as_float(v[1][j])));
+                    const int i01 = i0 * 256 + __float2int_rn(__uint_as_float(v[1][j]));
+                    long long t;
+                    if constexpr (S == 6) {
+                        // levels 4 and 5 combined in FP32 at level 4's unit (2^8 of T):
+                        // one rounding of the sum and one of the conversion, at most
+                        // 1.5 units of level 4 (384 of T), against up to K 2^7 of T
+                        // from the rounding of the operands to 48 bits
+                        const int i45 = __float2int_rn(__fmaf_rn(__uint_as_float(v[5][j]), 0.00390625f,
+                                                                 __uint_as_float(v[4][j])));
+                        t = (long long)i01 * 4294967296LL;
+                        t = mad_wide_s32(__float2int_rn(__uint_as_float(v[2][j])), 1 << 24, t);
+                        t = mad_wide_s32(__float2int_rn(__uint_as_float(v[3][j])), 1 << 16, t);
+                        t = mad_wide_s32(i45, 1 << 8, t);
+                    } else {
+                        t = i01;
 #pragma unroll
-                    for (int a = 2; a < SC::NACC; ++a) t = t * 256 + __float2int_rn(__uint_as_float(v[a][j]));
+                        for (int a = 2; a < SC::NACC; ++a) t = t * 256 + __float2int_rn(__uint_as_float(v[a][j]));
+                    }
                     T[4 * c + j] = t;
                 }
             }
@@ -1524,12 +1574,19 @@ template <class Loader>
 int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
     if (J.rows <= 0) return ZEST_GPU_OK;
     if (J.K > SL_KMAX) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: K above 2048");
-    if (J.bits != 7 && J.bits != 8)
-        return fail(ZEST_GPU_ERR_INVALID, "split path: digit width");
-    J.R = slice_rows_per_block(J.K, Loader::TWO);
+    if (J.bits != 8) return fail(ZEST_GPU_ERR_INVALID, "split path: digit width");
+    constexpr int NA = staged_arrays<Loader>();
+    if ((J.Kp0 & 7) || (NA > 1 && (J.Kp1 & 7)) || J.Kp0 < J.K0 || (NA > 1 && J.Kp1 < J.K1))
+        return fail(ZEST_GPU_ERR_INVALID, "split path: slice row length");
+    if (std::max(J.Kp0, NA > 1 ? J.Kp1 : 0) == 0) return ZEST_GPU_OK;  // nothing to write
+    J.KS = std::max(J.Kp0, NA > 1 ? J.Kp1 : 0) + Loader::SHIFT;
+    if (J.K > J.KS) return fail(ZEST_GPU_ERR_INVALID, "split path: staged range");
+    J.Ks = sl_row_stride(J.KS);
+    J.R = slice_rows_per_block(NA * J.Ks * (int)sizeof(double));
     J.lr = 0;
     while ((1 << J.lr) < J.R) ++J.lr;
-    const size_t smem = (size_t)(Loader::TWO ? 2 : 1) * J.R * J.K * sizeof(double);
+    const size_t smem = (size_t)NA * J.R * J.Ks * sizeof(double);
+    if (smem > 100 * 1024) return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: slicing rows exceed shared memory");
     const long long blocks = (J.rows + J.R - 1) / J.R;
     auto go = [&](auto kern) -> int {
         ZG_TRY(set_attributes_once(kern, [](auto k) -> int {
@@ -1553,22 +1610,24 @@ int run_slice(cudaStream_t s, const Loader& ld, SliceJob J) {
 template <class Loader>
 int launch_slice(cudaStream_t s, const Loader& ld, long long rows, int K, int S, int bits, SliceArray& out) {
     static_assert(Loader::MODE == SL_ONE, "one-array loader");
+    if (out.copies != 1) return fail(ZEST_GPU_ERR_INVALID, "split path: slice copies");
     out.bits = bits;
     SliceJob J{};
     J.rows = rows;
-    J.K = J.K0 = K;
+    J.K = J.K0 = J.Ku = K;
     J.Kp0 = out.Kp;
     J.S = S;
     J.bits = bits;
-    J.copies = out.copies;
     J.out0 = out.ptr();
     J.stride0 = out.rows * out.Kp;
     J.ex0 = out.ex.as<int>();
     return run_slice(s, ld, J);
 }
 
-// Two operand arrays from one read: SL_FOLD (up + dn, up - dn) or SL_PAIR
-// (up, dn); the second holds k in [shift, shift + K1) at k - shift.
+// Two operand arrays from one read: SL_FOLD (up + dn, up - dn), SL_PAIR
+// (up, dn) or SL_PFOLD (up + up2, dn + dn2); the second holds k in
+// [shift, shift + K1) at k - shift.  A fold needs K0 = K1 + shift (both sums
+// end at the same input).
 template <class Loader>
 int launch_slice2(cudaStream_t s, const Loader& ld, long long rows, int K0, int K1, int shift, int S, int bits,
                   int mode, SliceArray& out0, SliceArray& out1) {
@@ -1577,15 +1636,17 @@ int launch_slice2(cudaStream_t s, const Loader& ld, long long rows, int K0, int 
     J.rows = rows;
     if (mode != Loader::MODE || shift != Loader::SHIFT)
         return fail(ZEST_GPU_ERR_INVALID, "split path: slicing mode of the loader");
+    if (mode == SL_FOLD && K0 != K1 + shift) return fail(ZEST_GPU_ERR_INVALID, "split path: fold ranges");
+    if (out0.copies != 1 || out1.copies != 1) return fail(ZEST_GPU_ERR_INVALID, "split path: slice copies");
     J.K0 = K0;
     J.K1 = K1;
     J.K = std::max(K0, K1 + shift);
+    J.Ku = mode == SL_FOLD ? J.K : K0;
+    J.Kd = mode == SL_FOLD ? J.K : K1 + shift;
     J.Kp0 = out0.Kp;
     J.Kp1 = out1.Kp;
     J.S = S;
     J.bits = bits;
-    J.copies = out0.copies;
-    if (out1.copies != out0.copies) return fail(ZEST_GPU_ERR_INVALID, "split path: slice copies differ");
     J.out0 = out0.ptr();
     J.out1 = out1.ptr();
     J.stride0 = out0.rows * out0.Kp;
@@ -2075,7 +2136,7 @@ int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t
     ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
     {
         StageScope sc(ctx, ST_SPLIT_SLICE);
-        ZG_TRY(launch_slice2(ctx->stream, ld, rows, Lg, Lg - 1, 1, S, bits, SL_PAIR, st->op[0], st->op[1]));
+        ZG_TRY(launch_slice2(ctx->stream, ld, rows, Lg, Lg - 1, 1, S, bits, SL_PFOLD, st->op[0], st->op[1]));
     }
     if (Lg > 1 && Lg <= KCHUNK && t.cos_bj.rows) {
       // single sums: the cos and sin results combined in integers (the pair of
