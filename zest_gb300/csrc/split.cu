@@ -212,21 +212,30 @@ __device__ __forceinline__ double u64_ldexp(unsigned long long a, bool neg, int 
 
 
 // The same for a signed 64-bit T, without branches (so that the epilogue's
-// independent elements interleave): the rounding carry runs into the
-// exponent field through the bit pattern; zero, results below the normal
-// range and overflow are selected at the end.  Bit-identical to u64_ldexp.
+// independent elements interleave), in 32-bit halves: |T| below 2^32 is moved
+// up by 32 bits first, so that one 32-bit leading-zero count and two funnel
+// shifts normalise it; the rounding carry runs into the exponent field through
+// the bit pattern; zero, results below the normal range and overflow are
+// selected at the end.  Bit-identical to u64_ldexp.
 __device__ __forceinline__ double i64_ldexp(long long T, int E) {
-    const unsigned long long sgn = (unsigned long long)T & (1ull << 63);
-    const unsigned long long a = T < 0 ? 0ull - (unsigned long long)T : (unsigned long long)T;
-    const int lz = __clzll((long long)a);  // 64 for a == 0
-    const unsigned long long n = a << (lz & 63);
-    const unsigned long long mant = n >> 11;  // 53 bits, the leading one at bit 52
-    const unsigned long long rest = n & 0x7FFull;
-    const unsigned long long mr = mant + ((rest > 0x400ull) | ((rest == 0x400ull) & mant));
-    const int biased = (63 - lz) + E + 1023;  // exponent field of the leading one
-    const int eff = biased + int(mr >> 53);   // after a rounding carry
-    const unsigned long long bits = ((unsigned long long)(long long)(biased - 1) << 52) + mr;
-    const double v = __longlong_as_double((long long)(sgn | (eff >= 2047 ? 0x7FF0000000000000ull : bits)));
+    const unsigned long long sm = (unsigned long long)(T >> 63);  // all ones for T < 0
+    const unsigned long long a = ((unsigned long long)T ^ sm) - sm;
+    const bool small = (a >> 32) == 0;
+    const unsigned ah = small ? (unsigned)a : (unsigned)(a >> 32);
+    const unsigned al = small ? 0u : (unsigned)a;
+    const int lz = __clz(ah);                           // 32 only for T = 0
+    const unsigned nh = __funnelshift_l(al, ah, lz);    // leading one at bit 31
+    const unsigned nl = al << (lz & 31);
+    const unsigned mh = nh >> 11;                       // mantissa bits 52..32 (the leading one at bit 20)
+    const unsigned ml = __funnelshift_r(nl, nh, 11);    // mantissa bits 31..0
+    const unsigned inc = ((nl & 0x7FFu) + (ml & 1u) + 0x3FFu) >> 11;  // round half to even
+    const int e = E + 1023 + 63 - (small ? 32 : 0) - lz;  // exponent field of the leading one
+    const unsigned lo = ml + inc;
+    const unsigned mc = mh + (lo < ml ? 1u : 0u);
+    const int eff = e + int(mc >> 21);                  // after a rounding carry
+    const unsigned hi = (eff >= 2047 ? 0x7FF00000u : ((unsigned)(e - 1) << 20) + mc) |
+                        ((unsigned)(sm >> 32) & 0x80000000u);
+    const double v = __hiloint2double((int)hi, eff >= 2047 ? 0 : (int)lo);
     return (a == 0 || eff <= 0) ? 0.0 : v;
 }
 
