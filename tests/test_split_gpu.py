@@ -198,17 +198,20 @@ def test_split_zt_vs_oracle(split, oracle):
     assert relmax(f, oracle.zt_forward(g, L)) < SPLIT_TOL
 
 
-def test_split_zt_truncation(ctx):
+@pytest.mark.parametrize("Le,Lg", [(12, 16), (9, 13), (20, 21)])
+def test_split_zt_truncation(ctx, Le, Lg):
+    # expansions of lower order than the grid (even and odd latitude counts):
+    # the spectra of orders m >= Le must enter the inverse DFT as zeros
     import zest_gb300
-    rng = np.random.default_rng(9)
-    c = rand_zt(rng, 12).ravel()
-    ref_b = ctx.zt_backward(c, 12, 16)
-    g = ctx.zt_backward(c, 12, 12)
-    ref_f = ctx.zt_forward(g, 12, 9)
+    rng = np.random.default_rng(9 + Le)
+    c = rand_zt(rng, Le).ravel()
+    ref_b = ctx.zt_backward(c, Le, Lg)
+    g = ctx.zt_backward(c, Le, Le)
+    ref_f = ctx.zt_forward(g, Le, Le - 3)
     ctx.set_precision(zest_gb300.PRECISION_SPLIT, 6)
     try:
-        assert relmax(ctx.zt_backward(c, 12, 16), ref_b) < SPLIT_TOL
-        assert relmax(ctx.zt_forward(g, 12, 9), ref_f) < SPLIT_TOL
+        assert relmax(ctx.zt_backward(c, Le, Lg), ref_b) < SPLIT_TOL
+        assert relmax(ctx.zt_forward(g, Le, Le - 3), ref_f) < SPLIT_TOL
     finally:
         ctx.set_precision(zest_gb300.PRECISION_FP64)
 

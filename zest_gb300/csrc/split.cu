@@ -415,6 +415,26 @@ struct LegBwdLoader {
 
 // SH coefficients [b][tri(l,m)][c], rows (m, b, c); k = i: the pair
 // (l = m + 2i, l + 1), zero from Lm on (the two parity operands).
+// rows (m, b, kc) of flm; k = q: flm(l = m + q), zero from Lm on (the data of
+// the unfolded backward Legendre sums, all l of one m in one operand)
+struct LegBwdULoader {
+    static constexpr bool ROW_FAST = true, TWO = false;
+    static constexpr int MODE = SL_ONE, SHIFT = 0;
+    const double* flm;
+    int B, nr2, Lm;
+    struct Row { const double* base; int m; };
+    __device__ Row row(long long r) const {
+        const long long mb = r / nr2;
+        const int kc = int(r - mb * nr2);
+        const int m = int(mb / B), b = int(mb - (long long)m * B);
+        return Row{flm + (long long)b * nr2 + kc, m};
+    }
+    __device__ void get(const Row& R, int k, double& up, double&) const {
+        const int l = R.m + k;
+        up = (l < Lm) ? R.base[tri_idx(l, R.m) * ((long long)B * nr2)] : 0.0;
+    }
+};
+
 struct StLegBwdLoader {
     static constexpr bool ROW_FAST = true, TWO = true;
     static constexpr int MODE = SL_PAIR, SHIFT = 0;
@@ -463,6 +483,28 @@ struct DftBwdLoader {
         v[1] = a.y;
         v[2] = __hiloint2double(__double2hiint(c.x) ^ R.neg, __double2loint(c.x));
         v[3] = __hiloint2double(__double2hiint(c.y) ^ R.neg, __double2loint(c.y));
+    }
+};
+
+// rows (b, col = (lat, rad)); k = m: the spectrum (Re F_m, Im F_m) at
+// latitude lat, E[b][m][lat][2 rad + {re, im}] of the unfolded backward
+// Legendre sums (the sin operand takes Im F_k at k - 1)
+struct DftBwdGridLoader {
+    static constexpr bool ROW_FAST = true, TWO = true;
+    static constexpr int MODE = SL_PAIR, SHIFT = 1;
+    const double* E;
+    int L, C, nrad, nlat;
+    struct Row { const double* e; };
+    __device__ Row row(long long r) const {
+        const long long b = r / C;
+        const int col = int(r - b * C);
+        const int lat = col / nrad, rad = col - lat * nrad;
+        return Row{E + ((b * L) * nlat + lat) * (2LL * nrad) + 2 * rad};
+    }
+    __device__ void get(const Row& R, int k, double& up, double& dn) const {
+        const double2 a = *reinterpret_cast<const double2*>(R.e + (long long)k * nlat * 2 * nrad);
+        up = a.x;
+        dn = a.y;
     }
 };
 
@@ -880,6 +922,28 @@ struct EpiLegBwdE {
     __device__ void load(const Row& R, int n, double* old) const { old[0] = R.p[(long long)n * nr2]; }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
         // the conjugate by a sign-bit flip (an integer operation, not an FP64 multiply)
+        const double w = __longlong_as_double(__double_as_longlong(v) ^ (long long)R.sgn);
+        R.p[(long long)n * nr2] = ACC ? old[0] + w : w;
+    }
+};
+
+// Unfolded backward Legendre sums: rows (m, b, kc), table rows (m, lat) for
+// every latitude node -> E[b][m][lat][kc], the imaginary parts conjugated.
+template <bool ACC>
+struct EpiLegBwdU {
+    static constexpr bool RMW = ACC;
+    static constexpr bool CHUNK = ACC;
+    double* E;
+    int B, L, nlat, nr2;
+    struct Row { double* p; unsigned long long sgn; };
+    __device__ Row row(const SplitUnit& u, int r) const {
+        const int m = u.g;
+        const long long local = r - (long long)m * B * nr2;
+        const int b = int(local / nr2), kc = int(local - (long long)b * nr2);
+        return Row{E + (((long long)b * L + m) * nlat + u.aux) * nr2 + kc, (kc & 1) ? (1ull << 63) : 0ull};
+    }
+    __device__ void load(const Row& R, int n, double* old) const { old[0] = R.p[(long long)n * nr2]; }
+    __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
         const double w = __longlong_as_double(__double_as_longlong(v) ^ (long long)R.sgn);
         R.p[(long long)n * nr2] = ACC ? old[0] + w : w;
     }
@@ -1511,6 +1575,9 @@ struct ZtSplitTables {
     int S = 0;
     const DftTables* dft = nullptr;
     SliceArray leg_f, rad_f, rad_bT, leg_bT;
+    // orders up to 256: the backward Legendre table at every latitude node,
+    // rows (m, lat), K = l - m (no fold over the equator)
+    SliceArray leg_bU;
 };
 
 // Sliced Legendre tables of one SH plan (the 128-row operand: no scaled copies).
@@ -1546,7 +1613,9 @@ struct SplitState {
     DevBuf cycles;              // role wait counters, kept when ZEST_GPU_SPLIT_CYCLES is set
     bool cycles_on = false;
     int narrow = 32;            // widest unit (valid table rows) run as one MMA per product
-    std::map<std::tuple<int, int, int, int>, int> tuned;  // timed column tile per (stage, Lg, Lm, batch)
+    bool narrow_fixed = false;  // set by the tuning override: the autotuner keeps it
+    // timed choice per (stage, Lg, Lm, batch): column tile | narrow threshold << 8
+    std::map<std::tuple<int, int, int, int>, int> tuned;
     int nt[16];                 // column tile of each work-list stage: 0 = chosen per launch, or 32 / 80
     SplitState();
     double useful_flops = 0.0, issued_flops = 0.0;  // accumulated while profiling
@@ -1673,7 +1742,10 @@ int get_state(zest_gpu_context* ctx, SplitState** out) {
         // issue one MMA per product instead of grouped full-width MMAs
         if (const char* e = std::getenv("ZEST_GPU_SPLIT_NARROW")) {
             const int v = std::atoi(e);
-            if (v >= 16 && v <= 64) ctx->split->narrow = v;
+            if (v >= 16 && v <= 64) {
+                ctx->split->narrow = v;
+                ctx->split->narrow_fixed = true;
+            }
         }
         // tuning override of the column tiles, "stage=nt,..." with stage one of
         // dft_f leg_f rad_f rad_b leg_b dft_b st_dft_f st_dft_b and nt 32 or 80
@@ -1759,6 +1831,27 @@ __global__ void transpose_blocks_kernel(const double* __restrict__ in, const lon
     if (e >= nrow * ld) return;
     const int k = e / ld, i = e - k * ld;
     out[((long long)blk * nrow + k) * ld + i] = (i < cnt[blk]) ? in[(off[blk] + i) * nrow + k] : 0.0;
+}
+
+// out[(m nlat + lat) ld + q] = P_{m+q}^m at latitude node lat, from the folded
+// backward blocks Pb[(off[2m + p] + i) kh + j] (l = m + p + 2i at folded node
+// j): north nodes lat = j0u + j as they are, south nodes lat = j0d - j with
+// the sign (-1)^(l - m); zero from q = L - m on.
+__global__ void unfold_leg_table_kernel(const double* __restrict__ Pb, const long long* __restrict__ off, int L,
+                                        int kh, int nlat, int j0u, int j0d, int ld, double* __restrict__ out) {
+    const long long rowi = blockIdx.y;  // m nlat + lat
+    const int m = int(rowi / nlat), lat = int(rowi - (long long)m * nlat);
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= ld) return;
+    double v = 0.0;
+    if (q < L - m) {
+        const int p = q & 1, i = q >> 1;
+        const bool north = lat >= j0u;
+        const int j = north ? lat - j0u : j0d - lat;
+        v = Pb[(off[2 * m + p] + i) * kh + j];
+        if (!north && p) v = -v;
+    }
+    out[rowi * ld + q] = v;
 }
 
 int slice_table(zest_gpu_context* ctx, const double* src, long long rows, int K, int ld, int S, int bits,
@@ -1862,6 +1955,17 @@ int build_zt_tables(zest_gpu_context* ctx, SplitState* st, ZtPlan& plan, int S, 
         ZG_TRY(slice_table(ctx, st->tmp.as<double>(), (long long)L * nr, kl, kl, S, digit_bits((L + 1) / 2),
                            t->rad_bT));
         ZG_CUDA_TRY(cudaStreamSynchronize(s));
+        if (L <= KCHUNK) {
+            const int nlat = int(plan.sh.nlat), ku = r16(L);
+            ZG_TRY(st->tmp.ensure((size_t)L * nlat * ku * sizeof(double)));
+            dim3 g3((ku + 127) / 128, (unsigned)((long long)L * nlat));
+            unfold_leg_table_kernel<<<g3, 128, 0, s>>>(plan.leg.Pb.as<double>(), plan.leg.off.as<long long>(), L,
+                                                       kh, nlat, plan.leg.j0u, plan.leg.j0d, ku,
+                                                       st->tmp.as<double>());
+            ZG_TRY(launch_check("unfold_leg_table_kernel"));
+            ZG_TRY(slice_table(ctx, st->tmp.as<double>(), (long long)L * nlat, L, ku, S, 8, t->leg_bU));
+            ZG_CUDA_TRY(cudaStreamSynchronize(s));
+        }
     }
     *out = t.get();
     st->zt_tables.emplace(key, std::move(t));
@@ -2031,21 +2135,31 @@ inline int stage_nt(const SplitState* st, int wk, int S, int ncols) {
 }
 inline int nt_pass(int nt) { return nt == 32 ? 1 << 16 : 0; }
 
-// Runs one split GEMM stage, `launch(nt)`, with its column tile: a tuning
-// override (ZEST_GPU_SPLIT_NT) if set; else, with the context's autotuner on,
-// outside graph capture and for a stage whose launches overwrite their
-// outputs (single sums), the faster of 80 and 32, timed with CUDA events on
+// Runs one split GEMM stage, `launch(nt)`, with its column tile and narrow
+// threshold: a tuning override (ZEST_GPU_SPLIT_NT) if set; else, with the
+// context's autotuner on, outside graph capture and for a stage whose
+// launches overwrite their outputs (single sums), the fastest of the
+// candidates (80 columns with units of up to 32, 48 or 64 valid table rows
+// issued as one MMA per product, or 32 columns), timed with CUDA events on
 // the context stream at the stage's first run at this size (each candidate
-// once untimed, then once timed; the tile changes no result); else the rule
-// of stage_nt.
+// once untimed, then once timed; neither choice changes a result); else the
+// rule of stage_nt.
 template <class Launch>
 int tuned_stage(zest_gpu_context* ctx, SplitState* st, int wk, int S, int Lg, int Lm, int batch, int ncols,
                 bool idempotent, Launch&& launch) {
     int nt = stage_nt(st, wk, S, ncols);
     if (S != 6 || st->nt[wk] || !ctx->autotune || !idempotent) return launch(nt);
+    const int narrow0 = st->narrow;
+    // runs candidate (t, w): tile t, narrow threshold w
+    auto run = [&](int t, int w) -> int {
+        st->narrow = w;
+        const int rc = launch(t);
+        st->narrow = narrow0;
+        return rc;
+    };
     const auto key = std::make_tuple(wk, Lg, Lm, batch);
     auto it = st->tuned.find(key);
-    if (it != st->tuned.end()) return launch(it->second);
+    if (it != st->tuned.end()) return run(it->second & 0xFF, it->second >> 8);
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     ZG_CUDA_TRY(cudaStreamIsCapturing(ctx->stream, &cap));
     if (cap != cudaStreamCaptureStatusNone) return launch(nt);
@@ -2054,13 +2168,17 @@ int tuned_stage(zest_gpu_context* ctx, SplitState* st, int wk, int S, int Lg, in
     ZG_CUDA_TRY(cudaEventCreate(&e1));
     const bool prof = ctx->prof.on;  // the timing runs stay out of the stage profile
     ctx->prof.on = false;
-    const int cand[2] = {80, 32};
+    const int cand[4][2] = {{80, 32}, {80, 48}, {80, 64}, {32, 32}};
     float best = 0.0f;
+    int choice = nt | (narrow0 << 8);
     int rc = ZEST_GPU_OK;
-    for (int i = 0; i < 2 && rc == ZEST_GPU_OK; ++i) {
-        rc = launch(cand[i]);
+    for (int i = 0; i < 4 && rc == ZEST_GPU_OK; ++i) {
+        // one tile of at most 32 columns: the thresholds agree; a fixed threshold is kept
+        if (i > 0 && i < 3 && (ncols <= 32 || st->narrow_fixed)) continue;
+        const int w = st->narrow_fixed ? narrow0 : cand[i][1];
+        rc = run(cand[i][0], w);
         if (rc == ZEST_GPU_OK && cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = fail(ZEST_GPU_ERR_CUDA, "event");
-        if (rc == ZEST_GPU_OK) rc = launch(cand[i]);
+        if (rc == ZEST_GPU_OK) rc = run(cand[i][0], w);
         if (rc == ZEST_GPU_OK && cudaEventRecord(e1, ctx->stream) != cudaSuccess) rc = fail(ZEST_GPU_ERR_CUDA, "event");
         float ms = 0.0f;
         if (rc == ZEST_GPU_OK &&
@@ -2068,15 +2186,15 @@ int tuned_stage(zest_gpu_context* ctx, SplitState* st, int wk, int S, int Lg, in
             rc = fail(ZEST_GPU_ERR_CUDA, "split tile autotuner: timing failed");
         if (rc == ZEST_GPU_OK && (i == 0 || ms < best)) {
             best = ms;
-            nt = cand[i];
+            choice = cand[i][0] | (w << 8);
         }
     }
     ctx->prof.on = prof;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc != ZEST_GPU_OK) return rc;
-    st->tuned.emplace(key, nt);
-    return launch(nt);
+    st->tuned.emplace(key, choice);
+    return run(choice & 0xFF, choice >> 8);
 }
 
 // Longitude DFT of `batch` grids x[b][lon][col] (C columns, item stride gsz)
@@ -2136,8 +2254,9 @@ int zero_parity_tails(zest_gpu_context* ctx, double* E, int batch, int Lg, int L
 // columns) to the grids x[b][lon][col] (item stride gsz): a cos pass writing
 // x_0 and the cos sums C_i (to Cs, batch * Lg * C doubles), then a sin pass
 // reading them and writing x_i = C_i + S_i, x_{N-i} = C_i - S_i; both K-chunked.
+template <class Loader>
 int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t, int S, int wk,
-                       const DftBwdLoader& ld, int C, int N, int Lg, int Lm, int batch, double* grids, long long gsz,
+                       const Loader& ld, int C, int N, int Lg, int Lm, int batch, double* grids, long long gsz,
                        double* Cs) {
     const int bits = digit_bits(Lg);
     const long long rows = (long long)batch * C;
@@ -2145,7 +2264,7 @@ int dft_backward_stage(zest_gpu_context* ctx, SplitState* st, const DftTables& t
     ZG_TRY(st->op[1].ensure(rows, r16(Lg), S));
     {
         StageScope sc(ctx, ST_SPLIT_SLICE);
-        ZG_TRY(launch_slice2(ctx->stream, ld, rows, Lg, Lg - 1, 1, S, bits, SL_PFOLD, st->op[0], st->op[1]));
+        ZG_TRY(launch_slice2(ctx->stream, ld, rows, Lg, Lg - 1, 1, S, bits, Loader::MODE, st->op[0], st->op[1]));
     }
     if (Lg > 1 && Lg <= KCHUNK && t.cos_bj.rows) {
       // single sums: the cos and sin results combined in integers (the pair of
@@ -2396,6 +2515,42 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
         }
         return ZEST_GPU_OK;
         }));
+    }
+    if (tb->leg_bU.rows > 0) {
+        // ---- Legendre, orders up to 256: flm -> E[b][m][lat][kc] at every
+        // latitude node, all l of one m in one sum (no fold over the equator) ----
+        const int nlat = int(sh.nlat);
+        const long long per_m = (long long)batch * nr2;
+        const long long rows = (long long)Lm * per_m;
+        ZG_TRY(st->op[0].ensure(rows, r16(Lm), S));
+        {
+            StageScope sc(ctx, ST_SPLIT_SLICE);
+            ZG_TRY(launch_slice(s, LegBwdULoader{flm, batch, nr2, Lm}, rows, Lm, S, 8, st->op[0]));
+        }
+        if (Lm < Lg) {  // orders m >= Lm of the spectra are zero
+            StageScope sc(ctx, ST_MEMSET);
+            const long long eb = (long long)Lg * nlat * nr2;  // one b
+            ZG_CUDA_TRY(cudaMemset2DAsync(E + (size_t)Lm * nlat * nr2, eb * sizeof(double), 0,
+                                          (size_t)(Lg - Lm) * nlat * nr2 * sizeof(double), batch, s));
+        }
+        ZG_TRY(tuned_stage(ctx, st, WK_LEG_B, S, Lg, Lm, batch, nlat, true, [&](int NT) -> int {
+            UnitList* u;
+            ZG_TRY(get_units(ctx, std::make_tuple(int(WK_LEG_B), Lg, Lm, batch, S, 4 + nt_pass(NT)), [&](UnitList& ul) {
+                for (int m = 0; m < Lm; ++m)
+                    add_units(ul, S, 8, (long long)m * per_m, per_m, (long long)m * nlat, nlat, NT, Lm - m, 0, m, 0);
+                // the algorithmic work is that of the sums folded over the equator
+                // (half the products); the unfolded form spends the other half to
+                // spare the inverse DFT's input a second array
+                ul.useful *= 0.5;
+            }, &u));
+            return run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->leg_bU, tb->leg_bU,
+                               EpiLegBwdU<false>{E, batch, Lg, nlat, nr2});
+        }));
+        // ---- longitude: inverse real DFT of the spectra at every latitude ----
+        // (the cos sums C_i go to the scratch of the spectra, consumed by the slicing)
+        ZG_TRY(dft_backward_stage(ctx, st, *tb->dft, S, WK_DFT_B, DftBwdGridLoader{E, Lg, C, nr, nlat}, C, N, Lg,
+                                  Lm, batch, grids, sh.size(), E));
+        return split_finish(ctx);
     }
     // ---- Legendre: flm -> G (north/south unfold; parity 1 read-modify-write) ----
     {
