@@ -180,6 +180,29 @@ def test_split_zt_column_tiles(ctx, monkeypatch, spec):
     assert relmax(fs, f64) < SPLIT_TOL
 
 
+@pytest.mark.parametrize("narrow", ["mixed", "64"])
+def test_split_zt_narrow_units(ctx, monkeypatch, narrow):
+    # ZEST_GPU_SPLIT_NARROW: units of at most 32 valid table rows in a second
+    # launch of 32-column tiles ("mixed"), or units of up to 64 rows issued as
+    # one MMA per product; the same split-form results as the FP64 form
+    import zest_gb300
+    monkeypatch.setenv("ZEST_GPU_SPLIT_NARROW", narrow)
+    rng = np.random.default_rng(78)
+    L, batch = 71, 2
+    c = rand_zt(rng, L, batch=batch).ravel()
+    g64 = ctx.zt_backward(c, L, batch=batch)
+    f64 = ctx.zt_forward(g64, L, batch=batch)
+    c2 = zest_gb300.Context(0)
+    try:
+        c2.set_precision(zest_gb300.PRECISION_SPLIT, 6)
+        gs = c2.zt_backward(c, L, batch=batch)
+        fs = c2.zt_forward(g64, L, batch=batch)
+    finally:
+        c2.close()
+    assert relmax(gs, g64) < SPLIT_TOL
+    assert relmax(fs, f64) < SPLIT_TOL
+
+
 def test_split_zt_config1_vs_golden(split, golden):
     g = golden("zt_config1")
     c = split.zt_forward(np.ascontiguousarray(g["grid"]).ravel(), 20)

@@ -63,6 +63,7 @@ namespace {
 constexpr int SP_EPI_WARPS = 16;                  // epilogue warps: four per TMEM lane quarter
 constexpr int SP_THREADS = 32 * (2 + SP_EPI_WARPS);  // + TMA producer + MMA issuer
 constexpr int SP_M = 128;
+constexpr int SP_MIXED = 1;      // narrow threshold value that selects mixed 80/32-column launches
 constexpr int SP_KB = 16;        // K elements per pipeline stage (32 bytes of bf16)
 constexpr long long SP_TIMEOUT_NS = 2000000000LL;
 
@@ -1594,6 +1595,9 @@ struct UnitList {
     double issued = 0.0;  // the same for full 128 x NT x 16k tiles
     DevBuf dev;
     std::vector<long long> rows;  // exact row offsets a hashed key stands for (ragged rotation)
+    // mixed launches: the units of more than 32 valid table rows (80-column
+    // tiles) and the others (32-column tiles), split on first use
+    std::unique_ptr<UnitList> wide, narrow;
 };
 
 struct SplitState {
@@ -1741,7 +1745,12 @@ int get_state(zest_gpu_context* ctx, SplitState** out) {
         // tuning override: units of at most this many valid table rows (16..64)
         // issue one MMA per product instead of grouped full-width MMAs
         if (const char* e = std::getenv("ZEST_GPU_SPLIT_NARROW")) {
-            const int v = std::atoi(e);
+            // "mixed": units of up to 32 rows in a second launch of 32-column tiles
+            const int v = std::string(e) == "mixed" ? SP_MIXED : std::atoi(e);
+            if (v == SP_MIXED) {
+                ctx->split->narrow = SP_MIXED;
+                ctx->split->narrow_fixed = true;
+            }
             if (v >= 16 && v <= 64) {
                 ctx->split->narrow = v;
                 ctx->split->narrow_fixed = true;
@@ -2083,6 +2092,26 @@ int run_gemm_nt(zest_gpu_context* ctx, int nt, int S, UnitList& ul, const SliceA
     if (bits != 8) return fail(ZEST_GPU_ERR_INVALID, "split GEMM: operands need 8-bit digits");
     if (Epi::CHUNK && S != 6)
         return fail(ZEST_GPU_ERR_UNSUPPORTED, "split path: sums longer than 256 terms need 6 slices");
+    SplitState* st;
+    ZG_TRY(get_state(ctx, &st));
+    if (S == 6 && nt == 80 && st->narrow == SP_MIXED) {
+        // mixed: units of at most 32 valid table rows run in a second launch of
+        // 32-column tiles (one MMA per A slice over all levels), the others in
+        // 80-column tiles; the two launches write disjoint outputs
+        if (!ul.wide) {
+            ul.wide.reset(new UnitList());
+            ul.narrow.reset(new UnitList());
+            for (const SplitUnit& u : ul.v) (u.n <= 32 ? ul.narrow : ul.wide)->v.push_back(u);
+            ul.wide->max_ksteps = ul.narrow->max_ksteps = ul.max_ksteps;
+        }
+        if (ctx->prof.on) {  // the halves carry no flop counts of their own
+            st->useful_flops += ul.useful;
+            st->issued_flops += ul.issued;
+        }
+        const int rc = run_gemm_t<6, 8, 80>(ctx, *ul.wide, A0, A1, B0, B1, epi);
+        if (rc != ZEST_GPU_OK) return rc;
+        return run_gemm_t<6, 8, 32>(ctx, *ul.narrow, A0, A1, B0, B1, epi);
+    }
     switch (S) {
     case 6: return nt == 32 ? run_gemm_t<6, 8, 32>(ctx, ul, A0, A1, B0, B1, epi)
                             : run_gemm_t<6, 8, 80>(ctx, ul, A0, A1, B0, B1, epi);
@@ -2140,7 +2169,8 @@ inline int nt_pass(int nt) { return nt == 32 ? 1 << 16 : 0; }
 // context's autotuner on, outside graph capture and for a stage whose
 // launches overwrite their outputs (single sums), the fastest of the
 // candidates (80 columns with units of up to 32, 48 or 64 valid table rows
-// issued as one MMA per product, or 32 columns), timed with CUDA events on
+// issued as one MMA per product; 80 columns with the units of up to 32 rows
+// in a second launch of 32-column tiles; or 32 columns), timed with CUDA events on
 // the context stream at the stage's first run at this size (each candidate
 // once untimed, then once timed; neither choice changes a result); else the
 // rule of stage_nt.
@@ -2168,13 +2198,13 @@ int tuned_stage(zest_gpu_context* ctx, SplitState* st, int wk, int S, int Lg, in
     ZG_CUDA_TRY(cudaEventCreate(&e1));
     const bool prof = ctx->prof.on;  // the timing runs stay out of the stage profile
     ctx->prof.on = false;
-    const int cand[4][2] = {{80, 32}, {80, 48}, {80, 64}, {32, 32}};
+    const int cand[5][2] = {{80, 32}, {80, 48}, {80, 64}, {80, SP_MIXED}, {32, 32}};
     float best = 0.0f;
     int choice = nt | (narrow0 << 8);
     int rc = ZEST_GPU_OK;
-    for (int i = 0; i < 4 && rc == ZEST_GPU_OK; ++i) {
+    for (int i = 0; i < 5 && rc == ZEST_GPU_OK; ++i) {
         // one tile of at most 32 columns: the thresholds agree; a fixed threshold is kept
-        if (i > 0 && i < 3 && (ncols <= 32 || st->narrow_fixed)) continue;
+        if (i > 0 && i < 4 && (ncols <= 32 || st->narrow_fixed)) continue;
         const int w = st->narrow_fixed ? narrow0 : cand[i][1];
         rc = run(cand[i][0], w);
         if (rc == ZEST_GPU_OK && cudaEventRecord(e0, ctx->stream) != cudaSuccess) rc = fail(ZEST_GPU_ERR_CUDA, "event");
