@@ -4,7 +4,9 @@ compiled from its own sources, wrapped by oracle/ref_shim.cpp.
 Test infrastructure only (golden fixtures, CPU baseline arm of bench.py).
 
 The reference checkout is named by `--reference DIR` or the environment
-variable ZEST_REFERENCE_DIR; there is no default.  Where one is given, its
+variable ZEST_REFERENCE_DIR; without either, a checkout in a directory named
+`reference` beside this repository's root is used if present.  Where one is
+found, its
 headers and the few translation units the transform/rotation path needs are
 staged into oracle/_ref/src/ and compiled with g++ directly -- the reference's
 own CMake build is not used.  Without one, the sources staged earlier are
@@ -30,8 +32,16 @@ STAGE = os.path.join(REF_OUT, "src")
 
 
 def reference_checkout(path: str | None = None) -> str | None:
-    """The reference checkout: `path`, else ZEST_REFERENCE_DIR, else None."""
-    return path or os.environ.get("ZEST_REFERENCE_DIR") or None
+    """The reference checkout: `path`, else ZEST_REFERENCE_DIR, else a
+    directory named `reference` beside this repository's root where one with
+    the reference's include/ and src/ exists, else None."""
+    given = path or os.environ.get("ZEST_REFERENCE_DIR")
+    if given:
+        return given
+    sibling = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    if os.path.isdir(os.path.join(sibling, "include")) and os.path.isdir(os.path.join(sibling, "src")):
+        return sibling
+    return None
 
 
 # Translation units of the reference needed by ref_shim.cpp.
