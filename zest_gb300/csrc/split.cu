@@ -394,6 +394,7 @@ struct RadBwdLoader {  // rows ((tri(l,m) B + b) 2 + c); k = i, n = l + 2i
         const int n = R.l + 2 * k;
         up = (n < Lm) ? R.base[zidx(n, R.l, R.m) * 2] : 0.0;
     }
+    __device__ int kvalid(const Row& R) const { return (Lm - R.l + 1) / 2; }  // n = l + 2k < Lm
 };
 
 // rows (m, b, kc) of flm; k = i: up = flm(l = m + 2i), dn = flm(l = m + 1 + 2i)
@@ -415,6 +416,7 @@ struct LegBwdLoader {
         up = (l < Lm) ? R.base[tri_idx(l, R.m) * st] : 0.0;
         dn = (l + 1 < Lm) ? R.base[tri_idx(l + 1, R.m) * st] : 0.0;
     }
+    __device__ int kvalid(const Row& R) const { return (Lm - R.m + 1) / 2; }  // l = m + 2k < Lm
 };
 
 // SH coefficients [b][tri(l,m)][c], rows (m, b, c); k = i: the pair
@@ -437,6 +439,7 @@ struct LegBwdULoader {
         const int l = R.m + k;
         up = (l < Lm) ? R.base[tri_idx(l, R.m) * ((long long)B * nr2)] : 0.0;
     }
+    __device__ int kvalid(const Row& R) const { return Lm - R.m; }  // l = m + k < Lm
 };
 
 struct StLegBwdLoader {
@@ -456,6 +459,7 @@ struct StLegBwdLoader {
         up = (l < Lm) ? R.base[2 * tri_idx(l, R.m)] : 0.0;
         dn = (l + 1 < Lm) ? R.base[2 * tri_idx(l + 1, R.m)] : 0.0;
     }
+    __device__ int kvalid(const Row& R) const { return (Lm - R.m + 1) / 2; }  // l = m + 2k < Lm
 };
 
 // rows (b, col = (lat, rad)); k = m: the spectrum (Re F_m, Im F_m) at
@@ -537,6 +541,18 @@ template <class Loader>
 __host__ __device__ constexpr int staged_arrays() {
     return Loader::MODE == SL_ONE ? 1 : (Loader::MODE == SL_PFOLD ? 4 : 2);
 }
+
+// Ragged loaders (a member kvalid(row): the row's inputs are zero from that k
+// on) feed triangular sums whose GEMM work lists read, for the rows of one
+// group, only the K blocks up to their valid length rounded up to 16.  A
+// slicing block then stages and writes only up to the largest such length of
+// its rows (rounded up to 16; the zeros in between are written), not the whole
+// row: the slices beyond are never read.
+template <class L, class = void>
+struct ragged_loader : std::false_type {};
+template <class L>
+struct ragged_loader<L, std::void_t<decltype(std::declval<const L&>().kvalid(std::declval<const typename L::Row&>()))>>
+    : std::true_type {};
 
 // Shared-memory position of element k of a staged row: one double of padding
 // after every 8, so that the lanes of a warp reading 8 consecutive elements
@@ -638,15 +654,28 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
     constexpr int UNR = NA == 4 ? SL_UNROLL / 2 : SL_UNROLL;  // loads in flight per thread and input
     static_assert((NA > 1) == Loader::TWO && (SHIFT == 0 || (NA > 1 && SHIFT == 1)), "loader mode");
     extern __shared__ double sl_smem[];
-    const int R = J.R, lr = J.lr, Ks = J.Ks, KS = J.KS;
+    constexpr bool RAGGED = ragged_loader<Loader>::value;
+    static_assert(!RAGGED || SHIFT == 0, "ragged loaders stage unshifted arrays");
+    const int R = J.R, lr = J.lr, Ks = J.Ks;
     const int astride = R * Ks;  // between the staged arrays
     __shared__ unsigned emax[32];  // largest |x| high word per row (sign cleared)
     __shared__ typename Loader::Row rowh[32];
+    __shared__ int kv_s;           // ragged loaders: the largest valid length of the block's rows
     const long long row0 = (long long)blockIdx.x * R;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if constexpr (RAGGED) {
+        if (threadIdx.x == 0) kv_s = 0;
+        __syncthreads();
+    }
     if (threadIdx.x < 32) emax[threadIdx.x] = 0;
-    if (threadIdx.x < R && row0 + threadIdx.x < J.rows) rowh[threadIdx.x] = ld.row(row0 + threadIdx.x);
+    if (threadIdx.x < R && row0 + threadIdx.x < J.rows) {
+        rowh[threadIdx.x] = ld.row(row0 + threadIdx.x);
+        if constexpr (RAGGED) atomicMax(&kv_s, ld.kvalid(rowh[threadIdx.x]));
+    }
     __syncthreads();
+    // staged (and written) k range of this block
+    int KS = J.KS;
+    if constexpr (RAGGED) KS = min(KS, (max(kv_s, 0) + 15) & ~15);
     // input a feeds the first array (a even) or the second (a odd): zero from Ku / Kd
     auto lim = [&](int a) { return (NA == 1 || (a & 1) == 0 || MODE == SL_FOLD) ? J.Ku : J.Kd; };
     if (Loader::ROW_FAST) {
@@ -720,8 +749,9 @@ __global__ void __launch_bounds__(256) slice_kernel(Loader ld, SliceJob J) {
         J.ex0[row0 + threadIdx.x] = er;
         if (NA > 1) J.ex1[row0 + threadIdx.x] = er;
     }
-    const int nch0 = J.Kp0 >> 3, nch1 = NA > 1 ? J.Kp1 >> 3 : 0;
+    const int nch0 = min(J.Kp0, KS) >> 3, nch1 = NA > 1 ? min(J.Kp1, KS) >> 3 : 0;
     const int nch = max(nch0, nch1);
+    if (nch == 0) return;  // a ragged block of rows with no valid k: exponents only
     const int items = R * nch;
     int r = threadIdx.x / nch, c = threadIdx.x - r * nch;
     const int dr = blockDim.x / nch, dc = blockDim.x - dr * nch;
@@ -2049,10 +2079,13 @@ int run_gemm_t(zest_gpu_context* ctx, UnitList& ul, const SliceArray& A0, const 
         ZG_CUDA_TRY(cudaStreamSynchronize(s));
         unsigned long long c[8];
         ZG_CUDA_TRY(cudaMemcpy(c, P.dbg, sizeof(c), cudaMemcpyDeviceToHost));
+        const char* fn = __PRETTY_FUNCTION__;
+        const char* tag = std::strstr(fn, "Epi = ");
         std::fprintf(stderr,
-                     "split_gemm S=%d units=%zu grid=%d: total %.0f | producer waits %.0f | mma waits tmem %.0f, "
-                     "smem %.0f | epilogue waits %.0f, drains %.0f, stores %.0f (cycles per CTA)\n",
-                     S, units.size(), grid, double(c[5]) / grid, double(c[0]) / grid, double(c[1]) / grid,
+                     "split_gemm S=%d NT=%d %.40s units=%zu grid=%d: total %.0f | producer waits %.0f | mma waits "
+                     "tmem %.0f, smem %.0f | epilogue waits %.0f, drains %.0f, stores %.0f (cycles per CTA)\n",
+                     S, NT, tag ? tag + 6 : "", units.size(), grid, double(c[5]) / grid, double(c[0]) / grid,
+                     double(c[1]) / grid,
                      double(c[2]) / grid, double(c[3]) / grid, double(c[4]) / grid, double(c[6]) / grid);
     }
     return ZEST_GPU_OK;
