@@ -35,9 +35,16 @@ sys.path.insert(0, ROOT)
 from zest_gb300.replicas import max_over_ranks, replica_seed0, whole_job_rate  # noqa: E402
 
 METRIC = "Zernike fwd+bwd transforms/s, order 200x64: split-prec vs FP64 GPU at 1e-11 err"
-# DRAM read + write bytes of the split GEMMs of one forward+backward step per
-# function at order 200 (ncu capture of all eight launches at batch 4: 6.70 GB)
-GEMM_DRAM_BYTES_PER_FUNCTION_ORDER200 = 6.701e9 / 4
+# DRAM read + write bytes of one forward+backward step per function at order
+# 200, from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of
+# the launches of a step at batch 4, which grow in proportion to the batch:
+# the seven split GEMM launches (6.464 GB) and the six slicing launches
+# (5.376 GB)
+GEMM_DRAM_BYTES_PER_FUNCTION_ORDER200 = 6.464e9 / 4
+SLICE_DRAM_BYTES_PER_FUNCTION_ORDER200 = 5.376e9 / 4
+# the least a forward+backward transform can move at order 200: the grid read
+# and written once, the coefficients written and read once
+MIN_BYTES_PER_FUNCTION_ORDER200 = 288.7e6
 UNIT = "transforms/s"
 
 
@@ -855,6 +862,15 @@ def main():
                     "dram_rate_tbs": (traffic * launches_per_step / (gemm_ms * 1e-3) / 1e12
                                       if traffic and gemm_ms == gemm_ms and gemm_ms > 0 else None),
                     "hbm_peak_tbs": peaks["hbm_gbs"] / 1e3 if peaks.get("hbm_gbs") else None}
+        if L == 200:
+            gb, sb = GEMM_DRAM_BYTES_PER_FUNCTION_ORDER200 * B, SLICE_DRAM_BYTES_PER_FUNCTION_ORDER200 * B
+            roofline["step_traffic"] = {
+                "gemm_bytes": gb, "slice_bytes": sb, "total_bytes": gb + sb,
+                "algorithmic_min_bytes": MIN_BYTES_PER_FUNCTION_ORDER200 * B,
+                "total_over_min": (gb + sb) / (MIN_BYTES_PER_FUNCTION_ORDER200 * B),
+                "slice_rate_tbs": (sb / (stage_ms["split_slice"] * 1e-3) / 1e12
+                                   if stage_ms.get("split_slice") else None),
+                "source": "ncu dram read + write of the launches of one step at batch 4, times batch / 4"}
     else:
         # FP64 form: the dominant stage is the folded Legendre contraction, bound by
         # the FP64 pipe (1.20 TFLOP/s DFMA measured on this GPU model)
