@@ -2904,6 +2904,7 @@ struct RotInLoader {
         up = xr * p.x - xi * p.y;
         dn = xr * p.y + xi * p.x;
     }
+    __device__ int kvalid(const Row& R) const { return R.l + 1; }  // m <= l
 };
 
 // row v: k = m: t_m e^{-i m beta'} (Re, Im), t = T[v][m][re, im]
@@ -2929,6 +2930,7 @@ struct RotMidLoader {
         up = tr * p.x - ti * p.y;
         dn = tr * p.y + ti * p.x;
     }
+    __device__ int kvalid(const Row& R) const { return R.l + 1; }  // m <= l
 };
 
 // rows v, columns m = aux + n: T[v][m][part], part = 0 (real) for the units
