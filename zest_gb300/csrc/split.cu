@@ -362,33 +362,52 @@ struct LegFwdLoader {
     }
 };
 
-struct RadFwdLoader {  // rows ((t B + b) 2 + c); k = radial node
+// Rows of the radial sums, grouped by degree l: row 2 (tri(l,0) B + b (l+1) + m) + c
+// is (l, b, m, c), so that neighbouring rows are neighbouring (m, c) of one
+// (l, b), whose Zernike coefficients zidx(n, l, m) + c are contiguous.
+struct RadRow {
+    int l, b, m, c;
+};
+__device__ __forceinline__ RadRow rad_row(long long r, int B) {
+    const long long q = (r >> 1) / B;  // in [tri(l,0), tri(l+1,0))
+    int l = int((sqrtf(8.0f * float(q) + 1.0f) - 1.0f) * 0.5f);
+    while ((long long)(l + 1) * (l + 2) / 2 <= q) ++l;
+    while ((long long)l * (l + 1) / 2 > q) --l;
+    const long long local = (r >> 1) - (long long)l * (l + 1) / 2 * B;  // b (l + 1) + m
+    const int b = int(local / (l + 1));
+    return RadRow{l, b, int(local - (long long)b * (l + 1)), int(r & 1)};
+}
+// the same decoding for a row of the known group l
+__device__ __forceinline__ RadRow rad_row_of(long long r, int l, int B) {
+    const long long local = (r >> 1) - (long long)l * (l + 1) / 2 * B;
+    const int b = int(local / (l + 1));
+    return RadRow{l, b, int(local - (long long)b * (l + 1)), int(r & 1)};
+}
+
+struct RadFwdLoader {  // rows (l, b, m, c) as rad_row; k = radial node: flm[(tri(l,m) B + b)][k][c]
     static constexpr bool ROW_FAST = false, TWO = false;
     static constexpr int MODE = SL_ONE, SHIFT = 0;
     const double* flm;
-    int nr;
+    int nr, B;
     struct Row { const double* p; };
-    __device__ Row row(long long r) const { return Row{flm + (r >> 1) * nr * 2 + (r & 1)}; }
+    __device__ Row row(long long r) const {
+        const RadRow w = rad_row(r, B);
+        return Row{flm + ((long long)tri_idx(w.l, w.m) * B + w.b) * nr * 2 + w.c};
+    }
     __device__ void get(const Row& R, int k, double& up, double&) const { up = R.p[(long long)k * 2]; }
 };
 
-struct RadBwdLoader {  // rows ((tri(l,m) B + b) 2 + c); k = i, n = l + 2i
-    static constexpr bool ROW_FAST = false, TWO = false;
+struct RadBwdLoader {  // rows (l, b, m, c) as rad_row; k = i, n = l + 2i
+    // row-fast: neighbouring rows read neighbouring coefficients
+    static constexpr bool ROW_FAST = true, TWO = false;
     static constexpr int MODE = SL_ONE, SHIFT = 0;
     const double* coeffs;
     long long cs;
     int B, Lm;
     struct Row { const double* base; int l, m; };
     __device__ Row row(long long r) const {
-        const long long tb = r >> 1;
-        const int c = int(r & 1);
-        const long long t = tb / B;
-        const int b = int(tb - t * B);
-        int l = int((sqrtf(8.0f * float(t) + 1.0f) - 1.0f) * 0.5f);
-        while ((long long)(l + 1) * (l + 2) / 2 <= t) ++l;
-        while ((long long)l * (l + 1) / 2 > t) --l;
-        const int m = int(t - (long long)l * (l + 1) / 2);
-        return Row{coeffs + b * cs + c, l, m};
+        const RadRow w = rad_row(r, B);
+        return Row{coeffs + w.b * cs + w.c, w.l, w.m};
     }
     __device__ void get(const Row& R, int k, double& up, double&) const {
         const int n = R.l + 2 * k;
@@ -896,7 +915,7 @@ struct EpiLegFwd {  // rows (m, b, kc) -> flm[tri(l,m)][b][kc], l = m + p + 2 (a
     }
 };
 template <bool ACC = false>
-struct EpiRadFwd {  // rows ((tri(l,m) B + b) 2 + c) -> coeffs[b][zidx(n,l,m)][c]
+struct EpiRadFwd {  // rows (l, b, m, c) as rad_row -> coeffs[b][zidx(n,l,m)][c]
     static constexpr bool RMW = ACC;
     static constexpr bool CHUNK = ACC;
     double* coeffs;
@@ -904,12 +923,9 @@ struct EpiRadFwd {  // rows ((tri(l,m) B + b) 2 + c) -> coeffs[b][zidx(n,l,m)][c
     long long cs;
     struct Row { double* p; long long zl0; int l; };
     __device__ Row row(const SplitUnit& u, int r) const {
-        const int l = u.g;
-        const int tb = r >> 1, c = r & 1;
-        const int t = tb / B, b = tb - t * B;
-        const int m = t - int(tri_idx(l, 0));
-        const long long n0 = l + 2 * u.aux;
-        return Row{coeffs + b * cs + 2 * m + c, n0, l};
+        const RadRow w = rad_row_of(r, u.g, B);
+        const long long n0 = w.l + 2 * u.aux;
+        return Row{coeffs + w.b * cs + 2 * w.m + w.c, n0, w.l};
     }
     __device__ double* at(const Row& R, int n) const {
         const long long nn = R.zl0 + 2 * n;
@@ -921,14 +937,15 @@ struct EpiRadFwd {  // rows ((tri(l,m) B + b) 2 + c) -> coeffs[b][zidx(n,l,m)][c
     }
 };
 template <bool ACC = false>
-struct EpiRadBwd {  // rows ((t B + b) 2 + c) -> flm[(t B + b)][k][c]
+struct EpiRadBwd {  // rows (l, b, m, c) as rad_row -> flm[(tri(l,m) B + b)][k][c]
     static constexpr bool RMW = ACC;
     static constexpr bool CHUNK = ACC;
     double* flm;
-    int nr;
+    int nr, B;
     struct Row { double* p; };
     __device__ Row row(const SplitUnit& u, int r) const {
-        return Row{flm + ((long long)(r >> 1) * nr + u.aux) * 2 + (r & 1)};
+        const RadRow w = rad_row_of(r, u.g, B);
+        return Row{flm + ((tri_idx(w.l, w.m) * B + w.b) * nr + u.aux) * 2 + w.c};
     }
     __device__ void load(const Row& R, int n, double* old) const { old[0] = R.p[2 * n]; }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
@@ -2511,7 +2528,7 @@ int split_zt_forward(zest_gpu_context* ctx, ZtPlan& plan, int Lg, int Le, int Lm
         ZG_TRY(st->op[0].ensure(rows, r16(nr), S));
         {
             StageScope sc(ctx, ST_SPLIT_SLICE);
-            ZG_TRY(launch_slice(s, RadFwdLoader{flm, nr}, rows, nr, S, bits, st->op[0]));
+            ZG_TRY(launch_slice(s, RadFwdLoader{flm, nr, batch}, rows, nr, S, bits, st->op[0]));
         }
         ZG_TRY(tuned_stage(ctx, st, WK_RAD_F, S, Lg, Lm, batch, (Lm + 1) / 2, nchunks(nr) == 1, [&](int NT) -> int {
         for (int ch = 0; ch < nchunks(nr); ++ch) {
@@ -2575,9 +2592,9 @@ int split_zt_backward(zest_gpu_context* ctx, ZtPlan& plan, int Le, int Lg, int L
                               std::min(KCHUNK, (Lm - l + 1) / 2 - k0), 0, l, k0);
             }, &u));
             if (ch == 0)
-                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<false>{flm, nr}));
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<false>{flm, nr, batch}));
             else
-                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<true>{flm, nr}));
+                ZG_TRY(run_gemm_nt(ctx, NT, S, *u, st->op[0], st->op[0], tb->rad_bT, tb->rad_bT, EpiRadBwd<true>{flm, nr, batch}));
         }
         return ZEST_GPU_OK;
         }));
