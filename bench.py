@@ -259,10 +259,12 @@ def run_sh(args, rank: int, world: int, barrier) -> None:
         torch.cuda.synchronize()
         clocks = sampler.stop()
         prof = ctx.profile_read(reset=True)
+        flops = ctx.profile_flops(reset=True)
         ctx.profile(False)
         ms = max_over_ranks(e0.elapsed_time(e1), None) / nsteps
         err = max(float(np.max(np.abs(x - y)) / np.max(np.abs(y)))
                   for x, y in zip(cout.cpu().numpy().reshape(B, -1), c.reshape(B, -1)))
+        timed.flops = (flops[0] / nsteps, flops[1] / nsteps)
         return ms, {k: v[0] / nsteps for k, v in prof.items()}, clocks, err
 
     ms64, st64, clocks64, err64 = timed(args.steps, args.warmup)
@@ -277,6 +279,33 @@ def run_sh(args, rank: int, world: int, barrier) -> None:
         ctx.set_precision(zg.PRECISION_FP64)
     else:
         ms, stages, clocks, err, d_grid = ms64, st64, clocks64, err64, None
+    roofline = None
+    if split and stages.get("split_gemm"):
+        useful, issued = timed.flops
+        achieved = useful / (stages["split_gemm"] * 1e-3) / 1e12
+        peaks = measured_peaks()
+        peak = peaks["bf16_tflops_sustained"] or peaks["bf16_tflops"]
+        roofline = {"bound": "tensor", "kernel": "split_gemm_kernel (all launches of a step)", "achieved": achieved,
+                    "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                    "algorithmic": "BF16 MMA flops of the slice products on valid rows",
+                    "useful_tflop_per_step": useful / 1e12, "issued_tflop_per_step": issued / 1e12,
+                    "peak_source": peaks["source"] + " bf16 sustained"}
+    # CPU baseline: the compiled reference, one transformer per item and thread
+    # built before the timing, one step of backward + forward of the 8 items
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            from oracle import Reference
+            ref = Reference()
+            nthreads = min(B, os.cpu_count() or 1)
+            secs, _, cref = ref.st_bwd_fwd_steps(c, L, nthreads, nsteps=1)
+            cpu = {"value": B / float(secs[0]), "unit": "transforms/s", "cores": nthreads, "kind": "reference",
+                   "sample": f"the whole batch: {B} items backward + forward, one per thread, transformers "
+                             "built before the timing",
+                   "roundtrip_max_rel_err": float(max(np.max(np.abs(x - y)) / np.max(np.abs(y))
+                                                      for x, y in zip(cref.reshape(B, -1), c.reshape(B, -1))))}
+        except (FileNotFoundError, OSError) as exc:
+            cpu = {"unavailable": str(exc)}
     if rank == 0:
         print(json.dumps({
             "metric": "SH backward+forward transforms/s, lmax 1023 x 8" + (", split-precision Legendre sums"
@@ -292,7 +321,7 @@ def run_sh(args, rank: int, world: int, barrier) -> None:
             "fp64_gpu": {"value": world * B / (ms64 * 1e-3), "ms_per_step": ms64, "stages_ms": st64,
                          "roundtrip_max_rel_err": err64},
             "split_vs_fp64": (ms64 / ms) if split else None,
-            "stages_ms": stages, "clocks": clocks}), flush=True)
+            "stages_ms": stages, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks}), flush=True)
 
 
 def run_evaluate(args, rank: int, world: int, barrier) -> None:

@@ -410,6 +410,21 @@ class Reference(_Lib):
         fn(zn, sn, sp, L, batch, _ptr(grids), _ptr(coeffs), _ptr(out), nthreads, nsteps, _ptr(secs))
         return secs, coeffs, out
 
+    def st_bwd_fwd_steps(self, coeffs, L, nthreads, nsteps=1, sn=0, sp=0):
+        """`nsteps` timed steps of backward + forward of every SH expansion
+        (LonLat grids) on `nthreads` threads; each thread builds its
+        transformer once, before the timing.  Returns (seconds per step,
+        grids, coefficients)."""
+        coeffs = np.ascontiguousarray(coeffs, dtype=np.float64)
+        batch = coeffs.shape[0]
+        grids = np.zeros((batch,) + tuple(st_grid_shape(L)))
+        out = np.zeros_like(coeffs)
+        secs = np.zeros(nsteps)
+        fn = self._f("st_bwd_fwd_steps", [_c_int, _c_int, _c_sz, _c_sz, _p_dbl, _p_dbl, _p_dbl, _c_int, _c_int,
+                                          _p_dbl])
+        fn(sn, sp, L, batch, _ptr(coeffs), _ptr(grids), _ptr(out), nthreads, nsteps, _ptr(secs))
+        return secs, grids, out
+
     def zt_rotate_backward_ragged(self, orders, coeffs, euler, nthreads, rtype=0, zn=1, sn=0, sp=0,
                                   want_grids=False):
         """Rotor::rotate then backward_transform of items of sorted, uneven

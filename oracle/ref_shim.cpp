@@ -398,6 +398,49 @@ int ref_zt_fwd_bwd_steps(int zn, int sn, int sp, std::size_t order, std::size_t 
     });
 }
 
+// CPU baseline of the SH workload: `nsteps` steps of backward then forward
+// transform of `batch` SH expansions of one order (LonLat grids) on
+// `nthreads` std::threads, items b = t, t + nthreads, ... on thread t.  Each
+// thread builds its reference transformer once, before the first step; only
+// the steps are timed.  Writes each step's seconds to step_secs[0..nsteps).
+int ref_st_bwd_fwd_steps(int sn, int sp, std::size_t order, std::size_t batch, const double* coeffs,
+                         double* grids, double* coeffs_out, int nthreads, int nsteps, double* step_secs) {
+    const std::size_t gsz = StLonLat::size(order);
+    const std::size_t csz = order * (order + 1) / 2;
+    return dispatch_st(sn, sp, [&]<SHNorm N, SHPhase P>() {
+        std::barrier sync(nthreads + 1);
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthreads; ++t) {
+            pool.emplace_back([&, t]() {
+                zest::st::GLQTransformer<N, P, StLonLat> tr(order);
+                sync.arrive_and_wait();  // tables built
+                for (int step = 0; step < nsteps; ++step) {
+                    sync.arrive_and_wait();  // step starts
+                    for (std::size_t b = t; b < batch; b += nthreads) {
+                        zest::st::RealSHSpan<const std::array<double, 2>, N, P> e(
+                            reinterpret_cast<const std::array<double, 2>*>(coeffs + 2 * b * csz), order);
+                        zest::st::SphereGLQGridSpan<double, StLonLat> g(grids + b * gsz, order);
+                        tr.backward_transform(e, g);
+                        zest::st::SphereGLQGridSpan<const double, StLonLat> gi(grids + b * gsz, order);
+                        zest::st::RealSHSpan<std::array<double, 2>, N, P> eo(
+                            reinterpret_cast<std::array<double, 2>*>(coeffs_out + 2 * b * csz), order);
+                        tr.forward_transform(gi, eo);
+                    }
+                    sync.arrive_and_wait();  // step ends
+                }
+            });
+        }
+        sync.arrive_and_wait();
+        for (int step = 0; step < nsteps; ++step) {
+            const auto t0 = std::chrono::steady_clock::now();
+            sync.arrive_and_wait();
+            sync.arrive_and_wait();
+            step_secs[step] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        }
+        for (auto& th : pool) th.join();
+    });
+}
+
 // CPU baseline of batches of uneven order: Rotor::rotate (in place) then
 // backward_transform of item i to a grid of its own order, for n_items items
 // sorted by order.  Thread t takes a contiguous run of items of about equal
