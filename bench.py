@@ -473,9 +473,10 @@ def run_lsq(args, rank: int, world: int, barrier) -> None:
     """Least-squares fits to scattered data (st::LSQTransformer): 16 data
     vectors at 20,000 seeded points fitted with SH expansions of order 32
     (1,024 real unknowns) per step; the design matrix is built on the device
-    and solved by QR (cuSOLVER).  Beside it, the Zernike fit of order 12.  The
-    CPU baseline is numpy's least-squares solve of the same design matrix,
-    built from the oracle's tables outside the timed region."""
+    and solved by the library's blocked Householder QR.  Beside it, the
+    Zernike fit of order 12.  The CPU baseline is numpy's least-squares solve
+    of the same design matrix, built from the oracle's tables outside the
+    timed region."""
     import torch
     import zest_gb300 as zg
     ctx = zg.Context(int(os.environ.get("LOCAL_RANK", "0")))

@@ -126,3 +126,18 @@ def test_lsq_device_memory_and_refusal(ctx, oracle):
     with pytest.raises(zg.ZestGPUError) as ex:
         ctx.st_lsq(data[:50], L, lat[:50], lon[:50])  # 50 points, 100 unknowns
     assert ex.value.code == zg.ERR_UNSUPPORTED
+
+
+def test_st_lsq_many_panels_vs_numpy(ctx, oracle):
+    """Order 32 (1,024 unknowns: 32 panels of the blocked QR) on 2,500 points
+    with 5 noisy data vectors, against numpy's least-squares solution."""
+    rng = np.random.default_rng(34)
+    L, N, batch = 32, 2500, 5
+    lat = np.arcsin(rng.uniform(-1, 1, N))
+    lon = rng.uniform(0, 2 * np.pi, N)
+    A, keys = st_design(oracle, L, lat, lon, 0, 0)
+    data = rng.normal(size=(batch, A.shape[1])) @ A.T + rng.normal(scale=0.1, size=(batch, N))
+    want = np.linalg.lstsq(A, data.T, rcond=None)[0].T
+    got = ctx.st_lsq(data.ravel(), L, lat, lon, batch=batch).reshape(batch, -1, 2)
+    for b in range(batch):
+        assert relmax(got[b], to_pairs(want[b], keys, tri_size(L))) < 1e-9

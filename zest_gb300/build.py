@@ -83,10 +83,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     if (os.path.exists(LIB) and _native(LIB)
             and all(os.path.getmtime(LIB) >= os.path.getmtime(o) for o in objs)):
         return LIB
-    # cuSOLVER and cuBLAS (least-squares fits) from the toolkit nvcc belongs to
-    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
-    cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB + ".tmp"] + objs + [
-        "-L", cuda_lib, "-lcusolver", "-lcublas", "-Xlinker", "-rpath", "-Xlinker", cuda_lib]
+    cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB + ".tmp"] + objs
     if verbose:
         print(" ".join(cmd), file=sys.stderr)
     subprocess.run(cmd, check=True)
