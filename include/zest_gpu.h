@@ -335,6 +335,14 @@ int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable);
  * default is 512 MiB; 0 turns the pipelining off.  Results do not depend on it.
  * Host buffers should be pinned for the copies to overlap. */
 int zest_gpu_set_host_chunk_bytes(zest_gpu_context* ctx, size_t bytes);
+/* Pins (page-locks) caller-owned host memory for the copies of ZEST_MEM_HOST
+ * calls, so that they run asynchronously and overlap the transforms
+ * (cudaHostRegister on the current device's context; no reference
+ * counterpart: the reference transforms host memory in place), e.g. a
+ * std::vector's data, for callers that do not link the CUDA runtime
+ * themselves.  Unregister before freeing the memory. */
+int zest_gpu_host_register(void* ptr, size_t bytes);
+int zest_gpu_host_unregister(void* ptr);
 /* Self-test of the failure path of the split GEMMs' bounded waits: one
  * kernel waits, for `seconds` (1 ms .. 2 s), on an mbarrier that nothing
  * arrives on, and a second wait in the same kernel gives up as soon as the

@@ -80,3 +80,30 @@ def test_chunked_pinned_round_trip(ctx):
         ctx.set_host_chunk_bytes(512 << 20)
     err = float((c2 - c).abs().max() / c.abs().max())
     assert err < 1e-12
+
+
+def test_registered_host_buffers_match_device_path(ctx):
+    """Host arrays pinned with zest_gpu_host_register go through the chunked
+    pipeline and give bit for bit the device-memory results; unregistering
+    them afterwards succeeds."""
+    torch = pytest.importorskip("torch")
+    import zest_gb300 as zg
+    rng = np.random.default_rng(9)
+    L, batch = 28, 6
+    coeffs = rand_zt(rng, L, batch)
+    ctx.set_host_chunk_bytes(2 * int(np.prod(zt_grid_shape(L))) * 8)
+    grids = np.zeros(batch * int(np.prod(zt_grid_shape(L))))
+    back = np.zeros_like(coeffs)
+    for h in (coeffs, grids, back):
+        zg.host_register(h)
+    try:
+        ctx.zt_backward(coeffs, L, batch=batch, out=grids)
+        ctx.zt_forward(grids, L, batch=batch, out=back)
+    finally:
+        for h in (coeffs, grids, back):
+            zg.host_unregister(h)
+        ctx.set_host_chunk_bytes(512 << 20)
+    g_dev = ctx.zt_backward(torch.from_numpy(coeffs).cuda(), L, batch=batch)
+    c_dev = ctx.zt_forward(g_dev, L, batch=batch)
+    assert np.array_equal(grids, g_dev.cpu().numpy())
+    assert np.array_equal(back, c_dev.cpu().numpy())

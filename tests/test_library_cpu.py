@@ -48,6 +48,12 @@ def test_sizes(zlib):
     assert zlib.st_grid_shape(1024) == (2047, 1024)
 
 
+def test_host_register_rejects_null_without_gpu(zlib):
+    lib = zlib.library()
+    assert lib.zest_gpu_host_register(None, 0) == 1  # ZEST_GPU_ERR_INVALID, before any CUDA call
+    assert lib.zest_gpu_host_unregister(None) == 1
+
+
 def test_null_context_is_rejected_without_gpu(zlib):
     lib = zlib.library()
     rc = lib.zest_gpu_zt_forward(None, 1, 0, 0, 4, 4, 1, None, None, 1)

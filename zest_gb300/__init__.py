@@ -105,6 +105,8 @@ _SIGNATURES = {
     "zest_gpu_zt_rotate_backward_ragged": [_vp, _i, _i, _i, _sz, _vp, _vp, _vp, _i, _vp],
     "zest_gpu_set_autotune": [_vp, _i],
     "zest_gpu_set_host_chunk_bytes": [_vp, _sz],
+    "zest_gpu_host_register": [_vp, _sz],
+    "zest_gpu_host_unregister": [_vp],
     "zest_gpu_selftest_wait_timeout": [_vp, ctypes.c_double],
     "zest_gpu_zt_grid_points": [_sz, _vp, _vp, _vp],
     "zest_gpu_st_grid_points": [_sz, _i, _vp, _vp],
@@ -148,6 +150,19 @@ def _declare(lib):
 def exported_symbols() -> list[str]:
     return sorted(list(_SIGNATURES) + list(_SIZE_FUNCS)
                   + ["zest_gpu_last_error", "zest_gpu_profile_stage_name", "zest_gpu_launch_count"])
+
+
+def host_register(array: np.ndarray) -> None:
+    """Pins a C-contiguous numpy array's memory (cudaHostRegister) so that
+    host-buffer transforms of it copy asynchronously; host_unregister undoes
+    it and must come before the array is freed."""
+    if not array.flags["C_CONTIGUOUS"]:
+        raise ValueError("host_register needs a C-contiguous array")
+    _check(library().zest_gpu_host_register(_vp(array.ctypes.data), int(array.nbytes)))
+
+
+def host_unregister(array: np.ndarray) -> None:
+    _check(library().zest_gpu_host_unregister(_vp(array.ctypes.data)))
 
 
 def launch_count() -> int:

@@ -81,7 +81,7 @@ __global__ void scatter_kernel(int ncol, int batch, const int4* __restrict__ col
 // a fixed order (per-block partials, then one pass over the blocks), so the
 // result does not depend on the launch.
 constexpr int QR_NB = 32;           // panel width
-constexpr int QR_PROWS = 512;       // rows per block of the panel reductions
+constexpr int QR_PROWS = 256;       // rows per block of the panel reductions (one per thread)
 constexpr int QR_CROWS = 512;       // rows per block of V^T C
 constexpr int QR_CCOLS = 64;        // columns per block of V^T C and of the update
 
@@ -290,31 +290,25 @@ __global__ void __launch_bounds__(256) qr_vtc(const double* __restrict__ A, long
     }
 }
 
-// W = T^T (sum over the row blocks of V^T C), one thread per trailing column.
-__global__ void qr_wmat(const double* __restrict__ part, int nblk, int jb, int ncols, const double* __restrict__ T,
-                        double* __restrict__ W) {
+// W = T^T (sum over the row blocks of V^T C).  A block of 32 x 8 threads
+// takes 8 trailing columns: thread (a, c) sums entry (a, c) over the row
+// blocks in a fixed order, then forms (T^T u)_a = sum_{q <= a} T[q][a] u_q.
+__global__ void __launch_bounds__(256) qr_wmat(const double* __restrict__ part, int nblk, int jb, int ncols,
+                                               const double* __restrict__ T, double* __restrict__ W) {
     __shared__ double Ts[QR_NB][QR_NB];
-    for (int e = threadIdx.x; e < QR_NB * QR_NB; e += blockDim.x) Ts[e / QR_NB][e % QR_NB] = T[e];
+    __shared__ double u[8][QR_NB];
+    const int a = threadIdx.x, cl = threadIdx.y;
+    for (int e = threadIdx.y * QR_NB + threadIdx.x; e < QR_NB * QR_NB; e += QR_NB * 8) Ts[e / QR_NB][e % QR_NB] = T[e];
+    const int c = blockIdx.x * 8 + cl;
+    double v = 0.0;
+    if (c < ncols && a < jb)
+        for (int b = 0; b < nblk; ++b) v += part[((long long)b * QR_NB + a) * ncols + c];
+    u[cl][a] = v;
     __syncthreads();
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncols) return;
-    double u[QR_NB];
-#pragma unroll
-    for (int a = 0; a < QR_NB; ++a) u[a] = 0.0;
-    for (int b = 0; b < nblk; ++b) {
-        const double* p = part + (long long)b * QR_NB * ncols + c;
-#pragma unroll
-        for (int a = 0; a < QR_NB; ++a)
-            if (a < jb) u[a] += p[(long long)a * ncols];
-    }
-#pragma unroll
-    for (int a = 0; a < QR_NB; ++a) {
-        if (a >= jb) break;
-        double v = 0.0;
-#pragma unroll
-        for (int q = 0; q <= a; ++q) v = fma(Ts[q][a], u[q], v);  // (T^T u)_a, T upper triangular
-        W[(long long)a * ncols + c] = v;
-    }
+    if (c >= ncols || a >= jb) return;
+    double w = 0.0;
+    for (int q = 0; q <= a; ++q) w = fma(Ts[q][a], u[cl][q], w);  // T upper triangular
+    W[(long long)a * ncols + c] = w;
 }
 
 // C[i][c] -= sum_a v_a[i] W[a][c] for rows j0 .. m-1: 64 x 64 tiles; thread
@@ -419,7 +413,7 @@ int qr_solve(zest_gpu_context* ctx, LsqState& Q, double* A, int m, int n, double
         const int vb = (m - j0 + QR_CROWS - 1) / QR_CROWS;
         qr_vtc<<<dim3((ntrail + QR_CCOLS - 1) / QR_CCOLS, vb), 256, 0, s>>>(A, lda, m, j0, jb, C, ntrail, part);
         ZG_TRY(launch_check("qr_vtc"));
-        qr_wmat<<<(ntrail + 127) / 128, 128, 0, s>>>(part, vb, jb, ntrail, T, W);
+        qr_wmat<<<(ntrail + 7) / 8, dim3(QR_NB, 8), 0, s>>>(part, vb, jb, ntrail, T, W);
         ZG_TRY(launch_check("qr_wmat"));
         qr_update<<<dim3((ntrail + 63) / 64, (m - j0 + 63) / 64), 256, 0, s>>>(A, lda, m, j0, jb, C, ntrail, W);
         ZG_TRY(launch_check("qr_update"));

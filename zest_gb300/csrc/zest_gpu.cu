@@ -1600,6 +1600,18 @@ int zest_gpu_set_host_chunk_bytes(zest_gpu_context* ctx, size_t bytes) {
     return ZEST_GPU_OK;
 }
 
+int zest_gpu_host_register(void* ptr, size_t bytes) {
+    if (!ptr || bytes == 0) return fail(ZEST_GPU_ERR_INVALID, "host register: null pointer or zero bytes");
+    ZG_CUDA_TRY(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+    return ZEST_GPU_OK;
+}
+
+int zest_gpu_host_unregister(void* ptr) {
+    if (!ptr) return fail(ZEST_GPU_ERR_INVALID, "host unregister: null pointer");
+    ZG_CUDA_TRY(cudaHostUnregister(ptr));
+    return ZEST_GPU_OK;
+}
+
 int zest_gpu_zt_rotate_backward_ragged(zest_gpu_context* ctx, int zn, int sn, int sp, size_t n_items,
                                        const int* orders, double* coeffs, const double* euler, int rotation_type,
                                        double* grids) {
