@@ -131,17 +131,42 @@ __global__ void __launch_bounds__(256) qr_panel_dots(const double* __restrict__ 
     if (blockIdx.x == 0 && threadIdx.x <= nc) rowk[threadIdx.x] = A[(long long)(k + threadIdx.x) * lda + k];
 }
 
-// Reflector k, second pass: every block sums the partials in the same order,
-// forms beta, tau and the scale 1 / (alpha - beta) of v, stores v below the
-// diagonal and beta on it, and applies H_k to the panel's columns k+1 .. k+nc
-// on its rows (rows k .. m-1 in blocks of QR_PROWS).  As dlarfg: tau = 0
-// (H_k = I) when the column below the diagonal is zero.
-__global__ void __launch_bounds__(256) qr_panel_apply(double* __restrict__ A, long long lda, int m, int k, int nc,
-                                                      int nblk, const double* __restrict__ part,
-                                                      const double* __restrict__ rowk, double* __restrict__ tau) {
+// Block reduction of QR_NB per-thread sums; thread t <= n then holds the
+// block's sum of entry t in red[0][t].
+__device__ __forceinline__ void qr_block_sums(double (&acc)[QR_NB], double (*red)[QR_NB]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < QR_NB; ++c) {
+        double v = acc[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][c] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < QR_NB) {
+        double v = 0.0;
+        for (int w = 0; w < 8; ++w) v += red[w][threadIdx.x];
+        red[0][threadIdx.x] = v;  // only warp 0 reads and writes red[0] from here on
+    }
+    __syncthreads();
+}
+
+// Reflector k, second pass, fused with the first pass of reflector k + 1.
+// Every block sums the partials of reflector k in the same order, forms beta,
+// tau and the scale 1 / (alpha - beta) of v, stores v below the diagonal and
+// beta on it, and applies H_k to the panel's columns k+1 .. k+nc on its rows
+// (rows k .. m-1, QR_PROWS per block, one per thread).  As dlarfg: tau = 0
+// (H_k = I) when the column below the diagonal is zero.  Then, on the same
+// rows (those below k + 1), it sums the first pass of reflector k + 1 into
+// part_out and block 0 records row k + 1 in rowk_out.
+__global__ void __launch_bounds__(256) qr_panel_step(double* __restrict__ A, long long lda, int m, int k, int nc,
+                                                     int nblk, const double* __restrict__ part,
+                                                     const double* __restrict__ rowk, double* __restrict__ part_out,
+                                                     double* __restrict__ rowk_out, double* __restrict__ tau) {
     __shared__ double sum[QR_NB];
     __shared__ double w[QR_NB];
     __shared__ double scale_s;
+    __shared__ double red[8][QR_NB];
     if (threadIdx.x <= nc) {
         double v = 0.0;
         for (int b = 0; b < nblk; ++b) v += part[(long long)b * QR_NB + threadIdx.x];
@@ -164,8 +189,9 @@ __global__ void __launch_bounds__(256) qr_panel_apply(double* __restrict__ A, lo
     }
     __syncthreads();
     const double scale = scale_s;
-    const int i0 = k + blockIdx.x * QR_PROWS, i1 = min(m, i0 + QR_PROWS);
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    const int i = k + blockIdx.x * QR_PROWS + threadIdx.x;  // this thread's row
+    const bool own = i < m && threadIdx.x < QR_PROWS;
+    if (own) {
         double* x = A + (long long)k * lda;
         double v;
         if (i == k) {
@@ -180,6 +206,21 @@ __global__ void __launch_bounds__(256) qr_panel_apply(double* __restrict__ A, lo
             a[i] = fma(-v, w[c], a[i]);
         }
     }
+    if (nc == 0) return;  // the panel's last reflector
+    // first pass of reflector k + 1 over this block's rows below k + 1
+    double acc[QR_NB];
+#pragma unroll
+    for (int c = 0; c < QR_NB; ++c) acc[c] = 0.0;
+    if (own && i > k + 1) {
+        const double xi = A[(long long)(k + 1) * lda + i];
+        acc[0] = xi * xi;
+#pragma unroll
+        for (int c = 1; c < QR_NB; ++c)
+            if (c < nc) acc[c] = xi * A[(long long)(k + 1 + c) * lda + i];
+    }
+    qr_block_sums(acc, red);  // also orders row k + 1's update before the read below
+    if (threadIdx.x < nc) part_out[(long long)blockIdx.x * QR_NB + threadIdx.x] = red[0][threadIdx.x];
+    if (blockIdx.x == 0 && threadIdx.x < nc) rowk_out[threadIdx.x] = A[(long long)(k + 1 + threadIdx.x) * lda + k + 1];
 }
 
 // v_a[i] of a panel starting at column j0 (v_a[j0 + a] = 1, 0 above)
@@ -381,9 +422,10 @@ int qr_solve(zest_gpu_context* ctx, LsqState& Q, double* A, int m, int n, double
     const int pblk = (m + QR_PROWS - 1) / QR_PROWS;
     const int cblk = (m + QR_CROWS - 1) / QR_CROWS;
     const int ncol_max = n + nrhs;
-    const size_t part_n = std::max<size_t>({(size_t)pblk * QR_NB, (size_t)pblk * QR_NB * QR_NB,
+    const size_t part_half = (size_t)pblk * QR_NB;  // panel partials, two halves
+    const size_t part_n = std::max<size_t>({2 * part_half, (size_t)pblk * QR_NB * QR_NB,
                                             (size_t)cblk * QR_NB * ncol_max});
-    ZG_TRY(Q.part.ensure((part_n + QR_NB + 8) * sizeof(double)));
+    ZG_TRY(Q.part.ensure((part_n + 2 * QR_NB + 8) * sizeof(double)));
     ZG_TRY(Q.T.ensure((QR_NB * QR_NB + n + 8) * sizeof(double)));
     ZG_TRY(Q.W.ensure((size_t)QR_NB * ncol_max * sizeof(double)));
     double* part = Q.part.as<double>();
@@ -393,14 +435,21 @@ int qr_solve(zest_gpu_context* ctx, LsqState& Q, double* A, int m, int n, double
     double* W = Q.W.as<double>();
     for (int j0 = 0; j0 < n; j0 += QR_NB) {
         const int jb = std::min(QR_NB, n - j0);
+        // first pass of the panel's first reflector, then one fused launch per
+        // reflector (its second pass and the next one's first pass), the
+        // partials alternating between two halves of the buffer
+        int nprev = std::max(1, (m - j0 - 1 + QR_PROWS - 1) / QR_PROWS);
+        qr_panel_dots<<<nprev, 256, 0, s>>>(A, lda, m, j0, jb - 1, part, rowk);
+        ZG_TRY(launch_check("qr_panel_dots"));
         for (int k = j0; k < j0 + jb; ++k) {
             const int nc = j0 + jb - 1 - k;  // panel columns right of k
-            const int nb1 = std::max(1, (m - k - 1 + QR_PROWS - 1) / QR_PROWS);
-            qr_panel_dots<<<nb1, 256, 0, s>>>(A, lda, m, k, nc, part, rowk);
-            ZG_TRY(launch_check("qr_panel_dots"));
-            const int nb2 = (m - k + QR_PROWS - 1) / QR_PROWS;
-            qr_panel_apply<<<nb2, 256, 0, s>>>(A, lda, m, k, nc, nb1, part, rowk, tau);
-            ZG_TRY(launch_check("qr_panel_apply"));
+            const int cur = (k - j0) & 1;
+            const int nb = (m - k + QR_PROWS - 1) / QR_PROWS;
+            qr_panel_step<<<nb, 256, 0, s>>>(A, lda, m, k, nc, nprev, part + (size_t)cur * part_half,
+                                             rowk + cur * QR_NB, part + (size_t)(cur ^ 1) * part_half,
+                                             rowk + (cur ^ 1) * QR_NB, tau);
+            ZG_TRY(launch_check("qr_panel_step"));
+            nprev = nb;
         }
         const int ntrail = (n - j0 - jb) + nrhs;
         if (ntrail == 0) continue;
