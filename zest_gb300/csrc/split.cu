@@ -940,6 +940,7 @@ template <bool ACC = false>
 struct EpiRadBwd {  // rows (l, b, m, c) as rad_row -> flm[(tri(l,m) B + b)][k][c]
     static constexpr bool RMW = ACC;
     static constexpr bool CHUNK = ACC;
+    static constexpr bool PAIR_ROWS = !ACC;  // rows c = 0, 1 of one (l, b, m): (re, im) at each k
     double* flm;
     int nr, B;
     struct Row { double* p; };
@@ -950,6 +951,10 @@ struct EpiRadBwd {  // rows (l, b, m, c) as rad_row -> flm[(tri(l,m) B + b)][k][
     __device__ void load(const Row& R, int n, double* old) const { old[0] = R.p[2 * n]; }
     __device__ void store(const Row& R, const SplitUnit&, int n, double v, const double* old) const {
         R.p[2 * n] = ACC ? old[0] + v : v;
+    }
+    // (re, im) of column n, from the row of part c (the pair starts c doubles before R.p)
+    __device__ void store_pair(const Row& R, int n, double2 v, int c) const {
+        *reinterpret_cast<double2*>(R.p - c + 2 * n) = v;
     }
 };
 // rows (m, b, kc) -> E_p[b][m][j'][kc] (conjugated): the parity-p Legendre
@@ -1112,6 +1117,13 @@ struct EpiDftBwdSin {
 // before one rounding each, with integer operations only (no FP64 adds).
 // The table digits are at most 64 in magnitude (|2 cos|, |2 sin| <= 2), so
 // |T| < 2^61 and the sums cannot overflow.
+// Epilogues whose rows 2i and 2i + 1 are the two halves of one 16-byte pair
+// at each column (PAIR_ROWS; store_pair writes both)
+template <class E, class = void>
+struct pair_rows_epi : std::false_type {};
+template <class E>
+struct pair_rows_epi<E, std::void_t<decltype(E::PAIR_ROWS)>> : std::integral_constant<bool, E::PAIR_ROWS> {};
+
 template <class E, class = void>
 struct raw_epi : std::false_type {};
 template <class E>
@@ -1449,6 +1461,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
 #pragma unroll
             for (int c = 0; c < CW / 4; ++c) {
                 double old[4][2];
+                double vv[4];  // pair-row epilogues: this row's values of the four columns
                 if constexpr (Epi::RMW) {
                     if (rv) {
 #pragma unroll
@@ -1468,7 +1481,22 @@ __global__ void __launch_bounds__(SP_THREADS, 1)
                         const int e2 = __shfl_sync(0xffffffffu, eb_b, idx & 31);
                         eb = idx < 32 ? e1 : e2;
                     }
-                    if (rv && n < u.n) {
+                    if constexpr (pair_rows_epi<Epi>::value) {
+                        // rows 2i and 2i + 1 are the two halves of one 16-byte
+                        // pair at every column: neighbouring lanes swap one
+                        // value, and each stores a whole pair, the even lane at
+                        // the even column of the two and the odd lane at the
+                        // odd one
+                        vv[j] = i64_ldexp(T[4 * c + j], ea + eb + TEXP);
+                        if (j & 1) {
+                            const bool odd = lane & 1;
+                            const double got = __shfl_xor_sync(0xffffffffu, odd ? vv[j - 1] : vv[j], 1);
+                            const int np = odd ? n : n - 1;
+                            if (rv && np < u.n)
+                                epi.store_pair(R, np, odd ? make_double2(got, vv[j]) : make_double2(vv[j - 1], got),
+                                               odd);
+                        }
+                    } else if (rv && n < u.n) {
                         const double v = i64_ldexp(T[4 * c + j], ea + eb + TEXP);
                         epi.store(R, u, n, v, old[j]);
                     }
