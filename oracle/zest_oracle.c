@@ -4,7 +4,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle: tests/, the
  * smoke check in __graft_entry__.py and the cpu_baseline leg of bench.py may
- * call it, as the checker.  The product (zest_gb300/, include/) never links
+ * call it, to check results.  The product (zest_gb300/, include/) never links
  * or calls it, and the product path fails loudly rather than fall back here.
  *
  * Parity pin: checked against golden vectors produced by the compiled
