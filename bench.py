@@ -951,7 +951,7 @@ def main():
                "mean_step_ms": float(np.mean(step_ms)),
                "median_step_ms": float(np.median(step_ms)),
                "rate_at_median_step": world * B / (float(np.median(step_ms)) * 1e-3),
-               "host_chunk_bytes": 512 << 20, "pipelined": "uploads, transforms and downloads overlap per chunk"}
+               "host_chunk_bytes": 256 << 20, "pipelined": "uploads, transforms and downloads overlap per chunk"}
         del gh, ch, go
 
     cpu = None

@@ -332,7 +332,7 @@ int zest_gpu_set_autotune(zest_gpu_context* ctx, int enable);
  * chunks of about `bytes`, and the upload of one chunk, the transform of the
  * previous one and the download of the one before run at the same time (two
  * copy streams of the context and two device slots per direction).  The
- * default is 512 MiB; 0 turns the pipelining off.  Results do not depend on it.
+ * default is 256 MiB; 0 turns the pipelining off.  Results do not depend on it.
  * Host buffers should be pinned for the copies to overlap. */
 int zest_gpu_set_host_chunk_bytes(zest_gpu_context* ctx, size_t bytes);
 /* Pins (page-locks) caller-owned host memory for the copies of ZEST_MEM_HOST

@@ -390,7 +390,7 @@ class Context:
 
     def set_host_chunk_bytes(self, nbytes: int):
         """Chunk size of the copy/compute pipeline of host-memory Zernike
-        transforms (default 512 MiB; 0 turns it off)."""
+        transforms (default 256 MiB; 0 turns it off)."""
         _check(self.lib.zest_gpu_set_host_chunk_bytes(self._h, int(nbytes)))
 
     def zt_rotate_backward_ragged(self, orders, coeffs, euler, grids, conv=ZT_GEO,

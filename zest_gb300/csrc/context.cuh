@@ -189,7 +189,7 @@ struct zest_gpu_context {
     std::map<std::tuple<int, int, int>, std::unique_ptr<UniformRotation>> uniform_rot;  // split rotations
     std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<TileEntry>> tiles;
     bool autotune = true;                                     // time the tile shapes on first use
-    size_t host_chunk_bytes = size_t(1) << 29;                // pipelined host calls: input bytes per chunk
+    size_t host_chunk_bytes = size_t(1) << 28;                // pipelined host calls: input bytes per chunk
     std::unique_ptr<RaggedPlan> ragged;                       // last batch of uneven orders, with its graph
     cudaStream_t graph_stream = nullptr;                      // own stream for graph capture and replay
     cudaStream_t copy_stream[2] = {nullptr, nullptr};         // host->device, device->host of pipelined calls
